@@ -1,0 +1,176 @@
+"""Host-side binding of the C ABI (include/gckpp_gb300.h) via ctypes.
+
+This mirrors, for Python callers, what a Fortran caller binds with
+ISO_C_BINDING: ``Solver.integrate`` is the batched INTEGRATE
+(KPP/fullchem/gckpp_Integrator.F90:80-162) over cells held in
+cell-interleaved arrays ``X[k, cell]``; ``Solver.update_rconst`` is the
+batched Update_RCONST (KPP/fullchem/gckpp_Rates.F90:408-1503).
+
+Arrays may be numpy arrays (host memory: the library stages them through the
+device) or CUDA torch tensors (device memory: no copies).  The library must be
+built (``gcchem.build.build()``); if it is missing, loading fails loudly --
+there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+GC_KPP_OK = 0
+GC_KPP_EINVAL = -101
+GC_KPP_ECUDA = -102
+GC_KPP_ENOMEM = -103
+GC_KPP_EUNSUPPORTED = -104
+MEM_HOST = 0
+MEM_DEVICE = 1
+OPT_ARITH = 1
+OPT_SCHEDULE = 2
+OPT_BLOCK = 3
+OPT_BLOCKS_PER_SM = 4
+OPT_MAX_SLOTS = 5
+
+EXPORTED = [
+    "gc_kpp_mechanism_dims",
+    "gc_kpp_ctx_create",
+    "gc_kpp_ctx_destroy",
+    "gc_kpp_ctx_set_option",
+    "gc_kpp_last_error",
+    "gc_kpp_integrate_batch",
+    "gc_kpp_update_rconst_batch",
+]
+
+_lib = None
+
+
+class GcKppError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gc_kpp error %d: %s" % (code, msg))
+        self.code = code
+
+
+def load_library(path=None):
+    """Load libgckpp_gb300.so (raises OSError if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    path = path or _build.lib_path()
+    if not os.path.exists(path):
+        raise OSError("CUDA library %s is not built; run gcchem.build.build()" % path)
+    lib = ctypes.CDLL(path)
+    vp, i32, i64, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
+    lib.gc_kpp_mechanism_dims.argtypes = [ctypes.POINTER(i32)] * 5
+    lib.gc_kpp_ctx_create.argtypes = [ctypes.POINTER(vp), i32]
+    lib.gc_kpp_ctx_destroy.argtypes = [vp]
+    lib.gc_kpp_ctx_set_option.argtypes = [vp, i32, i64]
+    lib.gc_kpp_last_error.restype = ctypes.c_char_p
+    lib.gc_kpp_integrate_batch.argtypes = [vp, i32, f64, f64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64,
+                                           vp, i32, vp]
+    lib.gc_kpp_update_rconst_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, vp, i64, i32, vp]
+    if path == _build.lib_path():
+        _lib = lib
+    return lib
+
+
+def dims():
+    lib = load_library()
+    out = [ctypes.c_int() for _ in range(5)]
+    lib.gc_kpp_mechanism_dims(*[ctypes.byref(o) for o in out])
+    return dict(zip(["nspec", "nvar", "nfix", "nreact", "lu_nonzero"], [o.value for o in out]))
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if _is_torch(x):
+        return ctypes.c_void_p(x.data_ptr())
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data_as(ctypes.c_void_p)
+    raise TypeError("unsupported array type %r" % type(x))
+
+
+def _ld(x, ncell):
+    if _is_torch(x):
+        return x.stride(0) if x.dim() == 2 else ncell
+    return x.strides[0] // x.itemsize if x.ndim == 2 else ncell
+
+
+class Solver:
+    """A solver context on one CUDA device (gc_kpp_ctx)."""
+
+    def __init__(self, device=0, arith="fast", schedule="plain", block=0, blocks_per_sm=0, max_slots=0):
+        self.lib = load_library()
+        self.ctx = ctypes.c_void_p()
+        self._check(self.lib.gc_kpp_ctx_create(ctypes.byref(self.ctx), device))
+        self.set(arith=arith, schedule=schedule, block=block, blocks_per_sm=blocks_per_sm, max_slots=max_slots)
+
+    def _check(self, rc):
+        if rc != GC_KPP_OK:
+            raise GcKppError(rc, self.lib.gc_kpp_last_error().decode())
+
+    def set(self, arith=None, schedule=None, block=None, blocks_per_sm=None, max_slots=None):
+        if arith is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1}[arith]))
+        if schedule is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_SCHEDULE, {"plain": 0, "queue": 1}[schedule]))
+        if block is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_BLOCK, int(block)))
+        if blocks_per_sm is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_BLOCKS_PER_SM, int(blocks_per_sm)))
+        if max_slots is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_MAX_SLOTS, int(max_slots)))
+
+    def close(self):
+        if self.ctx:
+            self.lib.gc_kpp_ctx_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def integrate(self, c, rconst, atol, rtol, tin, tout, icntrl=None, rcntrl=None, hstart=None,
+                  istatus=None, rstatus=None, ierr=None, stream=None):
+        """Batched INTEGRATE.  c: [NSPEC, ncell] (in/out); rconst: [NREACT, ncell];
+        istatus/rstatus: [20, ncell] outputs; ierr: [ncell] output."""
+        dev = _is_torch(c) and c.is_cuda
+        ncell = c.shape[1]
+        if icntrl is not None:
+            icntrl = np.ascontiguousarray(icntrl, dtype=np.int32)
+        if rcntrl is not None:
+            rcntrl = np.ascontiguousarray(rcntrl, dtype=np.float64)
+        if dev:
+            import torch  # noqa: F401
+            mem = MEM_DEVICE
+        else:
+            mem = MEM_HOST
+        args_ok = [a for a in (c, rconst, atol, rtol, ierr) if a is not None]
+        if len(args_ok) != 5:
+            raise ValueError("c, rconst, atol, rtol and ierr are required")
+        ldo = _ld(istatus, ncell) if istatus is not None else (_ld(rstatus, ncell) if rstatus is not None else ncell)
+        s = ctypes.c_void_p(stream) if stream else None
+        rc = self.lib.gc_kpp_integrate_batch(
+            self.ctx, ncell, float(tin), float(tout), _ptr(c), _ld(c, ncell), _ptr(rconst), _ld(rconst, ncell),
+            _ptr(atol), _ptr(rtol),
+            icntrl.ctypes.data_as(ctypes.c_void_p) if icntrl is not None else None,
+            rcntrl.ctypes.data_as(ctypes.c_void_p) if rcntrl is not None else None,
+            _ptr(hstart), _ptr(istatus), _ptr(rstatus), ldo, _ptr(ierr), mem, s)
+        self._check(rc)
+
+    def update_rconst(self, met, photol, c, rconst, stream=None):
+        """Batched Update_RCONST.  met: [NMET, ncell]; photol: [200, ncell];
+        c: [NSPEC, ncell]; rconst: [NREACT, ncell] output."""
+        dev = _is_torch(rconst) and rconst.is_cuda
+        ncell = rconst.shape[1]
+        s = ctypes.c_void_p(stream) if stream else None
+        rc = self.lib.gc_kpp_update_rconst_batch(
+            self.ctx, ncell, _ptr(met), _ld(met, ncell), _ptr(photol), _ld(photol, ncell), _ptr(c), _ld(c, ncell),
+            _ptr(rconst), _ld(rconst, ncell), MEM_DEVICE if dev else MEM_HOST, s)
+        self._check(rc)

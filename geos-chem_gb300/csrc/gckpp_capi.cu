@@ -1,0 +1,637 @@
+// C ABI of the GB300 KPP fullchem solve (include/gckpp_gb300.h).
+//
+// Host side of INTEGRATE/Rosenbrock (KPP/fullchem/gckpp_Integrator.F90:
+// 80-162, 333-477): merges ICNTRL_U/RCNTRL_U over the defaults, selects the
+// method, validates tolerances, then launches the per-cell kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gckpp_gb300.h"
+#include "_gen/mech_tables.inc"
+#include "_gen/rates_program.inc"
+#include "kpp_rates.h"
+#include "kpp_launch.h"
+#include "kpp_rosenbrock.cuh"
+
+using namespace gckpp;
+namespace T = gcmech_tables;
+namespace RT = gcrates_tables;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? GC_KPP_ENOMEM : GC_KPP_ECUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define GC_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t _e = (call);                            \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+template <typename X>
+cudaError_t upload(const X* host, size_t n, const X** dev, std::vector<void*>& owned) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(X) + 16);
+  if (e != cudaSuccess) return e;
+  owned.push_back(p);
+  e = cudaMemcpy(p, host, n * sizeof(X), cudaMemcpyHostToDevice);
+  *dev = static_cast<const X*>(p);
+  return e;
+}
+
+// Rosenbrock method coefficients (gckpp_Integrator.F90 Ros2 :2062, Ros3
+// :2112, Ros4 :2167, Rodas3 :2239, Rodas4 :2306, Rang3 :2398).
+bool method_table(int id, RosMethod& r) {
+  std::memset(&r, 0, sizeof(r));
+  switch (id) {
+    case 1: {  // Ros2
+      const double g = 1.0 + 1.0 / std::sqrt(2.0);
+      r.S = 2;
+      r.A[0] = (1.0) / g;
+      r.C[0] = (-2.0) / g;
+      r.NewF[0] = 1; r.NewF[1] = 1;
+      r.M[0] = (3.0) / (2.0 * g);
+      r.M[1] = (1.0) / (2.0 * g);
+      r.E[0] = 1.0 / (2.0 * g);
+      r.E[1] = 1.0 / (2.0 * g);
+      r.ELO = 2.0;
+      r.Alpha[0] = 0.0; r.Alpha[1] = 1.0;
+      r.Gamma[0] = g; r.Gamma[1] = -g;
+      return true;
+    }
+    case 2: {  // Ros3
+      r.S = 3;
+      r.A[0] = 1.0; r.A[1] = 1.0; r.A[2] = 0.0;
+      r.C[0] = -0.10156171083877702091975600115545E+01;
+      r.C[1] = 0.40759956452537699824805835358067E+01;
+      r.C[2] = 0.92076794298330791242156818474003E+01;
+      r.NewF[0] = 1; r.NewF[1] = 1; r.NewF[2] = 0;
+      r.M[0] = 0.1E+01;
+      r.M[1] = 0.61697947043828245592553615689730E+01;
+      r.M[2] = -0.42772256543218573326238373806514;
+      r.E[0] = 0.5;
+      r.E[1] = -0.29079558716805469821718236208017E+01;
+      r.E[2] = 0.22354069897811569627360909276199;
+      r.ELO = 3.0;
+      r.Alpha[0] = 0.0;
+      r.Alpha[1] = 0.43586652150845899941601945119356;
+      r.Alpha[2] = 0.43586652150845899941601945119356;
+      r.Gamma[0] = 0.43586652150845899941601945119356;
+      r.Gamma[1] = 0.24291996454816804366592249683314;
+      r.Gamma[2] = 0.21851380027664058511513169485832E+01;
+      return true;
+    }
+    case 3: {  // Ros4
+      r.S = 4;
+      r.A[0] = 0.2000000000000000E+01;
+      r.A[1] = 0.1867943637803922E+01;
+      r.A[2] = 0.2344449711399156;
+      r.A[3] = r.A[1];
+      r.A[4] = r.A[2];
+      r.A[5] = 0.0;
+      r.C[0] = -0.7137615036412310E+01;
+      r.C[1] = 0.2580708087951457E+01;
+      r.C[2] = 0.6515950076447975;
+      r.C[3] = -0.2137148994382534E+01;
+      r.C[4] = -0.3214669691237626;
+      r.C[5] = -0.6949742501781779;
+      r.NewF[0] = 1; r.NewF[1] = 1; r.NewF[2] = 1; r.NewF[3] = 0;
+      r.M[0] = 0.2255570073418735E+01;
+      r.M[1] = 0.2870493262186792;
+      r.M[2] = 0.4353179431840180;
+      r.M[3] = 0.1093502252409163E+01;
+      r.E[0] = -0.2815431932141155;
+      r.E[1] = -0.7276199124938920E-01;
+      r.E[2] = -0.1082196201495311;
+      r.E[3] = -0.1093502252409163E+01;
+      r.ELO = 4.0;
+      r.Alpha[0] = 0.0;
+      r.Alpha[1] = 0.1145640000000000E+01;
+      r.Alpha[2] = 0.6552168638155900;
+      r.Alpha[3] = r.Alpha[2];
+      r.Gamma[0] = 0.5728200000000000;
+      r.Gamma[1] = -0.1769193891319233E+01;
+      r.Gamma[2] = 0.7592633437920482;
+      r.Gamma[3] = -0.1049021087100450;
+      return true;
+    }
+    case 0:
+    case 4: {  // Rodas3
+      r.S = 4;
+      r.A[0] = 0.0; r.A[1] = 2.0; r.A[2] = 0.0; r.A[3] = 2.0; r.A[4] = 0.0; r.A[5] = 1.0;
+      r.C[0] = 4.0; r.C[1] = 1.0; r.C[2] = -1.0; r.C[3] = 1.0; r.C[4] = -1.0;
+      r.C[5] = -(8.0 / 3.0);
+      r.NewF[0] = 1; r.NewF[1] = 0; r.NewF[2] = 1; r.NewF[3] = 1;
+      r.M[0] = 2.0; r.M[1] = 0.0; r.M[2] = 1.0; r.M[3] = 1.0;
+      r.E[0] = 0.0; r.E[1] = 0.0; r.E[2] = 0.0; r.E[3] = 1.0;
+      r.ELO = 3.0;
+      r.Alpha[0] = 0.0; r.Alpha[1] = 0.0; r.Alpha[2] = 1.0; r.Alpha[3] = 1.0;
+      r.Gamma[0] = 0.5; r.Gamma[1] = 1.5; r.Gamma[2] = 0.0; r.Gamma[3] = 0.0;
+      return true;
+    }
+    case 5: {  // Rodas4
+      r.S = 6;
+      r.Alpha[0] = 0.000; r.Alpha[1] = 0.386; r.Alpha[2] = 0.210;
+      r.Alpha[3] = 0.630; r.Alpha[4] = 1.000; r.Alpha[5] = 1.000;
+      r.Gamma[0] = 0.2500000000000000;
+      r.Gamma[1] = -0.1043000000000000;
+      r.Gamma[2] = 0.1035000000000000;
+      r.Gamma[3] = -0.3620000000000023E-01;
+      r.Gamma[4] = 0.0;
+      r.Gamma[5] = 0.0;
+      r.A[0] = 0.1544000000000000E+01;
+      r.A[1] = 0.9466785280815826;
+      r.A[2] = 0.2557011698983284;
+      r.A[3] = 0.3314825187068521E+01;
+      r.A[4] = 0.2896124015972201E+01;
+      r.A[5] = 0.9986419139977817;
+      r.A[6] = 0.1221224509226641E+01;
+      r.A[7] = 0.6019134481288629E+01;
+      r.A[8] = 0.1253708332932087E+02;
+      r.A[9] = -0.6878860361058950;
+      r.A[10] = r.A[6];
+      r.A[11] = r.A[7];
+      r.A[12] = r.A[8];
+      r.A[13] = r.A[9];
+      r.A[14] = 1.0;
+      r.C[0] = -0.5668800000000000E+01;
+      r.C[1] = -0.2430093356833875E+01;
+      r.C[2] = -0.2063599157091915;
+      r.C[3] = -0.1073529058151375;
+      r.C[4] = -0.9594562251023355E+01;
+      r.C[5] = -0.2047028614809616E+02;
+      r.C[6] = 0.7496443313967647E+01;
+      r.C[7] = -0.1024680431464352E+02;
+      r.C[8] = -0.3399990352819905E+02;
+      r.C[9] = 0.1170890893206160E+02;
+      r.C[10] = 0.8083246795921522E+01;
+      r.C[11] = -0.7981132988064893E+01;
+      r.C[12] = -0.3152159432874371E+02;
+      r.C[13] = 0.1631930543123136E+02;
+      r.C[14] = -0.6058818238834054E+01;
+      r.M[0] = r.A[6]; r.M[1] = r.A[7]; r.M[2] = r.A[8]; r.M[3] = r.A[9];
+      r.M[4] = 1.0; r.M[5] = 1.0;
+      r.E[5] = 1.0;
+      for (int i = 0; i < 6; ++i) r.NewF[i] = 1;
+      r.ELO = 4.0;
+      return true;
+    }
+    case 6: {  // Rang3
+      r.S = 4;
+      r.A[0] = 5.09052051067020e+00; r.A[1] = 5.09052051067020e+00; r.A[2] = 0.0;
+      r.A[3] = 4.97628111010787e+00; r.A[4] = 2.77268164715849e-02; r.A[5] = 2.29428036027904e-01;
+      r.C[0] = -1.16790812312283e+01; r.C[1] = -1.64057326467367e+01; r.C[2] = -2.77268164715850e-01;
+      r.C[3] = -8.38103960500476e+00; r.C[4] = -8.48328409199343e-01; r.C[5] = 2.87009860433106e-01;
+      r.M[0] = 5.22582761233094e+00; r.M[1] = -5.56971148154165e-01;
+      r.M[2] = 3.57979469353645e-01; r.M[3] = 1.72337398521064e+00;
+      r.E[0] = -5.16845212784040e+00; r.E[1] = -1.26351942603842e+00;
+      r.E[2] = -1.11022302462516e-16; r.E[3] = 2.22044604925031e-16;
+      r.Alpha[0] = 0.0; r.Alpha[1] = 2.21878746765329e+00;
+      r.Alpha[2] = 2.21878746765329e+00; r.Alpha[3] = 1.55392337535788e+00;
+      r.Gamma[0] = 4.35866521508459e-01; r.Gamma[1] = -1.78292094614483e+00;
+      r.Gamma[2] = -2.46541900496934e+00; r.Gamma[3] = -8.05529997906370e-01;
+      for (int i = 0; i < 4; ++i) r.NewF[i] = 1;
+      r.ELO = 3.0;
+      return true;
+    }
+    default:
+      return false;
+  }
+}
+
+WsLayout make_layout() {
+  WsLayout l;
+  int o = 0;
+  l.aux = o; o += T::NFIX + T::NREACT;
+  l.y0 = o; o += T::NVAR;
+  l.y1 = o; o += T::NVAR;
+  l.fcn0 = o; o += T::NVAR;
+  l.fcn = o; o += T::NVAR;
+  l.dfdt = o; o += T::NVAR;
+  l.k = o; o += SMAX * T::NVAR;
+  l.a = o; o += T::NREACT;
+  l.b = o; o += T::NB;
+  l.j0 = o; o += T::LU_NONZERO;
+  l.g = o; o += T::LU_NONZERO;
+  l.total = o;
+  return l;
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+}  // namespace
+
+struct gc_kpp_ctx {
+  int device = 0;
+  int nsm = 0;
+  MechDev mech{};
+  gcrates::RatesDev rates{};
+  std::vector<void*> owned;
+  WsLayout lay{};
+  DevBuf ws, counter;
+  DevBuf h_c, h_r, h_at, h_rt, h_hs, h_is, h_rs, h_ie;  // staging for host-memory calls
+  DevBuf h_met, h_ph;
+  int arith = 0;     // 0 fast, 1 strict
+  int schedule = 0;  // 0 plain, 1 queue
+  int block = 128;
+  int blocks_per_sm = 0;
+  long long max_slots = 0;
+};
+
+extern "C" {
+
+int gc_kpp_mechanism_dims(int* nspec, int* nvar, int* nfix, int* nreact, int* lu_nonzero) {
+  if (nspec) *nspec = T::NSPEC;
+  if (nvar) *nvar = T::NVAR;
+  if (nfix) *nfix = T::NFIX;
+  if (nreact) *nreact = T::NREACT;
+  if (lu_nonzero) *lu_nonzero = T::LU_NONZERO;
+  return GC_KPP_OK;
+}
+
+const char* gc_kpp_last_error(void) { return g_last_error.c_str(); }
+
+int gc_kpp_ctx_create(gc_kpp_ctx** out, int device) {
+  if (!out) return fail(GC_KPP_EINVAL, "ctx pointer is NULL");
+  *out = nullptr;
+  GC_CUDA(cudaSetDevice(device));
+  gc_kpp_ctx* c = new gc_kpp_ctx();
+  c->device = device;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "cudaGetDeviceProperties");
+  }
+  c->nsm = prop.multiProcessorCount;
+  MechDev& m = c->mech;
+  m.nvar = T::NVAR; m.nfix = T::NFIX; m.nreact = T::NREACT; m.nspec = T::NSPEC;
+  m.lu_nonzero = T::LU_NONZERO; m.nb = T::NB; m.lit0 = T::LIT0;
+#define UP(field, arr)                                                         \
+  e = upload(T::arr, sizeof(T::arr) / sizeof(T::arr[0]), &m.field, c->owned); \
+  if (e != cudaSuccess) { gc_kpp_ctx_destroy(c); return cuda_fail(e, "upload " #arr); }
+  UP(prod_start, prod_start) UP(prod_fac, prod_fac) UP(p_start, p_start) UP(p_term, p_term)
+  UP(d_start, d_start) UP(d_term, d_term) UP(j_start, j_start) UP(j_term, j_term)
+  UP(lu_crow, lu_crow) UP(lu_diag, lu_diag) UP(lu_icol, lu_icol) UP(lrow_start, lrow_start)
+  UP(lop_kk, lop_kk) UP(lop_dj, lop_dj) UP(lop_u, lop_u) UP(uop, uop) UP(lit, lit)
+#undef UP
+  gcrates::RatesDev& rp = c->rates;
+  rp.nreact = T::NREACT;
+  rp.nmet = RT::NMET;
+  e = upload(RT::code, sizeof(RT::code) / sizeof(int), &rp.code, c->owned);
+  if (e == cudaSuccess) e = upload(RT::start, sizeof(RT::start) / sizeof(int), &rp.start, c->owned);
+  if (e == cudaSuccess) e = upload(RT::consts, sizeof(RT::consts) / sizeof(double), &rp.consts, c->owned);
+  if (e == cudaSuccess) e = upload(RT::law_nargs, sizeof(RT::law_nargs) / sizeof(int), &rp.law_nargs, c->owned);
+  if (e != cudaSuccess) {
+    gc_kpp_ctx_destroy(c);
+    return cuda_fail(e, "upload rate program");
+  }
+  c->lay = make_layout();
+  *out = c;
+  return GC_KPP_OK;
+}
+
+int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
+  if (!c) return GC_KPP_OK;
+  cudaSetDevice(c->device);
+  for (void* p : c->owned) cudaFree(p);
+  DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
+                    &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph};
+  for (DevBuf* b : bufs) b->release();
+  delete c;
+  return GC_KPP_OK;
+}
+
+int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  switch (key) {
+    case GC_KPP_OPT_ARITH:
+      if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "arith must be 0 or 1");
+      c->arith = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_SCHEDULE:
+      if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "schedule must be 0 or 1");
+      c->schedule = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_BLOCK:
+      if (v == 0) v = 128;
+      if (v < 32 || v > 256 || v % 32) return fail(GC_KPP_EINVAL, "block must be a multiple of 32 in [32,256]");
+      c->block = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_BLOCKS_PER_SM:
+      if (v < 0 || v > 64) return fail(GC_KPP_EINVAL, "blocks per SM out of range");
+      c->blocks_per_sm = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_MAX_SLOTS:
+      if (v < 0) return fail(GC_KPP_EINVAL, "max slots must be >= 0");
+      c->max_slots = v;
+      return GC_KPP_OK;
+    default:
+      return fail(GC_KPP_EINVAL, "unknown option key");
+  }
+}
+
+int gc_kpp_integrate_batch(gc_kpp_ctx* c, int ncell, double tin, double tout, double* cc, long long ldc,
+                           const double* rconst, long long ldr, const double* atol, const double* rtol,
+                           const int* icntrl_u, const double* rcntrl_u, const double* hstart, int* istatus,
+                           double* rstatus, long long ldo, int* ierr, int mem, void* stream) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
+  if (ncell == 0) return GC_KPP_OK;
+  if (!cc || !rconst || !atol || !rtol || !ierr) return fail(GC_KPP_EINVAL, "required array is NULL");
+  if (ldc < ncell || ldr < ncell || ((istatus || rstatus) && ldo < ncell))
+    return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
+  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  GC_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+  // INTEGRATE: zero, default ICNTRL(15)=5, then merge nonzero / positive
+  // user entries (gckpp_Integrator.F90:101-117).
+  int icntrl[20] = {0};
+  double rcntrl[20] = {0.0};
+  icntrl[14] = 5;
+  if (icntrl_u)
+    for (int i = 0; i < 20; ++i)
+      if (icntrl_u[i] != 0) icntrl[i] = icntrl_u[i];
+  if (rcntrl_u)
+    for (int i = 0; i < 20; ++i)
+      if (rcntrl_u[i] > 0) rcntrl[i] = rcntrl_u[i];
+  // Integrator_Update_Options (gckpp_Util.F90:179-205): rate or sun updates
+  // inside the integrator need the met state, which this path does not take.
+  if (icntrl[14] != -1 && (icntrl[14] & 5))
+    return fail(GC_KPP_EUNSUPPORTED, "ICNTRL(15) requests Update_RCONST/Update_SUN inside the integrator");
+  if (icntrl[11] == 1) return fail(GC_KPP_EUNSUPPORTED, "auto-reduce (ICNTRL(12)=1) is not implemented");
+
+  // Rosenbrock option resolution (:333-477).  A failing check gives the
+  // reference's per-cell IERR for every cell.
+  int code = 0;
+  RosMethod meth;
+  const double roundoff = DBL_EPSILON;  // WLAMCH('E') = 2**-52
+  const bool vector_tol = icntrl[1] == 0;
+  if (!method_table(icntrl[2], meth)) code = -2;
+  int max_steps = 200000;
+  if (!code) {
+    if (icntrl[3] > 0) max_steps = icntrl[3];
+    else if (icntrl[3] < 0) code = -1;
+  }
+  const double hmin = rcntrl[0];
+  const double span = std::fabs(tout - tin);
+  const double hmax = rcntrl[1] == 0.0 ? span : std::min(std::fabs(rcntrl[1]), span);
+  const double hstart_default = rcntrl[2] == 0.0 ? std::max(hmin, 1.0e-5) : std::min(std::fabs(rcntrl[2]), span);
+  const double facmin = rcntrl[3] == 0.0 ? 0.2 : rcntrl[3];
+  const double facmax = rcntrl[4] == 0.0 ? 6.0 : rcntrl[4];
+  const double facrej = rcntrl[5] == 0.0 ? 0.1 : rcntrl[5];
+  const double facsafe = rcntrl[6] == 0.0 ? 0.9 : rcntrl[6];
+
+  const size_t nvar = T::NVAR, nspec = T::NSPEC, nreact = T::NREACT;
+  const size_t ntol = vector_tol ? nvar : 1;
+  // tolerance check needs host values
+  if (!code) {
+    std::vector<double> at(ntol), rt(ntol);
+    if (mem == GC_KPP_MEM_HOST) {
+      std::memcpy(at.data(), atol, ntol * sizeof(double));
+      std::memcpy(rt.data(), rtol, ntol * sizeof(double));
+    } else {
+      GC_CUDA(cudaMemcpyAsync(at.data(), atol, ntol * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GC_CUDA(cudaMemcpyAsync(rt.data(), rtol, ntol * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GC_CUDA(cudaStreamSynchronize(s));
+    }
+    for (size_t i = 0; i < ntol; ++i)
+      if (!(at[i] > 0.0) || rt[i] <= 10.0 * roundoff || rt[i] >= 1.0) code = -5;
+  }
+
+  // device views of the caller's arrays
+  double* d_c = cc;
+  const double* d_r = rconst;
+  const double* d_at = atol;
+  const double* d_rt = rtol;
+  const double* d_hs = hstart;
+  int* d_is = istatus;
+  double* d_rs = rstatus;
+  int* d_ie = ierr;
+  long long lc = ldc, lr = ldr, lo = ldo;
+  if (mem == GC_KPP_MEM_HOST) {
+    // pack into dense device arrays with ld = ncell
+    lc = lr = lo = ncell;
+    GC_CUDA(c->h_c.ensure(nspec * ncell * sizeof(double)));
+    GC_CUDA(c->h_r.ensure(nreact * ncell * sizeof(double)));
+    GC_CUDA(c->h_at.ensure(nvar * sizeof(double)));
+    GC_CUDA(c->h_rt.ensure(nvar * sizeof(double)));
+    GC_CUDA(c->h_ie.ensure(ncell * sizeof(int)));
+    d_c = (double*)c->h_c.p;
+    d_r = (const double*)c->h_r.p;
+    d_at = (const double*)c->h_at.p;
+    d_rt = (const double*)c->h_rt.p;
+    d_ie = (int*)c->h_ie.p;
+    GC_CUDA(cudaMemcpy2DAsync(d_c, ncell * sizeof(double), cc, ldc * sizeof(double), ncell * sizeof(double),
+                              nspec, cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpy2DAsync((void*)d_r, ncell * sizeof(double), rconst, ldr * sizeof(double),
+                              ncell * sizeof(double), nreact, cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpyAsync((void*)d_at, atol, ntol * sizeof(double), cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpyAsync((void*)d_rt, rtol, ntol * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (hstart) {
+      GC_CUDA(c->h_hs.ensure(ncell * sizeof(double)));
+      d_hs = (const double*)c->h_hs.p;
+      GC_CUDA(cudaMemcpyAsync((void*)d_hs, hstart, ncell * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    if (istatus) {
+      GC_CUDA(c->h_is.ensure(20 * (size_t)ncell * sizeof(int)));
+      d_is = (int*)c->h_is.p;
+    }
+    if (rstatus) {
+      GC_CUDA(c->h_rs.ensure(20 * (size_t)ncell * sizeof(double)));
+      d_rs = (double*)c->h_rs.p;
+    }
+  }
+
+  if (code) {
+    // per-call option error: every cell gets the reference's IERR, zero stats
+    std::vector<int> e(ncell, code);
+    if (mem == GC_KPP_MEM_HOST) {
+      std::memcpy(ierr, e.data(), ncell * sizeof(int));
+      if (istatus)
+        for (int q = 0; q < 20; ++q) std::memset(istatus + q * ldo, 0, ncell * sizeof(int));
+      if (rstatus)
+        for (int q = 0; q < 20; ++q) std::memset(rstatus + q * ldo, 0, ncell * sizeof(double));
+    } else {
+      GC_CUDA(cudaMemcpyAsync(ierr, e.data(), ncell * sizeof(int), cudaMemcpyHostToDevice, s));
+      if (istatus) GC_CUDA(cudaMemset2DAsync(istatus, ldo * sizeof(int), 0, ncell * sizeof(int), 20, s));
+      if (rstatus) GC_CUDA(cudaMemset2DAsync(rstatus, ldo * sizeof(double), 0, ncell * sizeof(double), 20, s));
+      GC_CUDA(cudaStreamSynchronize(s));
+    }
+    return GC_KPP_OK;
+  }
+
+  // launch geometry and workspace
+  const int queue = c->schedule;
+  const int block = c->block;
+  long long nslot;
+  int grid;
+  if (queue) {
+    int per_sm = c->blocks_per_sm;
+    if (per_sm == 0) {
+      cudaError_t e = c->arith ? gckpp_occupancy_strict(1, block, &per_sm) : gckpp_occupancy_fast(1, block, &per_sm);
+      if (e != cudaSuccess) return cuda_fail(e, "occupancy");
+      per_sm = std::max(per_sm, 1);
+    }
+    grid = c->nsm * per_sm;
+    nslot = (long long)grid * block;
+    long long need = ((long long)ncell + block - 1) / block * block;
+    if (nslot > need) {
+      nslot = need;
+      grid = (int)(need / block);
+    }
+    if (c->max_slots > 0 && nslot > c->max_slots) {
+      grid = std::max(1LL, c->max_slots / block);
+      nslot = (long long)grid * block;
+    }
+  } else {
+    grid = (ncell + block - 1) / block;
+    nslot = (long long)grid * block;
+    if (c->max_slots > 0 && nslot > c->max_slots)
+      return fail(GC_KPP_EINVAL, "plain schedule needs one workspace slot per cell; raise MAX_SLOTS or use the queue");
+  }
+  const size_t ws_bytes = (size_t)nslot * (size_t)c->lay.total * sizeof(double);
+  GC_CUDA(c->ws.ensure(ws_bytes));
+  GC_CUDA(c->counter.ensure(sizeof(int)));
+  GC_CUDA(cudaMemsetAsync(c->counter.p, 0, sizeof(int), s));
+
+  RosParams p{};
+  p.ncell = ncell;
+  p.order = nullptr;
+  p.queue_counter = (int*)c->counter.p;
+  p.c_in = d_c;
+  p.c_out = d_c;
+  p.ldc = lc;
+  p.rconst = d_r;
+  p.ldr = lr;
+  p.hstart = d_hs;
+  p.istatus = d_is;
+  p.rstatus = d_rs;
+  p.ldo = lo;
+  p.ierr = d_ie;
+  p.atol = d_at;
+  p.rtol = d_rt;
+  p.vector_tol = vector_tol ? 1 : 0;
+  p.tstart = tin;
+  p.tend = tout;
+  p.hmin = hmin;
+  p.hmax = hmax;
+  p.hstart_default = hstart_default;
+  p.facmin = facmin;
+  p.facmax = facmax;
+  p.facrej = facrej;
+  p.facsafe = facsafe;
+  p.roundoff = roundoff;
+  p.autonomous = icntrl[0] != 0 ? 1 : 0;
+  p.max_steps = max_steps;
+  p.clamp_negative = icntrl[15] == 1 ? 1 : 0;
+  p.ws = (double*)c->ws.p;
+  p.lay = c->lay;
+  p.nslot = nslot;
+
+  cudaError_t e = c->arith ? gckpp_launch_ros_strict(queue, grid, block, c->mech, meth, p, s)
+                           : gckpp_launch_ros_fast(queue, grid, block, c->mech, meth, p, s);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(cudaMemcpy2DAsync(cc, ldc * sizeof(double), d_c, ncell * sizeof(double), ncell * sizeof(double), nvar,
+                              cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaMemcpyAsync(ierr, d_ie, ncell * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (istatus)
+      GC_CUDA(cudaMemcpy2DAsync(istatus, ldo * sizeof(int), d_is, ncell * sizeof(int), ncell * sizeof(int), 20,
+                                cudaMemcpyDeviceToHost, s));
+    if (rstatus)
+      GC_CUDA(cudaMemcpy2DAsync(rstatus, ldo * sizeof(double), d_rs, ncell * sizeof(double),
+                                ncell * sizeof(double), 20, cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+  }
+  return GC_KPP_OK;
+}
+
+int gc_kpp_update_rconst_batch(gc_kpp_ctx* c, int ncell, const double* met, long long ldm, const double* photol,
+                               long long ldp, const double* conc, long long ldc, double* rconst, long long ldr, int mem,
+                               void* stream) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
+  if (ncell == 0) return GC_KPP_OK;
+  if (!met || !photol || !conc || !rconst) return fail(GC_KPP_EINVAL, "required array is NULL");
+  if (ldm < ncell || ldp < ncell || ldc < ncell || ldr < ncell)
+    return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
+  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  GC_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  gcrates::RatesArgs a{};
+  a.ncell = ncell;
+  const size_t n = (size_t)ncell;
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(c->h_met.ensure(RT::NMET * n * sizeof(double)));
+    GC_CUDA(c->h_ph.ensure(GC_KPP_NPHOTOL * n * sizeof(double)));
+    GC_CUDA(c->h_c.ensure(T::NSPEC * n * sizeof(double)));
+    GC_CUDA(c->h_r.ensure(T::NREACT * n * sizeof(double)));
+    GC_CUDA(cudaMemcpy2DAsync(c->h_met.p, n * sizeof(double), met, ldm * sizeof(double), n * sizeof(double),
+                              RT::NMET, cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpy2DAsync(c->h_ph.p, n * sizeof(double), photol, ldp * sizeof(double), n * sizeof(double),
+                              GC_KPP_NPHOTOL, cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpy2DAsync(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
+                              T::NSPEC, cudaMemcpyHostToDevice, s));
+    a.met = (const double*)c->h_met.p;
+    a.photol = (const double*)c->h_ph.p;
+    a.c = (const double*)c->h_c.p;
+    a.rconst = (double*)c->h_r.p;
+    a.ldm = a.ldp = a.ldc = a.ldr = ncell;
+  } else {
+    a.met = met;
+    a.ldm = ldm;
+    a.photol = photol;
+    a.ldp = ldp;
+    a.c = conc;
+    a.ldc = ldc;
+    a.rconst = rconst;
+    a.ldr = ldr;
+  }
+  cudaError_t e = gcrates::launch_rates(c->rates, a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "rates kernel launch");
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(cudaMemcpy2DAsync(rconst, ldr * sizeof(double), a.rconst, n * sizeof(double), n * sizeof(double),
+                              T::NREACT, cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+  }
+  return GC_KPP_OK;
+}
+
+}  // extern "C"

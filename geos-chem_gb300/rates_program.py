@@ -1,0 +1,222 @@
+"""Lower the Update_RCONST expressions to a stack program for the GPU.
+
+Each of the 1058 rate expressions of Update_RCONST
+(KPP/fullchem/gckpp_Rates.F90:441-1502, normalised in the mechanism IR) is
+parsed with ordinary precedence and left associativity (the Fortran
+evaluation order) and emitted as postfix code for ``csrc/kpp_rates.cu``:
+every lane of a warp runs the same opcode for its own cell.
+
+Heterogeneous rate functions (those taking the HetState ``H``) are emitted as
+HETZERO: the rate kernel evaluates the zeroed HetState of the synthetic
+cells, for which each of them is a sum of Ars_L1k/CloudHet terms that vanish
+with zero aerosol area and radius and zero cloud fraction
+(KPP/fullchem/rateLawUtilFuncs.F90:77-96, :141-230).
+"""
+import os
+import re
+
+from . import mechanism
+
+OPS = ["END", "CONST", "VAR", "PHOTOL", "CONC", "ADD", "SUB", "MUL", "DIV", "NEG", "EXP", "LOG10", "CALL",
+       "HETZERO"]
+OP = {n: i for i, n in enumerate(OPS)}
+
+# Per-cell met/state fields, in the order of GC_KPP_MET_* in the C ABI.
+MET_FIELDS = ["TEMP", "NUMDEN", "H2O", "PRESS", "SRHOCl", "SRHOBr"] + \
+    ["K_MT%d" % i for i in range(6)] + ["K_CLD%d" % i for i in range(6)]
+
+# Gas-phase rate laws implemented in csrc/rate_laws.cuh: name -> (id, nargs)
+LAWS = [
+    ("GCARR_ab", 2), ("GCARR_ac", 2), ("GCARR_abc", 3), ("ARRPLUS_ade", 3), ("ARRPLUS_abde", 4),
+    ("TUNPLUS_abcde", 5), ("GC_ISO1", 7), ("GC_ISO2", 7), ("GC_EPO_a", 3), ("GC_PAN_abab", 5),
+    ("GC_PAN_acac", 5), ("GC_NIT", 6), ("GC_ALK", 6), ("GC_HO2HO2_acac", 4), ("GC_TBRANCH_1_acac", 4),
+    ("GC_RO2HO2_aca", 3), ("GC_DMSOH_acac", 4), ("GC_GLYXNO3_ac", 2), ("GC_GLYCOH_A_a", 1),
+    ("GC_GLYCOH_B_a", 1), ("GC_HACOH_A_ac", 2), ("GC_HACOH_B_ac", 2), ("GC_RO2NO_A1_ac", 2),
+    ("GC_RO2NO_B1_ac", 2), ("GC_RO2NO_A2_aca", 3), ("GC_RO2NO_B2_aca", 3), ("GCJPLEQ_acabab", 7),
+    ("GCJPLPR_aa", 3), ("GCJPLPR_aba", 4), ("GCJPLPR_abab", 5), ("GCJPLPR_abcabc", 7), ("GCJPLAC_ababac", 7),
+]
+LAW_ID = {n: (i, k) for i, (n, k) in enumerate(LAWS)}
+
+_TOKEN = re.compile(r"\s*(?:(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|\d+(?:[eE][+-]?\d+)?)|"
+                    r"([A-Za-z_][A-Za-z_0-9]*)|(.))")
+
+
+def _tokens(s):
+    out = []
+    pos = 0
+    while pos < len(s):
+        m = _TOKEN.match(s, pos)
+        if m.group(1):
+            out.append(("num", m.group(1)))
+        elif m.group(2):
+            out.append(("id", m.group(2)))
+        elif m.group(3).strip():
+            out.append(("op", m.group(3)))
+        pos = m.end()
+    return out
+
+
+class _Parser:
+    def __init__(self, text, consts):
+        self.t = _tokens(text)
+        self.i = 0
+        self.code = []
+        self.consts = consts
+        self.het = 0
+
+    def peek(self):
+        return self.t[self.i] if self.i < len(self.t) else (None, None)
+
+    def take(self, val=None):
+        tok = self.t[self.i]
+        if val is not None and tok[1] != val:
+            raise ValueError("expected %r got %r" % (val, tok))
+        self.i += 1
+        return tok
+
+    def const(self, v):
+        if v not in self.consts:
+            self.consts[v] = len(self.consts)
+        self.code += [OP["CONST"], self.consts[v]]
+
+    def expr(self):
+        self.term()
+        while self.peek()[1] in ("+", "-"):
+            op = self.take()[1]
+            self.term()
+            self.code.append(OP["ADD"] if op == "+" else OP["SUB"])
+
+    def term(self):
+        self.unary()
+        while self.peek()[1] in ("*", "/"):
+            op = self.take()[1]
+            self.unary()
+            self.code.append(OP["MUL"] if op == "*" else OP["DIV"])
+
+    def unary(self):
+        if self.peek()[1] == "-":
+            self.take()
+            self.unary()
+            self.code.append(OP["NEG"])
+        elif self.peek()[1] == "+":
+            self.take()
+            self.unary()
+        else:
+            self.atom()
+
+    def _args(self):
+        self.take("(")
+        n = 0
+        if self.peek()[1] != ")":
+            while True:
+                self.expr()
+                n += 1
+                if self.peek()[1] == ",":
+                    self.take()
+                    continue
+                break
+        self.take(")")
+        return n
+
+    def _skip_call(self):
+        depth = 0
+        while True:
+            tok = self.take()
+            if tok[1] == "(":
+                depth += 1
+            elif tok[1] == ")":
+                depth -= 1
+                if depth == 0:
+                    return
+
+    def atom(self):
+        kind, val = self.peek()
+        if kind == "num":
+            self.take()
+            self.const(float(val))
+        elif kind == "op" and val == "(":
+            self.take()
+            self.expr()
+            self.take(")")
+        elif kind == "id":
+            self.take()
+            nxt = self.peek()[1]
+            if nxt == "[":
+                self.take()
+                idx = int(self.take()[1])
+                self.take("]")
+                if val == "PHOTOL":
+                    self.code += [OP["PHOTOL"], idx]
+                elif val == "K_MT":
+                    self.code += [OP["VAR"], MET_FIELDS.index("K_MT%d" % idx)]
+                elif val == "K_CLD":
+                    self.code += [OP["VAR"], MET_FIELDS.index("K_CLD%d" % idx)]
+                elif val == "C":
+                    self.code += [OP["CONC"], idx]
+                else:
+                    raise ValueError("array %s" % val)
+            elif nxt == "(":
+                if val in ("exp", "log10"):
+                    n = self._args()
+                    assert n == 1
+                    self.code.append(OP["EXP"] if val == "exp" else OP["LOG10"])
+                elif val in LAW_ID:
+                    lid, k = LAW_ID[val]
+                    n = self._args()
+                    assert n == k, (val, n, k)
+                    self.code += [OP["CALL"], lid]
+                else:
+                    self._skip_call()
+                    self.code.append(OP["HETZERO"])
+                    self.het += 1
+            elif val in MET_FIELDS:
+                self.code += [OP["VAR"], MET_FIELDS.index(val)]
+            else:
+                raise ValueError("unknown identifier %s" % val)
+        else:
+            raise ValueError("unexpected %r" % (val,))
+
+
+def build_program(ir=None):
+    ir = ir or mechanism.load_ir()
+    consts = {}
+    code = []
+    start = [0]
+    nhet = 0
+    for e in ir["rconst"]:
+        p = _Parser(e, consts)
+        p.expr()
+        assert p.i == len(p.t), e
+        code += p.code + [OP["END"]]
+        start.append(len(code))
+        nhet += p.het
+    pool = [0.0] * len(consts)
+    for v, i in consts.items():
+        pool[i] = v
+    return {"code": code, "start": start, "consts": pool, "nhet": nhet}
+
+
+def emit_c(prog):
+    lines = ["// Generated by gcchem.rates_program from mechanism/fullchem.json. Do not edit.",
+             "#pragma once",
+             "namespace gcrates_tables {",
+             "constexpr int NMET = %d;" % len(MET_FIELDS),
+             "static const int code[%d] = {%s};" % (len(prog["code"]), ",".join(map(str, prog["code"]))),
+             "static const int start[%d] = {%s};" % (len(prog["start"]), ",".join(map(str, prog["start"]))),
+             "static const double consts[%d] = {%s};" % (len(prog["consts"]),
+                                                       ",".join(float(v).hex() for v in prog["consts"])),
+             "static const int law_nargs[%d] = {%s};" % (len(LAWS), ",".join(str(k) for _, k in LAWS)),
+             "}  // namespace gcrates_tables"]
+    return "\n".join(lines) + "\n"
+
+
+def write_generated(outdir, ir=None):
+    prog = build_program(ir)
+    os.makedirs(outdir, exist_ok=True)
+    path = os.path.join(outdir, "rates_program.inc")
+    text = emit_c(prog)
+    old = open(path).read() if os.path.exists(path) else None
+    if old != text:
+        with open(path, "w") as fh:
+            fh.write(text)
+    return path

@@ -1,0 +1,201 @@
+"""Device tables for the table-driven mechanism engine.
+
+The mechanism IR (``mechanism/fullchem.json``) is lowered here to flat integer
+tables that the CUDA engine (``csrc/kpp_mech.cuh``) walks with warp-uniform
+loops: every lane of a warp runs the same table entry for its own cell, so the
+table reads are broadcasts and the per-cell data reads are coalesced.
+
+Operand codes (int32) used by products:
+
+    [0, NVAR)                       V(i)    variable species (current point)
+    [NVAR, NVAR+NFIX)               F(i)    fixed species
+    [NVAR+NFIX, NVAR+NFIX+NREACT)   RCT(r)  rate constants
+    [LIT0, ...)                     literal constant LIT[code-LIT0]
+
+Products: ``prod_start``/``prod_fac``; products [0,NREACT) are the reaction
+rates A(r) of Fun_SPLIT (KPP/fullchem/gckpp_Function.F90:2172-2230ff), products
+[NREACT, NREACT+NB) are the Jacobian partials B(b) of Jac_SP
+(KPP/fullchem/gckpp_Jacobian.F90:48ff).  Every D_VAR term of Fun_SPLIT is the
+same product as one B(b); the tables record which.
+
+Signed coefficient terms (P_VAR over A, JVS over B, D_VAR over B products)
+are packed as ``sign<<31 | coef<<20 | index`` with ``coef == 0x7ff`` meaning
+no coefficient (a bare reference).
+
+The LU program follows KppDecomp (KPP/fullchem/gckpp_LinearAlgebra.F90:46-83):
+for each row k, for each L entry (k,j) in column order, a = W(j)/pivot(j) and
+W(c) -= a*U(j,c) for the U part of row j.  W is row k of the matrix itself
+(KPP's dense work vector only ever holds row k's pattern).  ``lop`` lists the
+L entries (position of (k,j), position of diag j, start of its U ops);
+``uop`` packs (position of (k,c)) << 16 | (position of (j,c)).
+"""
+import os
+import struct
+
+import numpy as np
+
+from . import mechanism
+
+NOCOEF = 0x7FF
+
+
+def _hexfloat(x):
+    return float(x).hex()
+
+
+class Tables:
+    def __init__(self, ir):
+        d = ir["dims"]
+        self.nvar, self.nfix, self.nreact = d["nvar"], d["nfix"], d["nreact"]
+        self.nspec = d["nspec"]
+        self.lu_nonzero = d["lu_nonzero"]
+        self.nb = len(ir["jac"]["B"])
+        self.lit0 = self.nvar + self.nfix + self.nreact
+        self.literals = []
+        self._lit_index = {}
+
+        def lit(tok):
+            v = float(tok.replace("d", "e").replace("D", "e"))
+            key = struct.pack("<d", v)
+            if key not in self._lit_index:
+                self._lit_index[key] = len(self.literals)
+                self.literals.append(v)
+            return self._lit_index[key]
+
+        def fac(tok):
+            kind, rest = tok[0], tok[1:]
+            if kind == "V":
+                return int(rest)
+            if kind == "F":
+                return self.nvar + int(rest)
+            if kind == "R":
+                return self.nvar + self.nfix + int(rest)
+            return self.lit0 + lit(tok)
+
+        prods = list(ir["fun"]["A"]) + [b if b is not None else [] for b in ir["jac"]["B"]]
+        self.prod_start = np.zeros(len(prods) + 1, np.int32)
+        facs = []
+        for i, p in enumerate(prods):
+            facs += [fac(t) for t in p]
+            self.prod_start[i + 1] = len(facs)
+        self.prod_fac = np.array(facs, np.int32)
+
+        def coef_terms(lists):
+            start = np.zeros(len(lists) + 1, np.int32)
+            out = []
+            for i, terms in enumerate(lists):
+                for sign, coef, idx in terms:
+                    c = NOCOEF if coef is None else lit(coef)
+                    assert (coef is None or c < NOCOEF) and idx < (1 << 20)
+                    out.append(((1 if sign == "-" else 0) << 31) | (c << 20) | idx)
+                start[i + 1] = len(out)
+            return start, np.array(out, np.uint32).view(np.int32)
+
+        self.p_start, self.p_term = coef_terms(ir["fun"]["P"])
+        self.j_start, self.j_term = coef_terms(ir["jac"]["JVS"])
+
+        bmap = {tuple(b): i for i, b in enumerate(ir["jac"]["B"]) if b is not None}
+        dl = []
+        for terms in ir["fun"]["D"]:
+            dl.append([[s, None, bmap[tuple(f)]] for s, f in terms])
+        self.d_start, self.d_term = coef_terms(dl)
+
+        lu = ir["lu"]
+        crow, diag, icol = lu["crow"], lu["diag"], lu["icol"]
+        self.crow = np.array(crow, np.int32)
+        self.diag = np.array(diag, np.int32)
+        self.icol = np.array(icol, np.int32)
+        self.irow = np.array(lu["irow"], np.int32)
+        lrow_start = [0]
+        lop = []
+        uop = []
+        for k in range(self.nvar):
+            pos = {icol[kk]: kk for kk in range(crow[k], crow[k + 1])}
+            for kk in range(crow[k], diag[k]):
+                j = icol[kk]
+                lop.append((kk, diag[j], len(uop)))
+                for jj in range(diag[j] + 1, crow[j + 1]):
+                    uop.append((pos[icol[jj]] << 16) | jj)
+            lrow_start.append(len(lop))
+        self.lrow_start = np.array(lrow_start, np.int32)
+        self.lop_kk = np.array([x[0] for x in lop], np.int32)
+        self.lop_dj = np.array([x[1] for x in lop], np.int32)
+        self.lop_u = np.array([x[2] for x in lop] + [len(uop)], np.int32)
+        self.uop = np.array(uop, np.uint32).view(np.int32)
+        assert self.lu_nonzero < (1 << 16)
+        self.lit = np.array(self.literals, np.float64)
+
+    # flop bookkeeping used by the roofline accounting (FP64 operations per
+    # call, counting a multiply-add as 2, a division as 1, in STRICT form)
+    def flops(self):
+        nfac_a = int(self.prod_start[self.nreact])
+        mul_a = nfac_a - self.nreact
+        mul_b = int(self.prod_start[-1] - self.prod_start[self.nreact]) - sum(
+            1 for i in range(self.nreact, len(self.prod_start) - 1) if self.prod_start[i + 1] > self.prod_start[i])
+        pt = self.p_term.view(np.uint32)
+        jt = self.j_term.view(np.uint32)
+        coefp = int(np.sum(((pt >> 20) & 0x7FF) != NOCOEF))
+        coefj = int(np.sum(((jt >> 20) & 0x7FF) != NOCOEF))
+        addp = len(pt) - np.count_nonzero(np.diff(self.p_start) > 0)
+        addj = len(jt) - np.count_nonzero(np.diff(self.j_start) > 0)
+        dfac = 0
+        for t in self.d_term.view(np.uint32):
+            b = int(t & 0xFFFFF) + self.nreact
+            dfac += int(self.prod_start[b + 1] - self.prod_start[b]) - 1
+        addd = len(self.d_term) - np.count_nonzero(np.diff(self.d_start) > 0)
+        fun = mul_a + coefp + int(addp) + dfac + int(addd) + 2 * self.nvar
+        jac = mul_b + coefj + int(addj)
+        lu_fma = len(self.uop)
+        decomp = 2 * lu_fma + len(self.lop_kk) + self.nvar  # FMA + L divisions + diag shift
+        solve = 2 * int(sum((self.crow[i + 1] - self.crow[i] - 1) for i in range(self.nvar))) + self.nvar
+        return {"fun": int(fun), "jac": int(jac), "decomp": int(decomp), "solve": int(solve)}
+
+    def emit_c(self):
+        """C source defining the tables (included by the CUDA library)."""
+        out = ["// Generated by gcchem.tables from mechanism/fullchem.json. Do not edit.",
+               "#pragma once",
+               "namespace gcmech_tables {",
+               "constexpr int NVAR = %d, NFIX = %d, NSPEC = %d, NREACT = %d, LU_NONZERO = %d, NB = %d, LIT0 = %d;"
+               % (self.nvar, self.nfix, self.nspec, self.nreact, self.lu_nonzero, self.nb, self.lit0),
+               "constexpr unsigned NOCOEF = 0x%x;" % NOCOEF]
+
+        def arr(name, a, ctype="int"):
+            vals = ",".join(str(int(v)) for v in a)
+            out.append("static const %s %s[%d] = {%s};" % (ctype, name, len(a), vals))
+
+        arr("prod_start", self.prod_start)
+        arr("prod_fac", self.prod_fac)
+        arr("p_start", self.p_start)
+        arr("p_term", self.p_term.view(np.uint32), "unsigned")
+        arr("d_start", self.d_start)
+        arr("d_term", self.d_term.view(np.uint32), "unsigned")
+        arr("j_start", self.j_start)
+        arr("j_term", self.j_term.view(np.uint32), "unsigned")
+        arr("lu_crow", self.crow)
+        arr("lu_diag", self.diag)
+        arr("lu_icol", self.icol)
+        arr("lrow_start", self.lrow_start)
+        arr("lop_kk", self.lop_kk)
+        arr("lop_dj", self.lop_dj)
+        arr("lop_u", self.lop_u)
+        arr("uop", self.uop.view(np.uint32), "unsigned")
+        out.append("static const double lit[%d] = {%s};" % (
+            len(self.literals), ",".join(_hexfloat(v) for v in self.literals)))
+        out.append("}  // namespace gcmech_tables")
+        return "\n".join(out) + "\n"
+
+
+def build_tables(ir=None):
+    return Tables(ir or mechanism.load_ir())
+
+
+def write_generated(outdir, ir=None):
+    t = build_tables(ir)
+    os.makedirs(outdir, exist_ok=True)
+    path = os.path.join(outdir, "mech_tables.inc")
+    text = t.emit_c()
+    old = open(path).read() if os.path.exists(path) else None
+    if old != text:
+        with open(path, "w") as fh:
+            fh.write(text)
+    return path

@@ -1,0 +1,138 @@
+/*
+ * gckpp_gb300.h -- C ABI of the GB300 KPP fullchem chemistry solve.
+ *
+ * A drop-in for the per-cell chemistry loop of GEOS-Chem's Do_FullChem
+ * (GeosCore/fullchem_mod.F90:528-1551).  Where the reference calls, once per
+ * grid cell and OpenMP thread,
+ *
+ *     CALL Update_RCONST()                                  ! fullchem_mod.F90:953
+ *     CALL Integrate( 0.0_dp, DT, ICNTRL, RCNTRL,
+ *                     ISTATUS, RSTATE, IERR )               ! fullchem_mod.F90:1033
+ *
+ * on thread-private module globals (C, RCONST, ATOL/RTOL: KPP/fullchem/
+ * gckpp_Global.F90:47-128), a caller of this library hands over a batch of
+ * cells at once.  Every per-cell array is cell-interleaved ("structure of
+ * arrays"): element k of cell i is at X[k*ld + i] with ld >= ncell, which is
+ * what a Fortran caller gets from an array declared X(ld, K) and indexed
+ * X(cell, k).  Species, reaction and ISTATUS/RSTATUS indices are 0-based
+ * here; index k here is index k+1 in the reference's Fortran.
+ *
+ * All entry points are plain C, take plain pointers and sizes, never abort
+ * and never print.  They return 0 on success or a negative GC_KPP_E* code;
+ * gc_kpp_last_error() describes the last failure of the calling thread.
+ * Per-cell integrator errors are not call failures: they are reported in
+ * ierr[] with the reference's IERR codes (1 = success, -1 ... -8 as in
+ * ros_ErrorMsg, KPP/fullchem/gckpp_Integrator.F90:538-575).
+ */
+#ifndef GCKPP_GB300_H
+#define GCKPP_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* call status codes */
+#define GC_KPP_OK 0
+#define GC_KPP_EINVAL (-101)      /* bad argument */
+#define GC_KPP_ECUDA (-102)       /* CUDA runtime error */
+#define GC_KPP_ENOMEM (-103)      /* device allocation failed */
+#define GC_KPP_EUNSUPPORTED (-104) /* option outside the implemented path */
+
+/* where the caller's arrays live */
+#define GC_KPP_MEM_HOST 0
+#define GC_KPP_MEM_DEVICE 1
+
+/* gc_kpp_ctx_set_option keys */
+#define GC_KPP_OPT_ARITH 1        /* 0 = fast (FMA, reciprocal pivots), 1 = strict (reference order, no FMA) */
+#define GC_KPP_OPT_SCHEDULE 2     /* 0 = plain (thread per cell), 1 = persistent work queue */
+#define GC_KPP_OPT_BLOCK 3        /* threads per block (multiple of 32), 0 = default */
+#define GC_KPP_OPT_BLOCKS_PER_SM 4 /* queue schedule: resident blocks per SM, 0 = default */
+#define GC_KPP_OPT_MAX_SLOTS 5    /* cap on workspace slots (cells in flight), 0 = no cap */
+
+/* Per-cell meteorology/state fields of gc_kpp_update_rconst_batch (rows of
+ * `met`), the thread-private globals that Set_Kpp_GridBox_Values and the
+ * sulfur/cloud routines fill before Update_RCONST
+ * (GeosCore/fullchem_mod.F90:2089-2167, KPP/fullchem/commonIncludeVars.H). */
+#define GC_KPP_MET_TEMP 0      /* TEMP [K] */
+#define GC_KPP_MET_NUMDEN 1    /* NUMDEN, air number density [molec/cm3] */
+#define GC_KPP_MET_H2O 2       /* H2O [molec/cm3] */
+#define GC_KPP_MET_PRESS 3     /* PRESS [hPa] */
+#define GC_KPP_MET_SRHOCL 4    /* SRHOCl [cm3/molec/s] */
+#define GC_KPP_MET_SRHOBR 5    /* SRHOBr [cm3/molec/s] */
+#define GC_KPP_MET_K_MT 6      /* K_MT(1:6), rows 6..11 */
+#define GC_KPP_MET_K_CLD 12    /* K_CLD(1:6), rows 12..17 */
+#define GC_KPP_NMET 18
+#define GC_KPP_NPHOTOL 200     /* PHOTOL(1:200) rows */
+
+typedef struct gc_kpp_ctx gc_kpp_ctx;
+
+/* Mechanism dimensions (NSPEC, NVAR, NFIX, NREACT, LU_NONZERO of
+ * KPP/fullchem/gckpp_Parameters.F90:34-54).  Any pointer may be NULL. */
+int gc_kpp_mechanism_dims(int* nspec, int* nvar, int* nfix, int* nreact, int* lu_nonzero);
+
+/* Create a solver context on CUDA device `device`: uploads the mechanism
+ * tables.  Workspace is allocated on first use and grown as needed.
+ * Replaces nothing in the reference (its state is module globals). */
+int gc_kpp_ctx_create(gc_kpp_ctx** ctx, int device);
+int gc_kpp_ctx_destroy(gc_kpp_ctx* ctx);
+int gc_kpp_ctx_set_option(gc_kpp_ctx* ctx, int key, long long value);
+
+/* Message for the last failed call on this thread ("" if none). */
+const char* gc_kpp_last_error(void);
+
+/* Batched INTEGRATE (KPP/fullchem/gckpp_Integrator.F90:80-162) over ncell
+ * independent cells, from TIN to TOUT.
+ *
+ *   c        [NSPEC][ldc]  in/out  concentrations (molec/cm3); variable
+ *                                  species are integrated, fixed ones read
+ *   rconst   [NREACT][ldr] in      rate constants from Update_RCONST
+ *   atol,rtol [NVAR]       in      tolerances (ICNTRL(2)=0) or [1] (scalar)
+ *   icntrl   [20], rcntrl [20]     as ICNTRL_U/RCNTRL_U of INTEGRATE; zero
+ *                                  ICNTRL entries and non-positive RCNTRL
+ *                                  entries keep the defaults (:112-117)
+ *   hstart   [ncell] or NULL       per-cell RCNTRL(3) (the KPPHvalue chain,
+ *                                  fullchem_AutoReduceFuncs.F90:287)
+ *   istatus  [20][ldo] out or NULL ISTATUS(1:8) counters, rest zero
+ *   rstatus  [20][ldo] out or NULL RSTATUS(1:3) = Texit, Hexit, Hnew
+ *   ierr     [ncell]   out         IERR per cell
+ *   mem      GC_KPP_MEM_HOST or GC_KPP_MEM_DEVICE for all arrays above
+ *   stream   cudaStream_t (NULL = default stream); with device memory the
+ *            call is asynchronous on that stream, with host memory it
+ *            returns after the results are copied back.
+ *
+ * Supported: Rosenbrock methods ICNTRL(3) = 0..6, autonomous or not,
+ * vector or scalar tolerances, ICNTRL(4) step cap, ICNTRL(16) clamping,
+ * RCNTRL(1:7).  ICNTRL(15) must disable in-integrator rate updates (-1, 0
+ * after merging, or 2) and ICNTRL(12) (auto-reduce) must be off; otherwise
+ * GC_KPP_EUNSUPPORTED. */
+int gc_kpp_integrate_batch(gc_kpp_ctx* ctx, int ncell, double tin, double tout,
+                           double* c, long long ldc,
+                           const double* rconst, long long ldr,
+                           const double* atol, const double* rtol,
+                           const int* icntrl, const double* rcntrl,
+                           const double* hstart,
+                           int* istatus, double* rstatus, long long ldo,
+                           int* ierr, int mem, void* stream);
+
+/* Batched Update_RCONST (KPP/fullchem/gckpp_Rates.F90:408-1503): the 1058
+ * rate constants of each cell from its met state.
+ *
+ *   met     [GC_KPP_NMET][ldm]    in   fields GC_KPP_MET_*
+ *   photol  [GC_KPP_NPHOTOL][ldp] in   J-values PHOTOL(1:200) [1/s]
+ *   c       [NSPEC][ldc]          in   concentrations (read by uptake rates)
+ *   rconst  [NREACT][ldr]         out  RCONST
+ *
+ * Gas-phase, photolysis, K_MT/K_CLD and constant rates are evaluated as the
+ * reference does.  Heterogeneous rates are evaluated for a zeroed HetState
+ * (no aerosol surface, no cloud), for which every one of them is 0. */
+int gc_kpp_update_rconst_batch(gc_kpp_ctx* ctx, int ncell, const double* met, long long ldm,
+                               const double* photol, long long ldp, const double* c, long long ldc,
+                               double* rconst, long long ldr, int mem, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GCKPP_GB300_H */

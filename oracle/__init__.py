@@ -1,0 +1,122 @@
+"""CPU oracle of the KPP fullchem solve -- TEST INFRASTRUCTURE.
+
+ctypes binding of the C restatement in this directory (kpp_oracle.c and the
+generated mechanism/rate code).  Imported only by the tests, by the smoke
+check and by the CPU-baseline leg of bench.py, always as the checker, never
+as the thing measured or shipped.
+
+Two builds of the same sources:
+  "strict"  -O2 -ffp-contract=off  (reference arithmetic, parity oracle)
+  "fast"    -O3                    (timed CPU baseline)
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_libs = {}
+
+
+def build(verbose=False):
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("_oracle_build", os.path.join(HERE, "build_oracle.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(verbose=verbose)
+
+
+def load(variant="strict"):
+    if variant in _libs:
+        return _libs[variant]
+    path = os.path.join(HERE, "_build", "liboracle_%s.so" % variant)
+    if not os.path.exists(path):
+        build()
+    lib = ctypes.CDLL(path)
+    vp, i32, i64, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
+    lib.oracle_integrate_batch.argtypes = [i32, f64, f64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64, vp, i32]
+    lib.oracle_update_rconst_batch.argtypes = [i32, vp, i64, vp, i64, vp, i64, vp, i64]
+    lib.oracle_fun_split.argtypes = [vp, vp, vp, vp]
+    lib.oracle_jac_sp.argtypes = [vp, vp, vp, vp]
+    lib.oracle_kpp_solve.argtypes = [vp, vp]
+    lib.oracle_kpp_decomp.argtypes = [vp]
+    lib.oracle_kpp_decomp.restype = i32
+    lib.oracle_max_threads.restype = i32
+    _libs[variant] = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def integrate(c, rconst, atol, rtol, tin, tout, icntrl=None, rcntrl=None, hstart=None, variant="strict",
+              nthreads=0):
+    """Batched INTEGRATE on the CPU.  c [NSPEC, n] (copied), rconst [NREACT, n].
+    Returns (c_out, istatus [20, n], rstatus [20, n], ierr [n])."""
+    lib = load(variant)
+    c = np.array(c, dtype=np.float64, order="C", copy=True)
+    rconst = _c(rconst, np.float64)
+    n = c.shape[1]
+    ist = np.zeros((20, n), np.int32)
+    rst = np.zeros((20, n), np.float64)
+    ierr = np.zeros(n, np.int32)
+    ic = _c(icntrl, np.int32) if icntrl is not None else None
+    rc = _c(rcntrl, np.float64) if rcntrl is not None else None
+    hs = _c(hstart, np.float64) if hstart is not None else None
+    lib.oracle_integrate_batch(n, float(tin), float(tout), _p(c), n, _p(rconst), n, _p(_c(atol, np.float64)),
+                               _p(_c(rtol, np.float64)), _p(ic), _p(rc), _p(hs), _p(ist), _p(rst), n, _p(ierr),
+                               int(nthreads))
+    return c, ist, rst, ierr
+
+
+def update_rconst(met, photol, c, variant="strict"):
+    lib = load(variant)
+    met = _c(met, np.float64)
+    photol = _c(photol, np.float64)
+    c = _c(c, np.float64)
+    n = met.shape[1]
+    nreact = 1058
+    out = np.zeros((nreact, n), np.float64)
+    lib.oracle_update_rconst_batch(n, _p(met), n, _p(photol), n, _p(c), n, _p(out), n)
+    return out
+
+
+def fun_split(v, f, rct):
+    lib = load("strict")
+    v, f, rct = _c(v, np.float64), _c(f, np.float64), _c(rct, np.float64)
+    out = np.zeros_like(v)
+    lib.oracle_fun_split(_p(v), _p(f), _p(rct), _p(out))
+    return out
+
+
+def jac_sp(v, f, rct, lu_nonzero=5683):
+    lib = load("strict")
+    v, f, rct = _c(v, np.float64), _c(f, np.float64), _c(rct, np.float64)
+    out = np.zeros(lu_nonzero, np.float64)
+    lib.oracle_jac_sp(_p(v), _p(f), _p(rct), _p(out))
+    return out
+
+
+def decomp(jvs):
+    lib = load("strict")
+    jvs = np.array(jvs, dtype=np.float64, copy=True)
+    ier = lib.oracle_kpp_decomp(_p(jvs))
+    return jvs, ier
+
+
+def solve(jvs, x):
+    lib = load("strict")
+    jvs = _c(jvs, np.float64)
+    x = np.array(x, dtype=np.float64, copy=True)
+    lib.oracle_kpp_solve(_p(jvs), _p(x))
+    return x
+
+
+def max_threads(variant="fast"):
+    return load(variant).oracle_max_threads()
