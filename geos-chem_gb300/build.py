@@ -40,6 +40,7 @@ def _units():
         (k, "kpp_kernels_strict.o", ["-DGCKPP_STRICT=1", "-fmad=false"]),
         (k, "kpp_kernels_fast.o", ["-DGCKPP_STRICT=0"]),
         (os.path.join(CSRC, "kpp_rates.cu"), "kpp_rates.o", []),
+        (os.path.join(CSRC, "kpp_util.cu"), "kpp_util.o", []),
         (os.path.join(CSRC, "gckpp_capi.cu"), "gckpp_capi.o", []),
     ]
 
@@ -82,7 +83,19 @@ def build(verbose=False, force=False):
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), r.stdout.decode()))
+    probe = probe_path()
+    src = os.path.join(CSRC, "fp64_probe.cu")
+    if force or not os.path.exists(probe) or os.path.getmtime(src) > os.path.getmtime(probe):
+        cmd = [exe] + NVCC_FLAGS + ["-shared", "-cudart", "shared", src, "-o", probe]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        if r.returncode != 0:
+            raise RuntimeError("probe build failed: %s\n%s" % (" ".join(cmd), r.stdout.decode()))
     return lib
+
+
+def probe_path():
+    """FP64 throughput probe library (the roofline denominator), not part of the C ABI."""
+    return os.path.join(LIBDIR, "libgckpp_probe.so")
 
 
 if __name__ == "__main__":

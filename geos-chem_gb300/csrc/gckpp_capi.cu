@@ -19,6 +19,7 @@
 #include "_gen/rates_program.inc"
 #include "kpp_rates.h"
 #include "kpp_launch.h"
+#include "kpp_util.h"
 #include "kpp_rosenbrock.cuh"
 
 using namespace gckpp;
@@ -265,6 +266,12 @@ struct gc_kpp_ctx {
   DevBuf ws, counter;
   DevBuf h_c, h_r, h_at, h_rt, h_hs, h_is, h_rs, h_ie;  // staging for host-memory calls
   DevBuf h_met, h_ph;
+  DevBuf rc_buf, cb_buf, ord_buf;  // chemistry-step scratch: RCONST, C_before, retry list
+  int last_launches = 0;
+  // optional CUDA-event timing of the Rosenbrock launches (GC_KPP_OPT_TIMING)
+  int timing = 0;
+  int ntimed = 0;
+  cudaEvent_t ev[8] = {};
   int arith = 0;     // 0 fast, 1 strict
   int schedule = 0;  // 0 plain, 1 queue
   int block = 128;
@@ -329,8 +336,11 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
   if (!c) return GC_KPP_OK;
   cudaSetDevice(c->device);
   for (void* p : c->owned) cudaFree(p);
+  for (cudaEvent_t ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
-                    &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph};
+                    &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
+                    &c->rc_buf, &c->cb_buf, &c->ord_buf};
   for (DevBuf* b : bufs) b->release();
   delete c;
   return GC_KPP_OK;
@@ -356,6 +366,9 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
       if (v < 0 || v > 64) return fail(GC_KPP_EINVAL, "blocks per SM out of range");
       c->blocks_per_sm = (int)v;
       return GC_KPP_OK;
+    case GC_KPP_OPT_TIMING:
+      c->timing = v ? 1 : 0;
+      return GC_KPP_OK;
     case GC_KPP_OPT_MAX_SLOTS:
       if (v < 0) return fail(GC_KPP_EINVAL, "max slots must be >= 0");
       c->max_slots = v;
@@ -365,22 +378,22 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
   }
 }
 
-int gc_kpp_integrate_batch(gc_kpp_ctx* c, int ncell, double tin, double tout, double* cc, long long ldc,
-                           const double* rconst, long long ldr, const double* atol, const double* rtol,
-                           const int* icntrl_u, const double* rcntrl_u, const double* hstart, int* istatus,
-                           double* rstatus, long long ldo, int* ierr, int mem, void* stream) {
-  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
-  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
-  if (ncell == 0) return GC_KPP_OK;
-  if (!cc || !rconst || !atol || !rtol || !ierr) return fail(GC_KPP_EINVAL, "required array is NULL");
-  if (ldc < ncell || ldr < ncell || ((istatus || rstatus) && ldo < ncell))
-    return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
-  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
-  GC_CUDA(cudaSetDevice(c->device));
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
+}  // extern "C"
 
-  // INTEGRATE: zero, default ICNTRL(15)=5, then merge nonzero / positive
-  // user entries (gckpp_Integrator.F90:101-117).
+namespace {
+
+// Options of INTEGRATE/Rosenbrock after merging the caller's ICNTRL_U/RCNTRL_U
+// (gckpp_Integrator.F90:101-117, :333-477).
+struct Resolved {
+  int code = 0;  // per-cell IERR for an option error, 0 if none
+  RosMethod meth{};
+  bool vector_tol = true;
+  int max_steps = 200000;
+  double hmin = 0, hmax = 0, hstart_default = 0, facmin = 0, facmax = 0, facrej = 0, facsafe = 0;
+  int autonomous = 1, clamp = 0;
+};
+
+int resolve(const int* icntrl_u, const double* rcntrl_u, double tin, double tout, Resolved& R) {
   int icntrl[20] = {0};
   double rcntrl[20] = {0.0};
   icntrl[14] = 5;
@@ -395,108 +408,62 @@ int gc_kpp_integrate_batch(gc_kpp_ctx* c, int ncell, double tin, double tout, do
   if (icntrl[14] != -1 && (icntrl[14] & 5))
     return fail(GC_KPP_EUNSUPPORTED, "ICNTRL(15) requests Update_RCONST/Update_SUN inside the integrator");
   if (icntrl[11] == 1) return fail(GC_KPP_EUNSUPPORTED, "auto-reduce (ICNTRL(12)=1) is not implemented");
-
-  // Rosenbrock option resolution (:333-477).  A failing check gives the
-  // reference's per-cell IERR for every cell.
-  int code = 0;
-  RosMethod meth;
-  const double roundoff = DBL_EPSILON;  // WLAMCH('E') = 2**-52
-  const bool vector_tol = icntrl[1] == 0;
-  if (!method_table(icntrl[2], meth)) code = -2;
-  int max_steps = 200000;
-  if (!code) {
-    if (icntrl[3] > 0) max_steps = icntrl[3];
-    else if (icntrl[3] < 0) code = -1;
+  R.vector_tol = icntrl[1] == 0;
+  if (!method_table(icntrl[2], R.meth)) R.code = -2;
+  if (!R.code) {
+    if (icntrl[3] > 0) R.max_steps = icntrl[3];
+    else if (icntrl[3] < 0) R.code = -1;
   }
-  const double hmin = rcntrl[0];
   const double span = std::fabs(tout - tin);
-  const double hmax = rcntrl[1] == 0.0 ? span : std::min(std::fabs(rcntrl[1]), span);
-  const double hstart_default = rcntrl[2] == 0.0 ? std::max(hmin, 1.0e-5) : std::min(std::fabs(rcntrl[2]), span);
-  const double facmin = rcntrl[3] == 0.0 ? 0.2 : rcntrl[3];
-  const double facmax = rcntrl[4] == 0.0 ? 6.0 : rcntrl[4];
-  const double facrej = rcntrl[5] == 0.0 ? 0.1 : rcntrl[5];
-  const double facsafe = rcntrl[6] == 0.0 ? 0.9 : rcntrl[6];
+  R.hmin = rcntrl[0];
+  R.hmax = rcntrl[1] == 0.0 ? span : std::min(std::fabs(rcntrl[1]), span);
+  R.hstart_default = rcntrl[2] == 0.0 ? std::max(R.hmin, 1.0e-5) : std::min(std::fabs(rcntrl[2]), span);
+  R.facmin = rcntrl[3] == 0.0 ? 0.2 : rcntrl[3];
+  R.facmax = rcntrl[4] == 0.0 ? 6.0 : rcntrl[4];
+  R.facrej = rcntrl[5] == 0.0 ? 0.1 : rcntrl[5];
+  R.facsafe = rcntrl[6] == 0.0 ? 0.9 : rcntrl[6];
+  R.autonomous = icntrl[0] != 0 ? 1 : 0;
+  R.clamp = icntrl[15] == 1 ? 1 : 0;
+  return GC_KPP_OK;
+}
 
-  const size_t nvar = T::NVAR, nspec = T::NSPEC, nreact = T::NREACT;
-  const size_t ntol = vector_tol ? nvar : 1;
-  // tolerance check needs host values
-  if (!code) {
-    std::vector<double> at(ntol), rt(ntol);
-    if (mem == GC_KPP_MEM_HOST) {
-      std::memcpy(at.data(), atol, ntol * sizeof(double));
-      std::memcpy(rt.data(), rtol, ntol * sizeof(double));
-    } else {
-      GC_CUDA(cudaMemcpyAsync(at.data(), atol, ntol * sizeof(double), cudaMemcpyDeviceToHost, s));
-      GC_CUDA(cudaMemcpyAsync(rt.data(), rtol, ntol * sizeof(double), cudaMemcpyDeviceToHost, s));
-      GC_CUDA(cudaStreamSynchronize(s));
-    }
-    for (size_t i = 0; i < ntol; ++i)
-      if (!(at[i] > 0.0) || rt[i] <= 10.0 * roundoff || rt[i] >= 1.0) code = -5;
-  }
-
-  // device views of the caller's arrays
-  double* d_c = cc;
-  const double* d_r = rconst;
-  const double* d_at = atol;
-  const double* d_rt = rtol;
-  const double* d_hs = hstart;
-  int* d_is = istatus;
-  double* d_rs = rstatus;
-  int* d_ie = ierr;
-  long long lc = ldc, lr = ldr, lo = ldo;
+// Tolerance check of Rosenbrock (:464-472) on host copies.
+int check_tolerances(const double* atol, const double* rtol, int mem, bool vector_tol, cudaStream_t s, Resolved& R) {
+  const size_t ntol = vector_tol ? T::NVAR : 1;
+  std::vector<double> at(ntol), rt(ntol);
   if (mem == GC_KPP_MEM_HOST) {
-    // pack into dense device arrays with ld = ncell
-    lc = lr = lo = ncell;
-    GC_CUDA(c->h_c.ensure(nspec * ncell * sizeof(double)));
-    GC_CUDA(c->h_r.ensure(nreact * ncell * sizeof(double)));
-    GC_CUDA(c->h_at.ensure(nvar * sizeof(double)));
-    GC_CUDA(c->h_rt.ensure(nvar * sizeof(double)));
-    GC_CUDA(c->h_ie.ensure(ncell * sizeof(int)));
-    d_c = (double*)c->h_c.p;
-    d_r = (const double*)c->h_r.p;
-    d_at = (const double*)c->h_at.p;
-    d_rt = (const double*)c->h_rt.p;
-    d_ie = (int*)c->h_ie.p;
-    GC_CUDA(cudaMemcpy2DAsync(d_c, ncell * sizeof(double), cc, ldc * sizeof(double), ncell * sizeof(double),
-                              nspec, cudaMemcpyHostToDevice, s));
-    GC_CUDA(cudaMemcpy2DAsync((void*)d_r, ncell * sizeof(double), rconst, ldr * sizeof(double),
-                              ncell * sizeof(double), nreact, cudaMemcpyHostToDevice, s));
-    GC_CUDA(cudaMemcpyAsync((void*)d_at, atol, ntol * sizeof(double), cudaMemcpyHostToDevice, s));
-    GC_CUDA(cudaMemcpyAsync((void*)d_rt, rtol, ntol * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (hstart) {
-      GC_CUDA(c->h_hs.ensure(ncell * sizeof(double)));
-      d_hs = (const double*)c->h_hs.p;
-      GC_CUDA(cudaMemcpyAsync((void*)d_hs, hstart, ncell * sizeof(double), cudaMemcpyHostToDevice, s));
-    }
-    if (istatus) {
-      GC_CUDA(c->h_is.ensure(20 * (size_t)ncell * sizeof(int)));
-      d_is = (int*)c->h_is.p;
-    }
-    if (rstatus) {
-      GC_CUDA(c->h_rs.ensure(20 * (size_t)ncell * sizeof(double)));
-      d_rs = (double*)c->h_rs.p;
-    }
+    std::memcpy(at.data(), atol, ntol * sizeof(double));
+    std::memcpy(rt.data(), rtol, ntol * sizeof(double));
+  } else {
+    GC_CUDA(cudaMemcpyAsync(at.data(), atol, ntol * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaMemcpyAsync(rt.data(), rtol, ntol * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaStreamSynchronize(s));
   }
+  for (size_t i = 0; i < ntol; ++i)
+    if (!(at[i] > 0.0) || rt[i] <= 10.0 * DBL_EPSILON || rt[i] >= 1.0) R.code = -5;
+  return GC_KPP_OK;
+}
 
-  if (code) {
-    // per-call option error: every cell gets the reference's IERR, zero stats
-    std::vector<int> e(ncell, code);
-    if (mem == GC_KPP_MEM_HOST) {
-      std::memcpy(ierr, e.data(), ncell * sizeof(int));
-      if (istatus)
-        for (int q = 0; q < 20; ++q) std::memset(istatus + q * ldo, 0, ncell * sizeof(int));
-      if (rstatus)
-        for (int q = 0; q < 20; ++q) std::memset(rstatus + q * ldo, 0, ncell * sizeof(double));
-    } else {
-      GC_CUDA(cudaMemcpyAsync(ierr, e.data(), ncell * sizeof(int), cudaMemcpyHostToDevice, s));
-      if (istatus) GC_CUDA(cudaMemset2DAsync(istatus, ldo * sizeof(int), 0, ncell * sizeof(int), 20, s));
-      if (rstatus) GC_CUDA(cudaMemset2DAsync(rstatus, ldo * sizeof(double), 0, ncell * sizeof(double), 20, s));
-      GC_CUDA(cudaStreamSynchronize(s));
-    }
-    return GC_KPP_OK;
-  }
+struct DevArgs {
+  int ncell;
+  const int* order;  // optional cell list
+  const double* c_in;
+  double* c_out;
+  long long ldc;
+  const double* rconst;
+  long long ldr;
+  const double* atol;
+  const double* rtol;
+  const double* hstart;
+  int* istatus;
+  double* rstatus;
+  long long ldo;
+  int* ierr;
+};
 
-  // launch geometry and workspace
+// Launch the Rosenbrock kernel over device arrays.
+int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, const DevArgs& a, cudaStream_t s,
+                     int* launches) {
   const int queue = c->schedule;
   const int block = c->block;
   long long nslot;
@@ -510,17 +477,17 @@ int gc_kpp_integrate_batch(gc_kpp_ctx* c, int ncell, double tin, double tout, do
     }
     grid = c->nsm * per_sm;
     nslot = (long long)grid * block;
-    long long need = ((long long)ncell + block - 1) / block * block;
+    const long long need = ((long long)a.ncell + block - 1) / block * block;
     if (nslot > need) {
       nslot = need;
       grid = (int)(need / block);
     }
     if (c->max_slots > 0 && nslot > c->max_slots) {
-      grid = std::max(1LL, c->max_slots / block);
+      grid = (int)std::max(1LL, c->max_slots / block);
       nslot = (long long)grid * block;
     }
   } else {
-    grid = (ncell + block - 1) / block;
+    grid = (a.ncell + block - 1) / block;
     nslot = (long long)grid * block;
     if (c->max_slots > 0 && nslot > c->max_slots)
       return fail(GC_KPP_EINVAL, "plain schedule needs one workspace slot per cell; raise MAX_SLOTS or use the queue");
@@ -529,57 +496,271 @@ int gc_kpp_integrate_batch(gc_kpp_ctx* c, int ncell, double tin, double tout, do
   GC_CUDA(c->ws.ensure(ws_bytes));
   GC_CUDA(c->counter.ensure(sizeof(int)));
   GC_CUDA(cudaMemsetAsync(c->counter.p, 0, sizeof(int), s));
-
   RosParams p{};
-  p.ncell = ncell;
-  p.order = nullptr;
+  p.ncell = a.ncell;
+  p.order = a.order;
   p.queue_counter = (int*)c->counter.p;
-  p.c_in = d_c;
-  p.c_out = d_c;
-  p.ldc = lc;
-  p.rconst = d_r;
-  p.ldr = lr;
-  p.hstart = d_hs;
-  p.istatus = d_is;
-  p.rstatus = d_rs;
-  p.ldo = lo;
-  p.ierr = d_ie;
-  p.atol = d_at;
-  p.rtol = d_rt;
-  p.vector_tol = vector_tol ? 1 : 0;
+  p.c_in = a.c_in;
+  p.c_out = a.c_out;
+  p.ldc = a.ldc;
+  p.rconst = a.rconst;
+  p.ldr = a.ldr;
+  p.hstart = a.hstart;
+  p.istatus = a.istatus;
+  p.rstatus = a.rstatus;
+  p.ldo = a.ldo;
+  p.ierr = a.ierr;
+  p.atol = a.atol;
+  p.rtol = a.rtol;
+  p.vector_tol = R.vector_tol ? 1 : 0;
   p.tstart = tin;
   p.tend = tout;
-  p.hmin = hmin;
-  p.hmax = hmax;
-  p.hstart_default = hstart_default;
-  p.facmin = facmin;
-  p.facmax = facmax;
-  p.facrej = facrej;
-  p.facsafe = facsafe;
-  p.roundoff = roundoff;
-  p.autonomous = icntrl[0] != 0 ? 1 : 0;
-  p.max_steps = max_steps;
-  p.clamp_negative = icntrl[15] == 1 ? 1 : 0;
+  p.hmin = R.hmin;
+  p.hmax = R.hmax;
+  p.hstart_default = R.hstart_default;
+  p.facmin = R.facmin;
+  p.facmax = R.facmax;
+  p.facrej = R.facrej;
+  p.facsafe = R.facsafe;
+  p.roundoff = DBL_EPSILON;  // WLAMCH('E') = 2**-52
+  p.autonomous = R.autonomous;
+  p.max_steps = R.max_steps;
+  p.clamp_negative = R.clamp;
   p.ws = (double*)c->ws.p;
   p.lay = c->lay;
   p.nslot = nslot;
-
-  cudaError_t e = c->arith ? gckpp_launch_ros_strict(queue, grid, block, c->mech, meth, p, s)
-                           : gckpp_launch_ros_fast(queue, grid, block, c->mech, meth, p, s);
+  const bool timed = c->timing && c->ntimed < 4;
+  if (timed) {
+    for (int i = 2 * c->ntimed; i < 2 * c->ntimed + 2; ++i)
+      if (!c->ev[i]) GC_CUDA(cudaEventCreate(&c->ev[i]));
+    GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed], s));
+  }
+  cudaError_t e = c->arith ? gckpp_launch_ros_strict(queue, grid, block, c->mech, R.meth, p, s)
+                           : gckpp_launch_ros_fast(queue, grid, block, c->mech, R.meth, p, s);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  if (timed) {
+    GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed + 1], s));
+    c->ntimed += 1;
+  }
+  if (launches) *launches += 1;
+  return GC_KPP_OK;
+}
 
+// Write the per-call option error into every cell's outputs (device arrays).
+int fill_option_error(int code, int ncell, int* ierr, int* istatus, double* rstatus, long long ldo, cudaStream_t s) {
+  std::vector<int> e(ncell, code);
+  GC_CUDA(cudaMemcpyAsync(ierr, e.data(), ncell * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (istatus) GC_CUDA(cudaMemset2DAsync(istatus, ldo * sizeof(int), 0, ncell * sizeof(int), 20, s));
+  if (rstatus) GC_CUDA(cudaMemset2DAsync(rstatus, ldo * sizeof(double), 0, ncell * sizeof(double), 20, s));
+  GC_CUDA(cudaStreamSynchronize(s));
+  return GC_KPP_OK;
+}
+
+template <typename X>
+int stage_in(DevBuf& buf, const X* host, long long ld, size_t ncell, size_t rows, cudaStream_t s, X** dev) {
+  GC_CUDA(buf.ensure(rows * ncell * sizeof(X)));
+  *dev = (X*)buf.p;
+  if (host)
+    GC_CUDA(cudaMemcpy2DAsync(buf.p, ncell * sizeof(X), host, ld * sizeof(X), ncell * sizeof(X), rows,
+                              cudaMemcpyHostToDevice, s));
+  return GC_KPP_OK;
+}
+
+template <typename X>
+int stage_out(X* host, long long ld, const X* dev, size_t ncell, size_t rows, cudaStream_t s) {
+  GC_CUDA(cudaMemcpy2DAsync(host, ld * sizeof(X), dev, ncell * sizeof(X), ncell * sizeof(X), rows,
+                            cudaMemcpyDeviceToHost, s));
+  return GC_KPP_OK;
+}
+
+#define GC_TRY(call)            \
+  do {                          \
+    int _rc = (call);           \
+    if (_rc != GC_KPP_OK) return _rc; \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int gc_kpp_integrate_batch(gc_kpp_ctx* c, int ncell, double tin, double tout, double* cc, long long ldc,
+                           const double* rconst, long long ldr, const double* atol, const double* rtol,
+                           const int* icntrl_u, const double* rcntrl_u, const double* hstart, int* istatus,
+                           double* rstatus, long long ldo, int* ierr, int mem, void* stream) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
+  if (ncell == 0) return GC_KPP_OK;
+  if (!cc || !rconst || !atol || !rtol || !ierr) return fail(GC_KPP_EINVAL, "required array is NULL");
+  if (ldc < ncell || ldr < ncell || ((istatus || rstatus) && ldo < ncell))
+    return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
+  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  GC_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  c->ntimed = 0;
+  Resolved R;
+  GC_TRY(resolve(icntrl_u, rcntrl_u, tin, tout, R));
+  if (!R.code) GC_TRY(check_tolerances(atol, rtol, mem, R.vector_tol, s, R));
+  const size_t n = (size_t)ncell, ntol = R.vector_tol ? T::NVAR : 1;
+  DevArgs a{};
+  a.ncell = ncell;
   if (mem == GC_KPP_MEM_HOST) {
-    GC_CUDA(cudaMemcpy2DAsync(cc, ldc * sizeof(double), d_c, ncell * sizeof(double), ncell * sizeof(double), nvar,
-                              cudaMemcpyDeviceToHost, s));
-    GC_CUDA(cudaMemcpyAsync(ierr, d_ie, ncell * sizeof(int), cudaMemcpyDeviceToHost, s));
-    if (istatus)
-      GC_CUDA(cudaMemcpy2DAsync(istatus, ldo * sizeof(int), d_is, ncell * sizeof(int), ncell * sizeof(int), 20,
-                                cudaMemcpyDeviceToHost, s));
-    if (rstatus)
-      GC_CUDA(cudaMemcpy2DAsync(rstatus, ldo * sizeof(double), d_rs, ncell * sizeof(double),
-                                ncell * sizeof(double), 20, cudaMemcpyDeviceToHost, s));
+    double *dc, *dr, *dat, *drt, *dhs = nullptr, *drs = nullptr;
+    int *dis = nullptr, *die;
+    GC_TRY(stage_in(c->h_c, cc, ldc, n, T::NSPEC, s, &dc));
+    GC_TRY(stage_in(c->h_r, rconst, ldr, n, T::NREACT, s, &dr));
+    GC_TRY(stage_in(c->h_at, atol, (long long)ntol, ntol, 1, s, &dat));
+    GC_TRY(stage_in(c->h_rt, rtol, (long long)ntol, ntol, 1, s, &drt));
+    if (hstart) GC_TRY(stage_in(c->h_hs, hstart, ncell, n, 1, s, &dhs));
+    if (istatus) GC_TRY(stage_in<int>(c->h_is, nullptr, ncell, n, 20, s, &dis));
+    if (rstatus) GC_TRY(stage_in<double>(c->h_rs, nullptr, ncell, n, 20, s, &drs));
+    GC_TRY(stage_in<int>(c->h_ie, nullptr, ncell, n, 1, s, &die));
+    a.c_in = dc; a.c_out = dc; a.ldc = ncell; a.rconst = dr; a.ldr = ncell; a.atol = dat; a.rtol = drt;
+    a.hstart = dhs; a.istatus = dis; a.rstatus = drs; a.ldo = ncell; a.ierr = die;
+  } else {
+    a.c_in = cc; a.c_out = cc; a.ldc = ldc; a.rconst = rconst; a.ldr = ldr; a.atol = atol; a.rtol = rtol;
+    a.hstart = hstart; a.istatus = istatus; a.rstatus = rstatus; a.ldo = ldo; a.ierr = ierr;
+  }
+  if (R.code) {
+    GC_TRY(fill_option_error(R.code, ncell, a.ierr, a.istatus, a.rstatus, a.ldo, s));
+  } else {
+    GC_TRY(launch_integrate(c, R, tin, tout, a, s, nullptr));
+  }
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_TRY(stage_out(cc, ldc, (const double*)a.c_out, n, T::NVAR, s));
+    GC_TRY(stage_out(ierr, ncell, (const int*)a.ierr, n, 1, s));
+    if (istatus) GC_TRY(stage_out(istatus, ldo, (const int*)a.istatus, n, 20, s));
+    if (rstatus) GC_TRY(stage_out(rstatus, ldo, (const double*)a.rstatus, n, 20, s));
     GC_CUDA(cudaStreamSynchronize(s));
   }
+  return GC_KPP_OK;
+}
+
+int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm,
+                         const double* photol, long long ldp, double* cc, long long ldc, const double* atol,
+                         const double* rtol, const int* icntrl_u, const double* rcntrl_u, double* hstart,
+                         int* istatus, double* rstatus, long long ldo, int* ierr, int* nretry, int mem,
+                         void* stream) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
+  if (nretry) *nretry = 0;
+  if (ncell == 0) return GC_KPP_OK;
+  if (!met || !photol || !cc || !atol || !rtol || !ierr) return fail(GC_KPP_EINVAL, "required array is NULL");
+  if (ldm < ncell || ldp < ncell || ldc < ncell || ((istatus || rstatus) && ldo < ncell))
+    return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
+  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  GC_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  c->ntimed = 0;
+  Resolved R;
+  GC_TRY(resolve(icntrl_u, rcntrl_u, 0.0, dt, R));
+  if (!R.code) GC_TRY(check_tolerances(atol, rtol, mem, R.vector_tol, s, R));
+  const size_t n = (size_t)ncell, ntol = R.vector_tol ? T::NVAR : 1;
+  const double *dmet, *dph, *dat, *drt;
+  double *dc, *dhs = nullptr, *drs;
+  int *dis, *die;
+  long long lm, lp, lc, lo;
+  if (mem == GC_KPP_MEM_HOST) {
+    double* tmp;
+    GC_TRY(stage_in(c->h_met, met, ldm, n, RT::NMET, s, &tmp)); dmet = tmp;
+    GC_TRY(stage_in(c->h_ph, photol, ldp, n, GC_KPP_NPHOTOL, s, &tmp)); dph = tmp;
+    GC_TRY(stage_in(c->h_c, (const double*)cc, ldc, n, T::NSPEC, s, &dc));
+    GC_TRY(stage_in(c->h_at, atol, (long long)ntol, ntol, 1, s, &tmp)); dat = tmp;
+    GC_TRY(stage_in(c->h_rt, rtol, (long long)ntol, ntol, 1, s, &tmp)); drt = tmp;
+    if (hstart) GC_TRY(stage_in(c->h_hs, (const double*)hstart, ncell, n, 1, s, &dhs));
+    GC_TRY(stage_in<int>(c->h_is, nullptr, ncell, n, 20, s, &dis));
+    GC_TRY(stage_in<double>(c->h_rs, nullptr, ncell, n, 20, s, &drs));
+    GC_TRY(stage_in<int>(c->h_ie, nullptr, ncell, n, 1, s, &die));
+    lm = lp = lc = lo = ncell;
+  } else {
+    dmet = met; dph = photol; dc = cc; dat = atol; drt = rtol; dhs = hstart; lm = ldm; lp = ldp; lc = ldc;
+    die = ierr;
+    if (istatus && rstatus) {
+      dis = istatus; drs = rstatus; lo = ldo;
+    } else {
+      GC_TRY(stage_in<int>(c->h_is, nullptr, ncell, n, 20, s, &dis));
+      GC_TRY(stage_in<double>(c->h_rs, nullptr, ncell, n, 20, s, &drs));
+      lo = ncell;
+    }
+  }
+  // zero the prod/loss family dummies (fullchem_mod.F90:943-946)
+  for (int f = 0; f < (int)(sizeof(T::family_species) / sizeof(int)); ++f)
+    GC_CUDA(cudaMemsetAsync(dc + (long long)T::family_species[f] * lc, 0, n * sizeof(double), s));
+  // Update_RCONST (fullchem_mod.F90:953)
+  double* drc;
+  GC_TRY(stage_in<double>(c->rc_buf, nullptr, ncell, n, T::NREACT, s, &drc));
+  gcrates::RatesArgs ra{};
+  ra.ncell = ncell; ra.met = dmet; ra.ldm = lm; ra.photol = dph; ra.ldp = lp; ra.c = dc; ra.ldc = lc;
+  ra.rconst = drc; ra.ldr = ncell;
+  cudaError_t e = gcrates::launch_rates(c->rates, ra, s);
+  if (e != cudaSuccess) return cuda_fail(e, "rates kernel launch");
+  c->last_launches = 1;
+  if (R.code) {
+    GC_TRY(fill_option_error(R.code, ncell, die, dis, drs, lo, s));
+  } else {
+    // C_before_integrate (fullchem_mod.F90:1023), same leading dimension as C
+    double* dcb;
+    GC_TRY(stage_in<double>(c->cb_buf, nullptr, lc, (size_t)lc, T::NSPEC, s, &dcb));
+    GC_CUDA(cudaMemcpyAsync(dcb, dc, (size_t)lc * T::NSPEC * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    DevArgs a{};
+    a.ncell = ncell; a.c_in = dc; a.c_out = dc; a.ldc = lc; a.rconst = drc; a.ldr = ncell; a.atol = dat;
+    a.rtol = drt; a.hstart = dhs; a.istatus = dis; a.rstatus = drs; a.ldo = lo; a.ierr = die;
+    GC_TRY(launch_integrate(c, R, 0.0, dt, a, s, &c->last_launches));
+    // retry failed cells once with Hstart = 0 from C_before
+    // (fullchem_mod.F90:1138-1162)
+    std::vector<int> hier(n);
+    GC_CUDA(cudaMemcpyAsync(hier.data(), die, n * sizeof(int), cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+    std::vector<int> failed;
+    for (int i = 0; i < ncell; ++i)
+      if (hier[i] < 0) failed.push_back(i);
+    if (!failed.empty()) {
+      int* dord;
+      GC_TRY(stage_in<int>(c->ord_buf, failed.data(), (long long)failed.size(), failed.size(), 1, s, &dord));
+      // the failed cells restart from C_before (c_in) and overwrite their
+      // entries of C (c_out); Hstart = RCNTRL(3) = 0 -> DeltaMin
+      DevArgs b = a;
+      b.ncell = (int)failed.size();
+      b.order = dord;
+      b.c_in = dcb;
+      b.hstart = nullptr;
+      Resolved R2 = R;
+      R2.hstart_default = std::max(R.hmin, 1.0e-5);
+      if (nretry) *nretry = (int)failed.size();
+      GC_TRY(launch_integrate(c, R2, 0.0, dt, b, s, &c->last_launches));
+    }
+    // C = MAX(C, 0) (fullchem_mod.F90:1329-1350)
+    e = gcutil::clamp_nonneg(dc, lc, T::NSPEC, ncell, s);
+    if (e != cudaSuccess) return cuda_fail(e, "clamp kernel launch");
+    c->last_launches += 1;
+    // KPPHvalue = RSTATE(Nhnew) (fullchem_mod.F90:1294)
+    if (dhs)
+      GC_CUDA(cudaMemcpyAsync(dhs, drs + 2 * lo, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_TRY(stage_out(cc, ldc, (const double*)dc, n, T::NSPEC, s));
+    GC_TRY(stage_out(ierr, ncell, (const int*)die, n, 1, s));
+    if (istatus) GC_TRY(stage_out(istatus, ldo, (const int*)dis, n, 20, s));
+    if (rstatus) GC_TRY(stage_out(rstatus, ldo, (const double*)drs, n, 20, s));
+    if (hstart) GC_TRY(stage_out(hstart, ncell, (const double*)dhs, n, 1, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+  }
+  return GC_KPP_OK;
+}
+
+int gc_kpp_last_launch_count(gc_kpp_ctx* c) { return c ? c->last_launches : 0; }
+
+int gc_kpp_last_kernel_ms(gc_kpp_ctx* c, double* ms, int* nlaunch) {
+  if (!c || !ms) return fail(GC_KPP_EINVAL, "NULL argument");
+  double total = 0.0;
+  for (int i = 0; i < c->ntimed; ++i) {
+    GC_CUDA(cudaEventSynchronize(c->ev[2 * i + 1]));
+    float t = 0.f;
+    GC_CUDA(cudaEventElapsedTime(&t, c->ev[2 * i], c->ev[2 * i + 1]));
+    total += t;
+  }
+  *ms = total;
+  if (nlaunch) *nlaunch = c->ntimed;
+  c->ntimed = 0;
   return GC_KPP_OK;
 }
 

@@ -124,6 +124,7 @@ class Tables:
         self.uop = np.array(uop, np.uint32).view(np.int32)
         assert self.lu_nonzero < (1 << 16)
         self.lit = np.array(self.literals, np.float64)
+        self.family_species = np.array([ir["species"].index(f) for f in ir.get("families", [])], np.int32)
 
     # flop bookkeeping used by the roofline accounting (FP64 operations per
     # call, counting a multiply-add as 2, a division as 1, in STRICT form)
@@ -179,6 +180,7 @@ class Tables:
         arr("lop_dj", self.lop_dj)
         arr("lop_u", self.lop_u)
         arr("uop", self.uop.view(np.uint32), "unsigned")
+        arr("family_species", self.family_species)
         out.append("static const double lit[%d] = {%s};" % (
             len(self.literals), ",".join(_hexfloat(v) for v in self.literals)))
         out.append("}  // namespace gcmech_tables")

@@ -50,6 +50,7 @@ extern "C" {
 #define GC_KPP_OPT_BLOCK 3        /* threads per block (multiple of 32), 0 = default */
 #define GC_KPP_OPT_BLOCKS_PER_SM 4 /* queue schedule: resident blocks per SM, 0 = default */
 #define GC_KPP_OPT_MAX_SLOTS 5    /* cap on workspace slots (cells in flight), 0 = no cap */
+#define GC_KPP_OPT_TIMING 6       /* 1 = time the Rosenbrock launches with CUDA events */
 
 /* Per-cell meteorology/state fields of gc_kpp_update_rconst_batch (rows of
  * `met`), the thread-private globals that Set_Kpp_GridBox_Values and the
@@ -130,6 +131,34 @@ int gc_kpp_integrate_batch(gc_kpp_ctx* ctx, int ncell, double tin, double tout,
 int gc_kpp_update_rconst_batch(gc_kpp_ctx* ctx, int ncell, const double* met, long long ldm,
                                const double* photol, long long ldp, const double* c, long long ldc,
                                double* rconst, long long ldr, int mem, void* stream);
+
+/* One chemistry step of Do_FullChem's cell loop for a batch of cells
+ * (GeosCore/fullchem_mod.F90:528-1551, the loop body from :817 to :1350):
+ *   zero the prod/loss family dummies (:943-946), Update_RCONST (:953),
+ *   save C (:1023), Integrate(0, DT) with RCNTRL(3) = hstart[cell] (:1033),
+ *   for cells with IERR < 0 integrate once more from the saved C with
+ *   Hstart = 0 (:1138-1162), hstart[cell] = RSTATE(Nhnew) (:1294), and
+ *   C = MAX(C, 0) (:1329-1350).
+ *
+ *   met/photol   as gc_kpp_update_rconst_batch
+ *   c            [NSPEC][ldc] in/out
+ *   hstart       [ncell] in/out or NULL: the KPPHvalue chain
+ *   istatus/rstatus/ierr as gc_kpp_integrate_batch (the final attempt)
+ *   nretry       out or NULL: number of cells integrated a second time
+ * A cell that fails twice keeps IERR < 0; like the reference with KppStop
+ * off, its concentrations are those of the failed attempt, clamped. */
+int gc_kpp_fullchem_step(gc_kpp_ctx* ctx, int ncell, double dt, const double* met, long long ldm,
+                         const double* photol, long long ldp, double* c, long long ldc,
+                         const double* atol, const double* rtol, const int* icntrl, const double* rcntrl,
+                         double* hstart, int* istatus, double* rstatus, long long ldo, int* ierr,
+                         int* nretry, int mem, void* stream);
+
+/* Number of kernels the last gc_kpp_fullchem_step call on ctx launched. */
+int gc_kpp_last_launch_count(gc_kpp_ctx* ctx);
+
+/* With GC_KPP_OPT_TIMING set: device time [ms] of the Rosenbrock kernel
+ * launches of the last integrate/step call (waits for them to finish). */
+int gc_kpp_last_kernel_ms(gc_kpp_ctx* ctx, double* ms, int* nlaunch);
 
 #ifdef __cplusplus
 }
