@@ -220,9 +220,9 @@ bool method_table(int id, RosMethod& r) {
 WsLayout make_layout() {
   WsLayout l;
   int o = 0;
-  l.aux = o; o += T::NFIX + T::NREACT;
-  l.y0 = o; o += T::NVAR;
-  l.y1 = o; o += T::NVAR;
+  l.aux = o; o += T::NAUX;
+  l.y0 = o; o += T::NSPEC;
+  l.y1 = o; o += T::NSPEC;
   l.fcn0 = o; o += T::NVAR;
   l.fcn = o; o += T::NVAR;
   l.dfdt = o; o += T::NVAR;
@@ -270,6 +270,7 @@ struct gc_kpp_ctx {
   int last_launches = 0;
   // optional CUDA-event timing of the Rosenbrock launches (GC_KPP_OPT_TIMING)
   int timing = 0;
+  int lu_form = 0;  // 0 row-wise dot products, 1 KppDecomp right-looking order
   int ntimed = 0;
   cudaEvent_t ev[8] = {};
   int arith = 0;     // 0 fast, 1 strict
@@ -311,10 +312,15 @@ int gc_kpp_ctx_create(gc_kpp_ctx** out, int device) {
 #define UP(field, arr)                                                         \
   e = upload(T::arr, sizeof(T::arr) / sizeof(T::arr[0]), &m.field, c->owned); \
   if (e != cudaSuccess) { gc_kpp_ctx_destroy(c); return cuda_fail(e, "upload " #arr); }
-  UP(prod_start, prod_start) UP(prod_fac, prod_fac) UP(p_start, p_start) UP(p_term, p_term)
-  UP(d_start, d_start) UP(d_term, d_term) UP(j_start, j_start) UP(j_term, j_term)
+  e = upload(reinterpret_cast<const uint2*>(T::prod_packed), sizeof(T::prod_packed) / (2 * sizeof(unsigned)),
+             &m.prod_packed, c->owned);
+  if (e != cudaSuccess) { gc_kpp_ctx_destroy(c); return cuda_fail(e, "upload prod_packed"); }
+  m.naux = T::NAUX;
+  UP(pre_lit, pre_literals) UP(p_start, p_start) UP(p_sterm, p_sterm) UP(slit, slit)
+  UP(d_start, d_start) UP(d_sterm, d_sterm) UP(j_start, j_start) UP(j_sterm, j_sterm)
   UP(lu_crow, lu_crow) UP(lu_diag, lu_diag) UP(lu_icol, lu_icol) UP(lrow_start, lrow_start)
   UP(lop_kk, lop_kk) UP(lop_dj, lop_dj) UP(lop_u, lop_u) UP(uop, uop) UP(lit, lit)
+  UP(dot_start, dot_start) UP(dot_term, dot_term)
 #undef UP
   gcrates::RatesDev& rp = c->rates;
   rp.nreact = T::NREACT;
@@ -359,12 +365,16 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
       return GC_KPP_OK;
     case GC_KPP_OPT_BLOCK:
       if (v == 0) v = 128;
-      if (v < 32 || v > 256 || v % 32) return fail(GC_KPP_EINVAL, "block must be a multiple of 32 in [32,256]");
+      if (v < 32 || v > 128 || v % 32) return fail(GC_KPP_EINVAL, "block must be a multiple of 32 in [32,128]");
       c->block = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_BLOCKS_PER_SM:
       if (v < 0 || v > 64) return fail(GC_KPP_EINVAL, "blocks per SM out of range");
       c->blocks_per_sm = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_LU:
+      if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "lu form must be 0 or 1");
+      c->lu_form = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_TIMING:
       c->timing = v ? 1 : 0;
@@ -526,6 +536,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   p.autonomous = R.autonomous;
   p.max_steps = R.max_steps;
   p.clamp_negative = R.clamp;
+  p.lu_form = c->lu_form;
   p.ws = (double*)c->ws.p;
   p.lay = c->lay;
   p.nslot = nslot;

@@ -13,10 +13,17 @@
 #define GCKPP_OCC gckpp_occupancy_fast
 #endif
 
+#ifndef GCKPP_MAX_BLOCK
+#define GCKPP_MAX_BLOCK 128
+#endif
+#ifndef GCKPP_MIN_BLOCKS
+#define GCKPP_MIN_BLOCKS 8
+#endif
+
 namespace gckpp {
 
 template <bool QUEUE>
-__global__ void __launch_bounds__(256) ros_kernel(MechDev m, RosMethod r, RosParams p) {
+__global__ void __launch_bounds__(GCKPP_MAX_BLOCK, GCKPP_MIN_BLOCKS) ros_kernel(MechDev m, RosMethod r, RosParams p) {
   ros_driver<GCKPP_ARITH, QUEUE>(m, r, p);
 }
 

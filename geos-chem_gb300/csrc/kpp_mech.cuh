@@ -25,14 +25,16 @@ constexpr int TS = 32;  // lanes per tile
 
 struct MechDev {
   int nvar, nfix, nreact, nspec, lu_nonzero, nb, lit0;
-  const int* prod_start;
-  const int* prod_fac;
+  const uint2* prod_packed;  // pre | times2<<12 | nspecies<<13 | s1<<16, s2 | s3<<16
+  const double* pre_lit;     // constant-rate literals, appended to RCT in aux
+  int naux;
   const int* p_start;
-  const unsigned* p_term;
+  const unsigned* p_sterm;
   const int* d_start;
-  const unsigned* d_term;
+  const unsigned* d_sterm;
   const int* j_start;
-  const unsigned* j_term;
+  const unsigned* j_sterm;
+  const double* slit;  // signed term coefficients
   const int* lu_crow;
   const int* lu_diag;
   const int* lu_icol;
@@ -41,10 +43,11 @@ struct MechDev {
   const int* lop_dj;
   const int* lop_u;
   const unsigned* uop;
+  const int* dot_start;
+  const unsigned* dot_term;
   const double* lit;
 };
 
-constexpr unsigned NOCOEF = 0x7ffu;
 
 __device__ __forceinline__ int ldi(const int* p) { return __ldg(p); }
 __device__ __forceinline__ unsigned ldu(const unsigned* p) { return __ldg(p); }
@@ -55,96 +58,74 @@ __device__ __forceinline__ bool tiny_abs(double x) {
          0x0010000000000000ULL;
 }
 
-__device__ __forceinline__ double operand(const MechDev& m, int code, const double* V, const double* aux) {
-  if (code < m.nvar) return V[code * TS];
-  if (code < m.lit0) return aux[(code - m.nvar) * TS];
-  return __ldg(m.lit + (code - m.lit0));
+// One product of the mechanism, pre [* 2] * s1 * s2 * s3, in the Fortran's
+// left-to-right order.  aux holds RCT (and the constant-rate literals), Y the
+// species [V | F].  The species loads are issued unconditionally so that the
+// loads of consecutive products overlap.
+__device__ __forceinline__ double product(const MechDev& m, int p, const double* Y, const double* aux) {
+  const uint2 t = __ldg(m.prod_packed + p);
+  double a = aux[(t.x & 0xfffu) * TS];
+  const unsigned ns = (t.x >> 13) & 3u;
+  const double v1 = Y[(t.x >> 16) * TS], v2 = Y[(t.y & 0xffffu) * TS], v3 = Y[(t.y >> 16) * TS];
+  if (t.x & 0x1000u) a = a * 2.0;
+  if (ns >= 1u) a = a * v1;
+  if (ns >= 2u) a = a * v2;
+  if (ns >= 3u) a = a * v3;
+  return a;
 }
 
-// Left-to-right product of a factor list (Fortran evaluation order).
-__device__ __forceinline__ double product(const MechDev& m, int p, const double* V, const double* aux) {
-  const int s = ldi(m.prod_start + p), e = ldi(m.prod_start + p + 1);
-  double acc = operand(m, ldi(m.prod_fac + s), V, aux);
-  for (int i = s + 1; i < e; ++i) acc = acc * operand(m, ldi(m.prod_fac + i), V, aux);
-  return acc;
-}
-
-// Signed sum of [coef*]X(idx) terms; FLIP negates every term (exact).
+// Sum of signed terms  slit[c] * X[idx]  (sterm = c << 20 | idx) in the
+// reference's left-to-right order.  The sign is folded into the coefficient
+// (a bare X(idx) is +/-1.0 * X(idx), exact), so the loop has no branch and
+// consecutive terms' loads overlap.  FLIP negates the sum (exact).
 template <bool STRICT, bool FLIP>
-__device__ __forceinline__ double coef_sum(const MechDev& m, const unsigned* terms, int s, int e, const double* X) {
-  if (s == e) return 0.0;
-  double acc;
-  {
-    const unsigned t = ldu(terms + s);
-    const unsigned c = (t >> 20) & 0x7ffu;
-    const double x = X[(t & 0xfffffu) * TS];
-    const double v = (c == NOCOEF) ? x : __ldg(m.lit + c) * x;
-    const bool neg = ((t >> 31) != 0) != FLIP;
-    acc = neg ? -v : v;
-  }
-  for (int i = s + 1; i < e; ++i) {
+__device__ __forceinline__ double term_sum(const MechDev& m, const unsigned* __restrict__ terms, int s, int e,
+                                           const double* __restrict__ X) {
+  double acc = 0.0;
+#pragma unroll 4
+  for (int i = s; i < e; ++i) {
     const unsigned t = ldu(terms + i);
-    const unsigned c = (t >> 20) & 0x7ffu;
+    const double cf = __ldg(m.slit + (t >> 20));
     const double x = X[(t & 0xfffffu) * TS];
-    const bool neg = ((t >> 31) != 0) != FLIP;
     if (STRICT) {
-      const double v = (c == NOCOEF) ? x : __ldg(m.lit + c) * x;
-      acc = neg ? acc - v : acc + v;
+      const double v = cf * x;
+      acc = (i == s) ? (FLIP ? -v : v) : (FLIP ? acc - v : acc + v);
     } else {
-      if (c == NOCOEF) {
-        acc = neg ? acc - x : acc + x;
-      } else {
-        const double cf = __ldg(m.lit + c);
-        acc = fma(neg ? -cf : cf, x, acc);
-      }
+      acc = fma(FLIP ? -cf : cf, x, acc);
     }
   }
   return acc;
 }
 
-// Sum of signed B products (D_VAR of Fun_SPLIT).  With Bv the products are
-// read from an earlier Jacobian evaluation at the same point.
-template <bool STRICT>
-__device__ __forceinline__ double dsum(const MechDev& m, int s, int e, const double* V, const double* aux,
-                                       const double* Bv) {
-  if (s == e) return 0.0;
-  double acc = 0.0;
-  for (int i = s; i < e; ++i) {
-    const unsigned t = ldu(m.d_term + i);
-    const int b = static_cast<int>(t & 0xfffffu);
-    const double v = Bv ? Bv[b * TS] : product(m, m.nreact + b, V, aux);
-    const bool neg = (t >> 31) != 0;
-    if (i == s) acc = neg ? -v : v;
-    else acc = neg ? acc - v : acc + v;
-  }
-  return acc;
+// B(b): the partial-derivative products of Jac_SP, which are also the
+// D_VAR products of Fun_SPLIT (same factor lists, same order).
+__device__ __forceinline__ void b_products(const MechDev& m, const double* __restrict__ Y,
+                                           const double* __restrict__ aux, double* __restrict__ B) {
+#pragma unroll 4
+  for (int b = 0; b < m.nb; ++b) B[b * TS] = product(m, m.nreact + b, Y, aux);
 }
 
-// Fun_SPLIT: Vdot = P_VAR - D_VAR*V at point V (aux = [F, RCT]).
+// Fun_SPLIT: Vdot = P_VAR - D_VAR*V at point Y = [V | F] (aux = RCT).
+// B must hold the B products at Y (b_products).
 template <bool STRICT>
 __device__ void fun_split(const MechDev& m, const double* __restrict__ V, const double* __restrict__ aux,
-                          double* __restrict__ A, const double* __restrict__ Bv, double* __restrict__ Vdot) {
-#pragma unroll 2
+                          double* __restrict__ A, const double* __restrict__ B, double* __restrict__ Vdot) {
+#pragma unroll 4
   for (int r = 0; r < m.nreact; ++r) A[r * TS] = product(m, r, V, aux);
   for (int i = 0; i < m.nvar; ++i) {
-    const double p = coef_sum<STRICT, false>(m, m.p_term, ldi(m.p_start + i), ldi(m.p_start + i + 1), A);
-    const double d = dsum<STRICT>(m, ldi(m.d_start + i), ldi(m.d_start + i + 1), V, aux, Bv);
+    const double p = term_sum<STRICT, false>(m, m.p_sterm, ldi(m.p_start + i), ldi(m.p_start + i + 1), A);
+    const double d = term_sum<STRICT, false>(m, m.d_sterm, ldi(m.d_start + i), ldi(m.d_start + i + 1), B);
     const double v = V[i * TS];
     Vdot[i * TS] = STRICT ? p - d * v : fma(-d, v, p);
   }
 }
 
-// Jac_SP: B partials then JVS in LU order.  STRICT stores JVS; the fast form
-// stores -JVS (what ros_PrepareMatrix needs).
+// Jac_SP: JVS in LU order from the B products.  STRICT stores JVS; the fast
+// form stores -JVS (what ros_PrepareMatrix needs).
 template <bool STRICT>
-__device__ void jac_sp(const MechDev& m, const double* __restrict__ V, const double* __restrict__ aux,
-                       double* __restrict__ B, double* __restrict__ J) {
-  for (int b = 0; b < m.nb; ++b) {
-    const int p = m.nreact + b;
-    if (ldi(m.prod_start + p + 1) > ldi(m.prod_start + p)) B[b * TS] = product(m, p, V, aux);
-  }
+__device__ void jac_sp(const MechDev& m, const double* __restrict__ B, double* __restrict__ J) {
   for (int k = 0; k < m.lu_nonzero; ++k)
-    J[k * TS] = coef_sum<STRICT, !STRICT>(m, m.j_term, ldi(m.j_start + k), ldi(m.j_start + k + 1), B);
+    J[k * TS] = term_sum<STRICT, !STRICT>(m, m.j_sterm, ldi(m.j_start + k), ldi(m.j_start + k + 1), B);
 }
 
 // Ghimj = -Jac0 + diag(ghinv), then KppDecomp in place.  Returns 0 or the
@@ -188,6 +169,43 @@ __device__ int decomp(const MechDev& m, const double* __restrict__ J0, double gh
     if (!STRICT) {
       const int d = ldi(m.lu_diag + k);
       G[d * TS] = 1.0 / G[d * TS];
+    }
+  }
+  return 0;
+}
+
+// The same factorization, with every entry (k,c) of row k computed as one
+// accumulation in a register:  W(c) = Ghimj(k,c) - sum_j L(k,j)*U(j,c) over
+// the L entries j < c of row k in ascending order -- the updates KppDecomp
+// applies to W(c), in the same order, so STRICT stays bit-for-bit.  Each
+// entry is loaded from Jac0 and stored once (no read-modify-write of the
+// row in memory), and Ghimj is never materialised.
+template <bool STRICT>
+__device__ int decomp_rows(const MechDev& m, const double* __restrict__ J0, double ghinv, double* __restrict__ G) {
+  for (int i = 0; i < m.nvar; ++i) {
+    const int d = ldi(m.lu_diag + i);
+    const double g = (STRICT ? -J0[d * TS] : J0[d * TS]) + ghinv;
+    if (tiny_abs(g)) return i + 1;
+  }
+  for (int k = 0; k < m.nvar; ++k) {
+    const int e0 = ldi(m.lu_crow + k), e1 = ldi(m.lu_crow + k + 1), dk = ldi(m.lu_diag + k);
+    for (int e = e0; e < e1; ++e) {
+      double acc = STRICT ? -J0[e * TS] : J0[e * TS];
+      if (e == dk) acc = acc + ghinv;
+      const int t0 = ldi(m.dot_start + e), t1 = ldi(m.dot_start + e + 1);
+#pragma unroll 4
+      for (int t = t0; t < t1; ++t) {
+        const unsigned op = ldu(m.dot_term + t);
+        const double l = G[(op >> 16) * TS], u = G[(op & 0xffffu) * TS];
+        acc = STRICT ? acc - l * u : fma(-l, u, acc);
+      }
+      if (e < dk) {
+        const int dc = ldi(m.lu_diag + ldi(m.lu_icol + e));
+        acc = STRICT ? acc / G[dc * TS] : acc * G[dc * TS];  // fast: diag holds 1/pivot
+      } else if (e == dk && !STRICT) {
+        acc = 1.0 / acc;
+      }
+      G[e * TS] = acc;
     }
   }
   return 0;

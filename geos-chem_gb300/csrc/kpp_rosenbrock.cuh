@@ -55,6 +55,7 @@ struct RosParams {
   double tstart, tend;
   double hmin, hmax, hstart_default, facmin, facmax, facrej, facsafe, roundoff;
   int autonomous, max_steps, clamp_negative;
+  int lu_form;  // 0 decomp_rows, 1 decomp (KppDecomp order)
   // workspace
   double* ws;
   WsLayout lay;
@@ -88,11 +89,18 @@ struct Rosenbrock {
 
   __device__ void load_cell(double* w, Lane& L, int cell) {
     const int nvar = m.nvar;
+    // aux = [RCT | constant-rate literals]; Y buffers = [V | F]
     double* aux = w + p.lay.aux * TS;
-    for (int f = 0; f < m.nfix; ++f) aux[f * TS] = p.c_in[(long long)(nvar + f) * p.ldc + cell];
-    for (int q = 0; q < m.nreact; ++q) aux[(m.nfix + q) * TS] = p.rconst[(long long)q * p.ldr + cell];
+    for (int q = 0; q < m.nreact; ++q) aux[q * TS] = p.rconst[(long long)q * p.ldr + cell];
+    for (int q = m.nreact; q < m.naux; ++q) aux[q * TS] = __ldg(m.pre_lit + (q - m.nreact));
     double* y = w + p.lay.y0 * TS;
+    double* y1 = w + p.lay.y1 * TS;
     for (int i = 0; i < nvar; ++i) y[i * TS] = p.c_in[(long long)i * p.ldc + cell];
+    for (int f = 0; f < m.nfix; ++f) {
+      const double v = p.c_in[(long long)(nvar + f) * p.ldc + cell];
+      y[(nvar + f) * TS] = v;
+      y1[(nvar + f) * TS] = v;
+    }
     L.cell = cell;
     L.ybuf = 0;
     L.nfun = L.njac = L.nstp = L.nacc = L.nrej = L.ndec = L.nsol = L.nsng = 0;
@@ -164,9 +172,9 @@ struct Rosenbrock {
     const double* aux = w + p.lay.aux * TS;
     const double* Y = w + (L.ybuf ? p.lay.y1 : p.lay.y0) * TS;
     double* B = w + p.lay.b * TS;
-    // Jacobian first so that Fun0 can reuse its B partials (the D_VAR
-    // products of Fun_SPLIT are the same factor lists in the same order).
-    jac_sp<STRICT>(m, Y, aux, B, w + p.lay.j0 * TS);
+    // B products once for both Jac_SP and Fun0's D_VAR terms.
+    b_products(m, Y, aux, B);
+    jac_sp<STRICT>(m, B, w + p.lay.j0 * TS);
     fun_split<STRICT>(m, Y, aux, w + p.lay.a * TS, B, w + p.lay.fcn0 * TS);
     L.nfun += 1;
     if (!p.autonomous) {
@@ -198,7 +206,7 @@ struct Rosenbrock {
     int nconsec = 0;
     while (true) {
       const double ghinv = 1.0 / (dir * L.H * r.Gamma[0]);
-      const int ier = decomp<STRICT>(m, J0, ghinv, G);
+      const int ier = p.lu_form ? decomp<STRICT>(m, J0, ghinv, G) : decomp_rows<STRICT>(m, J0, ghinv, G);
       L.ndec += 1;
       if (ier == 0) break;
       L.nsng += 1;
@@ -228,7 +236,8 @@ struct Rosenbrock {
           }
           Ynew[i * TS] = y;
         }
-        fun_split<STRICT>(m, Ynew, aux, w + p.lay.a * TS, nullptr, w + p.lay.fcn * TS);
+        b_products(m, Ynew, aux, w + p.lay.b * TS);
+        fun_split<STRICT>(m, Ynew, aux, w + p.lay.a * TS, w + p.lay.b * TS, w + p.lay.fcn * TS);
         L.nfun += 1;
         fcn = w + p.lay.fcn * TS;
       }

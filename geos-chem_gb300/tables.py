@@ -80,6 +80,43 @@ class Tables:
             self.prod_start[i + 1] = len(facs)
         self.prod_fac = np.array(facs, np.int32)
 
+        # Packed products for the engine: every product of the mechanism has
+        # the shape  pre [* 2] * s1 * s2 * s3  with pre a rate constant (or
+        # one of the two constant-rate literals, kept as extra rate slots),
+        # an optional literal 2 right after it, and up to three species
+        # factors (variable or fixed species, indices into [V | F]).
+        #   x = pre | times2 << 12 | nspecies << 13 | s1 << 16
+        #   y = s2 | s3 << 16
+        self.pre_literals = []
+        packed = []
+        for p in prods:
+            if not p:
+                packed.append((0, 0))
+                continue
+            head = p[0]
+            if head[0] == "R":
+                pre = int(head[1:])
+            else:
+                v = float(head)
+                if v not in self.pre_literals:
+                    self.pre_literals.append(v)
+                pre = self.nreact + self.pre_literals.index(v)
+            rest = p[1:]
+            two = 0
+            if rest and not rest[0][0].isalpha():
+                assert float(rest[0]) == 2.0, p
+                two = 1
+                rest = rest[1:]
+            sp = []
+            for t in rest:
+                assert t[0] in "VF", p
+                sp.append(int(t[1:]) if t[0] == "V" else self.nvar + int(t[1:]))
+            assert len(sp) <= 3 and pre < 4096
+            s = sp + [0] * (3 - len(sp))
+            packed.append((pre | (two << 12) | (len(sp) << 13) | (s[0] << 16), s[1] | (s[2] << 16)))
+        self.prod_packed = np.array(packed, np.uint32)
+        self.naux = self.nreact + len(self.pre_literals)
+
         def coef_terms(lists):
             start = np.zeros(len(lists) + 1, np.int32)
             out = []
@@ -99,6 +136,33 @@ class Tables:
         for terms in ir["fun"]["D"]:
             dl.append([[s, None, bmap[tuple(f)]] for s, f in terms])
         self.d_start, self.d_term = coef_terms(dl)
+
+        # Device form of the same terms: the sign folded into a signed
+        # coefficient table (a bare reference becomes +/-1.0, which multiplies
+        # exactly), so every term is  acc += slit[c] * X[idx]  with no branch.
+        #   sterm = c << 20 | idx
+        self.slit = []
+        slit_index = {}
+
+        def sterms(packed):
+            out = []
+            for u in packed.view(np.uint32):
+                u = int(u)
+                c = (u >> 20) & 0x7FF
+                v = 1.0 if c == NOCOEF else self.literals[c]
+                if u >> 31:
+                    v = -v
+                key = struct.pack("<d", v)
+                if key not in slit_index:
+                    slit_index[key] = len(self.slit)
+                    self.slit.append(v)
+                out.append((slit_index[key] << 20) | (u & 0xFFFFF))
+            return np.array(out, np.uint32)
+
+        self.p_sterm = sterms(self.p_term)
+        self.j_sterm = sterms(self.j_term)
+        self.d_sterm = sterms(self.d_term)
+        assert len(self.slit) < 4096
 
         lu = ir["lu"]
         crow, diag, icol = lu["crow"], lu["diag"], lu["icol"]
@@ -122,6 +186,27 @@ class Tables:
         self.lop_dj = np.array([x[1] for x in lop], np.int32)
         self.lop_u = np.array([x[2] for x in lop] + [len(uop)], np.int32)
         self.uop = np.array(uop, np.uint32).view(np.int32)
+        # The same updates regrouped per target entry (row-wise "dot product"
+        # form): entry e = (k,c) receives W(c) -= L(k,j)*U(j,c) for the L
+        # entries j of row k in ascending order, exactly the sequence of
+        # updates KppDecomp applies to W(c).  ``dot_start[e]`` indexes
+        # ``dot_term`` = (position of (k,j)) << 16 | (position of (j,c)).
+        upos = [{icol[jj]: jj for jj in range(diag[j] + 1, crow[j + 1])} for j in range(self.nvar)]
+        self.dot_start = np.zeros(self.lu_nonzero + 1, np.int32)
+        dot = []
+        for k in range(self.nvar):
+            for e in range(crow[k], crow[k + 1]):
+                c = icol[e]
+                for kk in range(crow[k], diag[k]):
+                    j = icol[kk]
+                    if j >= c:
+                        break
+                    jj = upos[j].get(c)
+                    if jj is not None:
+                        dot.append((kk << 16) | jj)
+                self.dot_start[e + 1] = len(dot)
+        self.dot_term = np.array(dot, np.uint32).view(np.int32)
+        assert len(self.dot_term) == len(self.uop)
         assert self.lu_nonzero < (1 << 16)
         self.lit = np.array(self.literals, np.float64)
         self.family_species = np.array([ir["species"].index(f) for f in ir.get("families", [])], np.int32)
@@ -166,6 +251,14 @@ class Tables:
 
         arr("prod_start", self.prod_start)
         arr("prod_fac", self.prod_fac)
+        arr("prod_packed", self.prod_packed.reshape(-1), "unsigned")
+        arr("p_sterm", self.p_sterm, "unsigned")
+        arr("d_sterm", self.d_sterm, "unsigned")
+        arr("j_sterm", self.j_sterm, "unsigned")
+        out.append("static const double slit[%d] = {%s};" % (len(self.slit), ",".join(_hexfloat(v) for v in self.slit)))
+        out.append("constexpr int NAUX = %d;" % self.naux)
+        out.append("static const double pre_literals[%d] = {%s};" % (
+            max(1, len(self.pre_literals)), ",".join(_hexfloat(v) for v in self.pre_literals) or "0.0"))
         arr("p_start", self.p_start)
         arr("p_term", self.p_term.view(np.uint32), "unsigned")
         arr("d_start", self.d_start)
@@ -181,6 +274,8 @@ class Tables:
         arr("lop_u", self.lop_u)
         arr("uop", self.uop.view(np.uint32), "unsigned")
         arr("family_species", self.family_species)
+        arr("dot_start", self.dot_start)
+        arr("dot_term", self.dot_term.view(np.uint32), "unsigned")
         out.append("static const double lit[%d] = {%s};" % (
             len(self.literals), ",".join(_hexfloat(v) for v in self.literals)))
         out.append("}  // namespace gcmech_tables")

@@ -47,10 +47,11 @@ extern "C" {
 /* gc_kpp_ctx_set_option keys */
 #define GC_KPP_OPT_ARITH 1        /* 0 = fast (FMA, reciprocal pivots), 1 = strict (reference order, no FMA) */
 #define GC_KPP_OPT_SCHEDULE 2     /* 0 = plain (thread per cell), 1 = persistent work queue */
-#define GC_KPP_OPT_BLOCK 3        /* threads per block (multiple of 32), 0 = default */
+#define GC_KPP_OPT_BLOCK 3        /* threads per block (32, 64, 96 or 128), 0 = default 128 */
 #define GC_KPP_OPT_BLOCKS_PER_SM 4 /* queue schedule: resident blocks per SM, 0 = default */
 #define GC_KPP_OPT_MAX_SLOTS 5    /* cap on workspace slots (cells in flight), 0 = no cap */
 #define GC_KPP_OPT_TIMING 6       /* 1 = time the Rosenbrock launches with CUDA events */
+#define GC_KPP_OPT_LU 7           /* 0 = row-wise LU (default), 1 = KppDecomp right-looking order */
 
 /* Per-cell meteorology/state fields of gc_kpp_update_rconst_batch (rows of
  * `met`), the thread-private globals that Set_Kpp_GridBox_Values and the

@@ -124,12 +124,26 @@ def _tables_fun(t, V, F, RCT):
             return aux[code - t.nvar]
         return lit[code - t.lit0]
 
+    Y = list(V) + list(F)
+    auxp = list(RCT) + list(t.pre_literals)
+
     def product(p):
-        s, e = t.prod_start[p], t.prod_start[p + 1]
-        acc = operand(t.prod_fac[s])
-        for i in range(s + 1, e):
-            acc = acc * operand(t.prod_fac[i])
-        return acc
+        # packed form used by the CUDA engine: pre [* 2] * s1 * s2 * s3
+        x, y = (int(v) for v in t.prod_packed[p])
+        a = auxp[x & 0xFFF]
+        if x & 0x1000:
+            a = a * 2.0
+        for k, s in enumerate((x >> 16, y & 0xFFFF, y >> 16)):
+            if k < ((x >> 13) & 3):
+                a = a * Y[s]
+        # the generic factor-list form agrees bit for bit
+        s0, e0 = t.prod_start[p], t.prod_start[p + 1]
+        if e0 > s0:
+            acc = operand(t.prod_fac[s0])
+            for i in range(s0 + 1, e0):
+                acc = acc * operand(t.prod_fac[i])
+            assert acc == a or (acc != acc and a != a)
+        return a
 
     def csum(terms, s, e, X):
         acc = None
@@ -173,6 +187,17 @@ def test_product_tables_reproduce_oracle(ir, orc, point):
                 tt, ss = int(u) >> 16, int(u) & 0xFFFF
                 g[tt] = g[tt] + a * g[ss]
     assert np.array_equal(np.array(g), ref)
+    # row-wise dot-product form (decomp_rows): same updates, same order
+    h = [0.0] * t.lu_nonzero
+    for k in range(t.nvar):
+        for e in range(t.crow[k], t.crow[k + 1]):
+            acc = G[e]
+            for u in t.dot_term[t.dot_start[e]:t.dot_start[e + 1]].view(np.uint32):
+                acc = acc - h[int(u) >> 16] * h[int(u) & 0xFFFF]
+            if e < t.diag[k]:
+                acc = acc / h[t.diag[t.icol[e]]]
+            h[e] = acc
+    assert np.array_equal(np.array(h), ref)
 
 
 def test_flop_counts(ir):
