@@ -41,6 +41,8 @@ def _units():
         (k, "kpp_kernels_fast.o", ["-DGCKPP_STRICT=0"]),
         (os.path.join(CSRC, "kpp_rates.cu"), "kpp_rates.o", []),
         (os.path.join(CSRC, "kpp_util.cu"), "kpp_util.o", []),
+        (os.path.join(CSRC, "kpp_mlp.cu"), "kpp_mlp.o", []),
+        (os.path.join(CSRC, "gckpp_mlp_capi.cu"), "gckpp_mlp_capi.o", []),
         (os.path.join(CSRC, "gckpp_capi.cu"), "gckpp_capi.o", []),
     ]
 
@@ -59,7 +61,7 @@ def build(verbose=False, force=False):
     rates_program.write_generated(GEN)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
     deps += [os.path.join(GEN, f) for f in os.listdir(GEN)]
-    deps.append(os.path.join(PKG, "..", "include", "gckpp_gb300.h"))
+    deps += [os.path.join(PKG, "..", "include", f) for f in ("gckpp_gb300.h", "gckpp_gb300_mlp.h")]
     exe = nvcc()
     procs = []
     objs = []

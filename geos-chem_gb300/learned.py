@@ -1,0 +1,237 @@
+"""Learned step-size / stiffness proposer: host side.
+
+A 56 -> 128 -> 128 -> 5 MLP (GELU), BF16 weights with FP32 master copies,
+trained on the GPU by this package's own kernels (csrc/kpp_mlp.cu through
+include/gckpp_gb300_mlp.h).  Inputs are a cell's state: log T, log P, log
+H2O mixing ratio, cos SZA, 20 log J-values and 32 log key-species mixing
+ratios, normalised.  Outputs: log of a proposed initial step size H0 and
+logits of 4 stiffness bins.
+
+Training targets come from plain GPU integrations (``collect``): the
+integrator's own next-step prediction at the end of the step, RSTATUS(3)
+(Hnew, what GEOS-Chem carries to the next step as KPPHvalue), and the
+quartile bin of the step count ISTATUS(3).  The proposal seeds RCNTRL(3)
+(scaled down by ``h0_scale``) and orders the persistent solver's queue by
+predicted bin, heaviest first; error-controlled Rosenbrock still decides
+every step.
+
+torch tensors are used only as device allocations and streams.
+"""
+import ctypes
+import json
+
+import numpy as np
+
+from . import capi, inputs, mechanism
+
+NFEAT, HID, NOUT, NJ, NSPC, NBIN = 56, 128, 5, 20, 32, 4
+
+J_SPECIES = ["NO2", "O3", "O3", "HNO2", "H2O2", "HNO3", "HNO4", "NO3", "NO3", "N2O5", "CH2O", "CH2O", "MP",
+             "Cl2", "Br2", "BrO", "ClNO3", "HOBr", "MGLY", "ALD2"]
+KEY_SPECIES = ["O3", "NO", "NO2", "NO3", "N2O5", "HNO3", "HNO2", "HNO4", "OH", "HO2", "H2O2", "CO", "CH4", "CH2O",
+               "MP", "PAN", "ISOP", "ALD2", "ACET", "SO2", "DMS", "Cl", "ClO", "HCl", "HOCl", "Br", "BrO", "HBr",
+               "HOBr", "IO", "C2H6", "MVK"]
+
+
+def feature_rows(ir=None):
+    """(PHOTOL rows [20], species rows [32]) of the feature vector."""
+    ir = ir or mechanism.load_ir()
+    slots = inputs.photolysis_slots(ir)
+    by_sp = {}
+    for slot, sp in sorted(slots.items()):
+        by_sp.setdefault(sp, []).append(slot)
+    used = {}
+    jrows = []
+    for sp in J_SPECIES:
+        k = used.get(sp, 0)
+        jrows.append(by_sp[sp][min(k, len(by_sp[sp]) - 1)])
+        used[sp] = k + 1
+    srows = [ir["species"].index(s) for s in KEY_SPECIES]
+    assert len(jrows) == NJ and len(srows) == NSPC
+    return np.array(jrows, np.int32), np.array(srows, np.int32)
+
+
+def _lib():
+    lib = capi.load_library()
+    vp, i32, i64, f32, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_float, ctypes.c_double
+    lib.gc_mlp_features.argtypes = [i32, vp, i64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp]
+    lib.gc_mlp_forward.argtypes = [i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.gc_mlp_loss.argtypes = [i32, vp, vp, vp, f32, vp, vp, vp]
+    lib.gc_mlp_backward.argtypes = [i32] + [vp] * 16 + [vp]
+    lib.gc_mlp_adam.argtypes = [i32, vp, vp, vp, vp, vp, f32, f32, f32, f32, i32, vp]
+    lib.gc_mlp_propose.argtypes = [i32, vp, f64, f64, f64, vp, vp, vp]
+    lib.gc_mlp_bin_order.argtypes = [i32, vp, vp, vp, vp, vp]
+    return lib
+
+
+def _p(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError("%s failed (%d)" % (what, rc))
+
+
+class Proposer:
+    """MLP parameters, optimiser state and the GPU kernels that use them."""
+
+    def __init__(self, device=0, seed=0, h0_scale=0.5):
+        import torch
+
+        self.torch = torch
+        self.dev = torch.device("cuda", device)
+        self.lib = _lib()
+        rng = np.random.default_rng(seed)
+        shapes = {"w1": (HID, NFEAT), "w2": (HID, HID), "w3": (NOUT, HID)}
+        self.master = {}
+        for k, (n, m) in shapes.items():
+            w = rng.normal(0.0, np.sqrt(2.0 / (n + m)), (n, m)).astype(np.float32)
+            self.master[k] = torch.tensor(w, device=self.dev)
+        for k, n in (("b1", HID), ("b2", HID), ("b3", NOUT)):
+            self.master[k] = torch.zeros(n, dtype=torch.float32, device=self.dev)
+        self.bf = {k: self.master[k].to(torch.bfloat16) for k in ("w1", "w2", "w3")}
+        self.grad = {k: torch.zeros_like(v) for k, v in self.master.items()}
+        self.m1 = {k: torch.zeros_like(v) for k, v in self.master.items()}
+        self.m2 = {k: torch.zeros_like(v) for k, v in self.master.items()}
+        self.step_count = 0
+        jrows, srows = feature_rows()
+        self.jrows = torch.tensor(jrows, device=self.dev)
+        self.srows = torch.tensor(srows, device=self.dev)
+        self.mean = torch.zeros(NFEAT, dtype=torch.float64, device=self.dev)
+        self.inv_std = torch.ones(NFEAT, dtype=torch.float64, device=self.dev)
+        self.h0_scale = h0_scale
+        self.bin_edges = [0.0, 0.0, 0.0]
+        self.y_mean = 0.0
+
+    # -- features -----------------------------------------------------------
+    def features(self, met, photol, c, suncos=None, stream=None):
+        n = c.shape[1]
+        x = self.torch.empty((n, NFEAT), dtype=self.torch.float32, device=self.dev)
+        _check(self.lib.gc_mlp_features(n, _p(met), met.stride(0), _p(photol), photol.stride(0), _p(c), c.stride(0),
+                                        _p(suncos), _p(self.jrows), _p(self.srows), _p(self.mean), _p(self.inv_std),
+                                        _p(x), stream), "features")
+        return x
+
+    def fit_normalisation(self, met, photol, c, suncos=None):
+        self.mean.zero_()
+        self.inv_std.fill_(1.0)
+        x = self.features(met, photol, c, suncos).double()
+        self.mean = x.mean(0).contiguous()
+        self.inv_std = (1.0 / x.std(0).clamp_min(1e-6)).contiguous()
+
+    # -- forward / backward -------------------------------------------------
+    def _acts(self, M, train):
+        t = self.torch
+        f = lambda *s: t.empty(s, dtype=t.float32, device=self.dev)
+        return {"z1": f(M, HID) if train else None, "h1": f(M, HID), "z2": f(M, HID) if train else None,
+                "h2": f(M, HID), "out": f(M, NOUT)}
+
+    def forward(self, x, train=False, stream=None):
+        M = x.shape[0]
+        a = self._acts(M, train)
+        m, b = self.master, self.bf
+        _check(self.lib.gc_mlp_forward(M, _p(x), _p(b["w1"]), _p(m["b1"]), _p(b["w2"]), _p(m["b2"]), _p(b["w3"]),
+                                       _p(m["b3"]), _p(a["z1"]), _p(a["h1"]), _p(a["z2"]), _p(a["h2"]), _p(a["out"]),
+                                       stream), "forward")
+        return a
+
+    def loss_grad(self, x, y_h, y_bin, w_ce=0.5):
+        """Forward + loss + backward; gradients accumulate into self.grad."""
+        t = self.torch
+        M = x.shape[0]
+        a = self.forward(x, train=True)
+        dout = t.empty((M, NOUT), dtype=t.float32, device=self.dev)
+        loss = t.zeros(1, dtype=t.float32, device=self.dev)
+        _check(self.lib.gc_mlp_loss(M, _p(a["out"]), _p(y_h), _p(y_bin), float(w_ce), _p(dout), _p(loss), None),
+               "loss")
+        scratch = t.empty(M * (NOUT + 4 * HID), dtype=t.float32, device=self.dev)
+        g, b = self.grad, self.bf
+        _check(self.lib.gc_mlp_backward(M, _p(x), _p(b["w1"]), _p(b["w2"]), _p(b["w3"]), _p(a["z1"]), _p(a["h1"]),
+                                        _p(a["z2"]), _p(a["h2"]), _p(dout), _p(g["w1"]), _p(g["b1"]), _p(g["w2"]),
+                                        _p(g["b2"]), _p(g["w3"]), _p(g["b3"]), _p(scratch), None), "backward")
+        return loss, a
+
+    def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        self.step_count += 1
+        for k, w in self.master.items():
+            _check(self.lib.gc_mlp_adam(w.numel(), _p(w), _p(self.bf.get(k)), _p(self.grad[k]), _p(self.m1[k]),
+                                        _p(self.m2[k]), lr, b1, b2, eps, self.step_count, None), "adam")
+
+    # -- training -------------------------------------------------------------
+    def targets(self, rstatus, istatus):
+        """log(Hnew) (centred) and the step-count quartile bin."""
+        t = self.torch
+        h = t.log(rstatus[2].clamp_min(1e-10)).float() - self.y_mean
+        steps = istatus[2].double()
+        e = t.tensor(self.bin_edges, dtype=t.float64, device=self.dev)
+        b = t.bucketize(steps, e, right=True).int()
+        return h.contiguous(), b.contiguous()
+
+    def fit_targets(self, rstatus, istatus):
+        t = self.torch
+        self.y_mean = float(t.log(rstatus[2].clamp_min(1e-10)).mean().item())
+        q = t.quantile(istatus[2].double()[:1_000_000], t.tensor([0.25, 0.5, 0.75], dtype=t.float64,
+                                                                  device=self.dev))
+        self.bin_edges = [float(v) for v in q.tolist()]
+
+    def train(self, x, y_h, y_bin, epochs=4, batch=4096, lr=2e-3, w_ce=0.5, seed=0, log=None):
+        t = self.torch
+        n = x.shape[0]
+        gen = t.Generator(device=self.dev)
+        gen.manual_seed(seed)
+        hist = []
+        for ep in range(epochs):
+            perm = t.randperm(n, device=self.dev, generator=gen)
+            tot = t.zeros(1, dtype=t.float32, device=self.dev)
+            nb = 0
+            lr_ep = lr * (0.5 ** ep)
+            for s in range(0, n - batch + 1, batch):
+                idx = perm[s:s + batch]
+                loss, _ = self.loss_grad(x[idx].contiguous(), y_h[idx].contiguous(), y_bin[idx].contiguous(), w_ce)
+                self.adam_step(lr_ep)
+                tot += loss
+                nb += 1
+            hist.append(float((tot / max(nb, 1)).item()))
+            if log:
+                log("epoch %d loss %.4f" % (ep, hist[-1]))
+        return hist
+
+    # -- inference ------------------------------------------------------------
+    def propose(self, x, hmin=1e-5, hmax=1.0e9, stream=None):
+        t = self.torch
+        M = x.shape[0]
+        a = self.forward(x, stream=stream)
+        a["out"][:, 0] += self.y_mean
+        h0 = t.empty(M, dtype=t.float64, device=self.dev)
+        b = t.empty(M, dtype=t.int32, device=self.dev)
+        _check(self.lib.gc_mlp_propose(M, _p(a["out"]), float(self.h0_scale), hmin, hmax, _p(h0), _p(b), stream),
+               "propose")
+        return h0, b
+
+    def bin_order(self, bins, stream=None):
+        t = self.torch
+        M = bins.shape[0]
+        order = t.empty(M, dtype=t.int32, device=self.dev)
+        counts = t.empty(NBIN, dtype=t.int32, device=self.dev)
+        cursor = t.empty(NBIN, dtype=t.int32, device=self.dev)
+        _check(self.lib.gc_mlp_bin_order(M, _p(bins), _p(counts), _p(cursor), _p(order), stream), "bin_order")
+        return order
+
+    # -- persistence -----------------------------------------------------------
+    def state(self):
+        d = {k: v.cpu().numpy() for k, v in self.master.items()}
+        d.update(mean=self.mean.cpu().numpy(), inv_std=self.inv_std.cpu().numpy())
+        d["meta"] = np.array(json.dumps({"h0_scale": self.h0_scale, "bin_edges": self.bin_edges,
+                                         "y_mean": self.y_mean}))
+        return d
+
+    def load_state(self, d):
+        t = self.torch
+        for k in ("w1", "w2", "w3", "b1", "b2", "b3"):
+            self.master[k] = t.tensor(d[k], dtype=t.float32, device=self.dev)
+        self.bf = {k: self.master[k].to(t.bfloat16) for k in ("w1", "w2", "w3")}
+        self.mean = t.tensor(d["mean"], dtype=t.float64, device=self.dev)
+        self.inv_std = t.tensor(d["inv_std"], dtype=t.float64, device=self.dev)
+        meta = json.loads(str(d["meta"]))
+        self.h0_scale, self.bin_edges, self.y_mean = meta["h0_scale"], meta["bin_edges"], meta["y_mean"]

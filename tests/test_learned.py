@@ -1,0 +1,95 @@
+"""Learned proposer: CPU oracle self-consistency, GPU kernels against the
+oracle (forward, loss, gradients), and training reducing the loss."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import mlp_oracle  # noqa: E402
+
+
+def _params(seed=0, scale=0.3):
+    rng = np.random.default_rng(seed)
+    p = {"w1": rng.normal(0, scale, (128, 56)).astype(np.float32), "w2": rng.normal(0, scale / 2, (128, 128)).astype(np.float32),
+         "w3": rng.normal(0, scale, (5, 128)).astype(np.float32), "b1": rng.normal(0, 0.1, 128).astype(np.float32),
+         "b2": rng.normal(0, 0.1, 128).astype(np.float32), "b3": rng.normal(0, 0.1, 5).astype(np.float32)}
+    return p
+
+
+def _batch(M=96, seed=1):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0, 1, (M, 56)).astype(np.float32)
+    y = rng.normal(0, 1, M).astype(np.float32)
+    b = rng.integers(0, 4, M).astype(np.int32)
+    return x, y, b
+
+
+def test_oracle_gradients_match_finite_differences():
+    p = _params()
+    x, y, b = _batch(16)
+    loss, g, _ = mlp_oracle.loss_and_grads(x.astype(np.float64), y, b, p)
+    # perturb biases (weights are bf16-rounded, so finite differences on them
+    # would see the rounding steps)
+    for k in ("b1", "b2", "b3"):
+        for i in (0, 3):
+            q = {kk: vv.copy() for kk, vv in p.items()}
+            h = 1e-3
+            q[k] = q[k].astype(np.float64)
+            q[k][i] += h
+            lp, _, _ = mlp_oracle.loss_and_grads(x.astype(np.float64), y, b, q)
+            q[k][i] -= 2 * h
+            lm, _, _ = mlp_oracle.loss_and_grads(x.astype(np.float64), y, b, q)
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - g[k][i]) <= 1e-5 + 1e-3 * abs(fd), (k, i, fd, g[k][i])
+
+
+def test_bf16_rounding_is_nearest_even():
+    v = np.array([1.0, 1.00390625, 1.005859375, -3.1415926], np.float32)
+    r = mlp_oracle.bf16(v)
+    assert r[0] == 1.0 and r[1] == 1.0 and abs(r[3] + 3.140625) < 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_forward_and_gradients_match_oracle():
+    import torch
+    import gcchem.learned as learned
+
+    pr = learned.Proposer(0)
+    p = _params()
+    for k, v in p.items():
+        pr.master[k] = torch.tensor(v, device=pr.dev)
+    pr.bf = {k: pr.master[k].to(torch.bfloat16) for k in ("w1", "w2", "w3")}
+    for k in pr.grad:
+        pr.grad[k] = torch.zeros_like(pr.master[k])
+    x, y, b = _batch(200)
+    xt = torch.tensor(x, device=pr.dev)
+    loss, a = pr.loss_grad(xt, torch.tensor(y, device=pr.dev), torch.tensor(b, device=pr.dev), w_ce=0.5)
+    loss_ref, g_ref, f_ref = mlp_oracle.loss_and_grads(x.astype(np.float64), y, b, p, w_ce=0.5)
+    out = a["out"].cpu().numpy()
+    assert np.max(np.abs(out - f_ref["out"])) < 1e-3 * max(1.0, np.max(np.abs(f_ref["out"])))
+    assert abs(loss.item() - loss_ref) < 1e-4 * max(1.0, loss_ref)
+    for k in ("w1", "b1", "w2", "b2", "w3", "b3"):
+        gg = pr.grad[k].cpu().numpy()
+        ref = g_ref[k]
+        scale = np.max(np.abs(ref)) + 1e-12
+        assert np.max(np.abs(gg - ref)) / scale < 2e-3, k
+
+
+@pytest.mark.gpu
+def test_gpu_training_reduces_loss():
+    import torch
+    import gcchem.learned as learned
+
+    rng = np.random.default_rng(5)
+    M = 16384
+    x = rng.normal(0, 1, (M, 56)).astype(np.float32)
+    w = rng.normal(0, 1, 56)
+    y = (x @ w / 8.0 + 0.3 * np.sin(x[:, 0])).astype(np.float32)
+    b = np.digitize(x[:, 1] + x[:, 2], [-1.0, 0.0, 1.0]).astype(np.int32)
+    pr = learned.Proposer(0, seed=3)
+    t = lambda a: torch.tensor(a, device=pr.dev)
+    hist = pr.train(t(x), t(y), t(b), epochs=3, batch=1024, lr=2e-3)
+    assert hist[-1] < 0.5 * hist[0], hist
