@@ -37,8 +37,10 @@ def lib_path():
 def _units():
     k = os.path.join(CSRC, "kpp_kernels.cu")
     return [
-        (k, "kpp_kernels_strict.o", ["-DGCKPP_STRICT=1", "-fmad=false"]),
-        (k, "kpp_kernels_fast.o", ["-DGCKPP_STRICT=0"]),
+        (k, "kpp_kernels_strict.o", ["-DGCKPP_STRICT=1", "-DGCKPP_VARIANT=strict", "-fmad=false"]),
+        (k, "kpp_kernels_fast.o", ["-DGCKPP_STRICT=0", "-DGCKPP_VARIANT=fast"]),
+        (k, "kpp_kernels_fastcg.o", ["-DGCKPP_STRICT=0", "-DGCKPP_VARIANT=fastcg", "-DGCKPP_LDCG=1"]),
+        (k, "kpp_kernels_fast128.o", ["-DGCKPP_STRICT=0", "-DGCKPP_VARIANT=fast128", "-DGCKPP_MAX_THREADS=512"]),
         (os.path.join(CSRC, "kpp_rates.cu"), "kpp_rates.o", []),
         (os.path.join(CSRC, "kpp_util.cu"), "kpp_util.o", []),
         (os.path.join(CSRC, "kpp_mlp.cu"), "kpp_mlp.o", []),

@@ -115,7 +115,7 @@ class Solver:
 
     def set(self, arith=None, schedule=None, block=None, blocks_per_sm=None, max_slots=None):
         if arith is not None:
-            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1}[arith]))
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1, "fastcg": 2, "fast128": 3}[arith]))
         if schedule is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_SCHEDULE, {"plain": 0, "queue": 1}[schedule]))
         if block is not None:

@@ -21,6 +21,7 @@
 #include "kpp_launch.h"
 #include "kpp_util.h"
 #include "kpp_rosenbrock.cuh"
+#include "ros_methods.h"
 
 using namespace gckpp;
 namespace T = gcmech_tables;
@@ -55,166 +56,6 @@ cudaError_t upload(const X* host, size_t n, const X** dev, std::vector<void*>& o
   e = cudaMemcpy(p, host, n * sizeof(X), cudaMemcpyHostToDevice);
   *dev = static_cast<const X*>(p);
   return e;
-}
-
-// Rosenbrock method coefficients (gckpp_Integrator.F90 Ros2 :2062, Ros3
-// :2112, Ros4 :2167, Rodas3 :2239, Rodas4 :2306, Rang3 :2398).
-bool method_table(int id, RosMethod& r) {
-  std::memset(&r, 0, sizeof(r));
-  switch (id) {
-    case 1: {  // Ros2
-      const double g = 1.0 + 1.0 / std::sqrt(2.0);
-      r.S = 2;
-      r.A[0] = (1.0) / g;
-      r.C[0] = (-2.0) / g;
-      r.NewF[0] = 1; r.NewF[1] = 1;
-      r.M[0] = (3.0) / (2.0 * g);
-      r.M[1] = (1.0) / (2.0 * g);
-      r.E[0] = 1.0 / (2.0 * g);
-      r.E[1] = 1.0 / (2.0 * g);
-      r.ELO = 2.0;
-      r.Alpha[0] = 0.0; r.Alpha[1] = 1.0;
-      r.Gamma[0] = g; r.Gamma[1] = -g;
-      return true;
-    }
-    case 2: {  // Ros3
-      r.S = 3;
-      r.A[0] = 1.0; r.A[1] = 1.0; r.A[2] = 0.0;
-      r.C[0] = -0.10156171083877702091975600115545E+01;
-      r.C[1] = 0.40759956452537699824805835358067E+01;
-      r.C[2] = 0.92076794298330791242156818474003E+01;
-      r.NewF[0] = 1; r.NewF[1] = 1; r.NewF[2] = 0;
-      r.M[0] = 0.1E+01;
-      r.M[1] = 0.61697947043828245592553615689730E+01;
-      r.M[2] = -0.42772256543218573326238373806514;
-      r.E[0] = 0.5;
-      r.E[1] = -0.29079558716805469821718236208017E+01;
-      r.E[2] = 0.22354069897811569627360909276199;
-      r.ELO = 3.0;
-      r.Alpha[0] = 0.0;
-      r.Alpha[1] = 0.43586652150845899941601945119356;
-      r.Alpha[2] = 0.43586652150845899941601945119356;
-      r.Gamma[0] = 0.43586652150845899941601945119356;
-      r.Gamma[1] = 0.24291996454816804366592249683314;
-      r.Gamma[2] = 0.21851380027664058511513169485832E+01;
-      return true;
-    }
-    case 3: {  // Ros4
-      r.S = 4;
-      r.A[0] = 0.2000000000000000E+01;
-      r.A[1] = 0.1867943637803922E+01;
-      r.A[2] = 0.2344449711399156;
-      r.A[3] = r.A[1];
-      r.A[4] = r.A[2];
-      r.A[5] = 0.0;
-      r.C[0] = -0.7137615036412310E+01;
-      r.C[1] = 0.2580708087951457E+01;
-      r.C[2] = 0.6515950076447975;
-      r.C[3] = -0.2137148994382534E+01;
-      r.C[4] = -0.3214669691237626;
-      r.C[5] = -0.6949742501781779;
-      r.NewF[0] = 1; r.NewF[1] = 1; r.NewF[2] = 1; r.NewF[3] = 0;
-      r.M[0] = 0.2255570073418735E+01;
-      r.M[1] = 0.2870493262186792;
-      r.M[2] = 0.4353179431840180;
-      r.M[3] = 0.1093502252409163E+01;
-      r.E[0] = -0.2815431932141155;
-      r.E[1] = -0.7276199124938920E-01;
-      r.E[2] = -0.1082196201495311;
-      r.E[3] = -0.1093502252409163E+01;
-      r.ELO = 4.0;
-      r.Alpha[0] = 0.0;
-      r.Alpha[1] = 0.1145640000000000E+01;
-      r.Alpha[2] = 0.6552168638155900;
-      r.Alpha[3] = r.Alpha[2];
-      r.Gamma[0] = 0.5728200000000000;
-      r.Gamma[1] = -0.1769193891319233E+01;
-      r.Gamma[2] = 0.7592633437920482;
-      r.Gamma[3] = -0.1049021087100450;
-      return true;
-    }
-    case 0:
-    case 4: {  // Rodas3
-      r.S = 4;
-      r.A[0] = 0.0; r.A[1] = 2.0; r.A[2] = 0.0; r.A[3] = 2.0; r.A[4] = 0.0; r.A[5] = 1.0;
-      r.C[0] = 4.0; r.C[1] = 1.0; r.C[2] = -1.0; r.C[3] = 1.0; r.C[4] = -1.0;
-      r.C[5] = -(8.0 / 3.0);
-      r.NewF[0] = 1; r.NewF[1] = 0; r.NewF[2] = 1; r.NewF[3] = 1;
-      r.M[0] = 2.0; r.M[1] = 0.0; r.M[2] = 1.0; r.M[3] = 1.0;
-      r.E[0] = 0.0; r.E[1] = 0.0; r.E[2] = 0.0; r.E[3] = 1.0;
-      r.ELO = 3.0;
-      r.Alpha[0] = 0.0; r.Alpha[1] = 0.0; r.Alpha[2] = 1.0; r.Alpha[3] = 1.0;
-      r.Gamma[0] = 0.5; r.Gamma[1] = 1.5; r.Gamma[2] = 0.0; r.Gamma[3] = 0.0;
-      return true;
-    }
-    case 5: {  // Rodas4
-      r.S = 6;
-      r.Alpha[0] = 0.000; r.Alpha[1] = 0.386; r.Alpha[2] = 0.210;
-      r.Alpha[3] = 0.630; r.Alpha[4] = 1.000; r.Alpha[5] = 1.000;
-      r.Gamma[0] = 0.2500000000000000;
-      r.Gamma[1] = -0.1043000000000000;
-      r.Gamma[2] = 0.1035000000000000;
-      r.Gamma[3] = -0.3620000000000023E-01;
-      r.Gamma[4] = 0.0;
-      r.Gamma[5] = 0.0;
-      r.A[0] = 0.1544000000000000E+01;
-      r.A[1] = 0.9466785280815826;
-      r.A[2] = 0.2557011698983284;
-      r.A[3] = 0.3314825187068521E+01;
-      r.A[4] = 0.2896124015972201E+01;
-      r.A[5] = 0.9986419139977817;
-      r.A[6] = 0.1221224509226641E+01;
-      r.A[7] = 0.6019134481288629E+01;
-      r.A[8] = 0.1253708332932087E+02;
-      r.A[9] = -0.6878860361058950;
-      r.A[10] = r.A[6];
-      r.A[11] = r.A[7];
-      r.A[12] = r.A[8];
-      r.A[13] = r.A[9];
-      r.A[14] = 1.0;
-      r.C[0] = -0.5668800000000000E+01;
-      r.C[1] = -0.2430093356833875E+01;
-      r.C[2] = -0.2063599157091915;
-      r.C[3] = -0.1073529058151375;
-      r.C[4] = -0.9594562251023355E+01;
-      r.C[5] = -0.2047028614809616E+02;
-      r.C[6] = 0.7496443313967647E+01;
-      r.C[7] = -0.1024680431464352E+02;
-      r.C[8] = -0.3399990352819905E+02;
-      r.C[9] = 0.1170890893206160E+02;
-      r.C[10] = 0.8083246795921522E+01;
-      r.C[11] = -0.7981132988064893E+01;
-      r.C[12] = -0.3152159432874371E+02;
-      r.C[13] = 0.1631930543123136E+02;
-      r.C[14] = -0.6058818238834054E+01;
-      r.M[0] = r.A[6]; r.M[1] = r.A[7]; r.M[2] = r.A[8]; r.M[3] = r.A[9];
-      r.M[4] = 1.0; r.M[5] = 1.0;
-      r.E[5] = 1.0;
-      for (int i = 0; i < 6; ++i) r.NewF[i] = 1;
-      r.ELO = 4.0;
-      return true;
-    }
-    case 6: {  // Rang3
-      r.S = 4;
-      r.A[0] = 5.09052051067020e+00; r.A[1] = 5.09052051067020e+00; r.A[2] = 0.0;
-      r.A[3] = 4.97628111010787e+00; r.A[4] = 2.77268164715849e-02; r.A[5] = 2.29428036027904e-01;
-      r.C[0] = -1.16790812312283e+01; r.C[1] = -1.64057326467367e+01; r.C[2] = -2.77268164715850e-01;
-      r.C[3] = -8.38103960500476e+00; r.C[4] = -8.48328409199343e-01; r.C[5] = 2.87009860433106e-01;
-      r.M[0] = 5.22582761233094e+00; r.M[1] = -5.56971148154165e-01;
-      r.M[2] = 3.57979469353645e-01; r.M[3] = 1.72337398521064e+00;
-      r.E[0] = -5.16845212784040e+00; r.E[1] = -1.26351942603842e+00;
-      r.E[2] = -1.11022302462516e-16; r.E[3] = 2.22044604925031e-16;
-      r.Alpha[0] = 0.0; r.Alpha[1] = 2.21878746765329e+00;
-      r.Alpha[2] = 2.21878746765329e+00; r.Alpha[3] = 1.55392337535788e+00;
-      r.Gamma[0] = 4.35866521508459e-01; r.Gamma[1] = -1.78292094614483e+00;
-      r.Gamma[2] = -2.46541900496934e+00; r.Gamma[3] = -8.05529997906370e-01;
-      for (int i = 0; i < 4; ++i) r.NewF[i] = 1;
-      r.ELO = 3.0;
-      return true;
-    }
-    default:
-      return false;
-  }
 }
 
 WsLayout make_layout() {
@@ -356,7 +197,7 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
   if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
   switch (key) {
     case GC_KPP_OPT_ARITH:
-      if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "arith must be 0 or 1");
+      if (v < 0 || v > 3) return fail(GC_KPP_EINVAL, "arith must be 0 (fast), 1 (strict), 2 (fast, L1 bypass) or 3 (fast, 128 registers)");
       c->arith = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_SCHEDULE:
@@ -365,7 +206,7 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
       return GC_KPP_OK;
     case GC_KPP_OPT_BLOCK:
       if (v == 0) v = 128;
-      if (v < 32 || v > 128 || v % 32) return fail(GC_KPP_EINVAL, "block must be a multiple of 32 in [32,128]");
+      if (v < 32 || v > 1024 || v % 32) return fail(GC_KPP_EINVAL, "block must be a multiple of 32 in [32,1024]");
       c->block = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_BLOCKS_PER_SM:
@@ -471,6 +312,27 @@ struct DevArgs {
   int* ierr;
 };
 
+// Kernel variant by GC_KPP_OPT_ARITH: 0 fast, 1 strict, 2 fast with L1
+// bypass for per-cell reads, 3 fast with a 128-register budget.
+cudaError_t variant_launch(int arith, int queue, int grid, int block, const MechDev& m, const RosMethod& r,
+                           const RosParams& p, cudaStream_t s) {
+  switch (arith) {
+    case 1: return gckpp_launch_ros_strict(queue, grid, block, m, r, p, s);
+    case 2: return gckpp_launch_ros_fastcg(queue, grid, block, m, r, p, s);
+    case 3: return gckpp_launch_ros_fast128(queue, grid, block, m, r, p, s);
+    default: return gckpp_launch_ros_fast(queue, grid, block, m, r, p, s);
+  }
+}
+
+cudaError_t variant_occupancy(int arith, int block, int* nblocks) {
+  switch (arith) {
+    case 1: return gckpp_occupancy_strict(1, block, nblocks);
+    case 2: return gckpp_occupancy_fastcg(1, block, nblocks);
+    case 3: return gckpp_occupancy_fast128(1, block, nblocks);
+    default: return gckpp_occupancy_fast(1, block, nblocks);
+  }
+}
+
 // Launch the Rosenbrock kernel over device arrays.
 int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, const DevArgs& a, cudaStream_t s,
                      int* launches) {
@@ -481,7 +343,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   if (queue) {
     int per_sm = c->blocks_per_sm;
     if (per_sm == 0) {
-      cudaError_t e = c->arith ? gckpp_occupancy_strict(1, block, &per_sm) : gckpp_occupancy_fast(1, block, &per_sm);
+      cudaError_t e = variant_occupancy(c->arith, block, &per_sm);
       if (e != cudaSuccess) return cuda_fail(e, "occupancy");
       per_sm = std::max(per_sm, 1);
     }
@@ -546,8 +408,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
       if (!c->ev[i]) GC_CUDA(cudaEventCreate(&c->ev[i]));
     GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed], s));
   }
-  cudaError_t e = c->arith ? gckpp_launch_ros_strict(queue, grid, block, c->mech, R.meth, p, s)
-                           : gckpp_launch_ros_fast(queue, grid, block, c->mech, R.meth, p, s);
+  cudaError_t e = variant_launch(c->arith, queue, grid, block, c->mech, R.meth, p, s);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
   if (timed) {
     GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed + 1], s));

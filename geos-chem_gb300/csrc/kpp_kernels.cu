@@ -1,34 +1,30 @@
-// Rosenbrock kernels, compiled twice: -DGCKPP_STRICT=1 with -fmad=false
-// (reference evaluation order, no contraction) and -DGCKPP_STRICT=0 (fast).
+// Rosenbrock kernels, compiled once per variant (build.py):
+//   strict   -DGCKPP_STRICT=1 -fmad=false   reference evaluation order
+//   fast     -DGCKPP_STRICT=0               FMA, reciprocal pivots
+//   fastcg   fast + per-cell reads bypass L1 (GCKPP_LDCG)
+//   fast128  fast with a 128-register budget (half the resident warps)
 #include "kpp_launch.h"
 #include "kpp_rosenbrock.cuh"
 
-#if GCKPP_STRICT
-#define GCKPP_ARITH true
-#define GCKPP_LAUNCH gckpp_launch_ros_strict
-#define GCKPP_OCC gckpp_occupancy_strict
-#else
-#define GCKPP_ARITH false
-#define GCKPP_LAUNCH gckpp_launch_ros_fast
-#define GCKPP_OCC gckpp_occupancy_fast
+#ifndef GCKPP_MAX_THREADS
+#define GCKPP_MAX_THREADS 1024  // 1024 threads x 64 registers fill an SM
 #endif
-
-#ifndef GCKPP_MAX_BLOCK
-#define GCKPP_MAX_BLOCK 128
+#ifndef GCKPP_VARIANT
+#define GCKPP_VARIANT fast
 #endif
-#ifndef GCKPP_MIN_BLOCKS
-#define GCKPP_MIN_BLOCKS 8
-#endif
+#define GCKPP_CAT2(a, b) a##b
+#define GCKPP_CAT(a, b) GCKPP_CAT2(a, b)
 
 namespace gckpp {
 
 template <bool QUEUE>
-__global__ void __launch_bounds__(GCKPP_MAX_BLOCK, GCKPP_MIN_BLOCKS) ros_kernel(MechDev m, RosMethod r, RosParams p) {
-  ros_driver<GCKPP_ARITH, QUEUE>(m, r, p);
+__global__ void __launch_bounds__(GCKPP_MAX_THREADS, 1) ros_kernel(MechDev m, RosMethod r, RosParams p) {
+  ros_driver<GCKPP_STRICT != 0, QUEUE>(m, r, p);
 }
 
-cudaError_t GCKPP_LAUNCH(int queue, int grid, int block, const MechDev& m, const RosMethod& r,
-                         const RosParams& p, cudaStream_t s) {
+cudaError_t GCKPP_CAT(gckpp_launch_ros_, GCKPP_VARIANT)(int queue, int grid, int block, const MechDev& m,
+                                                        const RosMethod& r, const RosParams& p, cudaStream_t s) {
+  if (block > GCKPP_MAX_THREADS) return cudaErrorInvalidConfiguration;
   if (queue)
     ros_kernel<true><<<grid, block, 0, s>>>(m, r, p);
   else
@@ -36,7 +32,7 @@ cudaError_t GCKPP_LAUNCH(int queue, int grid, int block, const MechDev& m, const
   return cudaGetLastError();
 }
 
-cudaError_t GCKPP_OCC(int queue, int block, int* nblocks) {
+cudaError_t GCKPP_CAT(gckpp_occupancy_, GCKPP_VARIANT)(int queue, int block, int* nblocks) {
   if (queue) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_kernel<true>, block, 0);
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_kernel<false>, block, 0);
 }

@@ -1,5 +1,5 @@
 // Host-side launch interface between the C ABI and the kernel translation
-// units (one per arithmetic mode).
+// units (one per arithmetic/code variant, see kpp_kernels.cu).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -7,10 +7,15 @@ namespace gckpp {
 struct MechDev;
 struct RosMethod;
 struct RosParams;
-cudaError_t gckpp_launch_ros_strict(int queue, int grid, int block, const MechDev& m, const RosMethod& r,
-                                    const RosParams& p, cudaStream_t s);
-cudaError_t gckpp_launch_ros_fast(int queue, int grid, int block, const MechDev& m, const RosMethod& r,
-                                  const RosParams& p, cudaStream_t s);
-cudaError_t gckpp_occupancy_strict(int queue, int block, int* nblocks);
-cudaError_t gckpp_occupancy_fast(int queue, int block, int* nblocks);
+
+#define GCKPP_DECLARE_VARIANT(name)                                                                        \
+  cudaError_t gckpp_launch_ros_##name(int queue, int grid, int block, const MechDev& m, const RosMethod& r, \
+                                      const RosParams& p, cudaStream_t s);                                 \
+  cudaError_t gckpp_occupancy_##name(int queue, int block, int* nblocks);
+
+GCKPP_DECLARE_VARIANT(strict)
+GCKPP_DECLARE_VARIANT(fast)
+GCKPP_DECLARE_VARIANT(fastcg)
+GCKPP_DECLARE_VARIANT(fast128)
+#undef GCKPP_DECLARE_VARIANT
 }  // namespace gckpp

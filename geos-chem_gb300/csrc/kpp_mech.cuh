@@ -50,6 +50,16 @@ struct MechDev {
 
 
 __device__ __forceinline__ int ldi(const int* p) { return __ldg(p); }
+
+// Per-cell workspace read.  With GCKPP_LDCG the read bypasses L1 (the tables
+// then keep L1 to themselves); otherwise it is an ordinary cached load.
+__device__ __forceinline__ double ldw(const double* p) {
+#if defined(GCKPP_LDCG) && GCKPP_LDCG
+  return __ldcg(p);
+#else
+  return *p;
+#endif
+}
 __device__ __forceinline__ unsigned ldu(const unsigned* p) { return __ldg(p); }
 
 // |x| < TINY(1.0_dp), on the bit pattern
@@ -64,9 +74,9 @@ __device__ __forceinline__ bool tiny_abs(double x) {
 // loads of consecutive products overlap.
 __device__ __forceinline__ double product(const MechDev& m, int p, const double* Y, const double* aux) {
   const uint2 t = __ldg(m.prod_packed + p);
-  double a = aux[(t.x & 0xfffu) * TS];
+  double a = ldw(aux + (t.x & 0xfffu) * TS);
   const unsigned ns = (t.x >> 13) & 3u;
-  const double v1 = Y[(t.x >> 16) * TS], v2 = Y[(t.y & 0xffffu) * TS], v3 = Y[(t.y >> 16) * TS];
+  const double v1 = ldw(Y + (t.x >> 16) * TS), v2 = ldw(Y + (t.y & 0xffffu) * TS), v3 = ldw(Y + (t.y >> 16) * TS);
   if (t.x & 0x1000u) a = a * 2.0;
   if (ns >= 1u) a = a * v1;
   if (ns >= 2u) a = a * v2;
@@ -86,7 +96,7 @@ __device__ __forceinline__ double term_sum(const MechDev& m, const unsigned* __r
   for (int i = s; i < e; ++i) {
     const unsigned t = ldu(terms + i);
     const double cf = __ldg(m.slit + (t >> 20));
-    const double x = X[(t & 0xfffffu) * TS];
+    const double x = ldw(X + (t & 0xfffffu) * TS);
     if (STRICT) {
       const double v = cf * x;
       acc = (i == s) ? (FLIP ? -v : v) : (FLIP ? acc - v : acc + v);
@@ -190,18 +200,18 @@ __device__ int decomp_rows(const MechDev& m, const double* __restrict__ J0, doub
   for (int k = 0; k < m.nvar; ++k) {
     const int e0 = ldi(m.lu_crow + k), e1 = ldi(m.lu_crow + k + 1), dk = ldi(m.lu_diag + k);
     for (int e = e0; e < e1; ++e) {
-      double acc = STRICT ? -J0[e * TS] : J0[e * TS];
+      double acc = STRICT ? -ldw(J0 + e * TS) : ldw(J0 + e * TS);
       if (e == dk) acc = acc + ghinv;
       const int t0 = ldi(m.dot_start + e), t1 = ldi(m.dot_start + e + 1);
 #pragma unroll 4
       for (int t = t0; t < t1; ++t) {
         const unsigned op = ldu(m.dot_term + t);
-        const double l = G[(op >> 16) * TS], u = G[(op & 0xffffu) * TS];
+        const double l = ldw(G + (op >> 16) * TS), u = ldw(G + (op & 0xffffu) * TS);
         acc = STRICT ? acc - l * u : fma(-l, u, acc);
       }
       if (e < dk) {
         const int dc = ldi(m.lu_diag + ldi(m.lu_icol + e));
-        acc = STRICT ? acc / G[dc * TS] : acc * G[dc * TS];  // fast: diag holds 1/pivot
+        acc = STRICT ? acc / ldw(G + dc * TS) : acc * ldw(G + dc * TS);  // fast: diag holds 1/pivot
       } else if (e == dk && !STRICT) {
         acc = 1.0 / acc;
       }
@@ -220,7 +230,7 @@ __device__ void solve(const MechDev& m, const double* __restrict__ G, double* __
       double x = X[i * TS];
 #pragma unroll 4
       for (int kk = s; kk < d; ++kk) {
-        const double g = G[kk * TS], y = X[ldi(m.lu_icol + kk) * TS];
+        const double g = ldw(G + kk * TS), y = ldw(X + ldi(m.lu_icol + kk) * TS);
         x = STRICT ? x - g * y : fma(-g, y, x);
       }
       X[i * TS] = x;
@@ -231,7 +241,7 @@ __device__ void solve(const MechDev& m, const double* __restrict__ G, double* __
     double x = X[i * TS];
 #pragma unroll 4
     for (int kk = d + 1; kk < e; ++kk) {
-      const double g = G[kk * TS], y = X[ldi(m.lu_icol + kk) * TS];
+      const double g = ldw(G + kk * TS), y = ldw(X + ldi(m.lu_icol + kk) * TS);
       x = STRICT ? x - g * y : fma(-g, y, x);
     }
     X[i * TS] = STRICT ? x / G[d * TS] : x * G[d * TS];

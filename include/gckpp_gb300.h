@@ -45,9 +45,10 @@ extern "C" {
 #define GC_KPP_MEM_DEVICE 1
 
 /* gc_kpp_ctx_set_option keys */
-#define GC_KPP_OPT_ARITH 1        /* 0 = fast (FMA, reciprocal pivots), 1 = strict (reference order, no FMA) */
+#define GC_KPP_OPT_ARITH 1        /* 0 = fast (FMA, reciprocal pivots), 1 = strict (reference order, no FMA),
+                                     2 = fast with L1-bypassing workspace reads, 3 = fast, 128 registers */
 #define GC_KPP_OPT_SCHEDULE 2     /* 0 = plain (thread per cell), 1 = persistent work queue */
-#define GC_KPP_OPT_BLOCK 3        /* threads per block (32, 64, 96 or 128), 0 = default 128 */
+#define GC_KPP_OPT_BLOCK 3        /* threads per block (multiple of 32, <= 1024; <= 512 for arith 3), 0 = default 128 */
 #define GC_KPP_OPT_BLOCKS_PER_SM 4 /* queue schedule: resident blocks per SM, 0 = default */
 #define GC_KPP_OPT_MAX_SLOTS 5    /* cap on workspace slots (cells in flight), 0 = no cap */
 #define GC_KPP_OPT_TIMING 6       /* 1 = time the Rosenbrock launches with CUDA events */
