@@ -39,6 +39,10 @@ EXPORTED = [
     "gc_kpp_last_error",
     "gc_kpp_integrate_batch",
     "gc_kpp_update_rconst_batch",
+    "gc_kpp_fullchem_step",
+    "gc_kpp_fullchem_step_ordered",
+    "gc_kpp_last_launch_count",
+    "gc_kpp_last_kernel_ms",
 ]
 
 _lib = None
@@ -115,7 +119,7 @@ class Solver:
 
     def set(self, arith=None, schedule=None, block=None, blocks_per_sm=None, max_slots=None):
         if arith is not None:
-            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1, "fastcg": 2, "fast128": 3}[arith]))
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1, "fast1": 2, "fast4": 3}[arith]))
         if schedule is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_SCHEDULE, {"plain": 0, "queue": 1}[schedule]))
         if block is not None:
@@ -163,6 +167,39 @@ class Solver:
             rcntrl.ctypes.data_as(ctypes.c_void_p) if rcntrl is not None else None,
             _ptr(hstart), _ptr(istatus), _ptr(rstatus), ldo, _ptr(ierr), mem, s)
         self._check(rc)
+
+    def fullchem_step(self, dt, met, photol, c, atol, rtol, icntrl=None, rcntrl=None, hstart=None, istatus=None,
+                      rstatus=None, ierr=None, order=None, stream=None):
+        """One Do_FullChem chemistry step over all cells (gc_kpp_fullchem_step,
+        or gc_kpp_fullchem_step_ordered when a queue ``order`` is given).
+        Returns the number of cells integrated a second time (retry)."""
+        lib = self.lib
+        if not getattr(lib, "_step_typed", False):
+            vp, i32, i64, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
+            head = [vp, i32, f64, vp, i64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64, vp, vp]
+            lib.gc_kpp_fullchem_step.argtypes = head + [i32, vp]
+            lib.gc_kpp_fullchem_step_ordered.argtypes = head + [vp, i32, vp]
+            lib._step_typed = True
+        dev = _is_torch(c) and c.is_cuda
+        ncell = c.shape[1]
+        icn = np.ascontiguousarray(icntrl if icntrl is not None else np.zeros(20), dtype=np.int32)
+        rcn = np.ascontiguousarray(rcntrl if rcntrl is not None else np.zeros(20), dtype=np.float64)
+        nretry = ctypes.c_int(0)
+        ldo = _ld(istatus, ncell) if istatus is not None else ncell
+        s = ctypes.c_void_p(stream) if stream else None
+        args = [self.ctx, ncell, float(dt), _ptr(met), _ld(met, ncell), _ptr(photol), _ld(photol, ncell), _ptr(c),
+                _ld(c, ncell), _ptr(atol), _ptr(rtol), icn.ctypes.data_as(ctypes.c_void_p),
+                rcn.ctypes.data_as(ctypes.c_void_p), _ptr(hstart), _ptr(istatus), _ptr(rstatus), ldo, _ptr(ierr),
+                ctypes.byref(nretry)]
+        mem = MEM_DEVICE if dev else MEM_HOST
+        if order is None:
+            rc = lib.gc_kpp_fullchem_step(*args, mem, s)
+        else:
+            if not _is_torch(order):
+                order = np.ascontiguousarray(order, dtype=np.int32)
+            rc = lib.gc_kpp_fullchem_step_ordered(*args, _ptr(order), mem, s)
+        self._check(rc)
+        return nretry.value
 
     def update_rconst(self, met, photol, c, rconst, stream=None):
         """Batched Update_RCONST.  met: [NMET, ncell]; photol: [200, ncell];

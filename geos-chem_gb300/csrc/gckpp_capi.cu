@@ -106,7 +106,7 @@ struct gc_kpp_ctx {
   WsLayout lay{};
   DevBuf ws, counter;
   DevBuf h_c, h_r, h_at, h_rt, h_hs, h_is, h_rs, h_ie;  // staging for host-memory calls
-  DevBuf h_met, h_ph;
+  DevBuf h_met, h_ph, h_ord;
   DevBuf rc_buf, cb_buf, ord_buf;  // chemistry-step scratch: RCONST, C_before, retry list
   int last_launches = 0;
   // optional CUDA-event timing of the Rosenbrock launches (GC_KPP_OPT_TIMING)
@@ -187,7 +187,7 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
     if (ev) cudaEventDestroy(ev);
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
                     &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
-                    &c->rc_buf, &c->cb_buf, &c->ord_buf};
+                    &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord};
   for (DevBuf* b : bufs) b->release();
   delete c;
   return GC_KPP_OK;
@@ -298,6 +298,7 @@ int check_tolerances(const double* atol, const double* rtol, int mem, bool vecto
 struct DevArgs {
   int ncell;
   const int* order;  // optional cell list
+  int cell_limit;    // cell ids lie in [0, cell_limit); 0 = ncell
   const double* c_in;
   double* c_out;
   long long ldc;
@@ -312,14 +313,14 @@ struct DevArgs {
   int* ierr;
 };
 
-// Kernel variant by GC_KPP_OPT_ARITH: 0 fast, 1 strict, 2 fast with L1
-// bypass for per-cell reads, 3 fast with a 128-register budget.
+// Kernel variant by GC_KPP_OPT_ARITH: 0 fast (2 cells per thread), 1 strict
+// (1 cell per thread), 2 fast with 1 cell per thread, 3 fast with 4.
 cudaError_t variant_launch(int arith, int queue, int grid, int block, const MechDev& m, const RosMethod& r,
                            const RosParams& p, cudaStream_t s) {
   switch (arith) {
     case 1: return gckpp_launch_ros_strict(queue, grid, block, m, r, p, s);
-    case 2: return gckpp_launch_ros_fastcg(queue, grid, block, m, r, p, s);
-    case 3: return gckpp_launch_ros_fast128(queue, grid, block, m, r, p, s);
+    case 2: return gckpp_launch_ros_fast1(queue, grid, block, m, r, p, s);
+    case 3: return gckpp_launch_ros_fast4(queue, grid, block, m, r, p, s);
     default: return gckpp_launch_ros_fast(queue, grid, block, m, r, p, s);
   }
 }
@@ -327,17 +328,29 @@ cudaError_t variant_launch(int arith, int queue, int grid, int block, const Mech
 cudaError_t variant_occupancy(int arith, int block, int* nblocks) {
   switch (arith) {
     case 1: return gckpp_occupancy_strict(1, block, nblocks);
-    case 2: return gckpp_occupancy_fastcg(1, block, nblocks);
-    case 3: return gckpp_occupancy_fast128(1, block, nblocks);
+    case 2: return gckpp_occupancy_fast1(1, block, nblocks);
+    case 3: return gckpp_occupancy_fast4(1, block, nblocks);
     default: return gckpp_occupancy_fast(1, block, nblocks);
   }
 }
 
-// Launch the Rosenbrock kernel over device arrays.
+int variant_cells_per_thread(int arith) {
+  switch (arith) {
+    case 1: return gckpp_cells_per_thread_strict();
+    case 2: return gckpp_cells_per_thread_fast1();
+    case 3: return gckpp_cells_per_thread_fast4();
+    default: return gckpp_cells_per_thread_fast();
+  }
+}
+
+// Launch the Rosenbrock kernel over device arrays.  A thread holds `nc`
+// cells, so a block covers block*nc workspace slots.
 int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, const DevArgs& a, cudaStream_t s,
                      int* launches) {
   const int queue = c->schedule;
   const int block = c->block;
+  const int nc = variant_cells_per_thread(c->arith);
+  const long long per_block = (long long)block * nc;
   long long nslot;
   int grid;
   if (queue) {
@@ -348,19 +361,14 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
       per_sm = std::max(per_sm, 1);
     }
     grid = c->nsm * per_sm;
-    nslot = (long long)grid * block;
-    const long long need = ((long long)a.ncell + block - 1) / block * block;
-    if (nslot > need) {
-      nslot = need;
-      grid = (int)(need / block);
-    }
-    if (c->max_slots > 0 && nslot > c->max_slots) {
-      grid = (int)std::max(1LL, c->max_slots / block);
-      nslot = (long long)grid * block;
-    }
+    const long long need_blocks = ((long long)a.ncell + per_block - 1) / per_block;
+    if (grid > need_blocks) grid = (int)need_blocks;
+    if (c->max_slots > 0 && (long long)grid * per_block > c->max_slots)
+      grid = (int)std::max(1LL, c->max_slots / per_block);
+    nslot = (long long)grid * per_block;
   } else {
-    grid = (a.ncell + block - 1) / block;
-    nslot = (long long)grid * block;
+    grid = (int)(((long long)a.ncell + per_block - 1) / per_block);
+    nslot = (long long)grid * per_block;
     if (c->max_slots > 0 && nslot > c->max_slots)
       return fail(GC_KPP_EINVAL, "plain schedule needs one workspace slot per cell; raise MAX_SLOTS or use the queue");
   }
@@ -371,6 +379,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   RosParams p{};
   p.ncell = a.ncell;
   p.order = a.order;
+  p.cell_limit = a.cell_limit > 0 ? a.cell_limit : a.ncell;
   p.queue_counter = (int*)c->counter.p;
   p.c_in = a.c_in;
   p.c_out = a.c_out;
@@ -507,11 +516,11 @@ int gc_kpp_integrate_batch(gc_kpp_ctx* c, int ncell, double tin, double tout, do
   return GC_KPP_OK;
 }
 
-int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm,
-                         const double* photol, long long ldp, double* cc, long long ldc, const double* atol,
-                         const double* rtol, const int* icntrl_u, const double* rcntrl_u, double* hstart,
-                         int* istatus, double* rstatus, long long ldo, int* ierr, int* nretry, int mem,
-                         void* stream) {
+static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm,
+                              const double* photol, long long ldp, double* cc, long long ldc, const double* atol,
+                              const double* rtol, const int* icntrl_u, const double* rcntrl_u, double* hstart,
+                              int* istatus, double* rstatus, long long ldo, int* ierr, int* nretry,
+                              const int* order, int mem, void* stream) {
   if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
   if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
   if (nretry) *nretry = 0;
@@ -530,9 +539,24 @@ int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met,
   const double *dmet, *dph, *dat, *drt;
   double *dc, *dhs = nullptr, *drs;
   int *dis, *die;
+  const int* dorder = nullptr;
   long long lm, lp, lc, lo;
+  if (order && mem == GC_KPP_MEM_HOST) {
+    // a host order list must be a permutation of the cells
+    std::vector<char> seen(n, 0);
+    for (int i = 0; i < ncell; ++i) {
+      if (order[i] < 0 || order[i] >= ncell || seen[order[i]])
+        return fail(GC_KPP_EINVAL, "order is not a permutation of 0..ncell-1");
+      seen[order[i]] = 1;
+    }
+  }
   if (mem == GC_KPP_MEM_HOST) {
     double* tmp;
+    if (order) {
+      int* t;
+      GC_TRY(stage_in<int>(c->h_ord, order, ncell, n, 1, s, &t));
+      dorder = t;
+    }
     GC_TRY(stage_in(c->h_met, met, ldm, n, RT::NMET, s, &tmp)); dmet = tmp;
     GC_TRY(stage_in(c->h_ph, photol, ldp, n, GC_KPP_NPHOTOL, s, &tmp)); dph = tmp;
     GC_TRY(stage_in(c->h_c, (const double*)cc, ldc, n, T::NSPEC, s, &dc));
@@ -546,6 +570,7 @@ int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met,
   } else {
     dmet = met; dph = photol; dc = cc; dat = atol; drt = rtol; dhs = hstart; lm = ldm; lp = ldp; lc = ldc;
     die = ierr;
+    dorder = order;
     if (istatus && rstatus) {
       dis = istatus; drs = rstatus; lo = ldo;
     } else {
@@ -576,6 +601,7 @@ int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met,
     DevArgs a{};
     a.ncell = ncell; a.c_in = dc; a.c_out = dc; a.ldc = lc; a.rconst = drc; a.ldr = ncell; a.atol = dat;
     a.rtol = drt; a.hstart = dhs; a.istatus = dis; a.rstatus = drs; a.ldo = lo; a.ierr = die;
+    a.order = dorder; a.cell_limit = ncell;
     GC_TRY(launch_integrate(c, R, 0.0, dt, a, s, &c->last_launches));
     // retry failed cells once with Hstart = 0 from C_before
     // (fullchem_mod.F90:1138-1162)
@@ -593,6 +619,7 @@ int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met,
       DevArgs b = a;
       b.ncell = (int)failed.size();
       b.order = dord;
+      b.cell_limit = ncell;
       b.c_in = dcb;
       b.hstart = nullptr;
       Resolved R2 = R;
@@ -617,6 +644,24 @@ int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met,
     GC_CUDA(cudaStreamSynchronize(s));
   }
   return GC_KPP_OK;
+}
+
+int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm,
+                         const double* photol, long long ldp, double* cc, long long ldc, const double* atol,
+                         const double* rtol, const int* icntrl_u, const double* rcntrl_u, double* hstart,
+                         int* istatus, double* rstatus, long long ldo, int* ierr, int* nretry, int mem,
+                         void* stream) {
+  return fullchem_step_impl(c, ncell, dt, met, ldm, photol, ldp, cc, ldc, atol, rtol, icntrl_u, rcntrl_u, hstart,
+                            istatus, rstatus, ldo, ierr, nretry, nullptr, mem, stream);
+}
+
+int gc_kpp_fullchem_step_ordered(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm,
+                                 const double* photol, long long ldp, double* cc, long long ldc,
+                                 const double* atol, const double* rtol, const int* icntrl_u,
+                                 const double* rcntrl_u, double* hstart, int* istatus, double* rstatus,
+                                 long long ldo, int* ierr, int* nretry, const int* order, int mem, void* stream) {
+  return fullchem_step_impl(c, ncell, dt, met, ldm, photol, ldp, cc, ldc, atol, rtol, icntrl_u, rcntrl_u, hstart,
+                            istatus, rstatus, ldo, ierr, nretry, order, mem, stream);
 }
 
 int gc_kpp_last_launch_count(gc_kpp_ctx* c) { return c ? c->last_launches : 0; }

@@ -1,13 +1,16 @@
 // Rosenbrock kernels, compiled once per variant (build.py):
-//   strict   -DGCKPP_STRICT=1 -fmad=false   reference evaluation order
-//   fast     -DGCKPP_STRICT=0               FMA, reciprocal pivots
-//   fastcg   fast + per-cell reads bypass L1 (GCKPP_LDCG)
-//   fast128  fast with a 128-register budget (half the resident warps)
+//   strict   -DGCKPP_STRICT=1 -fmad=false   reference evaluation order, 1 cell/thread
+//   fast     -DGCKPP_STRICT=0               FMA, reciprocal pivots, GCKPP_NC cells/thread
+//   fast1    fast with 1 cell per thread
+//   fast4    fast with 4 cells per thread
 #include "kpp_launch.h"
 #include "kpp_rosenbrock.cuh"
 
 #ifndef GCKPP_MAX_THREADS
 #define GCKPP_MAX_THREADS 1024  // 1024 threads x 64 registers fill an SM
+#endif
+#ifndef GCKPP_NC
+#define GCKPP_NC 1  // cells per thread
 #endif
 #ifndef GCKPP_VARIANT
 #define GCKPP_VARIANT fast
@@ -19,7 +22,7 @@ namespace gckpp {
 
 template <bool QUEUE>
 __global__ void __launch_bounds__(GCKPP_MAX_THREADS, 1) ros_kernel(MechDev m, RosMethod r, RosParams p) {
-  ros_driver<GCKPP_STRICT != 0, QUEUE>(m, r, p);
+  ros_driver<GCKPP_STRICT != 0, QUEUE, GCKPP_NC>(m, r, p);
 }
 
 cudaError_t GCKPP_CAT(gckpp_launch_ros_, GCKPP_VARIANT)(int queue, int grid, int block, const MechDev& m,
@@ -31,6 +34,8 @@ cudaError_t GCKPP_CAT(gckpp_launch_ros_, GCKPP_VARIANT)(int queue, int grid, int
     ros_kernel<false><<<grid, block, 0, s>>>(m, r, p);
   return cudaGetLastError();
 }
+
+int GCKPP_CAT(gckpp_cells_per_thread_, GCKPP_VARIANT)() { return GCKPP_NC; }
 
 cudaError_t GCKPP_CAT(gckpp_occupancy_, GCKPP_VARIANT)(int queue, int block, int* nblocks) {
   if (queue) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_kernel<true>, block, 0);

@@ -11,11 +11,12 @@ struct RosParams;
 #define GCKPP_DECLARE_VARIANT(name)                                                                        \
   cudaError_t gckpp_launch_ros_##name(int queue, int grid, int block, const MechDev& m, const RosMethod& r, \
                                       const RosParams& p, cudaStream_t s);                                 \
-  cudaError_t gckpp_occupancy_##name(int queue, int block, int* nblocks);
+  cudaError_t gckpp_occupancy_##name(int queue, int block, int* nblocks);                                    \
+  int gckpp_cells_per_thread_##name();
 
 GCKPP_DECLARE_VARIANT(strict)
 GCKPP_DECLARE_VARIANT(fast)
-GCKPP_DECLARE_VARIANT(fastcg)
-GCKPP_DECLARE_VARIANT(fast128)
+GCKPP_DECLARE_VARIANT(fast1)
+GCKPP_DECLARE_VARIANT(fast4)
 #undef GCKPP_DECLARE_VARIANT
 }  // namespace gckpp

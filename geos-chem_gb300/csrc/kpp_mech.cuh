@@ -1,9 +1,12 @@
 // Table-driven per-cell mechanism engine: Fun_SPLIT, Jac_SP, KppDecomp
-// (fused with ros_PrepareMatrix) and KppSolve for one cell per thread.
+// (fused with ros_PrepareMatrix) and KppSolve, for NC cells per thread.
 //
-// Every lane of a warp executes the same table entry for its own cell, so
+// Every lane of a warp executes the same table entry for its own cells, so
 // table reads are warp-uniform broadcasts and the per-cell reads/writes are
-// coalesced: a lane's entry e lives at p[e * TS] in its warp's tile.
+// coalesced.  A warp's workspace tile interleaves 32*NC cells: entry e of the
+// thread's cell q sits at p[e * 32 * NC + q * 32] from the thread's base
+// pointer.  With NC > 1 every table entry drives NC independent loads and
+// FP64 operations, which is what hides memory and FP64-pipe latency.
 //
 // STRICT=true reproduces the KPP-generated Fortran statement by statement in
 // the same evaluation order (the translation unit is compiled -fmad=false):
@@ -21,7 +24,7 @@
 
 namespace gckpp {
 
-constexpr int TS = 32;  // lanes per tile
+constexpr int TS = 32;  // lanes per warp
 
 struct MechDev {
   int nvar, nfix, nreact, nspec, lu_nonzero, nb, lit0;
@@ -48,8 +51,8 @@ struct MechDev {
   const double* lit;
 };
 
-
 __device__ __forceinline__ int ldi(const int* p) { return __ldg(p); }
+__device__ __forceinline__ unsigned ldu(const unsigned* p) { return __ldg(p); }
 
 // Per-cell workspace read.  With GCKPP_LDCG the read bypasses L1 (the tables
 // then keep L1 to themselves); otherwise it is an ordinary cached load.
@@ -60,7 +63,6 @@ __device__ __forceinline__ double ldw(const double* p) {
   return *p;
 #endif
 }
-__device__ __forceinline__ unsigned ldu(const unsigned* p) { return __ldg(p); }
 
 // |x| < TINY(1.0_dp), on the bit pattern
 __device__ __forceinline__ bool tiny_abs(double x) {
@@ -69,182 +71,290 @@ __device__ __forceinline__ bool tiny_abs(double x) {
 }
 
 // One product of the mechanism, pre [* 2] * s1 * s2 * s3, in the Fortran's
-// left-to-right order.  aux holds RCT (and the constant-rate literals), Y the
-// species [V | F].  The species loads are issued unconditionally so that the
-// loads of consecutive products overlap.
-__device__ __forceinline__ double product(const MechDev& m, int p, const double* Y, const double* aux) {
+// left-to-right order, for the thread's NC cells.  aux holds RCT (and the
+// constant-rate literals), Y the species [V | F].  All loads are issued
+// before the multiplications.
+template <int NC>
+__device__ __forceinline__ void product(const MechDev& m, int p, const double* Y, const double* aux, double* out) {
+  constexpr int TSN = TS * NC;
   const uint2 t = __ldg(m.prod_packed + p);
-  double a = ldw(aux + (t.x & 0xfffu) * TS);
   const unsigned ns = (t.x >> 13) & 3u;
-  const double v1 = ldw(Y + (t.x >> 16) * TS), v2 = ldw(Y + (t.y & 0xffffu) * TS), v3 = ldw(Y + (t.y >> 16) * TS);
-  if (t.x & 0x1000u) a = a * 2.0;
-  if (ns >= 1u) a = a * v1;
-  if (ns >= 2u) a = a * v2;
-  if (ns >= 3u) a = a * v3;
-  return a;
+  const int ia = (t.x & 0xfffu) * TSN, i1 = (t.x >> 16) * TSN, i2 = (t.y & 0xffffu) * TSN, i3 = (t.y >> 16) * TSN;
+  double a[NC], v1[NC], v2[NC], v3[NC];
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    a[q] = ldw(aux + ia + q * TS);
+    v1[q] = ldw(Y + i1 + q * TS);
+    v2[q] = ldw(Y + i2 + q * TS);
+    v3[q] = ldw(Y + i3 + q * TS);
+  }
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    double r = a[q];
+    if (t.x & 0x1000u) r = r * 2.0;
+    if (ns >= 1u) r = r * v1[q];
+    if (ns >= 2u) r = r * v2[q];
+    if (ns >= 3u) r = r * v3[q];
+    out[q] = r;
+  }
 }
 
 // Sum of signed terms  slit[c] * X[idx]  (sterm = c << 20 | idx) in the
 // reference's left-to-right order.  The sign is folded into the coefficient
 // (a bare X(idx) is +/-1.0 * X(idx), exact), so the loop has no branch and
 // consecutive terms' loads overlap.  FLIP negates the sum (exact).
-template <bool STRICT, bool FLIP>
-__device__ __forceinline__ double term_sum(const MechDev& m, const unsigned* __restrict__ terms, int s, int e,
-                                           const double* __restrict__ X) {
-  double acc = 0.0;
+template <bool STRICT, bool FLIP, int NC>
+__device__ __forceinline__ void term_sum(const MechDev& m, const unsigned* __restrict__ terms, int s, int e,
+                                         const double* __restrict__ X, double* acc) {
+  constexpr int TSN = TS * NC;
+#pragma unroll
+  for (int q = 0; q < NC; ++q) acc[q] = 0.0;
 #pragma unroll 4
   for (int i = s; i < e; ++i) {
     const unsigned t = ldu(terms + i);
     const double cf = __ldg(m.slit + (t >> 20));
-    const double x = ldw(X + (t & 0xfffffu) * TS);
-    if (STRICT) {
-      const double v = cf * x;
-      acc = (i == s) ? (FLIP ? -v : v) : (FLIP ? acc - v : acc + v);
-    } else {
-      acc = fma(FLIP ? -cf : cf, x, acc);
+    const double* xp = X + (t & 0xfffffu) * TSN;
+    double x[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) x[q] = ldw(xp + q * TS);
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      if (STRICT) {
+        const double v = cf * x[q];
+        acc[q] = (i == s) ? (FLIP ? -v : v) : (FLIP ? acc[q] - v : acc[q] + v);
+      } else {
+        acc[q] = fma(FLIP ? -cf : cf, x[q], acc[q]);
+      }
     }
   }
-  return acc;
 }
 
 // B(b): the partial-derivative products of Jac_SP, which are also the
 // D_VAR products of Fun_SPLIT (same factor lists, same order).
+template <int NC>
 __device__ __forceinline__ void b_products(const MechDev& m, const double* __restrict__ Y,
                                            const double* __restrict__ aux, double* __restrict__ B) {
-#pragma unroll 4
-  for (int b = 0; b < m.nb; ++b) B[b * TS] = product(m, m.nreact + b, Y, aux);
+  constexpr int TSN = TS * NC;
+#pragma unroll 2
+  for (int b = 0; b < m.nb; ++b) {
+    double v[NC];
+    product<NC>(m, m.nreact + b, Y, aux, v);
+#pragma unroll
+    for (int q = 0; q < NC; ++q) B[b * TSN + q * TS] = v[q];
+  }
 }
 
 // Fun_SPLIT: Vdot = P_VAR - D_VAR*V at point Y = [V | F] (aux = RCT).
 // B must hold the B products at Y (b_products).
-template <bool STRICT>
+template <bool STRICT, int NC>
 __device__ void fun_split(const MechDev& m, const double* __restrict__ V, const double* __restrict__ aux,
                           double* __restrict__ A, const double* __restrict__ B, double* __restrict__ Vdot) {
-#pragma unroll 4
-  for (int r = 0; r < m.nreact; ++r) A[r * TS] = product(m, r, V, aux);
+  constexpr int TSN = TS * NC;
+#pragma unroll 2
+  for (int r = 0; r < m.nreact; ++r) {
+    double v[NC];
+    product<NC>(m, r, V, aux, v);
+#pragma unroll
+    for (int q = 0; q < NC; ++q) A[r * TSN + q * TS] = v[q];
+  }
   for (int i = 0; i < m.nvar; ++i) {
-    const double p = term_sum<STRICT, false>(m, m.p_sterm, ldi(m.p_start + i), ldi(m.p_start + i + 1), A);
-    const double d = term_sum<STRICT, false>(m, m.d_sterm, ldi(m.d_start + i), ldi(m.d_start + i + 1), B);
-    const double v = V[i * TS];
-    Vdot[i * TS] = STRICT ? p - d * v : fma(-d, v, p);
+    double p[NC], d[NC];
+    term_sum<STRICT, false, NC>(m, m.p_sterm, ldi(m.p_start + i), ldi(m.p_start + i + 1), A, p);
+    term_sum<STRICT, false, NC>(m, m.d_sterm, ldi(m.d_start + i), ldi(m.d_start + i + 1), B, d);
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      const double v = V[i * TSN + q * TS];
+      Vdot[i * TSN + q * TS] = STRICT ? p[q] - d[q] * v : fma(-d[q], v, p[q]);
+    }
   }
 }
 
 // Jac_SP: JVS in LU order from the B products.  STRICT stores JVS; the fast
 // form stores -JVS (what ros_PrepareMatrix needs).
-template <bool STRICT>
+template <bool STRICT, int NC>
 __device__ void jac_sp(const MechDev& m, const double* __restrict__ B, double* __restrict__ J) {
-  for (int k = 0; k < m.lu_nonzero; ++k)
-    J[k * TS] = term_sum<STRICT, !STRICT>(m, m.j_sterm, ldi(m.j_start + k), ldi(m.j_start + k + 1), B);
+  constexpr int TSN = TS * NC;
+  for (int k = 0; k < m.lu_nonzero; ++k) {
+    double v[NC];
+    term_sum<STRICT, !STRICT, NC>(m, m.j_sterm, ldi(m.j_start + k), ldi(m.j_start + k + 1), B, v);
+#pragma unroll
+    for (int q = 0; q < NC; ++q) J[k * TSN + q * TS] = v[q];
+  }
 }
 
-// Ghimj = -Jac0 + diag(ghinv), then KppDecomp in place.  Returns 0 or the
-// 1-based row whose diagonal was below TINY before elimination (KppDecomp
-// checks each row's diagonal at the start of that row, and rows are only
-// modified in their own iteration, so the check can run up front).
-template <bool STRICT>
-__device__ int decomp(const MechDev& m, const double* __restrict__ J0, double ghinv, double* __restrict__ G) {
-#pragma unroll 8
-  for (int e = 0; e < m.lu_nonzero; ++e) G[e * TS] = STRICT ? -J0[e * TS] : J0[e * TS];
-  int ier = 0;
+// Singular check of KppDecomp (gckpp_LinearAlgebra.F90:61-66): each row's
+// diagonal is tested at the start of that row, and rows are only modified in
+// their own iteration, so the test runs up front on Ghimj's diagonal.
+// ier[q] = 0 or the 1-based first row whose diagonal is below TINY.
+template <bool STRICT, int NC>
+__device__ __forceinline__ void singular_rows(const MechDev& m, const double* __restrict__ J0, const double* ghinv,
+                                              int* ier) {
+  constexpr int TSN = TS * NC;
+#pragma unroll
+  for (int q = 0; q < NC; ++q) ier[q] = 0;
   for (int i = 0; i < m.nvar; ++i) {
     const int d = ldi(m.lu_diag + i);
-    const double g = G[d * TS] + ghinv;
-    G[d * TS] = g;
-    if (ier == 0 && tiny_abs(g)) ier = i + 1;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      const double j = ldw(J0 + d * TSN + q * TS);
+      const double g = (STRICT ? -j : j) + ghinv[q];
+      if (ier[q] == 0 && tiny_abs(g)) ier[q] = i + 1;
+    }
   }
-  if (ier) return ier;
+}
+
+// Ghimj = -Jac0 + diag(ghinv), then KppDecomp in place, in KppDecomp's own
+// right-looking order (W(c) updated in memory for each L entry of a row).
+template <bool STRICT, int NC>
+__device__ void decomp(const MechDev& m, const double* __restrict__ J0, const double* ghinv, double* __restrict__ G,
+                       int* ier) {
+  constexpr int TSN = TS * NC;
+  singular_rows<STRICT, NC>(m, J0, ghinv, ier);
+  for (int e = 0; e < m.lu_nonzero; ++e)
+#pragma unroll
+    for (int q = 0; q < NC; ++q) G[e * TSN + q * TS] = STRICT ? -J0[e * TSN + q * TS] : J0[e * TSN + q * TS];
+  for (int i = 0; i < m.nvar; ++i) {
+    const int d = ldi(m.lu_diag + i);
+#pragma unroll
+    for (int q = 0; q < NC; ++q) G[d * TSN + q * TS] = G[d * TSN + q * TS] + ghinv[q];
+  }
   for (int k = 0; k < m.nvar; ++k) {
     const int l0 = ldi(m.lrow_start + k), l1 = ldi(m.lrow_start + k + 1);
     for (int l = l0; l < l1; ++l) {
       const int kk = ldi(m.lop_kk + l), dj = ldi(m.lop_dj + l);
       const int u0 = ldi(m.lop_u + l), u1 = ldi(m.lop_u + l + 1);
-      double a;
-      if (STRICT) {
-        a = -G[kk * TS] / G[dj * TS];
-        G[kk * TS] = -a;
-      } else {
-        a = G[kk * TS] * G[dj * TS];  // diag j holds 1/pivot
-        G[kk * TS] = a;
-        a = -a;
+      double a[NC];
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        if (STRICT) {
+          a[q] = -G[kk * TSN + q * TS] / G[dj * TSN + q * TS];
+          G[kk * TSN + q * TS] = -a[q];
+        } else {
+          const double v = G[kk * TSN + q * TS] * G[dj * TSN + q * TS];  // diag j holds 1/pivot
+          G[kk * TSN + q * TS] = v;
+          a[q] = -v;
+        }
       }
-#pragma unroll 4
       for (int u = u0; u < u1; ++u) {
         const unsigned op = ldu(m.uop + u);
-        const int t = static_cast<int>(op >> 16), s = static_cast<int>(op & 0xffffu);
-        if (STRICT) G[t * TS] = G[t * TS] + a * G[s * TS];
-        else G[t * TS] = fma(a, G[s * TS], G[t * TS]);
+        const int t = static_cast<int>(op >> 16) * TSN, s = static_cast<int>(op & 0xffffu) * TSN;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+          if (STRICT) G[t + q * TS] = G[t + q * TS] + a[q] * G[s + q * TS];
+          else G[t + q * TS] = fma(a[q], G[s + q * TS], G[t + q * TS]);
+        }
       }
     }
     if (!STRICT) {
       const int d = ldi(m.lu_diag + k);
-      G[d * TS] = 1.0 / G[d * TS];
+#pragma unroll
+      for (int q = 0; q < NC; ++q) G[d * TSN + q * TS] = 1.0 / G[d * TSN + q * TS];
     }
   }
-  return 0;
 }
 
 // The same factorization, with every entry (k,c) of row k computed as one
 // accumulation in a register:  W(c) = Ghimj(k,c) - sum_j L(k,j)*U(j,c) over
 // the L entries j < c of row k in ascending order -- the updates KppDecomp
 // applies to W(c), in the same order, so STRICT stays bit-for-bit.  Each
-// entry is loaded from Jac0 and stored once (no read-modify-write of the
-// row in memory), and Ghimj is never materialised.
-template <bool STRICT>
-__device__ int decomp_rows(const MechDev& m, const double* __restrict__ J0, double ghinv, double* __restrict__ G) {
-  for (int i = 0; i < m.nvar; ++i) {
-    const int d = ldi(m.lu_diag + i);
-    const double g = (STRICT ? -J0[d * TS] : J0[d * TS]) + ghinv;
-    if (tiny_abs(g)) return i + 1;
-  }
+// entry is loaded from Jac0 and stored once, and Ghimj is never stored.
+template <bool STRICT, int NC>
+__device__ void decomp_rows(const MechDev& m, const double* __restrict__ J0, const double* ghinv,
+                            double* __restrict__ G, int* ier) {
+  constexpr int TSN = TS * NC;
+  singular_rows<STRICT, NC>(m, J0, ghinv, ier);
   for (int k = 0; k < m.nvar; ++k) {
     const int e0 = ldi(m.lu_crow + k), e1 = ldi(m.lu_crow + k + 1), dk = ldi(m.lu_diag + k);
     for (int e = e0; e < e1; ++e) {
-      double acc = STRICT ? -ldw(J0 + e * TS) : ldw(J0 + e * TS);
-      if (e == dk) acc = acc + ghinv;
+      double acc[NC];
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        const double j = ldw(J0 + e * TSN + q * TS);
+        acc[q] = STRICT ? -j : j;
+        if (e == dk) acc[q] = acc[q] + ghinv[q];
+      }
       const int t0 = ldi(m.dot_start + e), t1 = ldi(m.dot_start + e + 1);
 #pragma unroll 4
       for (int t = t0; t < t1; ++t) {
         const unsigned op = ldu(m.dot_term + t);
-        const double l = ldw(G + (op >> 16) * TS), u = ldw(G + (op & 0xffffu) * TS);
-        acc = STRICT ? acc - l * u : fma(-l, u, acc);
+        const double* lp = G + (op >> 16) * TSN;
+        const double* up = G + (op & 0xffffu) * TSN;
+        double l[NC], u[NC];
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+          l[q] = ldw(lp + q * TS);
+          u[q] = ldw(up + q * TS);
+        }
+#pragma unroll
+        for (int q = 0; q < NC; ++q) acc[q] = STRICT ? acc[q] - l[q] * u[q] : fma(-l[q], u[q], acc[q]);
       }
       if (e < dk) {
-        const int dc = ldi(m.lu_diag + ldi(m.lu_icol + e));
-        acc = STRICT ? acc / ldw(G + dc * TS) : acc * ldw(G + dc * TS);  // fast: diag holds 1/pivot
+        const double* pv = G + ldi(m.lu_diag + ldi(m.lu_icol + e)) * TSN;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+          const double piv = ldw(pv + q * TS);
+          acc[q] = STRICT ? acc[q] / piv : acc[q] * piv;  // fast: diag holds 1/pivot
+        }
       } else if (e == dk && !STRICT) {
-        acc = 1.0 / acc;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) acc[q] = 1.0 / acc[q];
       }
-      G[e * TS] = acc;
+#pragma unroll
+      for (int q = 0; q < NC; ++q) G[e * TSN + q * TS] = acc[q];
     }
   }
-  return 0;
 }
 
 // KppSolve: forward (L, unit diagonal) then backward (U) substitution.
-template <bool STRICT>
+template <bool STRICT, int NC>
 __device__ void solve(const MechDev& m, const double* __restrict__ G, double* __restrict__ X) {
+  constexpr int TSN = TS * NC;
   for (int i = 0; i < m.nvar; ++i) {
     const int s = ldi(m.lu_crow + i), d = ldi(m.lu_diag + i);
     if (s < d) {
-      double x = X[i * TS];
+      double x[NC];
+#pragma unroll
+      for (int q = 0; q < NC; ++q) x[q] = X[i * TSN + q * TS];
 #pragma unroll 4
       for (int kk = s; kk < d; ++kk) {
-        const double g = ldw(G + kk * TS), y = ldw(X + ldi(m.lu_icol + kk) * TS);
-        x = STRICT ? x - g * y : fma(-g, y, x);
+        const double* gp = G + kk * TSN;
+        const double* yp = X + ldi(m.lu_icol + kk) * TSN;
+        double g[NC], y[NC];
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+          g[q] = ldw(gp + q * TS);
+          y[q] = ldw(yp + q * TS);
+        }
+#pragma unroll
+        for (int q = 0; q < NC; ++q) x[q] = STRICT ? x[q] - g[q] * y[q] : fma(-g[q], y[q], x[q]);
       }
-      X[i * TS] = x;
+#pragma unroll
+      for (int q = 0; q < NC; ++q) X[i * TSN + q * TS] = x[q];
     }
   }
   for (int i = m.nvar - 1; i >= 0; --i) {
     const int d = ldi(m.lu_diag + i), e = ldi(m.lu_crow + i + 1);
-    double x = X[i * TS];
+    double x[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) x[q] = X[i * TSN + q * TS];
 #pragma unroll 4
     for (int kk = d + 1; kk < e; ++kk) {
-      const double g = ldw(G + kk * TS), y = ldw(X + ldi(m.lu_icol + kk) * TS);
-      x = STRICT ? x - g * y : fma(-g, y, x);
+      const double* gp = G + kk * TSN;
+      const double* yp = X + ldi(m.lu_icol + kk) * TSN;
+      double g[NC], y[NC];
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        g[q] = ldw(gp + q * TS);
+        y[q] = ldw(yp + q * TS);
+      }
+#pragma unroll
+      for (int q = 0; q < NC; ++q) x[q] = STRICT ? x[q] - g[q] * y[q] : fma(-g[q], y[q], x[q]);
     }
-    X[i * TS] = STRICT ? x / G[d * TS] : x * G[d * TS];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      const double piv = ldw(G + d * TSN + q * TS);
+      X[i * TSN + q * TS] = STRICT ? x[q] / piv : x[q] * piv;
+    }
   }
 }
 

@@ -1,6 +1,6 @@
-// Rosenbrock integrator for one cell per thread, written as a per-lane state
+// Rosenbrock integrator, NC cells per thread, written as a per-cell state
 // machine so that a warp always executes the same phase code: every loop
-// iteration is one step attempt for every active lane.
+// iteration is one step attempt for every active cell of the thread.
 //
 // The control flow restates ros_Integrator
 // (KPP/fullchem/gckpp_Integrator.F90:578-786) with the method tables of
@@ -9,11 +9,16 @@
 // retry (:1921-1999).  ICNTRL/RCNTRL are resolved on the host exactly as
 // Rosenbrock does (:333-477) and passed in RosParams.
 //
+// The NC cells of a thread share every table walk; each keeps its own step
+// size, counters and accept/reject state.  When one cell needs a new
+// Jacobian and another is retrying a rejected step, both are evaluated
+// (re-evaluating Jac0/Fcn0 at an unchanged Y reproduces the same values) and
+// only the cell that needed it counts it.
+//
 // Two schedules share the state machine:
-//   plain  - thread i integrates cell i, workspace slot i;
-//   queue  - persistent threads; when a lane's cell finishes it claims the
-//            next cell of a device work queue (warp-aggregated atomics), so
-//            lanes never idle while cells remain.
+//   plain  - each thread integrates NC fixed cells, one workspace slot each;
+//   queue  - persistent threads; when a cell finishes, its slot claims the
+//            next cell of a device work queue (warp-aggregated atomics).
 #pragma once
 #include "kpp_mech.cuh"
 
@@ -35,6 +40,7 @@ struct RosParams {
   // cells
   int ncell;
   const int* order;       // optional queue order (cell ids), length ncell
+  int cell_limit;         // cell ids must lie in [0, cell_limit); others are skipped
   int* queue_counter;     // queue schedule: next queue position
   // boundary arrays, cell-interleaved: X[k*ld + cell]
   const double* c_in;
@@ -56,15 +62,11 @@ struct RosParams {
   double hmin, hmax, hstart_default, facmin, facmax, facrej, facsafe, roundoff;
   int autonomous, max_steps, clamp_negative;
   int lu_form;  // 0 decomp_rows, 1 decomp (KppDecomp order)
-  // workspace
+  // workspace: per warp a tile of 32*NC cells x lay.total entries
   double* ws;
   WsLayout lay;
   long long nslot;
 };
-
-__device__ __forceinline__ double* slot_base(const RosParams& p, long long slot) {
-  return p.ws + (slot / TS) * (long long)p.lay.total * TS + (slot % TS);
-}
 
 enum : int { PH_DONE = 0, PH_NEWSTEP = 1, PH_ATTEMPT = 2 };
 
@@ -76,33 +78,35 @@ struct Lane {
   int nfun, njac, nstp, nacc, nrej, ndec, nsol, nsng;
   double texit, hexit, hnew_out;
   int ierr;
-  int ybuf;  // which of y0/y1 holds Y
 };
 
-template <bool STRICT>
+template <bool STRICT, int NC>
 struct Rosenbrock {
+  static constexpr int TSN = TS * NC;
   const MechDev& m;
   const RosMethod& r;
   const RosParams& p;
 
   __device__ Rosenbrock(const MechDev& m_, const RosMethod& r_, const RosParams& p_) : m(m_), r(r_), p(p_) {}
 
-  __device__ void load_cell(double* w, Lane& L, int cell) {
+  // entry 0 of the workspace array at `off` for cell q of this thread
+  __device__ __forceinline__ double* arr(double* w, int off, int q) const { return w + off * TSN + q * TS; }
+
+  __device__ void load_cell(double* w, int q, Lane& L, int cell) {
     const int nvar = m.nvar;
-    // aux = [RCT | constant-rate literals]; Y buffers = [V | F]
-    double* aux = w + p.lay.aux * TS;
-    for (int q = 0; q < m.nreact; ++q) aux[q * TS] = p.rconst[(long long)q * p.ldr + cell];
-    for (int q = m.nreact; q < m.naux; ++q) aux[q * TS] = __ldg(m.pre_lit + (q - m.nreact));
-    double* y = w + p.lay.y0 * TS;
-    double* y1 = w + p.lay.y1 * TS;
-    for (int i = 0; i < nvar; ++i) y[i * TS] = p.c_in[(long long)i * p.ldc + cell];
+    // aux = [RCT | constant-rate literals]; Y0 (current Y) and Y1 (Ynew) = [V | F]
+    double* aux = arr(w, p.lay.aux, q);
+    for (int k = 0; k < m.nreact; ++k) aux[k * TSN] = p.rconst[(long long)k * p.ldr + cell];
+    for (int k = m.nreact; k < m.naux; ++k) aux[k * TSN] = __ldg(m.pre_lit + (k - m.nreact));
+    double* y = arr(w, p.lay.y0, q);
+    double* y1 = arr(w, p.lay.y1, q);
+    for (int i = 0; i < nvar; ++i) y[i * TSN] = p.c_in[(long long)i * p.ldc + cell];
     for (int f = 0; f < m.nfix; ++f) {
       const double v = p.c_in[(long long)(nvar + f) * p.ldc + cell];
-      y[(nvar + f) * TS] = v;
-      y1[(nvar + f) * TS] = v;
+      y[(nvar + f) * TSN] = v;
+      y1[(nvar + f) * TSN] = v;
     }
     L.cell = cell;
-    L.ybuf = 0;
     L.nfun = L.njac = L.nstp = L.nacc = L.nrej = L.ndec = L.nsol = L.nsng = 0;
     L.texit = 0.0;
     L.hexit = 0.0;
@@ -125,189 +129,251 @@ struct Rosenbrock {
     L.phase = PH_NEWSTEP;
   }
 
-  __device__ void store_cell(double* w, const Lane& L) {
+  __device__ void store_cell(double* w, int q, const Lane& L) {
     const int nvar = m.nvar;
-    const double* y = w + (L.ybuf ? p.lay.y1 : p.lay.y0) * TS;
+    const double* y = arr(w, p.lay.y0, q);
     const int cell = L.cell;
-    for (int i = 0; i < nvar; ++i) p.c_out[(long long)i * p.ldc + cell] = y[i * TS];
+    for (int i = 0; i < nvar; ++i) p.c_out[(long long)i * p.ldc + cell] = y[i * TSN];
     if (p.c_out != p.c_in)
       for (int f = 0; f < m.nfix; ++f)
         p.c_out[(long long)(nvar + f) * p.ldc + cell] = p.c_in[(long long)(nvar + f) * p.ldc + cell];
     if (p.istatus) {
       const int v[8] = {L.nfun, L.njac, L.nstp, L.nacc, L.nrej, L.ndec, L.nsol, L.nsng};
-      for (int q = 0; q < 20; ++q) p.istatus[(long long)q * p.ldo + cell] = q < 8 ? v[q] : 0;
+      for (int k = 0; k < 20; ++k) p.istatus[(long long)k * p.ldo + cell] = k < 8 ? v[k] : 0;
     }
     if (p.rstatus) {
-      for (int q = 0; q < 20; ++q) {
+      for (int k = 0; k < 20; ++k) {
         double v = 0.0;
-        if (q == 0) v = L.texit;
-        if (q == 1) v = L.hexit;
-        if (q == 2) v = L.hnew_out;
-        p.rstatus[(long long)q * p.ldo + cell] = v;
+        if (k == 0) v = L.texit;
+        if (k == 1) v = L.hexit;
+        if (k == 2) v = L.hnew_out;
+        p.rstatus[(long long)k * p.ldo + cell] = v;
       }
     }
     if (p.ierr) p.ierr[cell] = L.ierr;
   }
 
-  // TimeLoop head + Fun0 + Jac0 (ros_Integrator :652-677)
-  __device__ void new_step(double* w, Lane& L) {
+  // TimeLoop head (ros_Integrator :652-665): leaves the cell in NEWSTEP if
+  // it needs Fun0/Jac0, else DONE with its IERR.
+  __device__ void step_checks(Lane& L) const {
     const double dir = (p.tend >= p.tstart) ? 1.0 : -1.0;
     const bool go = (dir > 0.0) ? ((L.T - p.tend) + p.roundoff <= 0.0) : ((p.tend - L.T) + p.roundoff <= 0.0);
     if (!go) {
       L.ierr = 1;
       L.phase = PH_DONE;
-      return;
-    }
-    if (L.nstp > p.max_steps) {
+    } else if (L.nstp > p.max_steps) {
       L.ierr = -6;
       L.phase = PH_DONE;
-      return;
-    }
-    if (((L.T + 0.1 * L.H) == L.T) || (L.H <= p.roundoff)) {
+    } else if (((L.T + 0.1 * L.H) == L.T) || (L.H <= p.roundoff)) {
       L.ierr = -7;
       L.phase = PH_DONE;
-      return;
+    } else {
+      L.H = fmin(L.H, fabs(p.tend - L.T));
     }
-    L.H = fmin(L.H, fabs(p.tend - L.T));
-    const double* aux = w + p.lay.aux * TS;
-    const double* Y = w + (L.ybuf ? p.lay.y1 : p.lay.y0) * TS;
-    double* B = w + p.lay.b * TS;
-    // B products once for both Jac_SP and Fun0's D_VAR terms.
-    b_products(m, Y, aux, B);
-    jac_sp<STRICT>(m, B, w + p.lay.j0 * TS);
-    fun_split<STRICT>(m, Y, aux, w + p.lay.a * TS, B, w + p.lay.fcn0 * TS);
-    L.nfun += 1;
-    if (!p.autonomous) {
-      // ros_FunTimeDerivative (:1748-1769); rates are frozen for the step
-      // (ICNTRL(15)=-1) so FunTemplate(T+Delta) evaluates the same point.
-      double* dfdt = w + p.lay.dfdt * TS;
-      const double* f0 = w + p.lay.fcn0 * TS;
-      const double delta = sqrt(p.roundoff) * fmax(1.0e-6, fabs(L.T));
-      fun_split<STRICT>(m, Y, aux, w + p.lay.a * TS, B, dfdt);
-      L.nfun += 1;
-      const double rd = 1.0 / delta;
-      for (int i = 0; i < m.nvar; ++i) {
-        double v = dfdt[i * TS] + (-1.0) * f0[i * TS];
-        if (rd != 1.0) v = rd * v;
-        dfdt[i * TS] = v;
-      }
-    }
-    L.njac += 1;
-    L.phase = PH_ATTEMPT;
   }
 
-  // One pass of UntilAccepted (:681-778)
-  __device__ void attempt(double* w, Lane& L, int& ier_out) {
-    const double dir = (p.tend >= p.tstart) ? 1.0 : -1.0;
-    const int nvar = m.nvar;
-    double* G = w + p.lay.g * TS;
-    const double* J0 = w + p.lay.j0 * TS;
-    // ros_PrepareMatrix with singular retry (:1921-1999)
-    int nconsec = 0;
-    while (true) {
-      const double ghinv = 1.0 / (dir * L.H * r.Gamma[0]);
-      const int ier = p.lu_form ? decomp<STRICT>(m, J0, ghinv, G) : decomp_rows<STRICT>(m, J0, ghinv, G);
-      L.ndec += 1;
-      if (ier == 0) break;
-      L.nsng += 1;
-      nconsec += 1;
-      if (nconsec <= 5) {
-        L.H = L.H * 0.5;
-      } else {
-        L.ierr = -8;
-        L.phase = PH_DONE;
-        ier_out = ier;
-        return;
+  // Fun0 and Jac0 at Y for all NC cells (ros_Integrator :667-677), and the
+  // time derivative for non-autonomous problems (:1748-1769; rates are frozen
+  // for the step, ICNTRL(15)=-1, so FunTemplate(T+Delta) evaluates the same
+  // point).
+  __device__ void fun0_jac0(double* w, const Lane* L) {
+    const double* aux = arr(w, p.lay.aux, 0);
+    const double* Y = arr(w, p.lay.y0, 0);
+    double* B = arr(w, p.lay.b, 0);
+    // B products once for both Jac_SP and Fun0's D_VAR terms.
+    b_products<NC>(m, Y, aux, B);
+    jac_sp<STRICT, NC>(m, B, arr(w, p.lay.j0, 0));
+    fun_split<STRICT, NC>(m, Y, aux, arr(w, p.lay.a, 0), B, arr(w, p.lay.fcn0, 0));
+    if (!p.autonomous) {
+      double* dfdt = arr(w, p.lay.dfdt, 0);
+      const double* f0 = arr(w, p.lay.fcn0, 0);
+      fun_split<STRICT, NC>(m, Y, aux, arr(w, p.lay.a, 0), B, dfdt);
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        const double delta = sqrt(p.roundoff) * fmax(1.0e-6, fabs(L[q].T));
+        const double rd = 1.0 / delta;
+        for (int i = 0; i < m.nvar; ++i) {
+          double v = dfdt[i * TSN + q * TS] + (-1.0) * f0[i * TSN + q * TS];
+          if (rd != 1.0) v = rd * v;
+          dfdt[i * TSN + q * TS] = v;
+        }
       }
     }
-    const double* Y = w + (L.ybuf ? p.lay.y1 : p.lay.y0) * TS;
-    double* Ynew = w + (L.ybuf ? p.lay.y0 : p.lay.y1) * TS;
-    const double* aux = w + p.lay.aux * TS;
-    double* K = w + p.lay.k * TS;
-    const double* fcn = w + p.lay.fcn0 * TS;
-    const long long kst = (long long)nvar * TS;
+  }
+
+  // One pass of UntilAccepted (:681-778) for the cells with act[q].  The
+  // other cells are computed along (their results are never used).
+  __device__ void attempt(double* w, Lane* L, const bool* act) {
+    const double dir = (p.tend >= p.tstart) ? 1.0 : -1.0;
+    const int nvar = m.nvar;
+    double* G = arr(w, p.lay.g, 0);
+    const double* J0 = arr(w, p.lay.j0, 0);
+    bool live[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) live[q] = act[q];
+    // ros_PrepareMatrix with singular retry (:1921-1999): a cell whose
+    // matrix is singular halves H and decomposes again, up to 5 times.
+    {
+      int nconsec[NC];
+      bool pending[NC];
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        nconsec[q] = 0;
+        pending[q] = live[q];
+      }
+      while (true) {
+        double ghinv[NC];
+        int ier[NC];
+#pragma unroll
+        for (int q = 0; q < NC; ++q) ghinv[q] = 1.0 / (dir * L[q].H * r.Gamma[0]);
+        if (p.lu_form) decomp<STRICT, NC>(m, J0, ghinv, G, ier);
+        else decomp_rows<STRICT, NC>(m, J0, ghinv, G, ier);
+        bool again = false;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+          if (!pending[q]) continue;
+          L[q].ndec += 1;
+          if (ier[q] == 0) {
+            pending[q] = false;
+            continue;
+          }
+          L[q].nsng += 1;
+          nconsec[q] += 1;
+          if (nconsec[q] <= 5) {
+            L[q].H = L[q].H * 0.5;
+            again = true;
+          } else {
+            L[q].ierr = -8;
+            L[q].phase = PH_DONE;
+            pending[q] = false;
+            live[q] = false;
+          }
+        }
+        if (!again) break;
+      }
+    }
+    bool any_live = false;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) any_live |= live[q];
+    if (!any_live) return;
+
+    const double* Y = arr(w, p.lay.y0, 0);
+    double* Ynew = arr(w, p.lay.y1, 0);
+    const double* aux = arr(w, p.lay.aux, 0);
+    double* K = arr(w, p.lay.k, 0);
+    const double* fcn = arr(w, p.lay.fcn0, 0);
+    const long long kst = (long long)nvar * TSN;
     for (int s = 0; s < r.S; ++s) {
       if (s > 0 && r.NewF[s]) {
         for (int i = 0; i < nvar; ++i) {
-          double y = Y[i * TS];
-          for (int j = 0; j < s; ++j) {
-            const double a = r.A[(s * (s - 1)) / 2 + j];
-            if (a != 0.0) y = STRICT ? y + a * K[j * kst + i * TS] : fma(a, K[j * kst + i * TS], y);
+#pragma unroll
+          for (int q = 0; q < NC; ++q) {
+            double y = Y[i * TSN + q * TS];
+            for (int j = 0; j < s; ++j) {
+              const double a = r.A[(s * (s - 1)) / 2 + j];
+              const double kj = K[j * kst + i * TSN + q * TS];
+              if (a != 0.0) y = STRICT ? y + a * kj : fma(a, kj, y);
+            }
+            Ynew[i * TSN + q * TS] = y;
           }
-          Ynew[i * TS] = y;
         }
-        b_products(m, Ynew, aux, w + p.lay.b * TS);
-        fun_split<STRICT>(m, Ynew, aux, w + p.lay.a * TS, w + p.lay.b * TS, w + p.lay.fcn * TS);
-        L.nfun += 1;
-        fcn = w + p.lay.fcn * TS;
+        b_products<NC>(m, Ynew, aux, arr(w, p.lay.b, 0));
+        fun_split<STRICT, NC>(m, Ynew, aux, arr(w, p.lay.a, 0), arr(w, p.lay.b, 0), arr(w, p.lay.fcn, 0));
+#pragma unroll
+        for (int q = 0; q < NC; ++q)
+          if (live[q]) L[q].nfun += 1;
+        fcn = arr(w, p.lay.fcn, 0);
       }
-      double hc[SMAX];
-      for (int j = 0; j < s; ++j) hc[j] = r.C[(s * (s - 1)) / 2 + j] / (dir * L.H);
+      double hc[NC][SMAX], hg[NC];
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        for (int j = 0; j < s; ++j) hc[q][j] = r.C[(s * (s - 1)) / 2 + j] / (dir * L[q].H);
+        hg[q] = dir * L[q].H * r.Gamma[s];
+      }
       const bool use_dfdt = (!p.autonomous) && (r.Gamma[s] != 0.0);
-      const double hg = dir * L.H * r.Gamma[s];
-      const double* dfdt = w + p.lay.dfdt * TS;
+      const double* dfdt = arr(w, p.lay.dfdt, 0);
       double* Ks = K + s * kst;
       for (int i = 0; i < nvar; ++i) {
-        double k = fcn[i * TS];
-        for (int j = 0; j < s; ++j)
-          if (hc[j] != 0.0) k = STRICT ? k + hc[j] * K[j * kst + i * TS] : fma(hc[j], K[j * kst + i * TS], k);
-        if (use_dfdt && hg != 0.0) k = STRICT ? k + hg * dfdt[i * TS] : fma(hg, dfdt[i * TS], k);
-        Ks[i * TS] = k;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+          double k = fcn[i * TSN + q * TS];
+          for (int j = 0; j < s; ++j) {
+            const double kj = K[j * kst + i * TSN + q * TS];
+            if (hc[q][j] != 0.0) k = STRICT ? k + hc[q][j] * kj : fma(hc[q][j], kj, k);
+          }
+          if (use_dfdt && hg[q] != 0.0) {
+            const double dd = dfdt[i * TSN + q * TS];
+            k = STRICT ? k + hg[q] * dd : fma(hg[q], dd, k);
+          }
+          Ks[i * TSN + q * TS] = k;
+        }
       }
-      solve<STRICT>(m, G, Ks);
-      L.nsol += 1;
+      solve<STRICT, NC>(m, G, Ks);
+#pragma unroll
+      for (int q = 0; q < NC; ++q)
+        if (live[q]) L[q].nsol += 1;
     }
     // new solution, error estimate and norm (:729-740, :1715-1745)
-    const double* atol = p.atol;
-    const double* rtol = p.rtol;
-    double err = 0.0;
+    double err[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) err[q] = 0.0;
     for (int i = 0; i < nvar; ++i) {
-      double y = Y[i * TS];
-      double yerr = 0.0;
-      for (int j = 0; j < r.S; ++j) {
-        const double kj = K[j * kst + i * TS];
-        if (r.M[j] != 0.0) y = STRICT ? y + r.M[j] * kj : fma(r.M[j], kj, y);
-        if (r.E[j] != 0.0) yerr = STRICT ? yerr + r.E[j] * kj : fma(r.E[j], kj, yerr);
+      const double at = p.vector_tol ? __ldg(p.atol + i) : __ldg(p.atol);
+      const double rt = p.vector_tol ? __ldg(p.rtol + i) : __ldg(p.rtol);
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        const double y0 = Y[i * TSN + q * TS];
+        double y = y0;
+        double yerr = 0.0;
+        for (int j = 0; j < r.S; ++j) {
+          const double kj = K[j * kst + i * TSN + q * TS];
+          if (r.M[j] != 0.0) y = STRICT ? y + r.M[j] * kj : fma(r.M[j], kj, y);
+          if (r.E[j] != 0.0) yerr = STRICT ? yerr + r.E[j] * kj : fma(r.E[j], kj, yerr);
+        }
+        Ynew[i * TSN + q * TS] = y;
+        const double ymax = fmax(fabs(y0), fabs(y));
+        const double scale = STRICT ? at + rt * ymax : fma(rt, ymax, at);
+        const double e = yerr / scale;
+        err[q] = STRICT ? err[q] + e * e : fma(e, e, err[q]);
       }
-      Ynew[i * TS] = y;
-      const double ymax = fmax(fabs(Y[i * TS]), fabs(y));
-      const double at = p.vector_tol ? __ldg(atol + i) : __ldg(atol);
-      const double rt = p.vector_tol ? __ldg(rtol + i) : __ldg(rtol);
-      const double scale = STRICT ? at + rt * ymax : fma(rt, ymax, at);
-      const double q = yerr / scale;
-      err = STRICT ? err + q * q : fma(q, q, err);
     }
-    err = sqrt(err / (double)nvar);
-    err = fmax(err, 1.0e-10);
     // step size control (:742-778)
-    const double fac = fmin(r_facmax(), fmax(p.facmin, p.facsafe / pow(err, 1.0 / r.ELO)));
-    double hnew = L.H * fac;
-    L.nstp += 1;
-    if ((err <= 1.0) || (L.H <= p.hmin)) {
-      L.nacc += 1;
-      if (p.clamp_negative)
-        for (int i = 0; i < nvar; ++i) Ynew[i * TS] = fmax(Ynew[i * TS], 0.0);
-      L.ybuf ^= 1;
-      L.T = L.T + dir * L.H;
-      hnew = fmax(p.hmin, fmin(hnew, p.hmax));
-      if (L.rej_last) hnew = fmin(hnew, L.H);
-      L.hexit = L.H;
-      L.hnew_out = hnew;
-      L.texit = L.T;
-      L.rej_last = 0;
-      L.rej_more = 0;
-      L.H = hnew;
-      L.phase = PH_NEWSTEP;
-    } else {
-      if (L.rej_more) hnew = L.H * p.facrej;
-      L.rej_more = L.rej_last;
-      L.rej_last = 1;
-      L.H = hnew;
-      if (L.nacc >= 1) L.nrej += 1;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      if (!live[q]) continue;
+      Lane& c = L[q];
+      double e = sqrt(err[q] / (double)nvar);
+      e = fmax(e, 1.0e-10);
+      const double fac = fmin(p.facmax, fmax(p.facmin, p.facsafe / pow(e, 1.0 / r.ELO)));
+      double hnew = c.H * fac;
+      c.nstp += 1;
+      if ((e <= 1.0) || (c.H <= p.hmin)) {
+        c.nacc += 1;
+        double* yq = arr(w, p.lay.y0, q);
+        const double* ynq = arr(w, p.lay.y1, q);
+        for (int i = 0; i < nvar; ++i) {
+          const double v = ynq[i * TSN];
+          yq[i * TSN] = p.clamp_negative ? fmax(v, 0.0) : v;
+        }
+        c.T = c.T + dir * c.H;
+        hnew = fmax(p.hmin, fmin(hnew, p.hmax));
+        if (c.rej_last) hnew = fmin(hnew, c.H);
+        c.hexit = c.H;
+        c.hnew_out = hnew;
+        c.texit = c.T;
+        c.rej_last = 0;
+        c.rej_more = 0;
+        c.H = hnew;
+        c.phase = PH_NEWSTEP;
+      } else {
+        if (c.rej_more) hnew = c.H * p.facrej;
+        c.rej_more = c.rej_last;
+        c.rej_last = 1;
+        c.H = hnew;
+        if (c.nacc >= 1) c.nrej += 1;
+      }
     }
   }
-
-  __device__ __forceinline__ double r_facmax() const { return p.facmax; }
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
@@ -324,37 +390,80 @@ __device__ __forceinline__ int queue_claim(int* counter) {
   return base + __popc(lt);
 }
 
-template <bool STRICT, bool QUEUE>
+template <bool STRICT, bool QUEUE, int NC>
 __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams& p) {
+  constexpr int TSN = TS * NC;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  Rosenbrock<STRICT> ros(m, r, p);
-  double* w = slot_base(p, tid);
-  Lane L;
-  bool active = true;
-  if (QUEUE) {
-    const int q = queue_claim(p.queue_counter);
-    if (q >= p.ncell) return;
-    ros.load_cell(w, L, p.order ? p.order[q] : q);
-  } else {
-    if (tid >= p.ncell) return;
-    ros.load_cell(w, L, p.order ? p.order[tid] : (int)tid);
+  const long long warp = tid / TS;
+  const int lane = (int)(tid % TS);
+  Rosenbrock<STRICT, NC> ros(m, r, p);
+  double* w = p.ws + warp * (long long)p.lay.total * TSN + lane;
+  Lane L[NC];
+  bool has[NC];
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    int idx;
+    if (QUEUE) {
+      idx = queue_claim(p.queue_counter);
+    } else {
+      const long long g = warp * TSN + q * TS + lane;
+      idx = g < p.ncell ? (int)g : p.ncell;
+    }
+    has[q] = false;
+    if (idx < p.ncell) {
+      const int cell = p.order ? p.order[idx] : idx;
+      has[q] = (unsigned)cell < (unsigned)p.cell_limit;
+      if (has[q]) ros.load_cell(w, q, L[q], cell);
+    }
   }
-  while (active) {
-    if (L.phase == PH_DONE) {
-      ros.store_cell(w, L);
-      if (QUEUE) {
-        const int q = queue_claim(p.queue_counter);
-        if (q < p.ncell) ros.load_cell(w, L, p.order ? p.order[q] : q);
-        else active = false;
-      } else {
-        active = false;
+  while (true) {
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      if (has[q] && L[q].phase == PH_DONE) {
+        ros.store_cell(w, q, L[q]);
+        has[q] = false;
+        if (QUEUE) {
+          const int idx = queue_claim(p.queue_counter);
+          if (idx < p.ncell) {
+            const int cell = p.order ? p.order[idx] : idx;
+            if ((unsigned)cell < (unsigned)p.cell_limit) {
+              ros.load_cell(w, q, L[q], cell);
+              has[q] = true;
+            }
+          }
+        }
+      }
+      any |= has[q];
+    }
+    if (!any) break;
+    bool need = false;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      if (has[q] && L[q].phase == PH_NEWSTEP) {
+        ros.step_checks(L[q]);
+        need |= L[q].phase == PH_NEWSTEP;
       }
     }
-    if (active && L.phase == PH_NEWSTEP) ros.new_step(w, L);
-    if (active && L.phase == PH_ATTEMPT) {
-      int ier = 0;
-      ros.attempt(w, L, ier);
+    if (need) {
+      ros.fun0_jac0(w, L);
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        if (has[q] && L[q].phase == PH_NEWSTEP) {
+          L[q].nfun += p.autonomous ? 1 : 2;
+          L[q].njac += 1;
+          L[q].phase = PH_ATTEMPT;
+        }
+      }
     }
+    bool act[NC];
+    bool any_act = false;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      act[q] = has[q] && L[q].phase == PH_ATTEMPT;
+      any_act |= act[q];
+    }
+    if (any_act) ros.attempt(w, L, act);
   }
 }
 

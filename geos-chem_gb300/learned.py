@@ -105,11 +105,18 @@ class Proposer:
         self.y_mean = 0.0
 
     # -- features -----------------------------------------------------------
-    def features(self, met, photol, c, suncos=None, stream=None):
+    def features(self, met, photol, c, suncos=None, stream=None, raw=False):
+        """Network inputs of every cell ([ncell, 56] float32); raw=True skips
+        the normalisation (training data)."""
+        t = self.torch
         n = c.shape[1]
-        x = self.torch.empty((n, NFEAT), dtype=self.torch.float32, device=self.dev)
+        x = t.empty((n, NFEAT), dtype=t.float32, device=self.dev)
+        mean, inv_std = self.mean, self.inv_std
+        if raw:
+            mean = t.zeros(NFEAT, dtype=t.float64, device=self.dev)
+            inv_std = t.ones(NFEAT, dtype=t.float64, device=self.dev)
         _check(self.lib.gc_mlp_features(n, _p(met), met.stride(0), _p(photol), photol.stride(0), _p(c), c.stride(0),
-                                        _p(suncos), _p(self.jrows), _p(self.srows), _p(self.mean), _p(self.inv_std),
+                                        _p(suncos), _p(self.jrows), _p(self.srows), _p(mean), _p(inv_std),
                                         _p(x), stream), "features")
         return x
 
@@ -159,21 +166,33 @@ class Proposer:
                                         _p(self.m2[k]), lr, b1, b2, eps, self.step_count, None), "adam")
 
     # -- training -------------------------------------------------------------
-    def targets(self, rstatus, istatus):
-        """log(Hnew) (centred) and the step-count quartile bin."""
+    def fit_targets(self, hnew, steps, quantiles=(0.5, 0.85, 0.97)):
+        """Centre of log(Hnew) and the step-count edges of the 4 stiffness
+        bins.  The edges sit at upper quantiles so that the last bin holds the
+        few cells whose step counts form the tail of the launch."""
         t = self.torch
-        h = t.log(rstatus[2].clamp_min(1e-10)).float() - self.y_mean
-        steps = istatus[2].double()
-        e = t.tensor(self.bin_edges, dtype=t.float64, device=self.dev)
-        b = t.bucketize(steps, e, right=True).int()
+        self.y_mean = float(t.log(hnew.double().clamp_min(1e-10)).mean().item())
+        sub = steps.double()[:2_000_000]
+        q = t.quantile(sub, t.tensor(list(quantiles), dtype=t.float64, device=sub.device))
+        self.bin_edges = [float(v) for v in q.tolist()]
+
+    def targets(self, hnew, steps):
+        """log(Hnew) (centred) and the stiffness bin of each row."""
+        t = self.torch
+        h = (t.log(hnew.double().clamp_min(1e-10)) - self.y_mean).float()
+        e = t.tensor(self.bin_edges, dtype=t.float64, device=steps.device)
+        b = t.bucketize(steps.double(), e, right=True).int()
         return h.contiguous(), b.contiguous()
 
-    def fit_targets(self, rstatus, istatus):
-        t = self.torch
-        self.y_mean = float(t.log(rstatus[2].clamp_min(1e-10)).mean().item())
-        q = t.quantile(istatus[2].double()[:1_000_000], t.tensor([0.25, 0.5, 0.75], dtype=t.float64,
-                                                                  device=self.dev))
-        self.bin_edges = [float(v) for v in q.tolist()]
+    def normalise(self, x_raw):
+        """Rows of raw features -> the network's inputs (what the features
+        kernel produces with this normalisation)."""
+        return ((x_raw.double() - self.mean) * self.inv_std).float().contiguous()
+
+    def fit_normalisation_rows(self, x_raw):
+        x = x_raw.double()
+        self.mean = x.mean(0).contiguous()
+        self.inv_std = (1.0 / x.std(0).clamp_min(1e-6)).contiguous()
 
     def train(self, x, y_h, y_bin, epochs=4, batch=4096, lr=2e-3, w_ce=0.5, seed=0, log=None):
         t = self.torch
@@ -235,3 +254,85 @@ class Proposer:
         self.inv_std = t.tensor(d["inv_std"], dtype=t.float64, device=self.dev)
         meta = json.loads(str(d["meta"]))
         self.h0_scale, self.bin_edges, self.y_mean = meta["h0_scale"], meta["bin_edges"], meta["y_mean"]
+
+
+# -- training data from plain GPU runs -------------------------------------------
+def device_cells(cells, dev):
+    """The met / photol / C arrays of a cell set as contiguous CUDA tensors."""
+    import torch
+
+    return {k: torch.tensor(cells[k], dtype=torch.float64, device=dev).contiguous() for k in ("met", "photol", "c")}
+
+
+def collect(solver, prop, cells, dt=1200.0, nsteps=2, spinup=86400.0, log=None):
+    """Plain GPU chemistry steps over a cell set, as Do_FullChem runs them:
+    a spin-up step of `spinup` seconds, then `nsteps` steps of `dt` seconds
+    with the KPPHvalue chain.  Returns per cell-step rows: raw features at the
+    start of the step, Hnew (RSTATUS(3)) and the step count (ISTATUS(3)) at
+    its end -- the (state, accepted step size, step count) training pairs."""
+    import torch
+
+    d = device_cells(cells, prop.dev)
+    n = d["c"].shape[1]
+    atol, rtol = inputs.tolerances()
+    ic, rc = inputs.default_controls()
+    at = torch.tensor(atol, device=prop.dev)
+    rt = torch.tensor(rtol, device=prop.dev)
+    hs = torch.zeros(n, dtype=torch.float64, device=prop.dev)
+    ist = torch.zeros((20, n), dtype=torch.int32, device=prop.dev)
+    rst = torch.zeros((20, n), dtype=torch.float64, device=prop.dev)
+    ierr = torch.zeros(n, dtype=torch.int32, device=prop.dev)
+    if spinup > 0:
+        solver.fullchem_step(spinup, d["met"], d["photol"], d["c"], at, rt, ic, rc, hs, ist, rst, ierr)
+    xs, hn, st = [], [], []
+    for k in range(nsteps):
+        xs.append(prop.features(d["met"], d["photol"], d["c"], raw=True))
+        solver.fullchem_step(dt, d["met"], d["photol"], d["c"], at, rt, ic, rc, hs, ist, rst, ierr)
+        hn.append(rst[2].clone())
+        st.append(ist[2].clone())
+        if log:
+            log("step %d: mean steps %.2f" % (k, st[-1].double().mean().item()))
+    torch.cuda.synchronize()
+    return {"x": torch.cat(xs), "hnew": torch.cat(hn), "steps": torch.cat(st)}
+
+
+def fit(prop, data, epochs=6, batch=4096, lr=2e-3, w_ce=0.5, quantiles=(0.5, 0.85, 0.97), seed=0, log=None):
+    """Normalisation, targets and training of `prop` on collected rows."""
+    prop.fit_normalisation_rows(data["x"])
+    prop.fit_targets(data["hnew"], data["steps"], quantiles)
+    x = prop.normalise(data["x"])
+    y_h, y_b = prop.targets(data["hnew"], data["steps"])
+    return prop.train(x, y_h, y_b, epochs=epochs, batch=batch, lr=lr, w_ce=w_ce, seed=seed, log=log)
+
+
+def makespan(work, order, nslot):
+    """Completion time of a list schedule: `nslot` workers take cells in
+    `order`, each as soon as it is free; cell i costs work[i].  Models the
+    persistent queue kernel, whose slots claim the next cell when theirs is
+    done."""
+    import heapq
+
+    work = np.asarray(work, dtype=np.float64)
+    order = np.asarray(order)
+    k = min(nslot, len(order))
+    free = list(work[order[:k]])
+    heapq.heapify(free)
+    for c in order[k:]:
+        t = heapq.heappop(free)
+        heapq.heappush(free, t + work[c])
+    return max(free) if free else 0.0
+
+
+def evaluate(prop, data):
+    """Held-out quality: log-H RMSE, bin accuracy, and the simulated queue
+    makespan (in cell-steps) under natural, predicted-bin and true-count
+    orders."""
+    t = prop.torch
+    x = prop.normalise(data["x"])
+    a = prop.forward(x)
+    y_h, y_b = prop.targets(data["hnew"], data["steps"])
+    out = a["out"]
+    rmse = float(t.sqrt(((out[:, 0] - y_h) ** 2).mean()).item())
+    pred_b = out[:, 1:].argmax(1).int()
+    acc = float((pred_b == y_b).double().mean().item())
+    return {"logh_rmse": rmse, "bin_accuracy": acc}

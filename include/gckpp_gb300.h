@@ -46,9 +46,10 @@ extern "C" {
 
 /* gc_kpp_ctx_set_option keys */
 #define GC_KPP_OPT_ARITH 1        /* 0 = fast (FMA, reciprocal pivots), 1 = strict (reference order, no FMA),
-                                     2 = fast with L1-bypassing workspace reads, 3 = fast, 128 registers */
+                                     2 = fast, 1 cell per thread, 3 = fast, 4 cells per thread;
+                                     fast (0) integrates 2 cells per thread */
 #define GC_KPP_OPT_SCHEDULE 2     /* 0 = plain (thread per cell), 1 = persistent work queue */
-#define GC_KPP_OPT_BLOCK 3        /* threads per block (multiple of 32, <= 1024; <= 512 for arith 3), 0 = default 128 */
+#define GC_KPP_OPT_BLOCK 3        /* threads per block (multiple of 32, <= 1024), 0 = default 128 */
 #define GC_KPP_OPT_BLOCKS_PER_SM 4 /* queue schedule: resident blocks per SM, 0 = default */
 #define GC_KPP_OPT_MAX_SLOTS 5    /* cap on workspace slots (cells in flight), 0 = no cap */
 #define GC_KPP_OPT_TIMING 6       /* 1 = time the Rosenbrock launches with CUDA events */
@@ -154,6 +155,25 @@ int gc_kpp_fullchem_step(gc_kpp_ctx* ctx, int ncell, double dt, const double* me
                          const double* atol, const double* rtol, const int* icntrl, const double* rcntrl,
                          double* hstart, int* istatus, double* rstatus, long long ldo, int* ierr,
                          int* nretry, int mem, void* stream);
+
+/* gc_kpp_fullchem_step with a queue order: order[0..ncell-1] is a
+ * permutation of the cells, the order in which the persistent work-queue
+ * schedule starts them (GC_KPP_OPT_SCHEDULE = 1; the plain schedule assigns
+ * order[i] to thread slot i).  Each cell's integration is independent of
+ * the others, so the results are those of gc_kpp_fullchem_step for any
+ * order; the order changes only how the work packs onto the GPU.  Starting
+ * the cells that need the most steps first keeps a few stiff cells from
+ * running alone at the end of the launch.  No counterpart in the reference
+ * (its OpenMP loop hands out chunks of 24 cells in grid order,
+ * SCHEDULE(DYNAMIC, 24), fullchem_mod.F90:528-545).  With host memory the
+ * order is checked to be a permutation (GC_KPP_EINVAL otherwise); with
+ * device memory, entries outside [0, ncell) are skipped and their cells
+ * left untouched. */
+int gc_kpp_fullchem_step_ordered(gc_kpp_ctx* ctx, int ncell, double dt, const double* met, long long ldm,
+                                 const double* photol, long long ldp, double* c, long long ldc,
+                                 const double* atol, const double* rtol, const int* icntrl, const double* rcntrl,
+                                 double* hstart, int* istatus, double* rstatus, long long ldo, int* ierr,
+                                 int* nretry, const int* order, int mem, void* stream);
 
 /* Number of kernels the last gc_kpp_fullchem_step call on ctx launched. */
 int gc_kpp_last_launch_count(gc_kpp_ctx* ctx);

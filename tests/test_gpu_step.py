@@ -1,0 +1,211 @@
+"""GPU tests of the chemistry-step boundary (gc_kpp_fullchem_step) and of the
+reference's error behaviour, against the CPU oracle."""
+import numpy as np
+import pytest
+
+import gcchem.capi as capi
+import gcchem.inputs as inputs
+import gcchem.mechanism as mechanism
+
+pytestmark = pytest.mark.gpu
+NVAR = 353
+
+
+def _rel(a, b):
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+
+
+def _oracle_step(orc, ir, cells, dt, icntrl, rcntrl, atol, rtol, hstart=None):
+    """Do_FullChem loop body on the CPU: zero families, rates, integrate,
+    retry once from C_before with Hstart=0, clamp (fullchem_mod.F90:943-1350)."""
+    c = cells["c"].copy()
+    for fam in ir["families"]:
+        c[ir["species"].index(fam)] = 0.0
+    r = orc.update_rconst(cells["met"], cells["photol"], c)
+    c1, ist, rst, ierr = orc.integrate(c, r, atol, rtol, 0.0, dt, icntrl, rcntrl, hstart=hstart)
+    bad = ierr < 0
+    if bad.any():
+        c2, ist2, rst2, ierr2 = orc.integrate(c[:, bad], r[:, bad], atol, rtol, 0.0, dt, icntrl, rcntrl)
+        c1[:, bad], ist[:, bad], rst[:, bad], ierr[bad] = c2, ist2, rst2, ierr2
+    return np.maximum(c1, 0.0), ist, rst, ierr, int(bad.sum())
+
+
+@pytest.fixture(scope="module")
+def step_case():
+    n = 192
+    cells = inputs.box_cells(n, seed=21)
+    atol, rtol = inputs.tolerances()
+    icntrl, rcntrl = inputs.default_controls()
+    return dict(n=n, cells=cells, atol=atol, rtol=rtol, icntrl=icntrl, rcntrl=rcntrl)
+
+
+def _gpu_step(solver, case, icntrl=None, hstart=None, dt=600.0, arith="strict"):
+    solver.set(arith=arith, schedule="plain", block=0)
+    n = case["n"]
+    c = case["cells"]["c"].copy()
+    ist = np.zeros((20, n), np.int32)
+    rst = np.zeros((20, n))
+    ierr = np.zeros(n, np.int32)
+    hs = None if hstart is None else hstart.copy()
+    nretry = solver.fullchem_step(dt, case["cells"]["met"], case["cells"]["photol"], c, case["atol"], case["rtol"],
+                                  case["icntrl"] if icntrl is None else icntrl, case["rcntrl"], hs, ist, rst, ierr)
+    return c, ist, rst, ierr, nretry, hs
+
+
+def test_fullchem_step_matches_oracle(solver, orc, step_case):
+    ir = mechanism.load_ir()
+    c, ist, rst, ierr, nretry, _ = _gpu_step(solver, step_case)
+    c_ref, ist_ref, rst_ref, ierr_ref, nretry_ref = _oracle_step(orc, ir, step_case["cells"], 600.0,
+                                                                 step_case["icntrl"], step_case["rcntrl"],
+                                                                 step_case["atol"], step_case["rtol"])
+    assert nretry == nretry_ref == 0
+    assert np.array_equal(ierr, ierr_ref)
+    same = np.all(ist[:8] == ist_ref[:8], axis=0)
+    assert same.mean() >= 0.99
+    big = np.abs(c_ref) > 1e4
+    assert np.max(np.where(big, _rel(c, c_ref), 0.0)[:, same]) < 1e-9
+    assert np.all(c >= 0.0)
+    for fam in ir["families"]:
+        # dummies were zeroed before the integration, then produced again
+        assert np.all(np.isfinite(c[ir["species"].index(fam)]))
+
+
+def test_retry_policy_and_hnew_chain(solver, orc, step_case):
+    """Cells that fail (step cap, IERR=-6) are integrated once more from the
+    saved concentrations with Hstart = 0; KPPHvalue = RSTATE(Nhnew)."""
+    ir = mechanism.load_ir()
+    ic = step_case["icntrl"].copy()
+    ic[3] = 20  # Max_no_steps: most random cells fail at 600 s
+    hs = np.full(step_case["n"], 1.0)
+    c, ist, rst, ierr, nretry, hs_out = _gpu_step(solver, step_case, icntrl=ic, hstart=hs)
+    c_ref, ist_ref, rst_ref, ierr_ref, nretry_ref = _oracle_step(orc, ir, step_case["cells"], 600.0, ic,
+                                                                 step_case["rcntrl"], step_case["atol"],
+                                                                 step_case["rtol"], hstart=hs)
+    assert nretry == nretry_ref and nretry > 0
+    assert np.array_equal(ierr, ierr_ref)
+    assert set(np.unique(ierr)) <= {1, -6}
+    same = np.all(ist[:8] == ist_ref[:8], axis=0)
+    assert same.mean() >= 0.98
+    assert np.allclose(hs_out, rst[2])
+    big = np.abs(c_ref) > 1e4
+    assert np.max(np.where(big, _rel(c, c_ref), 0.0)[:, same]) < 1e-9
+
+
+@pytest.mark.parametrize("field,value,code", [("rtol", 1.0, -5), ("atol", 0.0, -5), ("method", 9, -2),
+                                              ("maxsteps", -1, -1)])
+def test_option_errors_give_reference_ierr(solver, step_case, field, value, code):
+    n = step_case["n"]
+    at, rt = step_case["atol"].copy(), step_case["rtol"].copy()
+    ic = step_case["icntrl"].copy()
+    if field == "rtol":
+        rt[5] = value
+    elif field == "atol":
+        at[7] = value
+    elif field == "method":
+        ic[2] = value
+    else:
+        ic[3] = value
+    c = step_case["cells"]["c"].copy()
+    r = np.ones((1058, n)) * 1e-12
+    ist = np.full((20, n), 7, np.int32)
+    ierr = np.zeros(n, np.int32)
+    solver.integrate(c, r, at, rt, 0.0, 60.0, ic, step_case["rcntrl"], istatus=ist, ierr=ierr)
+    assert np.all(ierr == code)
+    assert np.all(ist == 0)
+    assert np.array_equal(c, step_case["cells"]["c"])
+
+
+@pytest.mark.parametrize("which", ["rate_updates", "autoreduce"])
+def test_unsupported_options_are_rejected(solver, step_case, which):
+    n = step_case["n"]
+    ic = step_case["icntrl"].copy()
+    if which == "rate_updates":
+        ic[14] = 0  # INTEGRATE then defaults ICNTRL(15) to 5: updates inside the integrator
+    else:
+        ic[11] = 1
+    c = step_case["cells"]["c"].copy()
+    r = np.ones((1058, n)) * 1e-12
+    ierr = np.zeros(n, np.int32)
+    with pytest.raises(capi.GcKppError) as e:
+        solver.integrate(c, r, step_case["atol"], step_case["rtol"], 0.0, 60.0, ic, step_case["rcntrl"], ierr=ierr)
+    assert e.value.code == capi.GC_KPP_EUNSUPPORTED
+
+
+def test_host_and_device_paths_agree(solver, orc, step_case):
+    import torch
+
+    n = step_case["n"]
+    cells = step_case["cells"]
+    r = orc.update_rconst(cells["met"], cells["photol"], cells["c"])
+    solver.set(arith="fast", schedule="queue", block=64)
+    c_h = cells["c"].copy()
+    ist_h = np.zeros((20, n), np.int32)
+    ierr_h = np.zeros(n, np.int32)
+    solver.integrate(c_h, r, step_case["atol"], step_case["rtol"], 0.0, 300.0, step_case["icntrl"],
+                     step_case["rcntrl"], istatus=ist_h, ierr=ierr_h)
+    dev = torch.device("cuda", 0)
+    T = lambda a: torch.tensor(a, device=dev).contiguous()
+    c_d = T(cells["c"])
+    ist_d = torch.zeros((20, n), dtype=torch.int32, device=dev)
+    ierr_d = torch.zeros(n, dtype=torch.int32, device=dev)
+    solver.integrate(c_d, T(r), T(step_case["atol"]), T(step_case["rtol"]), 0.0, 300.0, step_case["icntrl"],
+                     step_case["rcntrl"], istatus=ist_d, ierr=ierr_d)
+    torch.cuda.synchronize()
+    assert np.array_equal(c_h, c_d.cpu().numpy())
+    assert np.array_equal(ist_h, ist_d.cpu().numpy())
+    assert np.array_equal(ierr_h, ierr_d.cpu().numpy())
+
+
+@pytest.mark.parametrize("schedule", ["queue", "plain"])
+def test_queue_order_changes_nothing_but_packing(solver, step_case, schedule):
+    """gc_kpp_fullchem_step_ordered: any permutation gives bit-identical
+    results to the unordered step, on host and device memory."""
+    import torch
+
+    n = step_case["n"]
+    cells = step_case["cells"]
+    ic = step_case["icntrl"]
+
+    def run(order, device=False):
+        solver.set(arith="fast", schedule=schedule, block=64)
+        if device:
+            dev = torch.device("cuda", 0)
+            T = lambda a: torch.tensor(a, device=dev).contiguous()
+            c = T(cells["c"])
+            hs = torch.full((n,), 30.0, dtype=torch.float64, device=dev)
+            ist = torch.zeros((20, n), dtype=torch.int32, device=dev)
+            rst = torch.zeros((20, n), dtype=torch.float64, device=dev)
+            ierr = torch.zeros(n, dtype=torch.int32, device=dev)
+            solver.fullchem_step(600.0, T(cells["met"]), T(cells["photol"]), c, T(step_case["atol"]),
+                                 T(step_case["rtol"]), ic, step_case["rcntrl"], hs, ist, rst, ierr,
+                                 order=None if order is None else torch.tensor(order, dtype=torch.int32, device=dev))
+            torch.cuda.synchronize()
+            return [x.cpu().numpy() for x in (c, hs, ist, rst, ierr)]
+        c = cells["c"].copy()
+        hs = np.full(n, 30.0)
+        ist = np.zeros((20, n), np.int32)
+        rst = np.zeros((20, n))
+        ierr = np.zeros(n, np.int32)
+        solver.fullchem_step(600.0, cells["met"], cells["photol"], c, step_case["atol"], step_case["rtol"], ic,
+                             step_case["rcntrl"], hs, ist, rst, ierr, order=order)
+        return [c, hs, ist, rst, ierr]
+
+    base = run(None)
+    perm = np.random.default_rng(5).permutation(n).astype(np.int32)
+    heavy_first = np.argsort(-base[2][2], kind="stable").astype(np.int32)
+    for got in (run(perm), run(heavy_first), run(perm, device=True)):
+        for a, b in zip(got, base):
+            assert np.array_equal(a, b)
+
+
+def test_host_order_must_be_a_permutation(solver, step_case):
+    n = step_case["n"]
+    cells = step_case["cells"]
+    bad = np.arange(n, dtype=np.int32)
+    bad[3] = 5
+    c = cells["c"].copy()
+    ierr = np.zeros(n, np.int32)
+    with pytest.raises(capi.GcKppError) as e:
+        solver.fullchem_step(600.0, cells["met"], cells["photol"], c, step_case["atol"], step_case["rtol"],
+                             step_case["icntrl"], step_case["rcntrl"], ierr=ierr, order=bad)
+    assert e.value.code == capi.GC_KPP_EINVAL
