@@ -41,6 +41,7 @@ EXPORTED = [
     "gc_kpp_update_rconst_batch",
     "gc_kpp_fullchem_step",
     "gc_kpp_fullchem_step_ordered",
+    "gc_kpp_integrate_batch_noalloc",
     "gc_kpp_last_launch_count",
     "gc_kpp_last_kernel_ms",
 ]

@@ -733,3 +733,185 @@ int gc_kpp_update_rconst_batch(gc_kpp_ctx* c, int ncell, const double* met, long
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// No-allocation entry point.  Everything it needs on the device lives in
+// file-scope __device__ arrays of this translation unit: the workspace for at
+// most NOALLOC_MAX_CELLS cells and copies of the mechanism tables.  Host code
+// cannot use those arrays' names as device addresses, so the first call on
+// each device, with that device current, copies the tables in with
+// cudaMemcpyToSymbol and takes every address with cudaGetSymbolAddress.
+namespace {
+
+constexpr int NOALLOC_MAX_CELLS = 1024;
+constexpr int NOALLOC_BLOCK = 128;
+constexpr int NOALLOC_WS_TOTAL = T::NAUX + 2 * T::NSPEC + 3 * T::NVAR + SMAX * T::NVAR + T::NREACT + T::NB +
+                                 2 * T::LU_NONZERO;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) double g_noalloc_ws[(size_t)NOALLOC_MAX_CELLS * NOALLOC_WS_TOTAL];
+
+#define GC_NA_TABLE(type, name) static __device__ type g_na_##name[sizeof(T::name) / sizeof(T::name[0])];
+GC_NA_TABLE(unsigned, prod_packed)
+GC_NA_TABLE(double, pre_literals)
+GC_NA_TABLE(int, p_start)
+GC_NA_TABLE(unsigned, p_sterm)
+GC_NA_TABLE(int, d_start)
+GC_NA_TABLE(unsigned, d_sterm)
+GC_NA_TABLE(int, j_start)
+GC_NA_TABLE(unsigned, j_sterm)
+GC_NA_TABLE(double, slit)
+GC_NA_TABLE(int, lu_crow)
+GC_NA_TABLE(int, lu_diag)
+GC_NA_TABLE(int, lu_icol)
+GC_NA_TABLE(int, lrow_start)
+GC_NA_TABLE(int, lop_kk)
+GC_NA_TABLE(int, lop_dj)
+GC_NA_TABLE(int, lop_u)
+GC_NA_TABLE(unsigned, uop)
+GC_NA_TABLE(int, dot_start)
+GC_NA_TABLE(unsigned, dot_term)
+GC_NA_TABLE(double, lit)
+#undef GC_NA_TABLE
+
+struct NoAllocDevice {
+  bool ready = false;
+  MechDev mech{};
+  double* ws = nullptr;
+};
+NoAllocDevice g_noalloc[NOALLOC_MAX_DEVICES];
+std::mutex g_noalloc_mutex;
+
+// Per-device set-up (the current device): fill the table copies and take the
+// device addresses of the tables and of the workspace.
+int noalloc_setup(int dev, NoAllocDevice** out) {
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(GC_KPP_EINVAL, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  NoAllocDevice& d = g_noalloc[dev];
+  if (!d.ready) {
+    if (make_layout().total != NOALLOC_WS_TOTAL) return fail(GC_KPP_EINVAL, "workspace layout mismatch");
+    MechDev& m = d.mech;
+    m.nvar = T::NVAR; m.nfix = T::NFIX; m.nreact = T::NREACT; m.nspec = T::NSPEC;
+    m.lu_nonzero = T::LU_NONZERO; m.nb = T::NB; m.lit0 = T::LIT0; m.naux = T::NAUX;
+    void* p = nullptr;
+#define GC_NA_FILL(field, name, type)                                                        \
+    GC_CUDA(cudaMemcpyToSymbol(g_na_##name, T::name, sizeof(T::name)));                      \
+    GC_CUDA(cudaGetSymbolAddress(&p, g_na_##name));                                          \
+    m.field = reinterpret_cast<type>(p);
+    GC_NA_FILL(prod_packed, prod_packed, const uint2*)
+    GC_NA_FILL(pre_lit, pre_literals, const double*)
+    GC_NA_FILL(p_start, p_start, const int*)
+    GC_NA_FILL(p_sterm, p_sterm, const unsigned*)
+    GC_NA_FILL(d_start, d_start, const int*)
+    GC_NA_FILL(d_sterm, d_sterm, const unsigned*)
+    GC_NA_FILL(j_start, j_start, const int*)
+    GC_NA_FILL(j_sterm, j_sterm, const unsigned*)
+    GC_NA_FILL(slit, slit, const double*)
+    GC_NA_FILL(lu_crow, lu_crow, const int*)
+    GC_NA_FILL(lu_diag, lu_diag, const int*)
+    GC_NA_FILL(lu_icol, lu_icol, const int*)
+    GC_NA_FILL(lrow_start, lrow_start, const int*)
+    GC_NA_FILL(lop_kk, lop_kk, const int*)
+    GC_NA_FILL(lop_dj, lop_dj, const int*)
+    GC_NA_FILL(lop_u, lop_u, const int*)
+    GC_NA_FILL(uop, uop, const unsigned*)
+    GC_NA_FILL(dot_start, dot_start, const int*)
+    GC_NA_FILL(dot_term, dot_term, const unsigned*)
+    GC_NA_FILL(lit, lit, const double*)
+#undef GC_NA_FILL
+    double* ws = nullptr;
+    GC_CUDA(cudaGetSymbolAddress((void**)&ws, g_noalloc_ws));
+    d.ws = ws;
+    d.ready = true;
+  }
+  *out = &d;
+  return GC_KPP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gc_kpp_integrate_batch_noalloc(int ncell, double tin, double tout, double* c, long long ldc, const double* rconst,
+                                   long long ldr, const double* atol, const double* rtol, const int* icntrl_u,
+                                   const double* rcntrl_u, const double* hstart, int* istatus, double* rstatus,
+                                   long long ldo, int* ierr, void* stream) {
+  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
+  if (ncell > NOALLOC_MAX_CELLS)
+    return fail(GC_KPP_EINVAL, "ncell exceeds the no-allocation workspace (GC_KPP_NOALLOC_MAX_CELLS = 1024 cells "
+                               "per call); split the batch");
+  if (ncell == 0) return GC_KPP_OK;
+  if (!c || !rconst || !atol || !rtol || !ierr) return fail(GC_KPP_EINVAL, "required array is NULL");
+  if (ldc < ncell || ldr < ncell || ((istatus || rstatus) && ldo < ncell))
+    return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
+  int dev = 0;
+  GC_CUDA(cudaGetDevice(&dev));
+  NoAllocDevice* d = nullptr;
+  GC_TRY(noalloc_setup(dev, &d));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Resolved R;
+  GC_TRY(resolve(icntrl_u, rcntrl_u, tin, tout, R));
+  if (!R.code) {
+    // Rosenbrock's tolerance check (:464-472) on host copies held on the stack
+    const int ntol = R.vector_tol ? T::NVAR : 1;
+    double at[T::NVAR], rt[T::NVAR];
+    GC_CUDA(cudaMemcpyAsync(at, atol, ntol * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaMemcpyAsync(rt, rtol, ntol * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < ntol; ++i)
+      if (!(at[i] > 0.0) || rt[i] <= 10.0 * DBL_EPSILON || rt[i] >= 1.0) R.code = -5;
+  }
+  if (R.code) {
+    int e[NOALLOC_MAX_CELLS];
+    for (int i = 0; i < ncell; ++i) e[i] = R.code;
+    GC_CUDA(cudaMemcpyAsync(ierr, e, ncell * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (istatus) GC_CUDA(cudaMemset2DAsync(istatus, ldo * sizeof(int), 0, ncell * sizeof(int), 20, s));
+    if (rstatus) GC_CUDA(cudaMemset2DAsync(rstatus, ldo * sizeof(double), 0, ncell * sizeof(double), 20, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+    return GC_KPP_OK;
+  }
+  // One thread and one workspace slot per cell (plain schedule).  Every slot
+  // entry the kernel reads it has written earlier in the same call, so the
+  // previous call's contents need no clearing.
+  const int nc = gckpp_cells_per_thread_fast();
+  const int grid = (ncell + NOALLOC_BLOCK * nc - 1) / (NOALLOC_BLOCK * nc);
+  RosParams p{};
+  p.ncell = ncell;
+  p.cell_limit = ncell;
+  p.c_in = c;
+  p.c_out = c;
+  p.ldc = ldc;
+  p.rconst = rconst;
+  p.ldr = ldr;
+  p.hstart = hstart;
+  p.istatus = istatus;
+  p.rstatus = rstatus;
+  p.ldo = ldo;
+  p.ierr = ierr;
+  p.atol = atol;
+  p.rtol = rtol;
+  p.vector_tol = R.vector_tol ? 1 : 0;
+  p.tstart = tin;
+  p.tend = tout;
+  p.hmin = R.hmin;
+  p.hmax = R.hmax;
+  p.hstart_default = R.hstart_default;
+  p.facmin = R.facmin;
+  p.facmax = R.facmax;
+  p.facrej = R.facrej;
+  p.facsafe = R.facsafe;
+  p.roundoff = DBL_EPSILON;
+  p.autonomous = R.autonomous;
+  p.max_steps = R.max_steps;
+  p.clamp_negative = R.clamp;
+  p.lu_form = 0;
+  p.ws = d->ws;
+  p.lay = make_layout();
+  p.nslot = (long long)grid * NOALLOC_BLOCK * nc;
+  if (p.nslot > NOALLOC_MAX_CELLS) return fail(GC_KPP_EINVAL, "no-allocation workspace too small");
+  cudaError_t e = gckpp_launch_ros_fast(0, grid, NOALLOC_BLOCK, d->mech, R.meth, p, s);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return GC_KPP_OK;
+}
+
+}  // extern "C"

@@ -175,6 +175,32 @@ int gc_kpp_fullchem_step_ordered(gc_kpp_ctx* ctx, int ncell, double dt, const do
                                  double* hstart, int* istatus, double* rstatus, long long ldo, int* ierr,
                                  int* nretry, const int* order, int mem, void* stream);
 
+/* Batched INTEGRATE that allocates nothing, for callers that cannot call
+ * cudaMalloc: code running inside a host application's memory-pool or
+ * graph-building phase, an embedding framework that owns all device memory,
+ * or a process whose allocator must not be touched mid-step.  No counterpart
+ * in the reference (whose state is module globals); arguments and results
+ * are those of gc_kpp_integrate_batch, with every array in device memory and
+ * the fast arithmetic with one thread per cell.
+ *
+ * It needs no context: its workspace for at most GC_KPP_NOALLOC_MAX_CELLS
+ * cells (about 157 MB) and its copy of the mechanism tables are file-scope
+ * device arrays of the library, held by every GPU that loads it until the
+ * process exits.  Larger batches are rejected with GC_KPP_EINVAL: split them.
+ * The first call on a device sets it up (copies the tables in and looks up
+ * the device addresses, with that device current), so make that first call
+ * before any stream capture.  All calls on a device share its one workspace:
+ * calls that overlap on the GPU (issued on different streams or from
+ * different host threads) race and must be serialised by the caller.  The
+ * workspace keeps the last call's contents; nothing in it needs to start at
+ * zero, since every entry a call reads it has written first. */
+#define GC_KPP_NOALLOC_MAX_CELLS 1024
+int gc_kpp_integrate_batch_noalloc(int ncell, double tin, double tout, double* c, long long ldc,
+                                   const double* rconst, long long ldr, const double* atol,
+                                   const double* rtol, const int* icntrl, const double* rcntrl,
+                                   const double* hstart, int* istatus, double* rstatus, long long ldo,
+                                   int* ierr, void* stream);
+
 /* Number of kernels the last gc_kpp_fullchem_step call on ctx launched. */
 int gc_kpp_last_launch_count(gc_kpp_ctx* ctx);
 
