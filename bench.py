@@ -36,6 +36,7 @@ METRIC = "fullchem cells/s per 1200 s step, learned-binned vs plain GPU, at RTOL
 GRID = (72, 46, 72)
 DT = 1200.0
 SPINUP_S = 86400.0
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "geos-chem_gb300", "weights", "proposer_4x5.npz")
 
 
 def parse():
@@ -50,6 +51,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample duration")
+    ap.add_argument("--weights", default=WEIGHTS, help="trained proposer weights (.npz)")
+    ap.add_argument("--error-cells", type=int, default=2048, help="cells integrated at RTOL 1e-8 for the error")
     return ap.parse_args()
 
 
@@ -126,7 +129,7 @@ def algorithmic_flops(tables, istatus, method_S=4):
     return float(tot)
 
 
-def cpu_baseline_sample(orc, cells_host, rconst_host, atol, rtol, icntrl, rcntrl, target_s, threads):
+def cpu_baseline_sample(orc, cells_host, rconst_host, atol, rtol, icntrl, rcntrl, target_s, threads, hstart=None):
     """Time the oracle's OpenMP cell loop on evenly spaced cells of the grid."""
     ncell = cells_host["c"].shape[1]
 
@@ -134,8 +137,9 @@ def cpu_baseline_sample(orc, cells_host, rconst_host, atol, rtol, icntrl, rcntrl
         idx = np.linspace(0, ncell - 1, m).astype(np.int64)
         c = cells_host["c"][:, idx]
         r = rconst_host[:, idx]
+        hs = None if hstart is None else np.ascontiguousarray(hstart[idx])
         t0 = time.perf_counter()
-        orc.integrate(c, r, atol, rtol, 0.0, DT, icntrl, rcntrl, variant="fast", nthreads=threads)
+        orc.integrate(c, r, atol, rtol, 0.0, DT, icntrl, rcntrl, hstart=hs, variant="fast", nthreads=threads)
         return time.perf_counter() - t0
 
     m = 4 * threads
@@ -216,6 +220,7 @@ def run_ours(args):
     __graft_entry__.load_package()
     import gcchem.capi as capi
     import gcchem.inputs as inputs
+    import gcchem.learned as learned
     import gcchem.tables as tables_mod
     from gcchem import build as gbuild
 
@@ -229,10 +234,6 @@ def run_ours(args):
 
     solver = capi.Solver(local, arith="fast", schedule=args.schedule)
     lib = solver.lib
-    lib.gc_kpp_fullchem_step.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double] + \
-        [ctypes.c_void_p, ctypes.c_longlong] * 3 + [ctypes.c_void_p] * 5 + \
-        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p,
-         ctypes.c_int, ctypes.c_void_p]
     lib.gc_kpp_last_kernel_ms.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_int)]
     lib.gc_kpp_last_launch_count.argtypes = [ctypes.c_void_p]
@@ -245,74 +246,95 @@ def run_ours(args):
     ist = torch.zeros((20, ncell), dtype=torch.int32, device=dev)
     rst = torch.zeros((20, ncell), dtype=torch.float64, device=dev)
     ierr = torch.zeros(ncell, dtype=torch.int32, device=dev)
-    icn = np.ascontiguousarray(icntrl, np.int32)
-    rcn = np.ascontiguousarray(rcntrl, np.float64)
-    nretry = ctypes.c_int(0)
+    dev_t = {"met": met, "ph": ph, "ist": ist, "rst": rst, "ierr": ierr, "at": at, "rt": rt}
+    last = {"nretry": 0}
 
-    def step(c, hstart=None, dt=DT, mem=capi.MEM_DEVICE, stream_ptr=sp, tensors=None):
-        tt = tensors or {"met": met, "ph": ph, "c": c, "ist": ist, "rst": rst, "ierr": ierr, "at": at, "rt": rt}
-        rc = lib.gc_kpp_fullchem_step(
-            solver.ctx, ncell, float(dt), capi._ptr(tt["met"]), ncell, capi._ptr(tt["ph"]), ncell,
-            capi._ptr(tt["c"]), ncell, capi._ptr(tt["at"]), capi._ptr(tt["rt"]),
-            icn.ctypes.data_as(ctypes.c_void_p), rcn.ctypes.data_as(ctypes.c_void_p),
-            capi._ptr(hstart), capi._ptr(tt["ist"]), capi._ptr(tt["rst"]), ncell, capi._ptr(tt["ierr"]),
-            ctypes.byref(nretry), mem, ctypes.c_void_p(stream_ptr))
-        if rc != 0:
-            raise capi.GcKppError(rc, lib.gc_kpp_last_error().decode())
+    def step(c, hs, order=None, nblock=0, dt=DT, tt=dev_t, solver_=solver, rtol_=None):
+        last["nretry"] = solver_.fullchem_step(dt, tt["met"], tt["ph"], c, tt["at"],
+                                               tt["rt"] if rtol_ is None else rtol_, icntrl, rcntrl, hs,
+                                               tt["ist"], tt["rst"], tt["ierr"], order=order, nblock=nblock,
+                                               stream=sp)
 
-    # spin-up (untimed): 24 h from the random initial state
+    # spin-up (untimed): 24 h from the random initial state; hs_spun receives
+    # the KPPHvalue chain (RSTATE(Nhnew)) that the timed steps start from
     t0 = time.perf_counter()
     c_spun = c0.clone()
+    hs_spun = torch.zeros(ncell, dtype=torch.float64, device=dev)
     if args.spinup > 0:
-        step(c_spun, dt=args.spinup)
+        step(c_spun, hs_spun, dt=args.spinup)
     torch.cuda.synchronize()
     spin_s = time.perf_counter() - t0
     spin_steps = float(ist[2].double().mean().item())
 
-    # rate constants of the spun-up state (for the roofline / CPU baseline)
-    work = c_spun.clone()
-    for _ in range(args.warmup):
-        work.copy_(c_spun)
-        step(work)
-    torch.cuda.synchronize()
+    prop = learned.Proposer(local)
+    prop.load_state(dict(np.load(args.weights)))
 
-    sampler = ClockSampler(local)
-    if world > 1:
-        torch.distributed.barrier()
-    solver.set_timing = None
-    lib.gc_kpp_ctx_set_option(solver.ctx, 6, 1)  # GC_KPP_OPT_TIMING
-    sampler.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    kernel_ms = []
-    launches = 0
-    ev0.record(stream)
-    for _ in range(args.steps):
-        work.copy_(c_spun)
-        step(work)
-        ms = ctypes.c_double(0.0)
-        nl = ctypes.c_int(0)
-        lib.gc_kpp_last_kernel_ms(solver.ctx, ctypes.byref(ms), ctypes.byref(nl))
-        kernel_ms.append(ms.value / max(nl.value, 1))
-        launches += lib.gc_kpp_last_launch_count(solver.ctx)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    lib.gc_kpp_ctx_set_option(solver.ctx, 6, 0)
-    ms_step = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * ncell / (ms_step * 1e-3)
+    def plain_arm(w, hs):
+        step(w, hs)
 
-    ist_h = ist.cpu().numpy()
-    ierr_h = ierr.cpu().numpy()
+    def learned_arm(w, hs, met_=met, ph_=ph, tt=dev_t):
+        # H0 proposals seed RCNTRL(3) where the cell has no KPPHvalue yet;
+        # stiffness bins order the queue and the top bin goes block-per-cell
+        _, _, order = learned.plan(prop, met_, ph_, w, stream=sp, hstart=hs, hmax=DT)
+        nheavy = int(prop.last_counts[learned.NBIN - 1].item())
+        last["nblock"] = nheavy
+        step(w, hs, order=order, nblock=nheavy, tt=tt)
+
+    # cold: every cell starts from RCNTRL(3) = 0 (DeltaMin) unless the network
+    # proposes H0; chained: every cell starts from its KPPHvalue
+    cold0 = torch.zeros_like(hs_spun)
+    arms = {"plain": (plain_arm, 0, cold0), "learned": (learned_arm, learned.PLAN_LAUNCHES, cold0),
+            "plain_chained": (plain_arm, 0, hs_spun),
+            "learned_chained": (learned_arm, learned.PLAN_LAUNCHES, hs_spun)}
+
+    def time_arm(name):
+        fn, extra, hs0 = arms[name]
+        work = c_spun.clone()
+        hs = hs0.clone()
+        for _ in range(args.warmup):
+            work.copy_(c_spun)
+            hs.copy_(hs0)
+            fn(work, hs)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        lib.gc_kpp_ctx_set_option(solver.ctx, 6, 1)  # GC_KPP_OPT_TIMING
+        sampler = ClockSampler(local)
+        sampler.start()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        kernel_ms, launches = [], 0
+        ev0.record(stream)
+        for _ in range(args.steps):
+            work.copy_(c_spun)  # reset to the spun-up state (and its KPPHvalue chain)
+            hs.copy_(hs0)
+            fn(work, hs)
+            ms = ctypes.c_double(0.0)
+            nl = ctypes.c_int(0)
+            lib.gc_kpp_last_kernel_ms(solver.ctx, ctypes.byref(ms), ctypes.byref(nl))
+            kernel_ms.append(ms.value)
+            launches += lib.gc_kpp_last_launch_count(solver.ctx) + extra
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        clocks = sampler.stop()
+        lib.gc_kpp_ctx_set_option(solver.ctx, 6, 0)
+        ms_step = ev0.elapsed_time(ev1) / args.steps
+        if world > 1:
+            t = torch.tensor([ms_step], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms_step = float(t.item())
+        return {"ms_per_step": ms_step, "value": world * ncell / (ms_step * 1e-3),
+                "kernel_ms": float(np.mean(kernel_ms)), "gpu_launches": int(launches), "clocks": clocks,
+                "ist": ist.cpu().numpy(), "ierr": ierr.cpu().numpy(), "retried_cells": int(last["nretry"]),
+                "block_per_cell_cells": int(last.get("nblock", 0)) if name == "learned" else 0,
+                "c": work.clone()}
+
+    res = {name: time_arm(name) for name in arms}
+    head = res["learned"]
     tabs = tables_mod.Tables(__import__("gcchem.mechanism", fromlist=["x"]).load_ir())
-    flops = algorithmic_flops(tabs, ist_h)
-    kms = float(np.mean(kernel_ms))
-    achieved_tf = flops / (kms * 1e-3) / 1e12
+    flops = algorithmic_flops(tabs, head["ist"])
+    achieved_tf = flops / (head["kernel_ms"] * 1e-3) / 1e12
 
     # FP64 peak measured on this GPU (roofline denominator)
     peak_gf = None
@@ -325,29 +347,61 @@ def run_ours(args):
     except OSError:
         pass
 
-    # end-to-end: the same chemistry step through the C ABI with host buffers
+    # error of both forms against an RTOL = 1e-8 FP64 integration (strict
+    # arithmetic) of evenly spaced cells, from the same state and chain
+    idx = torch.linspace(0, ncell - 1, min(ncell, args.error_cells), device=dev).long()
+    sub = {k: v.index_select(1, idx).contiguous() for k, v in (("met", met), ("ph", ph))}
+    m = idx.numel()
+    sub.update(ist=torch.zeros((20, m), dtype=torch.int32, device=dev),
+               rst=torch.zeros((20, m), dtype=torch.float64, device=dev),
+               ierr=torch.zeros(m, dtype=torch.int32, device=dev), at=at, rt=rt)
+    tight = capi.Solver(local, arith="strict", schedule="queue")
+    c_ref = c_spun.index_select(1, idx).contiguous()
+    step(c_ref, hs_spun.index_select(0, idx).contiguous(), tt=sub, solver_=tight,
+         rtol_=torch.full_like(rt, 1e-8))
+    torch.cuda.synchronize()
+    tight_steps = float(sub["ist"][2].double().mean().item())
+    tight.close()
+    nvar = 353
+
+    def rel_err(c):
+        got = c.index_select(1, idx)[:nvar]
+        ref = c_ref[:nvar]
+        mask = ref > 1e4
+        e = ((got - ref).abs() / ref.clamp_min(1e-300))[mask]
+        return {"max": float(e.max().item()), "median": float(e.median().item())}
+
+    errors = {name: rel_err(res[name]["c"]) for name in arms}
+
+    # end to end through the public API: pinned host inputs copied in, the
+    # learned plan and the ordered chemistry step, results copied out
     e2e = None
     if rank == 0 or world > 1:
-        pin = {
-            "met": torch.tensor(cells["met"]).pin_memory(), "ph": torch.tensor(cells["photol"]).pin_memory(),
-            "c": c_spun.cpu().pin_memory(), "ist": torch.zeros((20, ncell), dtype=torch.int32).pin_memory(),
-            "rst": torch.zeros((20, ncell), dtype=torch.float64).pin_memory(),
-            "ierr": torch.zeros(ncell, dtype=torch.int32).pin_memory(),
-            "at": torch.tensor(atol).contiguous(), "rt": torch.tensor(rtol).contiguous(),
-        }
-        c_host0 = pin["c"].clone()
+        pin = lambda x: x.cpu().pin_memory()
+        h = {"met": pin(met), "ph": pin(ph), "c": pin(c_spun), "hs": pin(cold0)}
+        out = {"c": pin(c_spun), "hs": pin(hs_spun), "ist": pin(ist), "rst": pin(rst), "ierr": pin(ierr)}
+        d = {k: torch.empty_like(v, device=dev) for k, v in h.items()}
+        tt = dict(dev_t, met=d["met"], ph=d["ph"])
         tms = []
         for it in range(1 + min(args.steps, 2)):
-            pin["c"].copy_(c_host0)
+            torch.cuda.synchronize()
             t0 = time.perf_counter()
-            step(None, mem=capi.MEM_HOST, stream_ptr=sp, tensors=pin)
-            dt = time.perf_counter() - t0
+            for k in h:
+                d[k].copy_(h[k], non_blocking=True)
+            learned_arm(d["c"], d["hs"], met_=d["met"], ph_=d["ph"], tt=tt)
+            out["c"].copy_(d["c"], non_blocking=True)
+            out["hs"].copy_(d["hs"], non_blocking=True)
+            out["ist"].copy_(ist, non_blocking=True)
+            out["rst"].copy_(rst, non_blocking=True)
+            out["ierr"].copy_(ierr, non_blocking=True)
+            torch.cuda.synchronize()
             if it > 0:
-                tms.append(dt)
-        h2d = ncell * 8 * (18 + 200 + 356) + 2 * 353 * 8
-        d2h = ncell * (8 * 356 + 4 + 20 * 4 + 20 * 8)
+                tms.append(time.perf_counter() - t0)
+        h2d = sum(v.numel() * v.element_size() for v in h.values())
+        d2h = sum(v.numel() * v.element_size() for v in out.values())
         e2e = {"value": world * ncell / float(np.mean(tms)), "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+               "d2h_bytes_per_step": int(d2h),
+               "path": "learned.plan + gc_kpp_fullchem_step_binned, pinned host buffers"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -359,32 +413,50 @@ def run_ours(args):
         m, dt = cpu_baseline_sample(orc, host, r_dev.cpu().numpy(), atol, rtol, icntrl, rcntrl, args.cpu_seconds,
                                     threads)
         cpu = {"value": m / dt, "unit": "cells/s", "cores": threads, "kind": "port",
-               "sample": "%d evenly spaced spun-up cells of the grid, one 1200 s Integrate each, oracle -O3 "
-                         "OpenMP DYNAMIC,24 (%.1f s)" % (m, dt)}
+               "sample": "%d evenly spaced spun-up cells of the grid, one 1200 s Integrate each from "
+                         "Hstart = 0, oracle -O3 OpenMP DYNAMIC,24 (%.1f s)" % (m, dt)}
 
     if rank == 0:
+        summary = lambda r, name: {"value": r["value"], "ms_per_step": r["ms_per_step"], "kernel_ms": r["kernel_ms"],
+                             "steps_per_cell": float(r["ist"][2].mean()),
+                             "max_steps_per_cell": int(r["ist"][2].max()),
+                             "ierr_ok_fraction": float((r["ierr"] == 1).mean()),
+                             "retried_cells": r["retried_cells"], "error_vs_rtol_1e-8": errors[name],
+                             "block_per_cell_cells": r["block_per_cell_cells"]}
+        arms_out = {name: summary(res[name], name) for name in arms}
         line = {
-            "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64",
+            "metric": METRIC, "value": head["value"], "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded standard-atmosphere 4x5x72 grid, 24 h GPU spin-up)",
             "config": {"workload": "fullchem 4x5x72 grid (238,464 cells), one 1200 s chemistry step, Rodas3, "
-                                   "RTOL 5e-3 / ATOL 1e-2, FP64",
-                       "cells_per_gpu": ncell, "dt_s": DT, "solver": "%s schedule, fast arithmetic" % args.schedule,
+                                   "RTOL 5e-3 / ATOL 1e-2, FP64, Hstart = 0 (DeltaMin) unless the network "
+                                   "proposes H0",
+                       "cells_per_gpu": ncell, "dt_s": DT,
+                       "solver": "%s schedule, fast arithmetic, 1 cell per thread" % args.schedule,
+                       "value_is": "learned-binned arm: MLP stiffness bins order the persistent queue and "
+                                   "send the top bin block-per-cell",
                        "l2": "inputs larger than L2 (C 0.68 GB, RCONST 2.0 GB per step)",
-                       "steps_per_cell": float(ist_h[2].mean()), "max_steps_per_cell": int(ist_h[2].max()),
-                       "ierr_ok_fraction": float((ierr_h == 1).mean()), "retried_cells": int(nretry.value),
-                       "spinup_s": args.spinup, "spinup_wall_s": spin_s, "spinup_steps_per_cell": spin_steps},
+                       "weights": os.path.basename(args.weights),
+                       "spinup_s": args.spinup, "spinup_wall_s": spin_s, "spinup_steps_per_cell": spin_steps,
+                       "error_cells": int(m), "rtol_1e-8_steps_per_cell": tight_steps},
+            "plain": arms_out["plain"],
+            "learned": arms_out["learned"],
+            "learned_over_plain": head["value"] / res["plain"]["value"],
+            "chained": {"note": "every cell starts from its KPPHvalue (RSTATE(Nhnew) of the spin-up), "
+                                "as Do_FullChem does after its first step",
+                        "plain": arms_out["plain_chained"], "learned": arms_out["learned_chained"],
+                        "learned_over_plain": res["learned_chained"]["value"] / res["plain_chained"]["value"]},
             "e2e": e2e,
-            "gpu_launches": int(launches),
+            "gpu_launches": head["gpu_launches"],
             "roofline": {"bound": "fp64", "achieved": achieved_tf,
                          "peak": (peak_gf / 1e3) if peak_gf else None, "unit": "TFLOP/s",
                          "frac": (achieved_tf / (peak_gf / 1e3)) if peak_gf else None, "traffic": None,
-                         "kernel": "gckpp::ros_kernel (Rosenbrock, thread per cell)",
-                         "kernel_ms": kms, "flops_per_launch": flops,
-                         "peak_source": "measured FP64 FMA probe on this GPU"},
+                         "kernel": "gckpp::ros_kernel (Rosenbrock, thread per cell), learned arm",
+                         "kernel_ms": head["kernel_ms"], "flops_per_launch": flops,
+                         "peak_source": "measured FP64 FMA probe on this GPU (of measured)"},
             "cpu_baseline": cpu,
-            "clocks": clocks,
+            "clocks": head["clocks"],
         }
         print(json.dumps(line), flush=True)
     if world > 1:

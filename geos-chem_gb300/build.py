@@ -38,14 +38,15 @@ def _units():
     k = os.path.join(CSRC, "kpp_kernels.cu")
     return [
         (k, "kpp_kernels_strict.o", ["-DGCKPP_STRICT=1", "-DGCKPP_VARIANT=strict", "-fmad=false"]),
-        (k, "kpp_kernels_fast.o", ["-DGCKPP_STRICT=0", "-DGCKPP_VARIANT=fast", "-DGCKPP_NC=2"]),
-        (k, "kpp_kernels_fast1.o", ["-DGCKPP_STRICT=0", "-DGCKPP_VARIANT=fast1", "-DGCKPP_NC=1"]),
+        (k, "kpp_kernels_fast.o", ["-DGCKPP_STRICT=0", "-DGCKPP_VARIANT=fast", "-DGCKPP_NC=1"]),
+        (k, "kpp_kernels_fast2.o", ["-DGCKPP_STRICT=0", "-DGCKPP_VARIANT=fast2", "-DGCKPP_NC=2"]),
         (k, "kpp_kernels_fast4.o", ["-DGCKPP_STRICT=0", "-DGCKPP_VARIANT=fast4", "-DGCKPP_NC=4"]),
         (os.path.join(CSRC, "kpp_rates.cu"), "kpp_rates.o", []),
         (os.path.join(CSRC, "kpp_util.cu"), "kpp_util.o", []),
         (os.path.join(CSRC, "kpp_mlp.cu"), "kpp_mlp.o", []),
         (os.path.join(CSRC, "gckpp_mlp_capi.cu"), "gckpp_mlp_capi.o", []),
         (os.path.join(CSRC, "gckpp_capi.cu"), "gckpp_capi.o", []),
+        (os.path.join(CSRC, "gckpp_learned_capi.cu"), "gckpp_learned_capi.o", []),
     ]
 
 

@@ -30,6 +30,9 @@ OPT_SCHEDULE = 2
 OPT_BLOCK = 3
 OPT_BLOCKS_PER_SM = 4
 OPT_MAX_SLOTS = 5
+OPT_TIMING = 6
+OPT_LU = 7
+OPT_CELL_BLOCK = 8
 
 EXPORTED = [
     "gc_kpp_mechanism_dims",
@@ -41,6 +44,10 @@ EXPORTED = [
     "gc_kpp_update_rconst_batch",
     "gc_kpp_fullchem_step",
     "gc_kpp_fullchem_step_ordered",
+    "gc_kpp_fullchem_step_binned",
+    "gc_kpp_fullchem_step_learned",
+    "gc_kpp_proposer_create",
+    "gc_kpp_proposer_destroy",
     "gc_kpp_integrate_batch_noalloc",
     "gc_kpp_last_launch_count",
     "gc_kpp_last_kernel_ms",
@@ -118,9 +125,9 @@ class Solver:
         if rc != GC_KPP_OK:
             raise GcKppError(rc, self.lib.gc_kpp_last_error().decode())
 
-    def set(self, arith=None, schedule=None, block=None, blocks_per_sm=None, max_slots=None):
+    def set(self, arith=None, schedule=None, block=None, blocks_per_sm=None, max_slots=None, cell_block=None):
         if arith is not None:
-            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1, "fast1": 2, "fast4": 3}[arith]))
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1, "fast2": 2, "fast4": 3}[arith]))
         if schedule is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_SCHEDULE, {"plain": 0, "queue": 1}[schedule]))
         if block is not None:
@@ -129,6 +136,8 @@ class Solver:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_BLOCKS_PER_SM, int(blocks_per_sm)))
         if max_slots is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_MAX_SLOTS, int(max_slots)))
+        if cell_block is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_CELL_BLOCK, int(cell_block)))
 
     def close(self):
         if self.ctx:
@@ -170,16 +179,19 @@ class Solver:
         self._check(rc)
 
     def fullchem_step(self, dt, met, photol, c, atol, rtol, icntrl=None, rcntrl=None, hstart=None, istatus=None,
-                      rstatus=None, ierr=None, order=None, stream=None):
-        """One Do_FullChem chemistry step over all cells (gc_kpp_fullchem_step,
-        or gc_kpp_fullchem_step_ordered when a queue ``order`` is given).
-        Returns the number of cells integrated a second time (retry)."""
+                      rstatus=None, ierr=None, order=None, nblock=0, stream=None):
+        """One Do_FullChem chemistry step over all cells (gc_kpp_fullchem_step;
+        gc_kpp_fullchem_step_ordered when a queue ``order`` is given;
+        gc_kpp_fullchem_step_binned when the first ``nblock`` cells of the
+        order run block-per-cell).  Returns the number of cells integrated a
+        second time (retry)."""
         lib = self.lib
         if not getattr(lib, "_step_typed", False):
             vp, i32, i64, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
             head = [vp, i32, f64, vp, i64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64, vp, vp]
             lib.gc_kpp_fullchem_step.argtypes = head + [i32, vp]
             lib.gc_kpp_fullchem_step_ordered.argtypes = head + [vp, i32, vp]
+            lib.gc_kpp_fullchem_step_binned.argtypes = head + [vp, i32, i32, vp]
             lib._step_typed = True
         dev = _is_torch(c) and c.is_cuda
         ncell = c.shape[1]
@@ -198,9 +210,37 @@ class Solver:
         else:
             if not _is_torch(order):
                 order = np.ascontiguousarray(order, dtype=np.int32)
-            rc = lib.gc_kpp_fullchem_step_ordered(*args, _ptr(order), mem, s)
+            if nblock:
+                rc = lib.gc_kpp_fullchem_step_binned(*args, _ptr(order), int(nblock), mem, s)
+            else:
+                rc = lib.gc_kpp_fullchem_step_ordered(*args, _ptr(order), mem, s)
         self._check(rc)
         return nretry.value
+
+    def fullchem_step_learned(self, proposer, dt, met, photol, c, atol, rtol, icntrl=None, rcntrl=None,
+                              hstart=None, istatus=None, rstatus=None, ierr=None, stream=None):
+        """gc_kpp_fullchem_step_learned with a gc_kpp_proposer handle
+        (``learned.CProposer``).  Returns (cells retried, cells block-per-cell)."""
+        lib = self.lib
+        if not getattr(lib, "_learned_typed", False):
+            vp, i32, i64, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
+            lib.gc_kpp_fullchem_step_learned.argtypes = [vp, vp, i32, f64, vp, i64, vp, i64, vp, i64, vp, vp, vp,
+                                                         vp, vp, vp, vp, i64, vp, vp, vp, i32, vp]
+            lib._learned_typed = True
+        dev = _is_torch(c) and c.is_cuda
+        ncell = c.shape[1]
+        icn = np.ascontiguousarray(icntrl if icntrl is not None else np.zeros(20), dtype=np.int32)
+        rcn = np.ascontiguousarray(rcntrl if rcntrl is not None else np.zeros(20), dtype=np.float64)
+        nretry, nblock = ctypes.c_int(0), ctypes.c_int(0)
+        ldo = _ld(istatus, ncell) if istatus is not None else ncell
+        s = ctypes.c_void_p(stream) if stream else None
+        rc = lib.gc_kpp_fullchem_step_learned(
+            self.ctx, proposer, ncell, float(dt), _ptr(met), _ld(met, ncell), _ptr(photol), _ld(photol, ncell),
+            _ptr(c), _ld(c, ncell), _ptr(atol), _ptr(rtol), icn.ctypes.data_as(ctypes.c_void_p),
+            rcn.ctypes.data_as(ctypes.c_void_p), _ptr(hstart), _ptr(istatus), _ptr(rstatus), ldo, _ptr(ierr),
+            ctypes.byref(nretry), ctypes.byref(nblock), MEM_DEVICE if dev else MEM_HOST, s)
+        self._check(rc)
+        return nretry.value, nblock.value
 
     def update_rconst(self, met, photol, c, rconst, stream=None):
         """Batched Update_RCONST.  met: [NMET, ncell]; photol: [200, ncell];

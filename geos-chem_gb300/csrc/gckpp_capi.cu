@@ -117,6 +117,9 @@ struct gc_kpp_ctx {
   int arith = 0;     // 0 fast, 1 strict
   int schedule = 0;  // 0 plain, 1 queue
   int block = 128;
+  int cell_block = 256;  // threads of the block-per-cell kernel
+  cudaStream_t side = nullptr;  // block-per-cell launches run beside the queue kernel
+  cudaEvent_t fork = nullptr, join = nullptr;
   int blocks_per_sm = 0;
   long long max_slots = 0;
 };
@@ -162,6 +165,10 @@ int gc_kpp_ctx_create(gc_kpp_ctx** out, int device) {
   UP(lu_crow, lu_crow) UP(lu_diag, lu_diag) UP(lu_icol, lu_icol) UP(lrow_start, lrow_start)
   UP(lop_kk, lop_kk) UP(lop_dj, lop_dj) UP(lop_u, lop_u) UP(uop, uop) UP(lit, lit)
   UP(dot_start, dot_start) UP(dot_term, dot_term)
+  UP(lu_irow, lu_irow) UP(lu_lvl_start, lu_lvl_start) UP(lu_lvl_entry, lu_lvl_entry)
+  UP(fs_lvl_start, fs_lvl_start) UP(fs_lvl_row, fs_lvl_row) UP(bs_lvl_start, bs_lvl_start)
+  UP(bs_lvl_row, bs_lvl_row) UP(fun_rows_by_len, fun_rows_by_len) UP(jac_by_len, jac_by_len)
+  m.lu_nlvl = T::LU_NLVL; m.fs_nlvl = T::FS_NLVL; m.bs_nlvl = T::BS_NLVL;
 #undef UP
   gcrates::RatesDev& rp = c->rates;
   rp.nreact = T::NREACT;
@@ -185,6 +192,9 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
   for (void* p : c->owned) cudaFree(p);
   for (cudaEvent_t ev : c->ev)
     if (ev) cudaEventDestroy(ev);
+  if (c->fork) cudaEventDestroy(c->fork);
+  if (c->join) cudaEventDestroy(c->join);
+  if (c->side) cudaStreamDestroy(c->side);
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
                     &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
                     &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord};
@@ -197,7 +207,8 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
   if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
   switch (key) {
     case GC_KPP_OPT_ARITH:
-      if (v < 0 || v > 3) return fail(GC_KPP_EINVAL, "arith must be 0 (fast), 1 (strict), 2 (fast, L1 bypass) or 3 (fast, 128 registers)");
+      if (v < 0 || v > 3)
+        return fail(GC_KPP_EINVAL, "arith must be 0 (fast), 1 (strict), 2 (fast, 2 cells per thread) or 3 (fast, 4)");
       c->arith = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_SCHEDULE:
@@ -219,6 +230,12 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
       return GC_KPP_OK;
     case GC_KPP_OPT_TIMING:
       c->timing = v ? 1 : 0;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_CELL_BLOCK:
+      if (v == 0) v = 256;
+      if (v < 32 || v > 1024 || v % 32)
+        return fail(GC_KPP_EINVAL, "block-per-cell threads must be a multiple of 32 in [32,1024]");
+      c->cell_block = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_MAX_SLOTS:
       if (v < 0) return fail(GC_KPP_EINVAL, "max slots must be >= 0");
@@ -299,6 +316,7 @@ struct DevArgs {
   int ncell;
   const int* order;  // optional cell list
   int cell_limit;    // cell ids lie in [0, cell_limit); 0 = ncell
+  int nblock;        // the first nblock cells of order run block-per-cell
   const double* c_in;
   double* c_out;
   long long ldc;
@@ -313,13 +331,13 @@ struct DevArgs {
   int* ierr;
 };
 
-// Kernel variant by GC_KPP_OPT_ARITH: 0 fast (2 cells per thread), 1 strict
-// (1 cell per thread), 2 fast with 1 cell per thread, 3 fast with 4.
+// Kernel variant by GC_KPP_OPT_ARITH: 0 fast, 1 strict (both 1 cell per
+// thread), 2 fast with 2 cells per thread, 3 fast with 4.
 cudaError_t variant_launch(int arith, int queue, int grid, int block, const MechDev& m, const RosMethod& r,
                            const RosParams& p, cudaStream_t s) {
   switch (arith) {
     case 1: return gckpp_launch_ros_strict(queue, grid, block, m, r, p, s);
-    case 2: return gckpp_launch_ros_fast1(queue, grid, block, m, r, p, s);
+    case 2: return gckpp_launch_ros_fast2(queue, grid, block, m, r, p, s);
     case 3: return gckpp_launch_ros_fast4(queue, grid, block, m, r, p, s);
     default: return gckpp_launch_ros_fast(queue, grid, block, m, r, p, s);
   }
@@ -328,7 +346,7 @@ cudaError_t variant_launch(int arith, int queue, int grid, int block, const Mech
 cudaError_t variant_occupancy(int arith, int block, int* nblocks) {
   switch (arith) {
     case 1: return gckpp_occupancy_strict(1, block, nblocks);
-    case 2: return gckpp_occupancy_fast1(1, block, nblocks);
+    case 2: return gckpp_occupancy_fast2(1, block, nblocks);
     case 3: return gckpp_occupancy_fast4(1, block, nblocks);
     default: return gckpp_occupancy_fast(1, block, nblocks);
   }
@@ -337,7 +355,7 @@ cudaError_t variant_occupancy(int arith, int block, int* nblocks) {
 int variant_cells_per_thread(int arith) {
   switch (arith) {
     case 1: return gckpp_cells_per_thread_strict();
-    case 2: return gckpp_cells_per_thread_fast1();
+    case 2: return gckpp_cells_per_thread_fast2();
     case 3: return gckpp_cells_per_thread_fast4();
     default: return gckpp_cells_per_thread_fast();
   }
@@ -351,6 +369,14 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   const int block = c->block;
   const int nc = variant_cells_per_thread(c->arith);
   const long long per_block = (long long)block * nc;
+  // the first a.nblock cells of a.order run block-per-cell, the rest on the
+  // thread-per-cell kernel
+  const int nb = a.nblock;
+  if (nb < 0 || nb > a.ncell) return fail(GC_KPP_EINVAL, "block-per-cell count outside [0, ncell]");
+  if (nb > 0 && !a.order) return fail(GC_KPP_EINVAL, "block-per-cell cells need a cell order");
+  if (nb > 0 && (c->arith > 1 || c->lu_form != 0))
+    return fail(GC_KPP_EUNSUPPORTED, "block-per-cell cells need ARITH 0 or 1 and the row-wise LU");
+  const long long nthread = (long long)a.ncell - nb;
   long long nslot;
   int grid;
   if (queue) {
@@ -361,24 +387,24 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
       per_sm = std::max(per_sm, 1);
     }
     grid = c->nsm * per_sm;
-    const long long need_blocks = ((long long)a.ncell + per_block - 1) / per_block;
+    const long long need_blocks = std::max(1LL, (nthread + per_block - 1) / per_block);
     if (grid > need_blocks) grid = (int)need_blocks;
     if (c->max_slots > 0 && (long long)grid * per_block > c->max_slots)
       grid = (int)std::max(1LL, c->max_slots / per_block);
     nslot = (long long)grid * per_block;
   } else {
-    grid = (int)(((long long)a.ncell + per_block - 1) / per_block);
+    grid = (int)std::max(1LL, (nthread + per_block - 1) / per_block);
     nslot = (long long)grid * per_block;
     if (c->max_slots > 0 && nslot > c->max_slots)
       return fail(GC_KPP_EINVAL, "plain schedule needs one workspace slot per cell; raise MAX_SLOTS or use the queue");
   }
   const size_t ws_bytes = (size_t)nslot * (size_t)c->lay.total * sizeof(double);
   GC_CUDA(c->ws.ensure(ws_bytes));
-  GC_CUDA(c->counter.ensure(sizeof(int)));
-  GC_CUDA(cudaMemsetAsync(c->counter.p, 0, sizeof(int), s));
+  GC_CUDA(c->counter.ensure(2 * sizeof(int)));
+  GC_CUDA(cudaMemsetAsync(c->counter.p, 0, 2 * sizeof(int), s));
   RosParams p{};
-  p.ncell = a.ncell;
-  p.order = a.order;
+  p.ncell = (int)nthread;
+  p.order = a.order ? a.order + nb : nullptr;
   p.cell_limit = a.cell_limit > 0 ? a.cell_limit : a.ncell;
   p.queue_counter = (int*)c->counter.p;
   p.c_in = a.c_in;
@@ -417,13 +443,35 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
       if (!c->ev[i]) GC_CUDA(cudaEventCreate(&c->ev[i]));
     GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed], s));
   }
-  cudaError_t e = variant_launch(c->arith, queue, grid, block, c->mech, R.meth, p, s);
-  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  if (nb > 0) {
+    if (!c->side) GC_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    if (!c->fork) GC_CUDA(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+    if (!c->join) GC_CUDA(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
+    GC_CUDA(cudaEventRecord(c->fork, s));
+    GC_CUDA(cudaStreamWaitEvent(c->side, c->fork, 0));
+    RosParams pb = p;
+    pb.ncell = nb;
+    pb.order = a.order;
+    pb.queue_counter = (int*)c->counter.p + 1;
+    pb.ws = nullptr;
+    pb.nslot = 0;
+    const int bgrid = std::min(nb, c->nsm);
+    cudaError_t eb = c->arith == 1 ? gckpp_launch_block_strict(bgrid, c->cell_block, c->mech, R.meth, pb, c->side)
+                                   : gckpp_launch_block_fast(bgrid, c->cell_block, c->mech, R.meth, pb, c->side);
+    if (eb != cudaSuccess) return cuda_fail(eb, "block-per-cell kernel launch");
+    GC_CUDA(cudaEventRecord(c->join, c->side));
+    if (launches) *launches += 1;
+  }
+  if (nthread > 0) {
+    cudaError_t e = variant_launch(c->arith, queue, grid, block, c->mech, R.meth, p, s);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    if (launches) *launches += 1;
+  }
+  if (nb > 0) GC_CUDA(cudaStreamWaitEvent(s, c->join, 0));
   if (timed) {
     GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed + 1], s));
     c->ntimed += 1;
   }
-  if (launches) *launches += 1;
   return GC_KPP_OK;
 }
 
@@ -520,7 +568,7 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
                               const double* photol, long long ldp, double* cc, long long ldc, const double* atol,
                               const double* rtol, const int* icntrl_u, const double* rcntrl_u, double* hstart,
                               int* istatus, double* rstatus, long long ldo, int* ierr, int* nretry,
-                              const int* order, int mem, void* stream) {
+                              const int* order, int nblock, int mem, void* stream) {
   if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
   if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
   if (nretry) *nretry = 0;
@@ -601,7 +649,7 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
     DevArgs a{};
     a.ncell = ncell; a.c_in = dc; a.c_out = dc; a.ldc = lc; a.rconst = drc; a.ldr = ncell; a.atol = dat;
     a.rtol = drt; a.hstart = dhs; a.istatus = dis; a.rstatus = drs; a.ldo = lo; a.ierr = die;
-    a.order = dorder; a.cell_limit = ncell;
+    a.order = dorder; a.cell_limit = ncell; a.nblock = nblock;
     GC_TRY(launch_integrate(c, R, 0.0, dt, a, s, &c->last_launches));
     // retry failed cells once with Hstart = 0 from C_before
     // (fullchem_mod.F90:1138-1162)
@@ -620,6 +668,7 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
       b.ncell = (int)failed.size();
       b.order = dord;
       b.cell_limit = ncell;
+      b.nblock = 0;
       b.c_in = dcb;
       b.hstart = nullptr;
       Resolved R2 = R;
@@ -652,7 +701,7 @@ int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met,
                          int* istatus, double* rstatus, long long ldo, int* ierr, int* nretry, int mem,
                          void* stream) {
   return fullchem_step_impl(c, ncell, dt, met, ldm, photol, ldp, cc, ldc, atol, rtol, icntrl_u, rcntrl_u, hstart,
-                            istatus, rstatus, ldo, ierr, nretry, nullptr, mem, stream);
+                            istatus, rstatus, ldo, ierr, nretry, nullptr, 0, mem, stream);
 }
 
 int gc_kpp_fullchem_step_ordered(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm,
@@ -661,7 +710,18 @@ int gc_kpp_fullchem_step_ordered(gc_kpp_ctx* c, int ncell, double dt, const doub
                                  const double* rcntrl_u, double* hstart, int* istatus, double* rstatus,
                                  long long ldo, int* ierr, int* nretry, const int* order, int mem, void* stream) {
   return fullchem_step_impl(c, ncell, dt, met, ldm, photol, ldp, cc, ldc, atol, rtol, icntrl_u, rcntrl_u, hstart,
-                            istatus, rstatus, ldo, ierr, nretry, order, mem, stream);
+                            istatus, rstatus, ldo, ierr, nretry, order, 0, mem, stream);
+}
+
+int gc_kpp_fullchem_step_binned(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm,
+                                const double* photol, long long ldp, double* cc, long long ldc, const double* atol,
+                                const double* rtol, const int* icntrl_u, const double* rcntrl_u, double* hstart,
+                                int* istatus, double* rstatus, long long ldo, int* ierr, int* nretry,
+                                const int* order, int nblock, int mem, void* stream) {
+  if (nblock < 0 || nblock > ncell) return fail(GC_KPP_EINVAL, "nblock outside [0, ncell]");
+  if (nblock > 0 && !order) return fail(GC_KPP_EINVAL, "nblock > 0 needs an order");
+  return fullchem_step_impl(c, ncell, dt, met, ldm, photol, ldp, cc, ldc, atol, rtol, icntrl_u, rcntrl_u, hstart,
+                            istatus, rstatus, ldo, ierr, nretry, order, nblock, mem, stream);
 }
 
 int gc_kpp_last_launch_count(gc_kpp_ctx* c) { return c ? c->last_launches : 0; }
@@ -915,3 +975,9 @@ int gc_kpp_integrate_batch_noalloc(int ncell, double tin, double tout, double* c
 }
 
 }  // extern "C"
+
+// Error text for the library's other translation units (gckpp_learned_capi.cu).
+int gckpp_set_error(int code, const char* msg) {
+  g_last_error = msg;
+  return code;
+}

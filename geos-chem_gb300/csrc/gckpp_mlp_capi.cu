@@ -77,14 +77,16 @@ int gc_mlp_adam(int n, float* w, void* w_bf16, float* g, float* m1, float* m2, f
 }
 
 int gc_mlp_propose(int M, const float* out, double scale, double hmin, double hmax, double* h0, int* bin,
-                   void* stream) {
+                   int keep, void* stream) {
   if (M < 0 || !out) return -101;
-  return rc(propose(out, M, scale, hmin, hmax, h0, bin, (cudaStream_t)stream));
+  return rc(propose(out, M, scale, hmin, hmax, h0, bin, keep, (cudaStream_t)stream));
 }
 
-int gc_mlp_bin_order(int M, const int* bin, int* counts, int* cursor, int* order, void* stream) {
-  if (M < 0 || !bin || !counts || !cursor || !order) return -101;
-  return rc(bin_order(bin, M, counts, cursor, order, (cudaStream_t)stream));
+int gc_mlp_bin_order_scratch(int M) { return M < 0 ? -101 : bin_order_scratch(M); }
+
+int gc_mlp_bin_order(int M, const int* bin, int* counts, int* scratch, int* order, void* stream) {
+  if (M < 0 || !bin || !counts || !scratch || !order) return -101;
+  return rc(bin_order(bin, M, counts, scratch, order, (cudaStream_t)stream));
 }
 
 }  // extern "C"

@@ -1,0 +1,387 @@
+// Block-per-cell Rosenbrock: all threads of one block integrate one cell,
+// whose whole working set (rates, Y, stage vectors, A/B products, Jac0 and
+// the LU factors, about 156 KB) sits in shared memory.
+//
+// This is the latency form of the solver, for the few stiff cells that need
+// tens of steps while most cells need one or two: a thread-per-cell warp
+// would run such a cell alone at the end of the launch, with every table
+// walk a chain of dependent global loads.  Here the independent items of
+// each phase run in parallel (products, Fun_SPLIT rows, Jac_SP entries, the
+// stage vectors), and the LU factorization and the two substitutions run in
+// dependency levels (tables.py _level_schedules) with a barrier between
+// levels.  Every item is evaluated by one thread with exactly the operations
+// and order of the thread-per-cell engine (kpp_mech.cuh), and the error norm
+// is summed by one thread in species order, so both forms give the same
+// numbers for a cell.  A block of 32 threads is the warp-per-cell layout.
+#pragma once
+#include <climits>
+
+#include "kpp_rosenbrock.cuh"
+
+namespace gckpp {
+
+// Shared-memory layout of one cell (offsets in doubles).
+struct BlockLayout {
+  int aux, y0, y1, fcn0, fcn, dfdt, k, a, b, j0, g, e, total;
+};
+
+__host__ __device__ inline BlockLayout block_layout(int naux, int nspec, int nvar, int nreact, int nb, int lunz) {
+  BlockLayout l{};
+  int o = 0;
+  l.aux = o; o += naux;
+  l.y0 = o; o += nspec;
+  l.y1 = o; o += nspec;
+  l.fcn0 = o; o += nvar;
+  l.fcn = o; o += nvar;
+  l.dfdt = o; o += nvar;
+  l.k = o; o += SMAX * nvar;
+  l.a = o; o += nreact;
+  l.b = o; o += nb;
+  l.j0 = o; o += lunz;
+  l.g = o; o += lunz;
+  l.e = o; o += nvar;
+  l.total = o;
+  return l;
+}
+
+// pre [* 2] * s1 * s2 * s3 in the Fortran's left-to-right order (the
+// operations of product<1> in kpp_mech.cuh).
+__device__ __forceinline__ double bk_product(const MechDev& m, int p, const double* Y, const double* aux) {
+  const uint2 t = __ldg(m.prod_packed + p);
+  const unsigned ns = (t.x >> 13) & 3u;
+  double r = aux[t.x & 0xfffu];
+  if (t.x & 0x1000u) r = r * 2.0;
+  if (ns >= 1u) r = r * Y[t.x >> 16];
+  if (ns >= 2u) r = r * Y[t.y & 0xffffu];
+  if (ns >= 3u) r = r * Y[t.y >> 16];
+  return r;
+}
+
+// Sum of signed terms slit[c] * X[idx] (the operations of term_sum<.,.,1>).
+template <bool STRICT, bool FLIP>
+__device__ __forceinline__ double bk_term_sum(const MechDev& m, const unsigned* __restrict__ terms, int s, int e,
+                                              const double* X) {
+  double acc = 0.0;
+#pragma unroll 4
+  for (int i = s; i < e; ++i) {
+    const unsigned t = __ldg(terms + i);
+    const double cf = __ldg(m.slit + (t >> 20));
+    const double x = X[t & 0xfffffu];
+    if (STRICT) {
+      const double v = cf * x;
+      acc = (i == s) ? (FLIP ? -v : v) : (FLIP ? acc - v : acc + v);
+    } else {
+      acc = fma(FLIP ? -cf : cf, x, acc);
+    }
+  }
+  return acc;
+}
+
+// B products at Y (Jac_SP partials, also Fun's D_VAR products).
+__device__ __forceinline__ void bk_b_products(const MechDev& m, const double* Y, const double* aux, double* B) {
+  for (int b = threadIdx.x; b < m.nb; b += blockDim.x) B[b] = bk_product(m, m.nreact + b, Y, aux);
+}
+
+// Fun_SPLIT at V; B must hold the B products at V and be visible to the
+// block.  Ends with a barrier.
+template <bool STRICT>
+__device__ void bk_fun(const MechDev& m, const double* V, const double* aux, double* A, const double* B,
+                       double* Vdot) {
+  for (int r = threadIdx.x; r < m.nreact; r += blockDim.x) A[r] = bk_product(m, r, V, aux);
+  __syncthreads();
+  for (int n = threadIdx.x; n < m.nvar; n += blockDim.x) {
+    const int i = __ldg(m.fun_rows_by_len + n);
+    const double p = bk_term_sum<STRICT, false>(m, m.p_sterm, __ldg(m.p_start + i), __ldg(m.p_start + i + 1), A);
+    const double d = bk_term_sum<STRICT, false>(m, m.d_sterm, __ldg(m.d_start + i), __ldg(m.d_start + i + 1), B);
+    Vdot[i] = STRICT ? p - d * V[i] : fma(-d, V[i], p);
+  }
+  __syncthreads();
+}
+
+// Jac_SP (STRICT stores JVS, the fast form -JVS).  No barrier.
+template <bool STRICT>
+__device__ void bk_jac(const MechDev& m, const double* B, double* J) {
+  for (int n = threadIdx.x; n < m.lu_nonzero; n += blockDim.x) {
+    const int e = __ldg(m.jac_by_len + n);
+    J[e] = bk_term_sum<STRICT, !STRICT>(m, m.j_sterm, __ldg(m.j_start + e), __ldg(m.j_start + e + 1), B);
+  }
+}
+
+// Ghimj = -Jac0 + diag(ghinv) and its LU factors (the operations of
+// decomp_rows), level by level.  *ier receives the 1-based first row whose
+// diagonal is below TINY (0 if none), as singular_rows finds it.  Ends with
+// a barrier.
+template <bool STRICT>
+__device__ void bk_decomp(const MechDev& m, const double* J0, double ghinv, double* G, int* ier) {
+  if (threadIdx.x == 0) *ier = INT_MAX;
+  __syncthreads();
+  for (int i = threadIdx.x; i < m.nvar; i += blockDim.x) {
+    const double j = J0[__ldg(m.lu_diag + i)];
+    const double g = (STRICT ? -j : j) + ghinv;
+    if (tiny_abs(g)) atomicMin(ier, i + 1);
+  }
+  for (int l = 0; l < m.lu_nlvl; ++l) {
+    const int n1 = __ldg(m.lu_lvl_start + l + 1);
+    for (int n = __ldg(m.lu_lvl_start + l) + threadIdx.x; n < n1; n += blockDim.x) {
+      const int e = __ldg(m.lu_lvl_entry + n);
+      const int k = __ldg(m.lu_irow + e);
+      const int dk = __ldg(m.lu_diag + k);
+      const double j = J0[e];
+      double acc = STRICT ? -j : j;
+      if (e == dk) acc = acc + ghinv;
+      const int t1 = __ldg(m.dot_start + e + 1);
+#pragma unroll 4
+      for (int t = __ldg(m.dot_start + e); t < t1; ++t) {
+        const unsigned op = __ldg(m.dot_term + t);
+        const double lv = G[op >> 16];
+        const double uv = G[op & 0xffffu];
+        acc = STRICT ? acc - lv * uv : fma(-lv, uv, acc);
+      }
+      if (e < dk) {
+        const double piv = G[__ldg(m.lu_diag + __ldg(m.lu_icol + e))];
+        acc = STRICT ? acc / piv : acc * piv;  // fast: diag holds 1/pivot
+      } else if (e == dk && !STRICT) {
+        acc = 1.0 / acc;
+      }
+      G[e] = acc;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && *ier == INT_MAX) *ier = 0;
+  __syncthreads();
+}
+
+// KppSolve (the operations of solve), forward then backward, row levels.
+// Ends with a barrier.
+template <bool STRICT>
+__device__ void bk_solve(const MechDev& m, const double* G, double* X) {
+  for (int l = 0; l < m.fs_nlvl; ++l) {
+    const int n1 = __ldg(m.fs_lvl_start + l + 1);
+    for (int n = __ldg(m.fs_lvl_start + l) + threadIdx.x; n < n1; n += blockDim.x) {
+      const int i = __ldg(m.fs_lvl_row + n);
+      const int s = __ldg(m.lu_crow + i), d = __ldg(m.lu_diag + i);
+      if (s < d) {
+        double x = X[i];
+#pragma unroll 4
+        for (int kk = s; kk < d; ++kk) {
+          const double g = G[kk];
+          const double y = X[__ldg(m.lu_icol + kk)];
+          x = STRICT ? x - g * y : fma(-g, y, x);
+        }
+        X[i] = x;
+      }
+    }
+    __syncthreads();
+  }
+  for (int l = 0; l < m.bs_nlvl; ++l) {
+    const int n1 = __ldg(m.bs_lvl_start + l + 1);
+    for (int n = __ldg(m.bs_lvl_start + l) + threadIdx.x; n < n1; n += blockDim.x) {
+      const int i = __ldg(m.bs_lvl_row + n);
+      const int d = __ldg(m.lu_diag + i), e = __ldg(m.lu_crow + i + 1);
+      double x = X[i];
+#pragma unroll 4
+      for (int kk = d + 1; kk < e; ++kk) {
+        const double g = G[kk];
+        const double y = X[__ldg(m.lu_icol + kk)];
+        x = STRICT ? x - g * y : fma(-g, y, x);
+      }
+      const double piv = G[d];
+      X[i] = STRICT ? x / piv : x * piv;
+    }
+    __syncthreads();
+  }
+}
+
+// Shared scalars of the block's cell.
+struct BlockShared {
+  Lane L;
+  int ier, flag, next, nconsec;
+};
+
+// One block integrates cells order[0..ncell) (or 0..ncell) taken from a
+// per-launch queue (p.queue_counter), one at a time.  Dynamic shared memory:
+// block_layout(...).total doubles.
+template <bool STRICT>
+__device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const RosParams& p) {
+  extern __shared__ double sm[];
+  __shared__ BlockShared sh;
+  const BlockLayout lay = block_layout(m.naux, m.nspec, m.nvar, m.nreact, m.nb, m.lu_nonzero);
+  double* aux = sm + lay.aux;
+  double* Y = sm + lay.y0;
+  double* Ynew = sm + lay.y1;
+  double* F0 = sm + lay.fcn0;
+  double* F = sm + lay.fcn;
+  double* dfdt = sm + lay.dfdt;
+  double* K = sm + lay.k;
+  double* A = sm + lay.a;
+  double* B = sm + lay.b;
+  double* J0 = sm + lay.j0;
+  double* G = sm + lay.g;
+  double* E = sm + lay.e;
+  const int nvar = m.nvar;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const double dir = (p.tend >= p.tstart) ? 1.0 : -1.0;
+  Rosenbrock<STRICT, 1> ros(m, r, p);
+  while (true) {
+    if (tid == 0) sh.next = atomicAdd(p.queue_counter, 1);
+    __syncthreads();
+    const int idx = sh.next;
+    if (idx >= p.ncell) break;
+    const int cell = p.order ? p.order[idx] : idx;
+    if ((unsigned)cell >= (unsigned)p.cell_limit) {
+      __syncthreads();
+      continue;
+    }
+    // load the cell (aux = [RCT | constant-rate literals], Y = [V | F])
+    for (int k = tid; k < m.naux; k += nt)
+      aux[k] = k < m.nreact ? p.rconst[(long long)k * p.ldr + cell] : __ldg(m.pre_lit + (k - m.nreact));
+    for (int i = tid; i < m.nspec; i += nt) {
+      const double v = p.c_in[(long long)i * p.ldc + cell];
+      Y[i] = v;
+      if (i >= nvar) Ynew[i] = v;
+    }
+    if (tid == 0) ros.init_lane(sh.L, cell);
+    __syncthreads();
+    while (true) {
+      // TimeLoop head
+      if (tid == 0 && sh.L.phase == PH_NEWSTEP) ros.step_checks(sh.L);
+      __syncthreads();
+      if (sh.L.phase == PH_DONE) break;
+      // Fun0 and Jac0 (B products shared)
+      bk_b_products(m, Y, aux, B);
+      __syncthreads();
+      bk_jac<STRICT>(m, B, J0);
+      bk_fun<STRICT>(m, Y, aux, A, B, F0);
+      if (!p.autonomous) {
+        bk_fun<STRICT>(m, Y, aux, A, B, dfdt);
+        const double delta = sqrt(p.roundoff) * fmax(1.0e-6, fabs(sh.L.T));
+        const double rd = 1.0 / delta;
+        for (int i = tid; i < nvar; i += nt) {
+          double v = dfdt[i] + (-1.0) * F0[i];
+          if (rd != 1.0) v = rd * v;
+          dfdt[i] = v;
+        }
+        __syncthreads();
+      }
+      if (tid == 0) {
+        sh.L.nfun += p.autonomous ? 1 : 2;
+        sh.L.njac += 1;
+        sh.L.phase = PH_ATTEMPT;
+      }
+      __syncthreads();
+      while (sh.L.phase == PH_ATTEMPT) {
+        // ros_PrepareMatrix with the singular-matrix retry
+        if (tid == 0) sh.nconsec = 0;
+        __syncthreads();
+        while (true) {
+          const double ghinv = 1.0 / (dir * sh.L.H * r.Gamma[0]);
+          bk_decomp<STRICT>(m, J0, ghinv, G, &sh.ier);
+          if (tid == 0) sh.flag = ros.singular_retry(sh.L, sh.ier, sh.nconsec) ? 1 : 0;
+          __syncthreads();
+          if (!sh.flag) break;
+        }
+        if (sh.L.phase == PH_DONE) break;
+        const double* fcn = F0;
+        for (int s = 0; s < r.S; ++s) {
+          if (s > 0 && r.NewF[s]) {
+            for (int i = tid; i < nvar; i += nt) {
+              double y = Y[i];
+              for (int j = 0; j < s; ++j) {
+                const double a = r.A[(s * (s - 1)) / 2 + j];
+                const double kj = K[j * nvar + i];
+                if (a != 0.0) y = STRICT ? y + a * kj : fma(a, kj, y);
+              }
+              Ynew[i] = y;
+            }
+            __syncthreads();
+            bk_b_products(m, Ynew, aux, B);
+            __syncthreads();
+            bk_fun<STRICT>(m, Ynew, aux, A, B, F);
+            if (tid == 0) sh.L.nfun += 1;
+            fcn = F;
+          }
+          double hc[SMAX];
+          for (int j = 0; j < s; ++j) hc[j] = r.C[(s * (s - 1)) / 2 + j] / (dir * sh.L.H);
+          const double hg = dir * sh.L.H * r.Gamma[s];
+          const bool use_dfdt = (!p.autonomous) && (r.Gamma[s] != 0.0);
+          double* Ks = K + s * nvar;
+          for (int i = tid; i < nvar; i += nt) {
+            double k = fcn[i];
+            for (int j = 0; j < s; ++j) {
+              const double kj = K[j * nvar + i];
+              if (hc[j] != 0.0) k = STRICT ? k + hc[j] * kj : fma(hc[j], kj, k);
+            }
+            if (use_dfdt && hg != 0.0) {
+              const double dd = dfdt[i];
+              k = STRICT ? k + hg * dd : fma(hg, dd, k);
+            }
+            Ks[i] = k;
+          }
+          __syncthreads();
+          bk_solve<STRICT>(m, G, Ks);
+          if (tid == 0) sh.L.nsol += 1;
+        }
+        // new solution, error estimate, scaled errors
+        for (int i = tid; i < nvar; i += nt) {
+          const double at = p.vector_tol ? __ldg(p.atol + i) : __ldg(p.atol);
+          const double rt = p.vector_tol ? __ldg(p.rtol + i) : __ldg(p.rtol);
+          const double y0 = Y[i];
+          double y = y0;
+          double yerr = 0.0;
+          for (int j = 0; j < r.S; ++j) {
+            const double kj = K[j * nvar + i];
+            if (r.M[j] != 0.0) y = STRICT ? y + r.M[j] * kj : fma(r.M[j], kj, y);
+            if (r.E[j] != 0.0) yerr = STRICT ? yerr + r.E[j] * kj : fma(r.E[j], kj, yerr);
+          }
+          Ynew[i] = y;
+          const double ymax = fmax(fabs(y0), fabs(y));
+          const double scale = STRICT ? at + rt * ymax : fma(rt, ymax, at);
+          E[i] = yerr / scale;
+        }
+        __syncthreads();
+        // error norm summed in species order, then the step size control
+        if (tid == 0) {
+          double err = 0.0;
+          for (int i = 0; i < nvar; ++i) {
+            const double e = E[i];
+            err = STRICT ? err + e * e : fma(e, e, err);
+          }
+          sh.flag = ros.control(sh.L, err, dir) ? 1 : 0;
+        }
+        __syncthreads();
+        if (sh.flag) {
+          for (int i = tid; i < nvar; i += nt) {
+            const double v = Ynew[i];
+            Y[i] = p.clamp_negative ? fmax(v, 0.0) : v;
+          }
+          __syncthreads();
+        }
+      }
+    }
+    // store the cell
+    for (int i = tid; i < nvar; i += nt) p.c_out[(long long)i * p.ldc + cell] = Y[i];
+    if (p.c_out != p.c_in)
+      for (int f = tid; f < m.nfix; f += nt)
+        p.c_out[(long long)(nvar + f) * p.ldc + cell] = p.c_in[(long long)(nvar + f) * p.ldc + cell];
+    if (tid == 0) {
+      const Lane& L = sh.L;
+      if (p.istatus) {
+        const int v[8] = {L.nfun, L.njac, L.nstp, L.nacc, L.nrej, L.ndec, L.nsol, L.nsng};
+        for (int k = 0; k < 20; ++k) p.istatus[(long long)k * p.ldo + cell] = k < 8 ? v[k] : 0;
+      }
+      if (p.rstatus) {
+        for (int k = 0; k < 20; ++k) {
+          double v = 0.0;
+          if (k == 0) v = L.texit;
+          if (k == 1) v = L.hexit;
+          if (k == 2) v = L.hnew_out;
+          p.rstatus[(long long)k * p.ldo + cell] = v;
+        }
+      }
+      if (p.ierr) p.ierr[cell] = L.ierr;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace gckpp

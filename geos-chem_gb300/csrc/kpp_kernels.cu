@@ -1,9 +1,12 @@
 // Rosenbrock kernels, compiled once per variant (build.py):
 //   strict   -DGCKPP_STRICT=1 -fmad=false   reference evaluation order, 1 cell/thread
-//   fast     -DGCKPP_STRICT=0               FMA, reciprocal pivots, GCKPP_NC cells/thread
-//   fast1    fast with 1 cell per thread
+//   fast     -DGCKPP_STRICT=0               FMA, reciprocal pivots, 1 cell/thread
+//   fast2    fast with 2 cells per thread
 //   fast4    fast with 4 cells per thread
+// On the 4x5x72 grid step the 1-cell form is the fastest (the 2- and 4-cell
+// forms spill registers and hold fewer warps per SM).
 #include "kpp_launch.h"
+#include "kpp_block.cuh"
 #include "kpp_rosenbrock.cuh"
 
 #ifndef GCKPP_MAX_THREADS
@@ -41,5 +44,29 @@ cudaError_t GCKPP_CAT(gckpp_occupancy_, GCKPP_VARIANT)(int queue, int block, int
   if (queue) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_kernel<true>, block, 0);
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_kernel<false>, block, 0);
 }
+
+#if GCKPP_NC == 1
+// Block-per-cell form (kpp_block.cuh), built in the 1-cell-per-thread units.
+// (a template, so that each variant's translation unit keeps its own kernel)
+template <bool STRICT>
+__global__ void __launch_bounds__(1024) ros_block_kernel(MechDev m, RosMethod r, RosParams p) {
+  ros_block_driver<STRICT>(m, r, p);
+}
+
+size_t GCKPP_CAT(gckpp_block_smem_, GCKPP_VARIANT)(const MechDev& m) {
+  return sizeof(double) * (size_t)block_layout(m.naux, m.nspec, m.nvar, m.nreact, m.nb, m.lu_nonzero).total;
+}
+
+cudaError_t GCKPP_CAT(gckpp_launch_block_, GCKPP_VARIANT)(int grid, int block, const MechDev& m, const RosMethod& r,
+                                                          const RosParams& p, cudaStream_t s) {
+  if (block < 32 || block > 1024 || block % 32) return cudaErrorInvalidConfiguration;
+  const size_t smem = GCKPP_CAT(gckpp_block_smem_, GCKPP_VARIANT)(m);
+  cudaError_t e = cudaFuncSetAttribute(ros_block_kernel<GCKPP_STRICT != 0>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  ros_block_kernel<GCKPP_STRICT != 0><<<grid, block, smem, s>>>(m, r, p);
+  return cudaGetLastError();
+}
+#endif
 
 }  // namespace gckpp

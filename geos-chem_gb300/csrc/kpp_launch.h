@@ -16,7 +16,15 @@ struct RosParams;
 
 GCKPP_DECLARE_VARIANT(strict)
 GCKPP_DECLARE_VARIANT(fast)
-GCKPP_DECLARE_VARIANT(fast1)
+GCKPP_DECLARE_VARIANT(fast2)
 GCKPP_DECLARE_VARIANT(fast4)
 #undef GCKPP_DECLARE_VARIANT
+
+// block-per-cell kernels (one block integrates one cell in shared memory)
+cudaError_t gckpp_launch_block_strict(int grid, int block, const MechDev& m, const RosMethod& r, const RosParams& p,
+                                      cudaStream_t s);
+cudaError_t gckpp_launch_block_fast(int grid, int block, const MechDev& m, const RosMethod& r, const RosParams& p,
+                                    cudaStream_t s);
+size_t gckpp_block_smem_strict(const MechDev& m);
+size_t gckpp_block_smem_fast(const MechDev& m);
 }  // namespace gckpp

@@ -49,6 +49,17 @@ struct MechDev {
   const int* dot_start;
   const unsigned* dot_term;
   const double* lit;
+  // level schedules of the block-per-cell kernel (tables.py _level_schedules)
+  const int* lu_irow;
+  const int* lu_lvl_start;
+  const int* lu_lvl_entry;
+  const int* fs_lvl_start;
+  const int* fs_lvl_row;
+  const int* bs_lvl_start;
+  const int* bs_lvl_row;
+  const int* fun_rows_by_len;
+  const int* jac_by_len;
+  int lu_nlvl, fs_nlvl, bs_nlvl;
 };
 
 __device__ __forceinline__ int ldi(const int* p) { return __ldg(p); }

@@ -15,6 +15,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kpp_mlp.h"
 
 namespace gcmlp {
@@ -265,47 +267,93 @@ __global__ void adam_kernel(float* __restrict__ w, __nv_bfloat16* __restrict__ w
 
 // ---------------------------------------------------------------- proposals
 // From the head outputs: H0 = scale * exp(out0), bin = argmax(out1..4).
+// With keep, an H0 entry that is already positive (a KPPHvalue) stays.
 __global__ void propose_kernel(const float* __restrict__ out, int M, double scale, double hmin, double hmax,
-                               double* __restrict__ h0, int* __restrict__ bin) {
+                               double* __restrict__ h0, int* __restrict__ bin, int keep) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= M) return;
   const float* o = out + (long long)r * NOUT;
   double h = scale * exp((double)o[0]);
   h = fmin(fmax(h, hmin), hmax);
-  if (h0) h0[r] = h;
+  if (h0 && !(keep && h0[r] > 0.0)) h0[r] = h;
   int b = 0;
   for (int k = 1; k < NBIN; ++k)
     if (o[1 + k] > o[1 + b]) b = k;
   if (bin) bin[r] = b;
 }
 
-// Counting sort of cells by bin, heaviest bin first (work-queue order).
-__global__ void bin_count_kernel(const int* __restrict__ bin, int M, int* __restrict__ counts) {
+// Stable counting sort of cells by bin, heaviest bin first (work-queue
+// order).  Cells keep ascending index order inside a bin, so that a warp of
+// the queue kernel that claims 32 consecutive positions of a dense bin reads
+// mostly consecutive cells, and the order is the same on every run.
+// Pass 1: per-block bin counts; pass 2: exclusive scan over (bin descending,
+// block ascending); pass 3: scatter with each cell's rank inside its block.
+constexpr int BO_BLOCK = 256;
+
+__global__ void bin_block_count_kernel(const int* __restrict__ bin, int M, int* __restrict__ blk) {
   __shared__ int local[NBIN];
   if (threadIdx.x < NBIN) local[threadIdx.x] = 0;
   __syncthreads();
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.x * BO_BLOCK + threadIdx.x;
   if (r < M) atomicAdd(&local[bin[r]], 1);
   __syncthreads();
-  if (threadIdx.x < NBIN) atomicAdd(counts + threadIdx.x, local[threadIdx.x]);
+  if (threadIdx.x < NBIN) blk[blockIdx.x * NBIN + threadIdx.x] = local[threadIdx.x];
 }
 
-__global__ void bin_scatter_kernel(const int* __restrict__ bin, int M, int* __restrict__ cursor,
-                                   int* __restrict__ order) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= M) return;
-  const int pos = atomicAdd(cursor + bin[r], 1);
-  order[pos] = r;
-}
-
-// cursor[b] = start of bin b in the order, heaviest (highest) bin first
-__global__ void bin_offsets_kernel(const int* __restrict__ counts, int* __restrict__ cursor) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    int s = 0;
-    for (int b = NBIN - 1; b >= 0; --b) {
-      cursor[b] = s;
-      s += counts[b];
+// One block of 1024 threads: blk[j*NBIN+b] <- start of block j's cells of
+// bin b in the order; counts[b] <- cells in bin b.
+__global__ void bin_block_scan_kernel(int* __restrict__ blk, int nblk, int* __restrict__ counts) {
+  __shared__ int part[1024];
+  __shared__ int base;
+  const int t = threadIdx.x;
+  const int per = (nblk + 1023) / 1024;
+  const int j0 = t * per, j1 = min(nblk, j0 + per);
+  if (t == 0) base = 0;
+  __syncthreads();
+  for (int b = NBIN - 1; b >= 0; --b) {
+    int sum = 0;
+    for (int j = j0; j < j1; ++j) sum += blk[j * NBIN + b];
+    part[t] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
+      const int v = t >= off ? part[t - off] : 0;
+      __syncthreads();
+      part[t] += v;
+      __syncthreads();
     }
+    int run = base + part[t] - sum;
+    for (int j = j0; j < j1; ++j) {
+      const int c = blk[j * NBIN + b];
+      blk[j * NBIN + b] = run;
+      run += c;
+    }
+    __syncthreads();
+    if (t == 1023) {
+      counts[b] = part[1023];
+      base += part[1023];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void bin_stable_scatter_kernel(const int* __restrict__ bin, int M, const int* __restrict__ blk,
+                                          int* __restrict__ order) {
+  __shared__ int wcnt[BO_BLOCK / 32][NBIN];
+  const int r = blockIdx.x * BO_BLOCK + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int b = r < M ? bin[r] : -1;
+  const unsigned lt = (1u << lane) - 1u;
+  int rank = 0;
+  for (int k = 0; k < NBIN; ++k) {
+    const unsigned mk = __ballot_sync(0xffffffffu, b == k);
+    if (lane == 0) wcnt[warp][k] = __popc(mk);
+    if (b == k) rank = __popc(mk & lt);
+  }
+  __syncthreads();
+  if (b >= 0) {
+    int pos = blk[blockIdx.x * NBIN + b] + rank;
+    for (int w = 0; w < warp; ++w) pos += wcnt[w][b];
+    order[pos] = r;
   }
 }
 
@@ -366,16 +414,18 @@ cudaError_t adam(float* w, __nv_bfloat16* wb, float* g, float* m1, float* m2, in
   return cudaGetLastError();
 }
 cudaError_t propose(const float* out, int M, double scale, double hmin, double hmax, double* h0, int* bin,
-                    cudaStream_t s) {
-  if (M > 0) propose_kernel<<<(M + 255) / 256, 256, 0, s>>>(out, M, scale, hmin, hmax, h0, bin);
+                    int keep, cudaStream_t s) {
+  if (M > 0) propose_kernel<<<(M + 255) / 256, 256, 0, s>>>(out, M, scale, hmin, hmax, h0, bin, keep);
   return cudaGetLastError();
 }
-cudaError_t bin_order(const int* bin, int M, int* counts, int* cursor, int* order, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(counts, 0, NBIN * sizeof(int), s);
-  if (e != cudaSuccess || M == 0) return e;
-  bin_count_kernel<<<(M + 255) / 256, 256, 0, s>>>(bin, M, counts);
-  bin_offsets_kernel<<<1, 32, 0, s>>>(counts, cursor);
-  bin_scatter_kernel<<<(M + 255) / 256, 256, 0, s>>>(bin, M, cursor, order);
+int bin_order_scratch(int M) { return NBIN * std::max(1, (M + BO_BLOCK - 1) / BO_BLOCK); }
+
+cudaError_t bin_order(const int* bin, int M, int* counts, int* scratch, int* order, cudaStream_t s) {
+  if (M == 0) return cudaMemsetAsync(counts, 0, NBIN * sizeof(int), s);
+  const int nblk = (M + BO_BLOCK - 1) / BO_BLOCK;
+  bin_block_count_kernel<<<nblk, BO_BLOCK, 0, s>>>(bin, M, scratch);
+  bin_block_scan_kernel<<<1, 1024, 0, s>>>(scratch, nblk, counts);
+  bin_stable_scatter_kernel<<<nblk, BO_BLOCK, 0, s>>>(bin, M, scratch, order);
   return cudaGetLastError();
 }
 

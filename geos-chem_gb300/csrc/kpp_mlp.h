@@ -39,7 +39,8 @@ cudaError_t head_loss(const float* out, const float* y_h, const int* y_bin, floa
 cudaError_t adam(float* w, __nv_bfloat16* wb, float* g, float* m1, float* m2, int n, float lr, float b1, float b2,
                  float eps, int step, cudaStream_t s);
 cudaError_t propose(const float* out, int M, double scale, double hmin, double hmax, double* h0, int* bin,
-                    cudaStream_t s);
-cudaError_t bin_order(const int* bin, int M, int* counts, int* cursor, int* order, cudaStream_t s);
+                    int keep, cudaStream_t s);
+cudaError_t bin_order(const int* bin, int M, int* counts, int* scratch, int* order, cudaStream_t s);
+int bin_order_scratch(int M);
 
 }  // namespace gcmlp

@@ -106,6 +106,11 @@ struct Rosenbrock {
       y[(nvar + f) * TSN] = v;
       y1[(nvar + f) * TSN] = v;
     }
+    init_lane(L, cell);
+  }
+
+  // Per-cell scalar state at the start of the integration.
+  __device__ void init_lane(Lane& L, int cell) const {
     L.cell = cell;
     L.nfun = L.njac = L.nstp = L.nacc = L.nrej = L.ndec = L.nsol = L.nsng = 0;
     L.texit = 0.0;
@@ -127,6 +132,53 @@ struct Rosenbrock {
     L.rej_last = 0;
     L.rej_more = 0;
     L.phase = PH_NEWSTEP;
+  }
+
+  // After a decomposition with singularity flag ier (:1977-1995): true if
+  // the cell retries with H halved, false if it proceeds; a sixth
+  // consecutive singular matrix ends the cell with IERR = -8.
+  __device__ bool singular_retry(Lane& c, int ier, int& nconsec) const {
+    c.ndec += 1;
+    if (ier == 0) return false;
+    c.nsng += 1;
+    nconsec += 1;
+    if (nconsec <= 5) {
+      c.H = c.H * 0.5;
+      return true;
+    }
+    c.ierr = -8;
+    c.phase = PH_DONE;
+    return false;
+  }
+
+  // Step size control (:742-778) from the error norm's sum of squares.
+  // Returns true if the step is accepted (the caller then copies Ynew).
+  __device__ bool control(Lane& c, double err_sum, double dir) const {
+    double e = sqrt(err_sum / (double)m.nvar);
+    e = fmax(e, 1.0e-10);
+    const double fac = fmin(p.facmax, fmax(p.facmin, p.facsafe / pow(e, 1.0 / r.ELO)));
+    double hnew = c.H * fac;
+    c.nstp += 1;
+    if ((e <= 1.0) || (c.H <= p.hmin)) {
+      c.nacc += 1;
+      c.T = c.T + dir * c.H;
+      hnew = fmax(p.hmin, fmin(hnew, p.hmax));
+      if (c.rej_last) hnew = fmin(hnew, c.H);
+      c.hexit = c.H;
+      c.hnew_out = hnew;
+      c.texit = c.T;
+      c.rej_last = 0;
+      c.rej_more = 0;
+      c.H = hnew;
+      c.phase = PH_NEWSTEP;
+      return true;
+    }
+    if (c.rej_more) hnew = c.H * p.facrej;
+    c.rej_more = c.rej_last;
+    c.rej_last = 1;
+    c.H = hnew;
+    if (c.nacc >= 1) c.nrej += 1;
+    return false;
   }
 
   __device__ void store_cell(double* w, int q, const Lane& L) {
@@ -232,21 +284,11 @@ struct Rosenbrock {
 #pragma unroll
         for (int q = 0; q < NC; ++q) {
           if (!pending[q]) continue;
-          L[q].ndec += 1;
-          if (ier[q] == 0) {
-            pending[q] = false;
-            continue;
-          }
-          L[q].nsng += 1;
-          nconsec[q] += 1;
-          if (nconsec[q] <= 5) {
-            L[q].H = L[q].H * 0.5;
+          if (singular_retry(L[q], ier[q], nconsec[q])) {
             again = true;
           } else {
-            L[q].ierr = -8;
-            L[q].phase = PH_DONE;
             pending[q] = false;
-            live[q] = false;
+            if (L[q].phase == PH_DONE) live[q] = false;
           }
         }
         if (!again) break;
@@ -341,36 +383,13 @@ struct Rosenbrock {
 #pragma unroll
     for (int q = 0; q < NC; ++q) {
       if (!live[q]) continue;
-      Lane& c = L[q];
-      double e = sqrt(err[q] / (double)nvar);
-      e = fmax(e, 1.0e-10);
-      const double fac = fmin(p.facmax, fmax(p.facmin, p.facsafe / pow(e, 1.0 / r.ELO)));
-      double hnew = c.H * fac;
-      c.nstp += 1;
-      if ((e <= 1.0) || (c.H <= p.hmin)) {
-        c.nacc += 1;
+      if (control(L[q], err[q], dir)) {
         double* yq = arr(w, p.lay.y0, q);
         const double* ynq = arr(w, p.lay.y1, q);
         for (int i = 0; i < nvar; ++i) {
           const double v = ynq[i * TSN];
           yq[i * TSN] = p.clamp_negative ? fmax(v, 0.0) : v;
         }
-        c.T = c.T + dir * c.H;
-        hnew = fmax(p.hmin, fmin(hnew, p.hmax));
-        if (c.rej_last) hnew = fmin(hnew, c.H);
-        c.hexit = c.H;
-        c.hnew_out = hnew;
-        c.texit = c.T;
-        c.rej_last = 0;
-        c.rej_more = 0;
-        c.H = hnew;
-        c.phase = PH_NEWSTEP;
-      } else {
-        if (c.rej_more) hnew = c.H * p.facrej;
-        c.rej_more = c.rej_last;
-        c.rej_last = 1;
-        c.H = hnew;
-        if (c.nacc >= 1) c.nrej += 1;
       }
     }
   }

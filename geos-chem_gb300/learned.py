@@ -19,12 +19,15 @@ torch tensors are used only as device allocations and streams.
 """
 import ctypes
 import json
+import os
 
 import numpy as np
 
 from . import capi, inputs, mechanism
 
 NFEAT, HID, NOUT, NJ, NSPC, NBIN = 56, 128, 5, 20, 32, 4
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "proposer_4x5.npz")
+BIN_EDGES = (2, 4, 16)  # Rosenbrock steps per chemistry step: 1 | 2-3 | 4-15 | >= 16
 
 J_SPECIES = ["NO2", "O3", "O3", "HNO2", "H2O2", "HNO3", "HNO4", "NO3", "NO3", "N2O5", "CH2O", "CH2O", "MP",
              "Cl2", "Br2", "BrO", "ClNO3", "HOBr", "MGLY", "ALD2"]
@@ -59,8 +62,9 @@ def _lib():
     lib.gc_mlp_loss.argtypes = [i32, vp, vp, vp, f32, vp, vp, vp]
     lib.gc_mlp_backward.argtypes = [i32] + [vp] * 16 + [vp]
     lib.gc_mlp_adam.argtypes = [i32, vp, vp, vp, vp, vp, f32, f32, f32, f32, i32, vp]
-    lib.gc_mlp_propose.argtypes = [i32, vp, f64, f64, f64, vp, vp, vp]
+    lib.gc_mlp_propose.argtypes = [i32, vp, f64, f64, f64, vp, vp, i32, vp]
     lib.gc_mlp_bin_order.argtypes = [i32, vp, vp, vp, vp, vp]
+    lib.gc_mlp_bin_order_scratch.argtypes = [i32]
     return lib
 
 
@@ -166,15 +170,14 @@ class Proposer:
                                         _p(self.m2[k]), lr, b1, b2, eps, self.step_count, None), "adam")
 
     # -- training -------------------------------------------------------------
-    def fit_targets(self, hnew, steps, quantiles=(0.5, 0.85, 0.97)):
+    def fit_targets(self, hnew, steps, edges=BIN_EDGES):
         """Centre of log(Hnew) and the step-count edges of the 4 stiffness
-        bins.  The edges sit at upper quantiles so that the last bin holds the
-        few cells whose step counts form the tail of the launch."""
+        bins (bin b holds cells with edges[b-1] <= steps < edges[b]).  The
+        last bin is the few cells that need tens of steps, the ones the
+        block-per-cell kernel takes."""
         t = self.torch
         self.y_mean = float(t.log(hnew.double().clamp_min(1e-10)).mean().item())
-        sub = steps.double()[:2_000_000]
-        q = t.quantile(sub, t.tensor(list(quantiles), dtype=t.float64, device=sub.device))
-        self.bin_edges = [float(v) for v in q.tolist()]
+        self.bin_edges = [float(v) for v in edges]
 
     def targets(self, hnew, steps):
         """log(Hnew) (centred) and the stiffness bin of each row."""
@@ -217,14 +220,19 @@ class Proposer:
         return hist
 
     # -- inference ------------------------------------------------------------
-    def propose(self, x, hmin=1e-5, hmax=1.0e9, stream=None):
+    def propose(self, x, hmin=1e-5, hmax=1.0e9, stream=None, h0=None):
+        """H0 proposals and stiffness bins.  If `h0` is given, it is filled in
+        place where it is not positive (cells without a KPPHvalue)."""
         t = self.torch
         M = x.shape[0]
         a = self.forward(x, stream=stream)
-        a["out"][:, 0] += self.y_mean
-        h0 = t.empty(M, dtype=t.float64, device=self.dev)
+        keep = h0 is not None
+        if h0 is None:
+            h0 = t.empty(M, dtype=t.float64, device=self.dev)
         b = t.empty(M, dtype=t.int32, device=self.dev)
-        _check(self.lib.gc_mlp_propose(M, _p(a["out"]), float(self.h0_scale), hmin, hmax, _p(h0), _p(b), stream),
+        # the network's log-H output is centred on y_mean: fold exp(y_mean) into the scale
+        scale = float(self.h0_scale * np.exp(self.y_mean))
+        _check(self.lib.gc_mlp_propose(M, _p(a["out"]), scale, hmin, hmax, _p(h0), _p(b), int(keep), stream),
                "propose")
         return h0, b
 
@@ -233,8 +241,9 @@ class Proposer:
         M = bins.shape[0]
         order = t.empty(M, dtype=t.int32, device=self.dev)
         counts = t.empty(NBIN, dtype=t.int32, device=self.dev)
-        cursor = t.empty(NBIN, dtype=t.int32, device=self.dev)
-        _check(self.lib.gc_mlp_bin_order(M, _p(bins), _p(counts), _p(cursor), _p(order), stream), "bin_order")
+        scratch = t.empty(max(NBIN, self.lib.gc_mlp_bin_order_scratch(M)), dtype=t.int32, device=self.dev)
+        _check(self.lib.gc_mlp_bin_order(M, _p(bins), _p(counts), _p(scratch), _p(order), stream), "bin_order")
+        self.last_counts = counts
         return order
 
     # -- persistence -----------------------------------------------------------
@@ -296,10 +305,10 @@ def collect(solver, prop, cells, dt=1200.0, nsteps=2, spinup=86400.0, log=None):
     return {"x": torch.cat(xs), "hnew": torch.cat(hn), "steps": torch.cat(st)}
 
 
-def fit(prop, data, epochs=6, batch=4096, lr=2e-3, w_ce=0.5, quantiles=(0.5, 0.85, 0.97), seed=0, log=None):
+def fit(prop, data, epochs=6, batch=4096, lr=2e-3, w_ce=0.5, edges=BIN_EDGES, seed=0, log=None):
     """Normalisation, targets and training of `prop` on collected rows."""
     prop.fit_normalisation_rows(data["x"])
-    prop.fit_targets(data["hnew"], data["steps"], quantiles)
+    prop.fit_targets(data["hnew"], data["steps"], edges)
     x = prop.normalise(data["x"])
     y_h, y_b = prop.targets(data["hnew"], data["steps"])
     return prop.train(x, y_h, y_b, epochs=epochs, batch=batch, lr=lr, w_ce=w_ce, seed=seed, log=log)
@@ -324,9 +333,8 @@ def makespan(work, order, nslot):
 
 
 def evaluate(prop, data):
-    """Held-out quality: log-H RMSE, bin accuracy, and the simulated queue
-    makespan (in cell-steps) under natural, predicted-bin and true-count
-    orders."""
+    """Held-out quality: log-H RMSE, bin accuracy and, per true bin, how
+    many cells the network puts there."""
     t = prop.torch
     x = prop.normalise(data["x"])
     a = prop.forward(x)
@@ -335,4 +343,60 @@ def evaluate(prop, data):
     rmse = float(t.sqrt(((out[:, 0] - y_h) ** 2).mean()).item())
     pred_b = out[:, 1:].argmax(1).int()
     acc = float((pred_b == y_b).double().mean().item())
-    return {"logh_rmse": rmse, "bin_accuracy": acc}
+    per_bin = {}
+    for b in range(NBIN):
+        sel = y_b == b
+        n = int(sel.sum().item())
+        per_bin[str(b)] = {"cells": n, "recall": float((pred_b[sel] == b).double().mean().item()) if n else None,
+                           "predicted": int((pred_b == b).sum().item())}
+    return {"logh_rmse": rmse, "bin_accuracy": acc, "bins": per_bin, "edges": prop.bin_edges}
+
+
+class CProposer:
+    """A Proposer's weights on the device behind the C ABI (gc_kpp_proposer),
+    for Solver.fullchem_step_learned."""
+
+    def __init__(self, prop, device=0):
+        lib = capi.load_library()
+        vp, i32, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        lib.gc_kpp_proposer_create.argtypes = [i32] + [vp] * 10 + [f64, ctypes.POINTER(vp)]
+        lib.gc_kpp_proposer_destroy.argtypes = [vp]
+        self.lib = lib
+        host = lambda t, dt: np.ascontiguousarray(t.detach().cpu().numpy(), dtype=dt)
+        arrs = [host(prop.master[k], np.float32) for k in ("w1", "b1", "w2", "b2", "w3", "b3")]
+        arrs += [host(prop.mean, np.float64), host(prop.inv_std, np.float64), host(prop.jrows, np.int32),
+                 host(prop.srows, np.int32)]
+        self._keep = arrs
+        self.handle = ctypes.c_void_p()
+        scale = float(prop.h0_scale * np.exp(prop.y_mean))
+        rc = lib.gc_kpp_proposer_create(device, *[a.ctypes.data_as(vp) for a in arrs], scale,
+                                        ctypes.byref(self.handle))
+        if rc != 0:
+            raise capi.GcKppError(rc, lib.gc_kpp_last_error().decode())
+
+    def close(self):
+        if self.handle:
+            self.lib.gc_kpp_proposer_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+PLAN_LAUNCHES = 8  # features 1, forward 3, propose 1, bin order 3
+
+
+def plan(prop, met, photol, c, stream=None, hstart=None, hmax=1.0e9):
+    """The learned part of a chemistry step, on the GPU: features of every
+    cell, the MLP, H0 proposals and stiffness bins, and the queue order
+    (heaviest predicted bin first).  Launches PLAN_LAUNCHES kernels.  The
+    per-bin cell counts are left in ``prop.last_counts`` (device).  With
+    `hstart` (the KPPHvalue array), proposals fill it in place where it is not
+    positive and it is returned as H0."""
+    x = prop.features(met, photol, c, stream=stream)
+    h0, bins = prop.propose(x, stream=stream, h0=hstart, hmax=hmax)
+    order = prop.bin_order(bins, stream=stream)
+    return h0, bins, order

@@ -1,0 +1,93 @@
+"""A small, self-contained chemistry case for profiling the kernels.
+
+    python geos-chem_gb300/profile_case.py --cells 4096 --tout 60 --arith fast [--probe]
+    python geos-chem_gb300/profile_case.py --grid 72x46x8 --step --binned 64
+
+Box cells (``inputs.box_cells``) are integrated once from 0 to TOUT with
+``Solver.integrate``; ``--grid`` instead spins up a grid and runs one 1200 s
+chemistry step (``--binned N``: the N cells with the most steps go
+block-per-cell).  It prints the ISTATUS sums and the algorithmic FP64
+operations of the reference routines for them; ``--probe`` also runs the FP64
+throughput probe.  Meant to run under ncu on one GPU with few launches.
+"""
+import argparse
+import ctypes
+import os
+import sys
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--cells", type=int, default=4096)
+    ap.add_argument("--tout", type=float, default=60.0)
+    ap.add_argument("--arith", default="fast", choices=["fast", "strict", "fast2", "fast4"])
+    ap.add_argument("--schedule", default="queue", choices=["plain", "queue"])
+    ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--grid", default=None, help="NLONxNLATxNLEV: grid step instead of box cells")
+    ap.add_argument("--binned", type=int, default=0, help="grid step: cells sent block-per-cell")
+    ap.add_argument("--probe", action="store_true")
+    args = ap.parse_args(argv)
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.dirname(here))
+    import __graft_entry__
+
+    __graft_entry__.load_package()
+    import numpy as np
+    import torch
+
+    import gcchem.build as build
+    import gcchem.capi as capi
+    import gcchem.inputs as inputs
+    from gcchem.mechanism import load_ir
+    from gcchem.tables import Tables
+
+    dev = torch.device("cuda", 0)
+    T = lambda x: torch.tensor(x, device=dev).contiguous()
+    s = capi.Solver(0, arith=args.arith, schedule=args.schedule, block=args.block)
+    atol, rtol = inputs.tolerances()
+    ic, rc = inputs.default_controls()
+    at, rt = T(atol), T(rtol)
+    if args.grid:
+        nlon, nlat, nlev = (int(v) for v in args.grid.split("x"))
+        cells = inputs.grid_cells(nlon, nlat, nlev, seed=0)
+    else:
+        cells = inputs.box_cells(args.cells, seed=1)
+    n = cells["c"].shape[1]
+    met, ph, c = T(cells["met"]), T(cells["photol"]), T(cells["c"])
+    ist = torch.zeros((20, n), dtype=torch.int32, device=dev)
+    rst = torch.zeros((20, n), dtype=torch.float64, device=dev)
+    ierr = torch.zeros(n, dtype=torch.int32, device=dev)
+    if args.grid:
+        hs = torch.zeros(n, dtype=torch.float64, device=dev)
+        s.fullchem_step(86400.0, met, ph, c, at, rt, ic, rc, hs, ist, rst, ierr)
+        order, nb = None, 0
+        if args.binned:
+            s.fullchem_step(1200.0, met, ph, c.clone(), at, rt, ic, rc, hs.clone(), ist, rst, ierr)
+            order = torch.argsort(ist[2], descending=True, stable=True).int()
+            nb = args.binned
+        s.fullchem_step(1200.0, met, ph, c, at, rt, ic, rc, hs, ist, rst, ierr, order=order, nblock=nb)
+    else:
+        r = torch.zeros((1058, n), dtype=torch.float64, device=dev)
+        s.update_rconst(met, ph, c, r)
+        s.integrate(c, r, at, rt, 0.0, args.tout, ic, rc, istatus=ist, ierr=ierr)
+    torch.cuda.synchronize()
+    ih = ist.cpu().numpy().astype(np.int64)
+    t = Tables(load_ir())
+    f = t.flops()
+    vec = 15 * 2 * t.nvar + 5 * t.nvar
+    flops = (ih[0].sum() * f["fun"] + ih[1].sum() * f["jac"] + ih[5].sum() * (f["decomp"] + 1)
+             + ih[6].sum() * f["solve"] + ih[2].sum() * vec)
+    print("cells %d steps/cell %.3f max %d" % (n, ih[2].mean(), ih[2].max()))
+    print("ISTATUS sums fun jac stp acc rej dec sol sng", ih[:8].sum(axis=1).tolist())
+    print("algorithmic FP64 flops %.4e" % flops)
+    if args.probe:
+        probe = ctypes.CDLL(build.probe_path())
+        probe.gc_probe_fp64_gflops.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        g = ctypes.c_double()
+        rcode = probe.gc_probe_fp64_gflops(0, ctypes.byref(g))
+        print("FP64 probe rc %d: %.1f GFLOP/s" % (rcode, g.value))
+
+
+if __name__ == "__main__":
+    main()

@@ -208,8 +208,58 @@ class Tables:
         self.dot_term = np.array(dot, np.uint32).view(np.int32)
         assert len(self.dot_term) == len(self.uop)
         assert self.lu_nonzero < (1 << 16)
+        self._level_schedules(crow, diag, icol)
         self.lit = np.array(self.literals, np.float64)
         self.family_species = np.array([ir["species"].index(f) for f in ir.get("families", [])], np.int32)
+
+    def _level_schedules(self, crow, diag, icol):
+        """Dependency levels for the block-per-cell kernel, where the threads
+        of a block share one cell.  Each LU entry (k,c) is still one
+        sequential dot product (the same operation order as the thread-per-cell
+        form); an entry's level is one more than the highest level among the
+        entries it reads (L(k,j), U(j,c), and the pivot (c,c) for c < k).  The
+        substitutions get row levels the same way.  Within a level, the
+        longest items come first so that round-robin assignment starts them
+        early.  Fun_SPLIT rows and Jac_SP entries are independent and are
+        listed longest first."""
+        nvar, nz = self.nvar, self.lu_nonzero
+        lvl = np.zeros(nz, np.int64)
+        cost = np.zeros(nz, np.int64)
+        terms = self.dot_term.view(np.uint32)
+        for k in range(nvar):
+            for e in range(crow[k], crow[k + 1]):
+                t0, t1 = self.dot_start[e], self.dot_start[e + 1]
+                m = 0
+                for t in terms[t0:t1]:
+                    m = max(m, lvl[int(t) >> 16], lvl[int(t) & 0xFFFF])
+                if icol[e] < k:
+                    m = max(m, lvl[diag[icol[e]]])
+                lvl[e] = m + 1
+                cost[e] = t1 - t0
+        order = sorted(range(nz), key=lambda e: (lvl[e], -cost[e], e))
+        self.lu_lvl_entry = np.array(order, np.int32)
+        nl = int(lvl.max())
+        self.lu_lvl_start = np.searchsorted(lvl[order], np.arange(1, nl + 2)).astype(np.int32)
+
+        def row_levels(rows, deps):
+            lv = np.zeros(nvar, np.int64)
+            ln = np.zeros(nvar, np.int64)
+            for i in rows:
+                d = deps(i)
+                lv[i] = 1 + max((lv[j] for j in d), default=0)
+                ln[i] = len(d)
+            o = sorted(range(nvar), key=lambda i: (lv[i], -ln[i], i))
+            n = int(lv.max())
+            return np.array(o, np.int32), np.searchsorted(lv[o], np.arange(1, n + 2)).astype(np.int32)
+
+        self.fs_lvl_row, self.fs_lvl_start = row_levels(
+            range(nvar), lambda i: [icol[kk] for kk in range(crow[i], diag[i])])
+        self.bs_lvl_row, self.bs_lvl_start = row_levels(
+            range(nvar - 1, -1, -1), lambda i: [icol[kk] for kk in range(diag[i] + 1, crow[i + 1])])
+        flen = np.diff(self.p_start) + np.diff(self.d_start)
+        self.fun_rows_by_len = np.array(sorted(range(nvar), key=lambda i: (-flen[i], i)), np.int32)
+        jlen = np.diff(self.j_start)
+        self.jac_by_len = np.array(sorted(range(nz), key=lambda e: (-jlen[e], e)), np.int32)
 
     # flop bookkeeping used by the roofline accounting (FP64 operations per
     # call, counting a multiply-add as 2, a division as 1, in STRICT form)
@@ -276,6 +326,17 @@ class Tables:
         arr("family_species", self.family_species)
         arr("dot_start", self.dot_start)
         arr("dot_term", self.dot_term.view(np.uint32), "unsigned")
+        arr("lu_irow", np.repeat(np.arange(self.nvar), np.diff(self.crow)))
+        arr("lu_lvl_start", self.lu_lvl_start)
+        arr("lu_lvl_entry", self.lu_lvl_entry)
+        arr("fs_lvl_start", self.fs_lvl_start)
+        arr("fs_lvl_row", self.fs_lvl_row)
+        arr("bs_lvl_start", self.bs_lvl_start)
+        arr("bs_lvl_row", self.bs_lvl_row)
+        arr("fun_rows_by_len", self.fun_rows_by_len)
+        arr("jac_by_len", self.jac_by_len)
+        out.append("constexpr int LU_NLVL = %d, FS_NLVL = %d, BS_NLVL = %d;" % (
+            len(self.lu_lvl_start) - 1, len(self.fs_lvl_start) - 1, len(self.bs_lvl_start) - 1))
         out.append("static const double lit[%d] = {%s};" % (
             len(self.literals), ",".join(_hexfloat(v) for v in self.literals)))
         out.append("}  // namespace gcmech_tables")

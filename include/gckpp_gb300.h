@@ -46,14 +46,16 @@ extern "C" {
 
 /* gc_kpp_ctx_set_option keys */
 #define GC_KPP_OPT_ARITH 1        /* 0 = fast (FMA, reciprocal pivots), 1 = strict (reference order, no FMA),
-                                     2 = fast, 1 cell per thread, 3 = fast, 4 cells per thread;
-                                     fast (0) integrates 2 cells per thread */
+                                     2 = fast with 2 cells per thread, 3 = fast with 4 cells per thread
+                                     (0 and 1 integrate 1 cell per thread) */
 #define GC_KPP_OPT_SCHEDULE 2     /* 0 = plain (thread per cell), 1 = persistent work queue */
 #define GC_KPP_OPT_BLOCK 3        /* threads per block (multiple of 32, <= 1024), 0 = default 128 */
 #define GC_KPP_OPT_BLOCKS_PER_SM 4 /* queue schedule: resident blocks per SM, 0 = default */
 #define GC_KPP_OPT_MAX_SLOTS 5    /* cap on workspace slots (cells in flight), 0 = no cap */
 #define GC_KPP_OPT_TIMING 6       /* 1 = time the Rosenbrock launches with CUDA events */
 #define GC_KPP_OPT_LU 7           /* 0 = row-wise LU (default), 1 = KppDecomp right-looking order */
+#define GC_KPP_OPT_CELL_BLOCK 8   /* threads of the block-per-cell kernel (multiple of 32, <= 1024),
+                                     0 = default 256; 32 is one warp per cell */
 
 /* Per-cell meteorology/state fields of gc_kpp_update_rconst_batch (rows of
  * `met`), the thread-private globals that Set_Kpp_GridBox_Values and the
@@ -174,6 +176,47 @@ int gc_kpp_fullchem_step_ordered(gc_kpp_ctx* ctx, int ncell, double dt, const do
                                  const double* atol, const double* rtol, const int* icntrl, const double* rcntrl,
                                  double* hstart, int* istatus, double* rstatus, long long ldo, int* ierr,
                                  int* nretry, const int* order, int mem, void* stream);
+
+/* gc_kpp_fullchem_step_ordered in which the first nblock cells of `order`
+ * are integrated block-per-cell: all threads of a block (GC_KPP_OPT_CELL_BLOCK)
+ * work on one cell whose Jacobian, LU factors and stage vectors are held in
+ * shared memory, on a second stream beside the thread-per-cell queue that
+ * takes the other cells.  Meant for the few stiff cells that need tens of
+ * steps while most need one or two; each cell gets the same arithmetic in
+ * either form.  Needs GC_KPP_OPT_ARITH 0 or 1 and the row-wise LU
+ * (GC_KPP_EUNSUPPORTED otherwise).  No counterpart in the reference. */
+int gc_kpp_fullchem_step_binned(gc_kpp_ctx* ctx, int ncell, double dt, const double* met, long long ldm,
+                                const double* photol, long long ldp, double* c, long long ldc,
+                                const double* atol, const double* rtol, const int* icntrl, const double* rcntrl,
+                                double* hstart, int* istatus, double* rstatus, long long ldo, int* ierr,
+                                int* nretry, const int* order, int nblock, int mem, void* stream);
+
+/* The learned proposer on the device: the MLP of the learned step-size /
+ * stiffness proposer (56 -> 128 -> 128 -> 5, GELU; include/gckpp_gb300_mlp.h
+ * has its kernels), created from host arrays: w1 [128][56], w2 [128][128],
+ * w3 [5][128] (rounded to BF16 on upload), biases b1 [128], b2 [128], b3 [5],
+ * the feature normalisation mean/inv_std [56], the PHOTOL rows jrows [20] and
+ * species rows srows [32] of the features, and scale: H0 = scale *
+ * exp(out[0]).  No counterpart in the reference. */
+typedef struct gc_kpp_proposer gc_kpp_proposer;
+int gc_kpp_proposer_create(int device, const float* w1, const float* b1, const float* w2, const float* b2,
+                           const float* w3, const float* b3, const double* mean, const double* inv_std,
+                           const int* jrows, const int* srows, double scale, gc_kpp_proposer** proposer);
+int gc_kpp_proposer_destroy(gc_kpp_proposer* proposer);
+
+/* gc_kpp_fullchem_step with the learned plan in front: features of every
+ * cell, the MLP, H0 proposals written into hstart where it is not positive
+ * (cells without a KPPHvalue; clamped to [1e-5, dt]), stiffness bins, the
+ * stable heaviest-bin-first queue order, and gc_kpp_fullchem_step_binned
+ * with the top bin block-per-cell (*nblock receives its size).  Same
+ * arguments and results as gc_kpp_fullchem_step; with device memory, hstart
+ * is required (zeros for a cold start).  The error-controlled integration
+ * decides every step: the proposals change the work, not the tolerance. */
+int gc_kpp_fullchem_step_learned(gc_kpp_ctx* ctx, gc_kpp_proposer* proposer, int ncell, double dt,
+                                 const double* met, long long ldm, const double* photol, long long ldp, double* c,
+                                 long long ldc, const double* atol, const double* rtol, const int* icntrl,
+                                 const double* rcntrl, double* hstart, int* istatus, double* rstatus,
+                                 long long ldo, int* ierr, int* nretry, int* nblock, int mem, void* stream);
 
 /* Batched INTEGRATE that allocates nothing, for callers that cannot call
  * cudaMalloc: code running inside a host application's memory-pool or

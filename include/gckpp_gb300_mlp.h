@@ -57,13 +57,19 @@ int gc_mlp_backward(int M, const float* x, const void* w1, const void* w2, const
 int gc_mlp_adam(int n, float* w, void* w_bf16, float* g, float* m1, float* m2, float lr, float b1, float b2,
                 float eps, int step, void* stream);
 
-/* h0 = clamp(scale * exp(out[:,0]), hmin, hmax); bin = argmax(out[:,1:5]). */
+/* h0 = clamp(scale * exp(out[:,0]), hmin, hmax); bin = argmax(out[:,1:5]).
+ * With keep != 0, entries of h0 that are already positive (a cell's
+ * KPPHvalue from its previous step) are left as they are. */
 int gc_mlp_propose(int M, const float* out, double scale, double hmin, double hmax, double* h0, int* bin,
-                   void* stream);
+                   int keep, void* stream);
 
-/* Counting sort of cells by bin, heaviest bin first: order[M]; counts and
- * cursor are [4] int scratch. */
-int gc_mlp_bin_order(int M, const int* bin, int* counts, int* cursor, int* order, void* stream);
+/* Stable counting sort of cells by bin, heaviest bin first: order[M] lists
+ * the cells of bin 3, then 2, 1, 0, each in ascending cell order; counts[4]
+ * receives the cells per bin.  scratch holds gc_mlp_bin_order_scratch(M)
+ * ints.  Three kernel launches, no atomics on the order: the same order on
+ * every run. */
+int gc_mlp_bin_order_scratch(int M);
+int gc_mlp_bin_order(int M, const int* bin, int* counts, int* scratch, int* order, void* stream);
 
 #ifdef __cplusplus
 }

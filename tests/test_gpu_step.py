@@ -209,3 +209,56 @@ def test_host_order_must_be_a_permutation(solver, step_case):
         solver.fullchem_step(600.0, cells["met"], cells["photol"], c, step_case["atol"], step_case["rtol"],
                              step_case["icntrl"], step_case["rcntrl"], ierr=ierr, order=bad)
     assert e.value.code == capi.GC_KPP_EINVAL
+
+
+@pytest.mark.parametrize("arith,cell_block", [("fast", 256), ("fast", 32), ("strict", 128)])
+def test_block_per_cell_matches_thread_per_cell(solver, step_case, arith, cell_block):
+    """gc_kpp_fullchem_step_binned: cells routed to the block-per-cell kernel
+    (shared-memory Jacobian/LU, level-scheduled factorization) get bit for
+    bit the results of the thread-per-cell kernel."""
+    n = step_case["n"]
+    cells = step_case["cells"]
+
+    def run(order=None, nblock=0):
+        solver.set(arith=arith, schedule="queue", block=64, cell_block=cell_block)
+        c = cells["c"].copy()
+        hs = np.full(n, 20.0)
+        ist = np.zeros((20, n), np.int32)
+        rst = np.zeros((20, n))
+        ierr = np.zeros(n, np.int32)
+        solver.fullchem_step(600.0, cells["met"], cells["photol"], c, step_case["atol"], step_case["rtol"],
+                             step_case["icntrl"], step_case["rcntrl"], hs, ist, rst, ierr, order=order,
+                             nblock=nblock)
+        return [c, hs, ist, rst, ierr]
+
+    base = run()
+    perm = np.random.default_rng(11).permutation(n).astype(np.int32)
+    for nblock in (1, 24, n):
+        got = run(perm, nblock)
+        for a, b in zip(got, base):
+            assert np.array_equal(a, b), nblock
+    solver.set(cell_block=0)
+
+
+def test_block_per_cell_strict_matches_oracle(solver, orc, step_case):
+    """Every cell block-per-cell, strict arithmetic, against the oracle."""
+    ir = mechanism.load_ir()
+    n = step_case["n"]
+    cells = step_case["cells"]
+    solver.set(arith="strict", schedule="queue", block=0, cell_block=256)
+    c = cells["c"].copy()
+    ist = np.zeros((20, n), np.int32)
+    rst = np.zeros((20, n))
+    ierr = np.zeros(n, np.int32)
+    solver.fullchem_step(600.0, cells["met"], cells["photol"], c, step_case["atol"], step_case["rtol"],
+                         step_case["icntrl"], step_case["rcntrl"], None, ist, rst, ierr,
+                         order=np.arange(n, dtype=np.int32), nblock=n)
+    c_ref, ist_ref, rst_ref, ierr_ref, _ = _oracle_step(orc, ir, cells, 600.0, step_case["icntrl"],
+                                                        step_case["rcntrl"], step_case["atol"], step_case["rtol"])
+    # the same bar as the thread-per-cell step (rates differ from the
+    # oracle's libm in the last bits)
+    assert np.array_equal(ierr, ierr_ref)
+    same = np.all(ist[:8] == ist_ref[:8], axis=0)
+    assert same.mean() >= 0.99
+    big = np.abs(c_ref) > 1e4
+    assert np.max(np.where(big, _rel(c, c_ref), 0.0)[:, same]) < 1e-9

@@ -108,3 +108,30 @@ def test_makespan_model_of_the_queue():
     assert learned.makespan(work, heavy_first, 4) == 20.0
     # one slot per cell: the order cannot matter
     assert learned.makespan(work, natural, 64) == learned.makespan(work, heavy_first, 64) == 20.0
+
+
+@pytest.mark.gpu
+def test_gpu_propose_and_bin_order():
+    """H0 = clamp(scale * exp(out[:,0])), bin = argmax(logits); the order is a
+    permutation of the cells with the heaviest bin first."""
+    import torch
+    import gcchem.learned as learned
+
+    pr = learned.Proposer(0, seed=4)
+    rng = np.random.default_rng(8)
+    M = 5000
+    x = torch.tensor(rng.normal(0, 1, (M, 56)).astype(np.float32), device=pr.dev)
+    pr.y_mean = 1.5
+    h0, bins = pr.propose(x, hmin=1e-5, hmax=1200.0)
+    out = pr.forward(x)["out"].cpu().numpy().astype(np.float64)
+    ref_h = np.clip(pr.h0_scale * np.exp(pr.y_mean) * np.exp(out[:, 0]), 1e-5, 1200.0)
+    assert np.allclose(h0.cpu().numpy(), ref_h, rtol=1e-6)
+    assert np.array_equal(bins.cpu().numpy(), out[:, 1:].argmax(1))
+    order = pr.bin_order(bins).cpu().numpy()
+    b = bins.cpu().numpy()
+    # heaviest bin first, ascending cells inside a bin (a stable sort)
+    assert np.array_equal(order, np.argsort(-b, kind="stable"))
+    assert np.array_equal(pr.last_counts.cpu().numpy(), np.bincount(b, minlength=4))
+    big = torch.tensor(np.random.default_rng(2).integers(0, 4, 700_001).astype(np.int32), device=pr.dev)
+    ob = pr.bin_order(big).cpu().numpy()
+    assert np.array_equal(ob, np.argsort(-big.cpu().numpy(), kind="stable"))
