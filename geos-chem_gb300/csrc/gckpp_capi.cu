@@ -112,6 +112,13 @@ struct gc_kpp_ctx {
   // optional CUDA-event timing of the Rosenbrock launches (GC_KPP_OPT_TIMING)
   int timing = 0;
   int lu_form = 0;  // 0 row-wise dot products, 1 KppDecomp right-looking order
+  int async = 0;    // chemistry steps never synchronise the host (GC_KPP_OPT_ASYNC)
+  int occ_arith = -1, occ_block = -1, occ_value = 1;  // cached occupancy query
+  DevBuf ranges;    // device queue ranges: [0,1] block-per-cell, [2,3] thread-per-cell, [4,5] retry
+  // tolerance arrays validated by the last synchronous step (async steps reuse them)
+  const void* tol_at = nullptr;
+  const void* tol_rt = nullptr;
+  int tol_vec = -1;
   int ntimed = 0;
   cudaEvent_t ev[8] = {};
   int arith = 0;     // 0 fast, 1 strict
@@ -197,7 +204,7 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
   if (c->side) cudaStreamDestroy(c->side);
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
                     &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
-                    &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord};
+                    &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges};
   for (DevBuf* b : bufs) b->release();
   delete c;
   return GC_KPP_OK;
@@ -227,6 +234,10 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
     case GC_KPP_OPT_LU:
       if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "lu form must be 0 or 1");
       c->lu_form = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_ASYNC:
+      if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "async must be 0 or 1");
+      c->async = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_TIMING:
       c->timing = v ? 1 : 0;
@@ -317,6 +328,8 @@ struct DevArgs {
   const int* order;  // optional cell list
   int cell_limit;    // cell ids lie in [0, cell_limit); 0 = ncell
   int nblock;        // the first nblock cells of order run block-per-cell
+  const int* nblock_dev;  // or: that count in device memory (no host synchronisation)
+  const int* qrange;      // or: device {begin, end} of the order positions to integrate
   const double* c_in;
   double* c_out;
   long long ldc;
@@ -374,17 +387,27 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   const int nb = a.nblock;
   if (nb < 0 || nb > a.ncell) return fail(GC_KPP_EINVAL, "block-per-cell count outside [0, ncell]");
   if (nb > 0 && !a.order) return fail(GC_KPP_EINVAL, "block-per-cell cells need a cell order");
-  if (nb > 0 && (c->arith > 1 || c->lu_form != 0))
+  const bool dev_split = a.nblock_dev != nullptr;
+  if ((nb > 0 || dev_split) && (c->arith > 1 || c->lu_form != 0))
     return fail(GC_KPP_EUNSUPPORTED, "block-per-cell cells need ARITH 0 or 1 and the row-wise LU");
-  const long long nthread = (long long)a.ncell - nb;
+  if ((dev_split || a.qrange) && !queue)
+    return fail(GC_KPP_EINVAL, "cell counts held on the device need the queue schedule");
+  if (dev_split && (!a.order || nb != 0)) return fail(GC_KPP_EINVAL, "device block-per-cell count needs an order");
+  // with counts on the device, size for every cell; the kernels read the ranges
+  const long long nthread = (dev_split || a.qrange) ? (long long)a.ncell : (long long)a.ncell - nb;
   long long nslot;
   int grid;
   if (queue) {
     int per_sm = c->blocks_per_sm;
     if (per_sm == 0) {
-      cudaError_t e = variant_occupancy(c->arith, block, &per_sm);
-      if (e != cudaSuccess) return cuda_fail(e, "occupancy");
-      per_sm = std::max(per_sm, 1);
+      // resident blocks per SM of this variant and block size (cached)
+      if (c->occ_arith != c->arith || c->occ_block != block) {
+        cudaError_t e = variant_occupancy(c->arith, block, &c->occ_value);
+        if (e != cudaSuccess) return cuda_fail(e, "occupancy");
+        c->occ_arith = c->arith;
+        c->occ_block = block;
+      }
+      per_sm = std::max(c->occ_value, 1);
     }
     grid = c->nsm * per_sm;
     const long long need_blocks = std::max(1LL, (nthread + per_block - 1) / per_block);
@@ -402,9 +425,17 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   GC_CUDA(c->ws.ensure(ws_bytes));
   GC_CUDA(c->counter.ensure(2 * sizeof(int)));
   GC_CUDA(cudaMemsetAsync(c->counter.p, 0, 2 * sizeof(int), s));
+  GC_CUDA(c->ranges.ensure(8 * sizeof(int)));
+  int* ranges = (int*)c->ranges.p;
+  if (dev_split) {
+    cudaError_t e = gcutil::split_ranges(a.nblock_dev, a.ncell, ranges, s);
+    if (e != cudaSuccess) return cuda_fail(e, "range kernel launch");
+    if (launches) *launches += 1;
+  }
   RosParams p{};
   p.ncell = (int)nthread;
   p.order = a.order ? a.order + nb : nullptr;
+  p.qrange = dev_split ? ranges + 2 : a.qrange;
   p.cell_limit = a.cell_limit > 0 ? a.cell_limit : a.ncell;
   p.queue_counter = (int*)c->counter.p;
   p.c_in = a.c_in;
@@ -437,25 +468,26 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   p.ws = (double*)c->ws.p;
   p.lay = c->lay;
   p.nslot = nslot;
-  const bool timed = c->timing && c->ntimed < 4;
+  const bool timed = c->timing && !c->async && c->ntimed < 4;
   if (timed) {
     for (int i = 2 * c->ntimed; i < 2 * c->ntimed + 2; ++i)
       if (!c->ev[i]) GC_CUDA(cudaEventCreate(&c->ev[i]));
     GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed], s));
   }
-  if (nb > 0) {
+  if (nb > 0 || dev_split) {
     if (!c->side) GC_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
     if (!c->fork) GC_CUDA(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
     if (!c->join) GC_CUDA(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
     GC_CUDA(cudaEventRecord(c->fork, s));
     GC_CUDA(cudaStreamWaitEvent(c->side, c->fork, 0));
     RosParams pb = p;
-    pb.ncell = nb;
+    pb.ncell = dev_split ? a.ncell : nb;
     pb.order = a.order;
+    pb.qrange = dev_split ? ranges : nullptr;
     pb.queue_counter = (int*)c->counter.p + 1;
     pb.ws = nullptr;
     pb.nslot = 0;
-    const int bgrid = std::min(nb, c->nsm);
+    const int bgrid = dev_split ? c->nsm : std::min(nb, c->nsm);
     cudaError_t eb = c->arith == 1 ? gckpp_launch_block_strict(bgrid, c->cell_block, c->mech, R.meth, pb, c->side)
                                    : gckpp_launch_block_fast(bgrid, c->cell_block, c->mech, R.meth, pb, c->side);
     if (eb != cudaSuccess) return cuda_fail(eb, "block-per-cell kernel launch");
@@ -467,7 +499,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     if (launches) *launches += 1;
   }
-  if (nb > 0) GC_CUDA(cudaStreamWaitEvent(s, c->join, 0));
+  if (nb > 0 || dev_split) GC_CUDA(cudaStreamWaitEvent(s, c->join, 0));
   if (timed) {
     GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed + 1], s));
     c->ntimed += 1;
@@ -568,7 +600,7 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
                               const double* photol, long long ldp, double* cc, long long ldc, const double* atol,
                               const double* rtol, const int* icntrl_u, const double* rcntrl_u, double* hstart,
                               int* istatus, double* rstatus, long long ldo, int* ierr, int* nretry,
-                              const int* order, int nblock, int mem, void* stream) {
+                              const int* order, int nblock, const int* nblock_dev, int mem, void* stream) {
   if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
   if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
   if (nretry) *nretry = 0;
@@ -582,8 +614,26 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
   c->ntimed = 0;
   Resolved R;
   GC_TRY(resolve(icntrl_u, rcntrl_u, 0.0, dt, R));
-  if (!R.code) GC_TRY(check_tolerances(atol, rtol, mem, R.vector_tol, s, R));
+  const bool async = c->async != 0;
+  if (async && (mem != GC_KPP_MEM_DEVICE || !c->schedule))
+    return fail(GC_KPP_EINVAL, "asynchronous steps need device memory and the queue schedule");
+  if (!R.code) {
+    if (async) {
+      // the tolerance check reads the arrays on the host; asynchronous steps
+      // reuse arrays that a synchronous step has checked
+      if (atol != c->tol_at || rtol != c->tol_rt || (int)R.vector_tol != c->tol_vec)
+        return fail(GC_KPP_EINVAL, "asynchronous steps need tolerance arrays checked by a synchronous step first");
+    } else {
+      GC_TRY(check_tolerances(atol, rtol, mem, R.vector_tol, s, R));
+      if (!R.code && mem == GC_KPP_MEM_DEVICE) {
+        c->tol_at = atol;
+        c->tol_rt = rtol;
+        c->tol_vec = R.vector_tol ? 1 : 0;
+      }
+    }
+  }
   const size_t n = (size_t)ncell, ntol = R.vector_tol ? T::NVAR : 1;
+  GC_CUDA(c->ord_buf.ensure(n * sizeof(int)));  // retry list, sized before any capture
   const double *dmet, *dph, *dat, *drt;
   double *dc, *dhs = nullptr, *drs;
   int *dis, *die;
@@ -639,7 +689,11 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
   cudaError_t e = gcrates::launch_rates(c->rates, ra, s);
   if (e != cudaSuccess) return cuda_fail(e, "rates kernel launch");
   c->last_launches = 1;
-  if (R.code) {
+  if (R.code && async) {
+    e = gcutil::fill_error(R.code, ncell, die, dis, drs, lo, s);
+    if (e != cudaSuccess) return cuda_fail(e, "error fill kernel launch");
+    c->last_launches += 1;
+  } else if (R.code) {
     GC_TRY(fill_option_error(R.code, ncell, die, dis, drs, lo, s));
   } else {
     // C_before_integrate (fullchem_mod.F90:1023), same leading dimension as C
@@ -649,11 +703,31 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
     DevArgs a{};
     a.ncell = ncell; a.c_in = dc; a.c_out = dc; a.ldc = lc; a.rconst = drc; a.ldr = ncell; a.atol = dat;
     a.rtol = drt; a.hstart = dhs; a.istatus = dis; a.rstatus = drs; a.ldo = lo; a.ierr = die;
-    a.order = dorder; a.cell_limit = ncell; a.nblock = nblock;
+    a.order = dorder; a.cell_limit = ncell; a.nblock = nblock; a.nblock_dev = nblock_dev;
     GC_TRY(launch_integrate(c, R, 0.0, dt, a, s, &c->last_launches));
+    if (async) {
+      // retry list built on the device; the retry launch reads its length there
+      int* ranges = (int*)c->ranges.p;
+      e = gcutil::collect_failed(die, ncell, (int*)c->ord_buf.p, ranges + 4, s);
+      if (e != cudaSuccess) return cuda_fail(e, "retry list kernel launch");
+      c->last_launches += 1;
+      DevArgs b = a;
+      b.order = (const int*)c->ord_buf.p;
+      b.qrange = ranges + 4;
+      b.nblock = 0;
+      b.nblock_dev = nullptr;
+      b.cell_limit = ncell;
+      b.c_in = dcb;
+      b.hstart = nullptr;
+      Resolved R2 = R;
+      R2.hstart_default = std::max(R.hmin, 1.0e-5);
+      if (nretry) *nretry = -1;
+      GC_TRY(launch_integrate(c, R2, 0.0, dt, b, s, &c->last_launches));
+    }
     // retry failed cells once with Hstart = 0 from C_before
     // (fullchem_mod.F90:1138-1162)
-    std::vector<int> hier(n);
+    std::vector<int> hier(async ? 0 : n);
+    if (!async) {
     GC_CUDA(cudaMemcpyAsync(hier.data(), die, n * sizeof(int), cudaMemcpyDeviceToHost, s));
     GC_CUDA(cudaStreamSynchronize(s));
     std::vector<int> failed;
@@ -669,12 +743,15 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
       b.order = dord;
       b.cell_limit = ncell;
       b.nblock = 0;
+      b.nblock_dev = nullptr;
+      b.qrange = nullptr;
       b.c_in = dcb;
       b.hstart = nullptr;
       Resolved R2 = R;
       R2.hstart_default = std::max(R.hmin, 1.0e-5);
       if (nretry) *nretry = (int)failed.size();
       GC_TRY(launch_integrate(c, R2, 0.0, dt, b, s, &c->last_launches));
+    }
     }
     // C = MAX(C, 0) (fullchem_mod.F90:1329-1350)
     e = gcutil::clamp_nonneg(dc, lc, T::NSPEC, ncell, s);
@@ -701,7 +778,7 @@ int gc_kpp_fullchem_step(gc_kpp_ctx* c, int ncell, double dt, const double* met,
                          int* istatus, double* rstatus, long long ldo, int* ierr, int* nretry, int mem,
                          void* stream) {
   return fullchem_step_impl(c, ncell, dt, met, ldm, photol, ldp, cc, ldc, atol, rtol, icntrl_u, rcntrl_u, hstart,
-                            istatus, rstatus, ldo, ierr, nretry, nullptr, 0, mem, stream);
+                            istatus, rstatus, ldo, ierr, nretry, nullptr, 0, nullptr, mem, stream);
 }
 
 int gc_kpp_fullchem_step_ordered(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm,
@@ -710,7 +787,7 @@ int gc_kpp_fullchem_step_ordered(gc_kpp_ctx* c, int ncell, double dt, const doub
                                  const double* rcntrl_u, double* hstart, int* istatus, double* rstatus,
                                  long long ldo, int* ierr, int* nretry, const int* order, int mem, void* stream) {
   return fullchem_step_impl(c, ncell, dt, met, ldm, photol, ldp, cc, ldc, atol, rtol, icntrl_u, rcntrl_u, hstart,
-                            istatus, rstatus, ldo, ierr, nretry, order, 0, mem, stream);
+                            istatus, rstatus, ldo, ierr, nretry, order, 0, nullptr, mem, stream);
 }
 
 int gc_kpp_fullchem_step_binned(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm,
@@ -721,7 +798,7 @@ int gc_kpp_fullchem_step_binned(gc_kpp_ctx* c, int ncell, double dt, const doubl
   if (nblock < 0 || nblock > ncell) return fail(GC_KPP_EINVAL, "nblock outside [0, ncell]");
   if (nblock > 0 && !order) return fail(GC_KPP_EINVAL, "nblock > 0 needs an order");
   return fullchem_step_impl(c, ncell, dt, met, ldm, photol, ldp, cc, ldc, atol, rtol, icntrl_u, rcntrl_u, hstart,
-                            istatus, rstatus, ldo, ierr, nretry, order, nblock, mem, stream);
+                            istatus, rstatus, ldo, ierr, nretry, order, nblock, nullptr, mem, stream);
 }
 
 int gc_kpp_last_launch_count(gc_kpp_ctx* c) { return c ? c->last_launches : 0; }
@@ -981,3 +1058,15 @@ int gckpp_set_error(int code, const char* msg) {
   g_last_error = msg;
   return code;
 }
+
+// The binned step with the block-per-cell count in device memory (the learned
+// step's asynchronous path, gckpp_learned_capi.cu).
+int gckpp_step_binned_dev(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm, const double* photol,
+                          long long ldp, double* cc, long long ldc, const double* atol, const double* rtol,
+                          const int* icntrl_u, const double* rcntrl_u, double* hstart, int* istatus, double* rstatus,
+                          long long ldo, int* ierr, int* nretry, const int* order, const int* nblock_dev, void* stream) {
+  return fullchem_step_impl(c, ncell, dt, met, ldm, photol, ldp, cc, ldc, atol, rtol, icntrl_u, rcntrl_u, hstart,
+                            istatus, rstatus, ldo, ierr, nretry, order, 0, nblock_dev, GC_KPP_MEM_DEVICE, stream);
+}
+
+int gckpp_ctx_async(const gc_kpp_ctx* c) { return c ? c->async : 0; }

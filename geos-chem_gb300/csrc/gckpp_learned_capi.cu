@@ -102,6 +102,11 @@ cudaError_t ensure_host_staging(gc_kpp_proposer* q, size_t n, int nspec, int nva
   } while (0)
 
 int gckpp_set_error(int code, const char* msg);
+int gckpp_ctx_async(const gc_kpp_ctx* c);
+int gckpp_step_binned_dev(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm, const double* photol,
+                          long long ldp, double* cc, long long ldc, const double* atol, const double* rtol,
+                          const int* icntrl_u, const double* rcntrl_u, double* hstart, int* istatus, double* rstatus,
+                          long long ldo, int* ierr, int* nretry, const int* order, const int* nblock_dev, void* stream);
 
 extern "C" {
 
@@ -195,6 +200,13 @@ int gc_kpp_fullchem_step_learned(gc_kpp_ctx* ctx, gc_kpp_proposer* q, int ncell,
   GC_L_CUDA(gemm_fwd(q->h2, q->w3, q->b3, nullptr, q->out, ncell, HID, NOUT, 0, s));
   GC_L_CUDA(propose(q->out, ncell, q->scale, 1.0e-5, dt, dhs, q->bins, 1, s));
   GC_L_CUDA(bin_order(q->bins, ncell, q->counts, q->scratch, q->order, s));
+  if (gckpp_ctx_async(ctx)) {
+    // the top bin's size stays on the device (no host synchronisation)
+    if (host) return gckpp_set_error(GC_KPP_EINVAL, "asynchronous steps need device memory");
+    if (nblock) *nblock = -1;
+    return gckpp_step_binned_dev(ctx, ncell, dt, dmet, lm, dph, lp, dc, lc, dat, drt, icntrl, rcntrl, dhs, dis, drs,
+                                 lo, die, nretry, q->order, q->counts + (NBIN - 1), stream);
+  }
   int counts[NBIN];
   GC_L_CUDA(cudaMemcpyAsync(counts, q->counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
   GC_L_CUDA(cudaStreamSynchronize(s));

@@ -222,11 +222,16 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
   const int tid = threadIdx.x, nt = blockDim.x;
   const double dir = (p.tend >= p.tstart) ? 1.0 : -1.0;
   Rosenbrock<STRICT, 1> ros(m, r, p);
+  int qlo = 0, qhi = p.ncell;
+  if (p.qrange) {
+    qlo = p.qrange[0];
+    qhi = p.qrange[1];
+  }
   while (true) {
-    if (tid == 0) sh.next = atomicAdd(p.queue_counter, 1);
+    if (tid == 0) sh.next = qlo + atomicAdd(p.queue_counter, 1);
     __syncthreads();
     const int idx = sh.next;
-    if (idx >= p.ncell) break;
+    if (idx >= qhi) break;
     const int cell = p.order ? p.order[idx] : idx;
     if ((unsigned)cell >= (unsigned)p.cell_limit) {
       __syncthreads();

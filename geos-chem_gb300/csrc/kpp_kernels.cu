@@ -61,9 +61,16 @@ cudaError_t GCKPP_CAT(gckpp_launch_block_, GCKPP_VARIANT)(int grid, int block, c
                                                           const RosParams& p, cudaStream_t s) {
   if (block < 32 || block > 1024 || block % 32) return cudaErrorInvalidConfiguration;
   const size_t smem = GCKPP_CAT(gckpp_block_smem_, GCKPP_VARIANT)(m);
-  cudaError_t e = cudaFuncSetAttribute(ros_block_kernel<GCKPP_STRICT != 0>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static int smem_set[64] = {};  // set once per device (the size is fixed by the mechanism)
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64 || smem_set[dev] < (int)smem) {
+    e = cudaFuncSetAttribute(ros_block_kernel<GCKPP_STRICT != 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64) smem_set[dev] = (int)smem;
+  }
   ros_block_kernel<GCKPP_STRICT != 0><<<grid, block, smem, s>>>(m, r, p);
   return cudaGetLastError();
 }

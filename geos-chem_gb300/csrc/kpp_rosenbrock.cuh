@@ -41,6 +41,8 @@ struct RosParams {
   int ncell;
   const int* order;       // optional queue order (cell ids), length ncell
   int cell_limit;         // cell ids must lie in [0, cell_limit); others are skipped
+  const int* qrange;      // optional device {begin, end}: queue positions [begin, end) of order
+                          // instead of [0, ncell) (sizes known only on the device)
   int* queue_counter;     // queue schedule: next queue position
   // boundary arrays, cell-interleaved: X[k*ld + cell]
   const double* c_in;
@@ -419,17 +421,21 @@ __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams
   double* w = p.ws + warp * (long long)p.lay.total * TSN + lane;
   Lane L[NC];
   bool has[NC];
+  int qlo = 0, qhi = p.ncell;
+  if (p.qrange) {
+    qlo = p.qrange[0];
+    qhi = p.qrange[1];
+  }
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
-    int idx;
+    long long idx;
     if (QUEUE) {
-      idx = queue_claim(p.queue_counter);
+      idx = (long long)qlo + queue_claim(p.queue_counter);
     } else {
-      const long long g = warp * TSN + q * TS + lane;
-      idx = g < p.ncell ? (int)g : p.ncell;
+      idx = (long long)qlo + warp * TSN + q * TS + lane;
     }
     has[q] = false;
-    if (idx < p.ncell) {
+    if (idx < qhi) {
       const int cell = p.order ? p.order[idx] : idx;
       has[q] = (unsigned)cell < (unsigned)p.cell_limit;
       if (has[q]) ros.load_cell(w, q, L[q], cell);
@@ -443,8 +449,8 @@ __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams
         ros.store_cell(w, q, L[q]);
         has[q] = false;
         if (QUEUE) {
-          const int idx = queue_claim(p.queue_counter);
-          if (idx < p.ncell) {
+          const long long idx = (long long)qlo + queue_claim(p.queue_counter);
+          if (idx < qhi) {
             const int cell = p.order ? p.order[idx] : idx;
             if ((unsigned)cell < (unsigned)p.cell_limit) {
               ros.load_cell(w, q, L[q], cell);

@@ -56,6 +56,14 @@ extern "C" {
 #define GC_KPP_OPT_LU 7           /* 0 = row-wise LU (default), 1 = KppDecomp right-looking order */
 #define GC_KPP_OPT_CELL_BLOCK 8   /* threads of the block-per-cell kernel (multiple of 32, <= 1024),
                                      0 = default 256; 32 is one warp per cell */
+#define GC_KPP_OPT_ASYNC 9        /* 1 = chemistry steps never synchronise the host, so that a
+                                     caller can capture them in a CUDA graph: the retry list and
+                                     the block-per-cell count stay on the device, *nretry (and
+                                     *nblock of the learned step) are set to -1.  Needs device
+                                     memory, the queue schedule, and tolerance arrays that a
+                                     synchronous step on this context has checked; make one
+                                     synchronous call of the largest batch before capturing
+                                     (buffers are sized then, never inside a capture). */
 
 /* Per-cell meteorology/state fields of gc_kpp_update_rconst_batch (rows of
  * `met`), the thread-private globals that Set_Kpp_GridBox_Values and the

@@ -262,3 +262,44 @@ def test_block_per_cell_strict_matches_oracle(solver, orc, step_case):
     assert same.mean() >= 0.99
     big = np.abs(c_ref) > 1e4
     assert np.max(np.where(big, _rel(c, c_ref), 0.0)[:, same]) < 1e-9
+
+
+def test_async_steps_capture_in_a_cuda_graph(step_case):
+    """GC_KPP_OPT_ASYNC: three chemistry steps (with the KPPHvalue chain and
+    the device-side retry) captured in one CUDA graph and replayed give the
+    results of three synchronous steps."""
+    import torch
+
+    n = step_case["n"]
+    cells = step_case["cells"]
+    dev = torch.device("cuda", 0)
+    T = lambda a: torch.tensor(a, device=dev).contiguous()
+    met, ph, c0, at, rt = (T(cells["met"]), T(cells["photol"]), T(cells["c"]), T(step_case["atol"]),
+                           T(step_case["rtol"]))
+    ic, rc = step_case["icntrl"], step_case["rcntrl"]
+    solver = capi.Solver(0, arith="fast", schedule="queue", block=64)
+    z = lambda *s, dt=torch.float64: torch.zeros(s, dtype=dt, device=dev)
+
+    def steps(c, hs, ist, rst, ierr, stream=None):
+        for _ in range(3):
+            solver.fullchem_step(600.0, met, ph, c, at, rt, ic, rc, hs, ist, rst, ierr, stream=stream)
+
+    c, hs, ist, rst, ierr = c0.clone(), z(n), z(20, n, dt=torch.int32), z(20, n), z(n, dt=torch.int32)
+    steps(c, hs, ist, rst, ierr)  # synchronous: checks the tolerances, sizes the buffers
+    torch.cuda.synchronize()
+    ref = [x.cpu().numpy() for x in (c, hs, ist, rst, ierr)]
+    solver.set(async_steps=True)
+    c, hs = c0.clone(), z(n)
+    ist, rst, ierr = z(20, n, dt=torch.int32), z(20, n), z(n, dt=torch.int32)
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g):
+        steps(c, hs, ist, rst, ierr, stream=torch.cuda.current_stream().cuda_stream)
+    for _ in range(2):  # replay twice from the same start
+        c.copy_(c0)
+        hs.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        for a, b in zip([x.cpu().numpy() for x in (c, hs, ist, rst, ierr)], ref):
+            assert np.array_equal(a, b)
+    solver.set(async_steps=False)

@@ -135,3 +135,56 @@ def test_gpu_propose_and_bin_order():
     big = torch.tensor(np.random.default_rng(2).integers(0, 4, 700_001).astype(np.int32), device=pr.dev)
     ob = pr.bin_order(big).cpu().numpy()
     assert np.array_equal(ob, np.argsort(-big.cpu().numpy(), kind="stable"))
+
+
+@pytest.mark.gpu
+def test_learned_step_c_abi_matches_python_plan():
+    """gc_kpp_fullchem_step_learned (host and device memory) = the Python
+    plan (features, MLP, proposals, stable bin order) + the binned step."""
+    import torch
+    import gcchem.capi as capi
+    import gcchem.inputs as inputs
+    import gcchem.learned as learned
+
+    prop = learned.Proposer(0)
+    prop.load_state(dict(np.load(learned.WEIGHTS)))
+    cp = learned.CProposer(prop)
+    solver = capi.Solver(0, arith="fast", schedule="queue")
+    n = 3000
+    cells = inputs.grid_cells(20, 10, 15, seed=3)
+    cells = {k: np.ascontiguousarray(cells[k][:, :n]) for k in ("met", "photol", "c")}
+    atol, rtol = inputs.tolerances()
+    ic, rc = inputs.default_controls()
+    T = lambda a: torch.tensor(a, device=prop.dev).contiguous()
+
+    def dev_arrays():
+        return (T(cells["c"]), torch.zeros(n, dtype=torch.float64, device=prop.dev),
+                torch.zeros((20, n), dtype=torch.int32, device=prop.dev),
+                torch.zeros((20, n), dtype=torch.float64, device=prop.dev),
+                torch.zeros(n, dtype=torch.int32, device=prop.dev))
+
+    # Python plan + binned step
+    c, hs, ist, rst, ierr = dev_arrays()
+    met, ph = T(cells["met"]), T(cells["photol"])
+    _, _, order = learned.plan(prop, met, ph, c, hstart=hs, hmax=600.0)
+    nb = int(prop.last_counts[3].item())
+    solver.fullchem_step(600.0, met, ph, c, T(atol), T(rtol), ic, rc, hs, ist, rst, ierr, order=order, nblock=nb)
+    ref = [x.cpu().numpy() for x in (c, hs, ist, rst, ierr)]
+    # C ABI, device memory
+    c, hs, ist, rst, ierr = dev_arrays()
+    _, nb_d = solver.fullchem_step_learned(cp.handle, 600.0, met, ph, c, T(atol), T(rtol), ic, rc, hs, ist, rst,
+                                           ierr)
+    got_d = [x.cpu().numpy() for x in (c, hs, ist, rst, ierr)]
+    # C ABI, host memory
+    ch = cells["c"].copy()
+    hsh = np.zeros(n)
+    isth = np.zeros((20, n), np.int32)
+    rsth = np.zeros((20, n))
+    ierrh = np.zeros(n, np.int32)
+    _, nb_h = solver.fullchem_step_learned(cp.handle, 600.0, cells["met"], cells["photol"], ch, atol, rtol, ic, rc,
+                                           hsh, isth, rsth, ierrh)
+    assert nb_d == nb_h == nb
+    for got in (got_d, [ch, hsh, isth, rsth, ierrh]):
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)
+    cp.close()
