@@ -36,6 +36,7 @@ METRIC = "fullchem cells/s per 1200 s step, learned-binned vs plain GPU, at RTOL
 GRID = (72, 46, 72)
 DT = 1200.0
 SPINUP_S = 86400.0
+EVICT_LEARNED = 2  # hand-over after 2 steps in the learned arms (best of the sweep)
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "geos-chem_gb300", "weights", "proposer_4x5.npz")
 
 
@@ -270,21 +271,34 @@ def run_ours(args):
     prop.load_state(dict(np.load(args.weights)))
 
     def plain_arm(w, hs):
+        solver.set(evict_after=0)
         step(w, hs)
+
+    def handover_arm(k):
+        # no learning: grid order, cells still running after k steps finish
+        # block-per-cell
+        def arm(w, hs):
+            solver.set(evict_after=k)
+            step(w, hs)
+        return arm
 
     def learned_arm(w, hs, met_=met, ph_=ph, tt=dev_t):
         # H0 proposals seed RCNTRL(3) where the cell has no KPPHvalue yet;
-        # stiffness bins order the queue and the top bin goes block-per-cell
+        # stiffness bins order the queue and the top bin goes block-per-cell;
+        # cells the network missed are handed over after EVICT_LEARNED steps
+        solver.set(evict_after=EVICT_LEARNED)
         _, _, order = learned.plan(prop, met_, ph_, w, stream=sp, hstart=hs, hmax=DT)
         nheavy = int(prop.last_counts[learned.NBIN - 1].item())
         last["nblock"] = nheavy
         step(w, hs, order=order, nblock=nheavy, tt=tt)
 
     # cold: every cell starts from RCNTRL(3) = 0 (DeltaMin) unless the network
-    # proposes H0; chained: every cell starts from its KPPHvalue
+    # proposes H0; chained: every cell starts from its KPPHvalue.  The
+    # hand-over-only arms use the best k of a sweep over 2, 4, 8, 16 steps.
     cold0 = torch.zeros_like(hs_spun)
-    arms = {"plain": (plain_arm, 0, cold0), "learned": (learned_arm, learned.PLAN_LAUNCHES, cold0),
-            "plain_chained": (plain_arm, 0, hs_spun),
+    arms = {"plain": (plain_arm, 0, cold0), "handover": (handover_arm(16), 0, cold0),
+            "learned": (learned_arm, learned.PLAN_LAUNCHES, cold0),
+            "plain_chained": (plain_arm, 0, hs_spun), "handover_chained": (handover_arm(2), 0, hs_spun),
             "learned_chained": (learned_arm, learned.PLAN_LAUNCHES, hs_spun)}
 
     def time_arm(name):
@@ -327,7 +341,7 @@ def run_ours(args):
         return {"ms_per_step": ms_step, "value": world * ncell / (ms_step * 1e-3),
                 "kernel_ms": float(np.mean(kernel_ms)), "gpu_launches": int(launches), "clocks": clocks,
                 "ist": ist.cpu().numpy(), "ierr": ierr.cpu().numpy(), "retried_cells": int(last["nretry"]),
-                "block_per_cell_cells": int(last.get("nblock", 0)) if name == "learned" else 0,
+                "block_per_cell_cells": int(last.get("nblock", 0)) if name.startswith("learned") else 0,
                 "c": work.clone()}
 
     res = {name: time_arm(name) for name in arms}
@@ -335,6 +349,8 @@ def run_ours(args):
     tabs = tables_mod.Tables(__import__("gcchem.mechanism", fromlist=["x"]).load_ir())
     flops = algorithmic_flops(tabs, head["ist"])
     achieved_tf = flops / (head["kernel_ms"] * 1e-3) / 1e12
+    flops_plain = algorithmic_flops(tabs, res["plain"]["ist"])
+    achieved_plain_tf = flops_plain / (res["plain"]["kernel_ms"] * 1e-3) / 1e12
 
     # FP64 peak measured on this GPU (roofline denominator)
     peak_gf = None
@@ -434,8 +450,9 @@ def run_ours(args):
                                    "proposes H0",
                        "cells_per_gpu": ncell, "dt_s": DT,
                        "solver": "%s schedule, fast arithmetic, 1 cell per thread" % args.schedule,
-                       "value_is": "learned-binned arm: MLP stiffness bins order the persistent queue and "
-                                   "send the top bin block-per-cell",
+                       "value_is": "learned-binned arm: MLP H0 proposals seed Hstart, stiffness bins order "
+                                   "the persistent queue and send the top bin block-per-cell, cells still "
+                                   "running after 2 steps finish block-per-cell",
                        "l2": "inputs larger than L2 (C 0.68 GB, RCONST 2.0 GB per step)",
                        "weights": os.path.basename(args.weights),
                        "spinup_s": args.spinup, "spinup_wall_s": spin_s, "spinup_steps_per_cell": spin_steps,
@@ -443,18 +460,26 @@ def run_ours(args):
             "plain": arms_out["plain"],
             "learned": arms_out["learned"],
             "learned_over_plain": head["value"] / res["plain"]["value"],
+            "handover_only": dict(arms_out["handover"], evict_after=16,
+                                  note="no network: grid order, cells past 16 steps finish block-per-cell"),
+            "learned_over_handover_only": head["value"] / res["handover"]["value"],
             "chained": {"note": "every cell starts from its KPPHvalue (RSTATE(Nhnew) of the spin-up), "
                                 "as Do_FullChem does after its first step",
                         "plain": arms_out["plain_chained"], "learned": arms_out["learned_chained"],
+                        "handover_only": dict(arms_out["handover_chained"], evict_after=2),
                         "learned_over_plain": res["learned_chained"]["value"] / res["plain_chained"]["value"]},
             "e2e": e2e,
             "gpu_launches": head["gpu_launches"],
             "roofline": {"bound": "fp64", "achieved": achieved_tf,
                          "peak": (peak_gf / 1e3) if peak_gf else None, "unit": "TFLOP/s",
                          "frac": (achieved_tf / (peak_gf / 1e3)) if peak_gf else None, "traffic": None,
-                         "kernel": "gckpp::ros_kernel (Rosenbrock, thread per cell), learned arm",
+                         "kernel": "gckpp::ros_kernel (thread per cell) + gckpp::ros_block_kernel (block per "
+                                   "cell), learned arm, one step's Rosenbrock launches",
                          "kernel_ms": head["kernel_ms"], "flops_per_launch": flops,
-                         "peak_source": "measured FP64 FMA probe on this GPU (of measured)"},
+                         "peak_source": "measured FP64 FMA probe on this GPU (of measured)",
+                         "plain_kernel": {"kernel": "gckpp::ros_kernel, plain arm", "achieved": achieved_plain_tf,
+                                          "frac": (achieved_plain_tf / (peak_gf / 1e3)) if peak_gf else None,
+                                          "kernel_ms": res["plain"]["kernel_ms"], "flops_per_launch": flops_plain}},
             "cpu_baseline": cpu,
             "clocks": head["clocks"],
         }

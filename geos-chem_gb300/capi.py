@@ -34,6 +34,7 @@ OPT_TIMING = 6
 OPT_LU = 7
 OPT_CELL_BLOCK = 8
 OPT_ASYNC = 9
+OPT_EVICT_AFTER = 10
 
 EXPORTED = [
     "gc_kpp_mechanism_dims",
@@ -127,7 +128,7 @@ class Solver:
             raise GcKppError(rc, self.lib.gc_kpp_last_error().decode())
 
     def set(self, arith=None, schedule=None, block=None, blocks_per_sm=None, max_slots=None, cell_block=None,
-            async_steps=None):
+            async_steps=None, evict_after=None):
         if arith is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1, "fast2": 2, "fast4": 3}[arith]))
         if schedule is not None:
@@ -140,6 +141,8 @@ class Solver:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_MAX_SLOTS, int(max_slots)))
         if cell_block is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_CELL_BLOCK, int(cell_block)))
+        if evict_after is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_EVICT_AFTER, int(evict_after)))
         if async_steps is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ASYNC, 1 if async_steps else 0))
 

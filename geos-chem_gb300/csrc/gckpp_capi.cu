@@ -114,6 +114,8 @@ struct gc_kpp_ctx {
   int lu_form = 0;  // 0 row-wise dot products, 1 KppDecomp right-looking order
   int async = 0;    // chemistry steps never synchronise the host (GC_KPP_OPT_ASYNC)
   int occ_arith = -1, occ_block = -1, occ_value = 1;  // cached occupancy query
+  int evict_after = 0;  // hand cells over to the block-per-cell kernel after this many steps
+  DevBuf evict_buf;     // ids of the handed-over cells
   DevBuf ranges;    // device queue ranges: [0,1] block-per-cell, [2,3] thread-per-cell, [4,5] retry
   // tolerance arrays validated by the last synchronous step (async steps reuse them)
   const void* tol_at = nullptr;
@@ -204,7 +206,7 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
   if (c->side) cudaStreamDestroy(c->side);
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
                     &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
-                    &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges};
+                    &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges, &c->evict_buf};
   for (DevBuf* b : bufs) b->release();
   delete c;
   return GC_KPP_OK;
@@ -234,6 +236,10 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
     case GC_KPP_OPT_LU:
       if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "lu form must be 0 or 1");
       c->lu_form = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_EVICT_AFTER:
+      if (v < 0 || v > 1000000) return fail(GC_KPP_EINVAL, "evict-after steps out of range");
+      c->evict_after = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_ASYNC:
       if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "async must be 0 or 1");
@@ -436,6 +442,15 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   p.ncell = (int)nthread;
   p.order = a.order ? a.order + nb : nullptr;
   p.qrange = dev_split ? ranges + 2 : a.qrange;
+  // hand-over of long-running cells (needs the status rows to carry their state)
+  const bool evict = c->evict_after > 0 && queue && c->arith <= 1 && c->lu_form == 0 && a.istatus && a.rstatus;
+  if (evict) {
+    GC_CUDA(c->evict_buf.ensure((size_t)std::max(a.ncell, 1) * sizeof(int)));
+    GC_CUDA(cudaMemsetAsync(ranges + 6, 0, 2 * sizeof(int), s));
+    p.evict_after = c->evict_after;
+    p.evict_list = (int*)c->evict_buf.p;
+    p.evict_count = ranges + 7;
+  }
   p.cell_limit = a.cell_limit > 0 ? a.cell_limit : a.ncell;
   p.queue_counter = (int*)c->counter.p;
   p.c_in = a.c_in;
@@ -500,6 +515,25 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     if (launches) *launches += 1;
   }
   if (nb > 0 || dev_split) GC_CUDA(cudaStreamWaitEvent(s, c->join, 0));
+  if (evict) {
+    // the handed-over cells continue block-per-cell from their saved state
+    RosParams pr = p;
+    pr.resume = 1;
+    pr.evict_after = 0;
+    pr.order = (const int*)c->evict_buf.p;
+    pr.qrange = ranges + 6;
+    pr.ncell = a.ncell;
+    pr.c_in = p.c_out;
+    pr.hstart = nullptr;
+    pr.queue_counter = (int*)c->counter.p + 1;
+    pr.ws = nullptr;
+    pr.nslot = 0;
+    GC_CUDA(cudaMemsetAsync(pr.queue_counter, 0, sizeof(int), s));
+    cudaError_t er = c->arith == 1 ? gckpp_launch_block_strict(c->nsm, c->cell_block, c->mech, R.meth, pr, s)
+                                   : gckpp_launch_block_fast(c->nsm, c->cell_block, c->mech, R.meth, pr, s);
+    if (er != cudaSuccess) return cuda_fail(er, "block-per-cell continuation launch");
+    if (launches) *launches += 1;
+  }
   if (timed) {
     GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed + 1], s));
     c->ntimed += 1;

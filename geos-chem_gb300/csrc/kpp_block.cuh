@@ -245,7 +245,12 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
       Y[i] = v;
       if (i >= nvar) Ynew[i] = v;
     }
-    if (tid == 0) ros.init_lane(sh.L, cell);
+    if (tid == 0) {
+      if (p.resume)
+        ros.load_lane(sh.L, cell);  // a cell handed over by the thread-per-cell kernel
+      else
+        ros.init_lane(sh.L, cell);
+    }
     __syncthreads();
     while (true) {
       // TimeLoop head

@@ -64,13 +64,22 @@ struct RosParams {
   double hmin, hmax, hstart_default, facmin, facmax, facrej, facsafe, roundoff;
   int autonomous, max_steps, clamp_negative;
   int lu_form;  // 0 decomp_rows, 1 decomp (KppDecomp order)
+  // hand-over of long-running cells to the block-per-cell kernel: a cell
+  // about to start step evict_after + 1 leaves its state (Y in c_out, T and H
+  // in RSTATUS(4:5), counters in ISTATUS(1:8)) and its id at
+  // evict_list[atomicAdd(evict_count, 1)]; the block kernel with resume = 1
+  // continues it from there with the same arithmetic
+  int evict_after;   // 0 = never
+  int* evict_list;
+  int* evict_count;
+  int resume;
   // workspace: per warp a tile of 32*NC cells x lay.total entries
   double* ws;
   WsLayout lay;
   long long nslot;
 };
 
-enum : int { PH_DONE = 0, PH_NEWSTEP = 1, PH_ATTEMPT = 2 };
+enum : int { PH_DONE = 0, PH_NEWSTEP = 1, PH_ATTEMPT = 2, PH_EVICTED = 3 };
 
 struct Lane {
   int cell;
@@ -109,6 +118,39 @@ struct Rosenbrock {
       y1[(nvar + f) * TSN] = v;
     }
     init_lane(L, cell);
+  }
+
+  // Hand a cell at a step boundary over to the block-per-cell kernel.
+  __device__ void evict_cell(double* w, int q, const Lane& L) {
+    const int nvar = m.nvar;
+    const double* y = arr(w, p.lay.y0, q);
+    const int cell = L.cell;
+    for (int i = 0; i < nvar; ++i) p.c_out[(long long)i * p.ldc + cell] = y[i * TSN];
+    if (p.c_out != p.c_in)
+      for (int f = 0; f < m.nfix; ++f)
+        p.c_out[(long long)(nvar + f) * p.ldc + cell] = p.c_in[(long long)(nvar + f) * p.ldc + cell];
+    save_lane(L);
+    p.evict_list[atomicAdd(p.evict_count, 1)] = cell;
+  }
+
+  // The scalar state of a cell at a step boundary, kept in its own status
+  // rows until the block kernel resumes it.
+  __device__ void save_lane(const Lane& L) const {
+    const int v[8] = {L.nfun, L.njac, L.nstp, L.nacc, L.nrej, L.ndec, L.nsol, L.nsng};
+    for (int k = 0; k < 8; ++k) p.istatus[(long long)k * p.ldo + L.cell] = v[k];
+    const double d[5] = {L.texit, L.hexit, L.hnew_out, L.T, L.H};
+    for (int k = 0; k < 5; ++k) p.rstatus[(long long)k * p.ldo + L.cell] = d[k];
+  }
+
+  __device__ void load_lane(Lane& L, int cell) const {
+    init_lane(L, cell);
+    int* v[8] = {&L.nfun, &L.njac, &L.nstp, &L.nacc, &L.nrej, &L.ndec, &L.nsol, &L.nsng};
+    for (int k = 0; k < 8; ++k) *v[k] = p.istatus[(long long)k * p.ldo + cell];
+    L.texit = p.rstatus[cell];
+    L.hexit = p.rstatus[p.ldo + cell];
+    L.hnew_out = p.rstatus[2 * p.ldo + cell];
+    L.T = p.rstatus[3 * p.ldo + cell];
+    L.H = p.rstatus[4 * p.ldo + cell];
   }
 
   // Per-cell scalar state at the start of the integration.
@@ -445,8 +487,11 @@ __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams
     bool any = false;
 #pragma unroll
     for (int q = 0; q < NC; ++q) {
-      if (has[q] && L[q].phase == PH_DONE) {
-        ros.store_cell(w, q, L[q]);
+      if (has[q] && (L[q].phase == PH_DONE || L[q].phase == PH_EVICTED)) {
+        if (L[q].phase == PH_DONE)
+          ros.store_cell(w, q, L[q]);
+        else
+          ros.evict_cell(w, q, L[q]);
         has[q] = false;
         if (QUEUE) {
           const long long idx = (long long)qlo + queue_claim(p.queue_counter);
@@ -467,6 +512,7 @@ __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams
     for (int q = 0; q < NC; ++q) {
       if (has[q] && L[q].phase == PH_NEWSTEP) {
         ros.step_checks(L[q]);
+        if (p.evict_after > 0 && L[q].phase == PH_NEWSTEP && L[q].nstp >= p.evict_after) L[q].phase = PH_EVICTED;
         need |= L[q].phase == PH_NEWSTEP;
       }
     }

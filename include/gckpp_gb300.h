@@ -56,6 +56,12 @@ extern "C" {
 #define GC_KPP_OPT_LU 7           /* 0 = row-wise LU (default), 1 = KppDecomp right-looking order */
 #define GC_KPP_OPT_CELL_BLOCK 8   /* threads of the block-per-cell kernel (multiple of 32, <= 1024),
                                      0 = default 256; 32 is one warp per cell */
+#define GC_KPP_OPT_EVICT_AFTER 10 /* > 0: a cell of the thread-per-cell queue that still runs after
+                                     this many steps is handed over, at a step boundary, to the
+                                     block-per-cell kernel, which finishes it with the same
+                                     arithmetic (same results); 0 = off (default).  Needs the queue
+                                     schedule, ARITH 0 or 1, the row-wise LU and ISTATUS/RSTATUS
+                                     arrays (the fullchem step always has them). */
 #define GC_KPP_OPT_ASYNC 9        /* 1 = chemistry steps never synchronise the host, so that a
                                      caller can capture them in a CUDA graph: the retry list and
                                      the block-per-cell count stay on the device, *nretry (and

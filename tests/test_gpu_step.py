@@ -303,3 +303,32 @@ def test_async_steps_capture_in_a_cuda_graph(step_case):
         for a, b in zip([x.cpu().numpy() for x in (c, hs, ist, rst, ierr)], ref):
             assert np.array_equal(a, b)
     solver.set(async_steps=False)
+
+
+@pytest.mark.parametrize("arith,evict_after", [("fast", 1), ("fast", 3), ("strict", 2)])
+def test_handover_to_block_per_cell_changes_nothing(solver, step_case, arith, evict_after):
+    """GC_KPP_OPT_EVICT_AFTER: cells still running after k steps finish in the
+    block-per-cell kernel from their saved state, with the results of an
+    uninterrupted integration (also combined with binned cells)."""
+    n = step_case["n"]
+    cells = step_case["cells"]
+
+    def run(evict, order=None, nblock=0):
+        solver.set(arith=arith, schedule="queue", block=64, cell_block=128, evict_after=evict)
+        c = cells["c"].copy()
+        hs = np.full(n, 20.0)
+        ist = np.zeros((20, n), np.int32)
+        rst = np.zeros((20, n))
+        ierr = np.zeros(n, np.int32)
+        solver.fullchem_step(600.0, cells["met"], cells["photol"], c, step_case["atol"], step_case["rtol"],
+                             step_case["icntrl"], step_case["rcntrl"], hs, ist, rst, ierr, order=order,
+                             nblock=nblock)
+        return [c, hs, ist, rst, ierr]
+
+    base = run(0)
+    assert base[2][2].max() > evict_after  # some cells are handed over
+    perm = np.random.default_rng(4).permutation(n).astype(np.int32)
+    for got in (run(evict_after), run(evict_after, perm, 16)):
+        for a, b in zip(got, base):
+            assert np.array_equal(a, b)
+    solver.set(evict_after=0, cell_block=0)
