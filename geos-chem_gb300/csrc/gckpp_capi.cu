@@ -36,6 +36,12 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+#define GC_TRY(call)            \
+  do {                          \
+    int _rc = (call);           \
+    if (_rc != GC_KPP_OK) return _rc; \
+  } while (0)
+
 int cuda_fail(cudaError_t e, const char* what) {
   return fail(e == cudaErrorMemoryAllocation ? GC_KPP_ENOMEM : GC_KPP_ECUDA,
               std::string(what) + ": " + cudaGetErrorString(e));
@@ -115,7 +121,10 @@ struct gc_kpp_ctx {
   int async = 0;    // chemistry steps never synchronise the host (GC_KPP_OPT_ASYNC)
   int occ_arith = -1, occ_block = -1, occ_value = 1;  // cached occupancy query
   int evict_after = 0;  // hand cells over to the block-per-cell kernel after this many steps
+  int evict_drained = 0;  // ... only once the queue has no unclaimed cell left
   DevBuf evict_buf;     // ids of the handed-over cells
+  DevBuf bws;           // Jac0 slots of the block-per-cell kernel, one per block of its grid
+  int bocc_key = -1, bocc_value = 1;  // cached occupancy of the block-per-cell kernel
   DevBuf ranges;    // device queue ranges: [0,1] block-per-cell, [2,3] thread-per-cell, [4,5] retry
   // tolerance arrays validated by the last synchronous step (async steps reuse them)
   const void* tol_at = nullptr;
@@ -206,7 +215,7 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
   if (c->side) cudaStreamDestroy(c->side);
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
                     &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
-                    &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges, &c->evict_buf};
+                    &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges, &c->evict_buf, &c->bws};
   for (DevBuf* b : bufs) b->release();
   delete c;
   return GC_KPP_OK;
@@ -240,6 +249,10 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
     case GC_KPP_OPT_EVICT_AFTER:
       if (v < 0 || v > 1000000) return fail(GC_KPP_EINVAL, "evict-after steps out of range");
       c->evict_after = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_EVICT_DRAINED:
+      if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "evict-drained must be 0 or 1");
+      c->evict_drained = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_ASYNC:
       if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "async must be 0 or 1");
@@ -380,6 +393,29 @@ int variant_cells_per_thread(int arith) {
   }
 }
 
+// Grid of the block-per-cell kernel (resident blocks per SM x SMs, at most
+// `want` if positive) and its Jac0 slots.
+int block_grid(gc_kpp_ctx* c, const Resolved& R, int autonomous, long long want, int* grid, double** ws) {
+  const size_t smem = c->arith == 1 ? gckpp_block_smem_strict(c->mech, R.meth, autonomous)
+                                    : gckpp_block_smem_fast(c->mech, R.meth, autonomous);
+  const int key = (int)smem + (c->arith << 18) + ((c->cell_block / 32) << 20);  // smem < 2^18 bytes
+  if (c->bocc_key != key) {
+    int occ = 0;
+    cudaError_t e = c->arith == 1 ? gckpp_block_occupancy_strict(c->cell_block, smem, &occ)
+                                  : gckpp_block_occupancy_fast(c->cell_block, smem, &occ);
+    if (e != cudaSuccess) return cuda_fail(e, "block-per-cell occupancy");
+    if (occ < 1) return fail(GC_KPP_EUNSUPPORTED, "block-per-cell kernel does not fit an SM");
+    c->bocc_key = key;
+    c->bocc_value = occ;
+  }
+  long long g = (long long)c->nsm * c->bocc_value;
+  if (want > 0 && want < g) g = want;
+  *grid = (int)g;
+  GC_CUDA(c->bws.ensure((size_t)g * T::LU_NONZERO * sizeof(double)));
+  *ws = (double*)c->bws.p;
+  return GC_KPP_OK;
+}
+
 // Launch the Rosenbrock kernel over device arrays.  A thread holds `nc`
 // cells, so a block covers block*nc workspace slots.
 int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, const DevArgs& a, cudaStream_t s,
@@ -448,6 +484,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     GC_CUDA(c->evict_buf.ensure((size_t)std::max(a.ncell, 1) * sizeof(int)));
     GC_CUDA(cudaMemsetAsync(ranges + 6, 0, 2 * sizeof(int), s));
     p.evict_after = c->evict_after;
+    p.evict_drained = c->evict_drained;
     p.evict_list = (int*)c->evict_buf.p;
     p.evict_count = ranges + 7;
   }
@@ -500,9 +537,9 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     pb.order = a.order;
     pb.qrange = dev_split ? ranges : nullptr;
     pb.queue_counter = (int*)c->counter.p + 1;
-    pb.ws = nullptr;
     pb.nslot = 0;
-    const int bgrid = dev_split ? c->nsm : std::min(nb, c->nsm);
+    int bgrid = 0;
+    GC_TRY(block_grid(c, R, p.autonomous, dev_split ? 0 : nb, &bgrid, &pb.ws));
     cudaError_t eb = c->arith == 1 ? gckpp_launch_block_strict(bgrid, c->cell_block, c->mech, R.meth, pb, c->side)
                                    : gckpp_launch_block_fast(bgrid, c->cell_block, c->mech, R.meth, pb, c->side);
     if (eb != cudaSuccess) return cuda_fail(eb, "block-per-cell kernel launch");
@@ -526,11 +563,12 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     pr.c_in = p.c_out;
     pr.hstart = nullptr;
     pr.queue_counter = (int*)c->counter.p + 1;
-    pr.ws = nullptr;
     pr.nslot = 0;
+    int rgrid = 0;
+    GC_TRY(block_grid(c, R, p.autonomous, 0, &rgrid, &pr.ws));
     GC_CUDA(cudaMemsetAsync(pr.queue_counter, 0, sizeof(int), s));
-    cudaError_t er = c->arith == 1 ? gckpp_launch_block_strict(c->nsm, c->cell_block, c->mech, R.meth, pr, s)
-                                   : gckpp_launch_block_fast(c->nsm, c->cell_block, c->mech, R.meth, pr, s);
+    cudaError_t er = c->arith == 1 ? gckpp_launch_block_strict(rgrid, c->cell_block, c->mech, R.meth, pr, s)
+                                   : gckpp_launch_block_fast(rgrid, c->cell_block, c->mech, R.meth, pr, s);
     if (er != cudaSuccess) return cuda_fail(er, "block-per-cell continuation launch");
     if (launches) *launches += 1;
   }
@@ -568,11 +606,6 @@ int stage_out(X* host, long long ld, const X* dev, size_t ncell, size_t rows, cu
   return GC_KPP_OK;
 }
 
-#define GC_TRY(call)            \
-  do {                          \
-    int _rc = (call);           \
-    if (_rc != GC_KPP_OK) return _rc; \
-  } while (0)
 
 }  // namespace
 

@@ -53,15 +53,14 @@ __global__ void __launch_bounds__(1024) ros_block_kernel(MechDev m, RosMethod r,
   ros_block_driver<STRICT>(m, r, p);
 }
 
-size_t GCKPP_CAT(gckpp_block_smem_, GCKPP_VARIANT)(const MechDev& m) {
-  return sizeof(double) * (size_t)block_layout(m.naux, m.nspec, m.nvar, m.nreact, m.nb, m.lu_nonzero).total;
+size_t GCKPP_CAT(gckpp_block_smem_, GCKPP_VARIANT)(const MechDev& m, const RosMethod& r, int autonomous) {
+  return sizeof(double) *
+         (size_t)block_layout(m.naux, m.nspec, m.nvar, m.nreact, m.nb, m.lu_nonzero, r.S, autonomous).total;
 }
 
-cudaError_t GCKPP_CAT(gckpp_launch_block_, GCKPP_VARIANT)(int grid, int block, const MechDev& m, const RosMethod& r,
-                                                          const RosParams& p, cudaStream_t s) {
-  if (block < 32 || block > 1024 || block % 32) return cudaErrorInvalidConfiguration;
-  const size_t smem = GCKPP_CAT(gckpp_block_smem_, GCKPP_VARIANT)(m);
-  static int smem_set[64] = {};  // set once per device (the size is fixed by the mechanism)
+// resident blocks per SM of the block-per-cell kernel
+cudaError_t GCKPP_CAT(gckpp_block_occupancy_, GCKPP_VARIANT)(int block, size_t smem, int* nblocks) {
+  static int smem_set[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -71,6 +70,17 @@ cudaError_t GCKPP_CAT(gckpp_launch_block_, GCKPP_VARIANT)(int grid, int block, c
     if (e != cudaSuccess) return e;
     if (dev >= 0 && dev < 64) smem_set[dev] = (int)smem;
   }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_block_kernel<GCKPP_STRICT != 0>, block, smem);
+}
+
+cudaError_t GCKPP_CAT(gckpp_launch_block_, GCKPP_VARIANT)(int grid, int block, const MechDev& m, const RosMethod& r,
+                                                          const RosParams& p, cudaStream_t s) {
+  if (block < 32 || block > 1024 || block % 32) return cudaErrorInvalidConfiguration;
+  const size_t smem = GCKPP_CAT(gckpp_block_smem_, GCKPP_VARIANT)(m, r, p.autonomous);
+  int nblk = 0;  // also sets the shared-memory attribute
+  cudaError_t e = GCKPP_CAT(gckpp_block_occupancy_, GCKPP_VARIANT)(block, smem, &nblk);
+  if (e != cudaSuccess) return e;
+  if (nblk < 1) return cudaErrorInvalidConfiguration;
   ros_block_kernel<GCKPP_STRICT != 0><<<grid, block, smem, s>>>(m, r, p);
   return cudaGetLastError();
 }

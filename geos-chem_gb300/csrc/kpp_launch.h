@@ -25,6 +25,8 @@ cudaError_t gckpp_launch_block_strict(int grid, int block, const MechDev& m, con
                                       cudaStream_t s);
 cudaError_t gckpp_launch_block_fast(int grid, int block, const MechDev& m, const RosMethod& r, const RosParams& p,
                                     cudaStream_t s);
-size_t gckpp_block_smem_strict(const MechDev& m);
-size_t gckpp_block_smem_fast(const MechDev& m);
+size_t gckpp_block_smem_strict(const MechDev& m, const RosMethod& r, int autonomous);
+size_t gckpp_block_smem_fast(const MechDev& m, const RosMethod& r, int autonomous);
+cudaError_t gckpp_block_occupancy_strict(int block, size_t smem, int* nblocks);
+cudaError_t gckpp_block_occupancy_fast(int block, size_t smem, int* nblocks);
 }  // namespace gckpp

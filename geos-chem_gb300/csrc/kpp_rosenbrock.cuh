@@ -70,6 +70,7 @@ struct RosParams {
   // evict_list[atomicAdd(evict_count, 1)]; the block kernel with resume = 1
   // continues it from there with the same arithmetic
   int evict_after;   // 0 = never
+  int evict_drained; // 1: only once the queue has no unclaimed cell left
   int* evict_list;
   int* evict_count;
   int resume;
@@ -512,7 +513,9 @@ __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams
     for (int q = 0; q < NC; ++q) {
       if (has[q] && L[q].phase == PH_NEWSTEP) {
         ros.step_checks(L[q]);
-        if (p.evict_after > 0 && L[q].phase == PH_NEWSTEP && L[q].nstp >= p.evict_after) L[q].phase = PH_EVICTED;
+        if (p.evict_after > 0 && L[q].phase == PH_NEWSTEP && L[q].nstp >= p.evict_after &&
+            (!p.evict_drained || (long long)qlo + *(volatile int*)p.queue_counter >= qhi))
+          L[q].phase = PH_EVICTED;
         need |= L[q].phase == PH_NEWSTEP;
       }
     }

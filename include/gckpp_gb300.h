@@ -62,6 +62,9 @@ extern "C" {
                                      arithmetic (same results); 0 = off (default).  Needs the queue
                                      schedule, ARITH 0 or 1, the row-wise LU and ISTATUS/RSTATUS
                                      arrays (the fullchem step always has them). */
+#define GC_KPP_OPT_EVICT_DRAINED 11 /* 1 = hand a cell over only once the work queue has no
+                                       unclaimed cell left (the tail of the launch); 0 = as soon
+                                       as it has taken GC_KPP_OPT_EVICT_AFTER steps (default) */
 #define GC_KPP_OPT_ASYNC 9        /* 1 = chemistry steps never synchronise the host, so that a
                                      caller can capture them in a CUDA graph: the retry list and
                                      the block-per-cell count stay on the device, *nretry (and

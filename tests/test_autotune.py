@@ -1,0 +1,29 @@
+"""The autotuner's candidates all give the default configuration's results
+bit for bit, and it returns the fastest one it timed."""
+import numpy as np
+import pytest
+
+
+@pytest.mark.gpu
+def test_autotune_small_grid():
+    import torch
+    import gcchem.autotune as autotune
+    import gcchem.capi as capi
+    import gcchem.inputs as inputs
+
+    cells = inputs.grid_cells(20, 10, 12, seed=5)
+    dev = torch.device("cuda", 0)
+    T = lambda a: torch.tensor(a, device=dev).contiguous()
+    n = cells["c"].shape[1]
+    atol, rtol = inputs.tolerances()
+    ic, rc = inputs.default_controls()
+    case = {"met": T(cells["met"]), "ph": T(cells["photol"]), "c": T(cells["c"]), "at": T(atol), "rt": T(rtol),
+            "ic": ic, "rc": rc, "dt": 600.0, "ist": torch.zeros((20, n), dtype=torch.int32, device=dev),
+            "rst": torch.zeros((20, n), dtype=torch.float64, device=dev),
+            "ierr": torch.zeros(n, dtype=torch.int32, device=dev)}
+    solver = capi.Solver(0, arith="fast", schedule="queue")
+    axes = {"block": [64, 128], "arith": ["fast", "fast2"], "cell_block": [128], "evict_after": [0, 3]}
+    best, t, table = autotune.tune(solver, case, torch.zeros(n, dtype=torch.float64, device=dev), sweeps=1,
+                                   reps=1, axes=axes)
+    assert all(best[k] in axes[k] for k in axes)
+    assert len(table) >= 4 and np.isclose(table[0]["ms"], t * 1e3)

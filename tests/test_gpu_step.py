@@ -305,8 +305,9 @@ def test_async_steps_capture_in_a_cuda_graph(step_case):
     solver.set(async_steps=False)
 
 
-@pytest.mark.parametrize("arith,evict_after", [("fast", 1), ("fast", 3), ("strict", 2)])
-def test_handover_to_block_per_cell_changes_nothing(solver, step_case, arith, evict_after):
+@pytest.mark.parametrize("arith,evict_after,drained", [("fast", 1, 0), ("fast", 3, 0), ("strict", 2, 0),
+                                                       ("fast", 2, 1)])
+def test_handover_to_block_per_cell_changes_nothing(solver, step_case, arith, evict_after, drained):
     """GC_KPP_OPT_EVICT_AFTER: cells still running after k steps finish in the
     block-per-cell kernel from their saved state, with the results of an
     uninterrupted integration (also combined with binned cells)."""
@@ -314,7 +315,8 @@ def test_handover_to_block_per_cell_changes_nothing(solver, step_case, arith, ev
     cells = step_case["cells"]
 
     def run(evict, order=None, nblock=0):
-        solver.set(arith=arith, schedule="queue", block=64, cell_block=128, evict_after=evict)
+        solver.set(arith=arith, schedule="queue", block=64, cell_block=128, evict_after=evict,
+                   evict_drained=drained)
         c = cells["c"].copy()
         hs = np.full(n, 20.0)
         ist = np.zeros((20, n), np.int32)
@@ -331,4 +333,4 @@ def test_handover_to_block_per_cell_changes_nothing(solver, step_case, arith, ev
     for got in (run(evict_after), run(evict_after, perm, 16)):
         for a, b in zip(got, base):
             assert np.array_equal(a, b)
-    solver.set(evict_after=0, cell_block=0)
+    solver.set(evict_after=0, evict_drained=0, cell_block=0)

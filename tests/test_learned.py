@@ -188,3 +188,52 @@ def test_learned_step_c_abi_matches_python_plan():
         for a, b in zip(got, ref):
             assert np.array_equal(a, b)
     cp.close()
+
+
+@pytest.mark.gpu
+def test_learned_steps_capture_in_a_cuda_graph():
+    """Two learned chemistry steps (plan + binned step + hand-over) captured in
+    one CUDA graph give the results of two synchronous learned steps."""
+    import torch
+    import gcchem.capi as capi
+    import gcchem.inputs as inputs
+    import gcchem.learned as learned
+
+    prop = learned.Proposer(0)
+    prop.load_state(dict(np.load(learned.WEIGHTS)))
+    cp = learned.CProposer(prop)
+    solver = capi.Solver(0, arith="fast", schedule="queue", block=64)
+    solver.set(evict_after=2, cell_block=128)
+    cells = inputs.grid_cells(20, 10, 16, seed=6)
+    n = cells["c"].shape[1]
+    atol, rtol = inputs.tolerances()
+    ic, rc = inputs.default_controls()
+    dev = prop.dev
+    T = lambda a: torch.tensor(a, device=dev).contiguous()
+    met, ph, c0, at, rt = T(cells["met"]), T(cells["photol"]), T(cells["c"]), T(atol), T(rtol)
+    z = lambda *s, dt=torch.float64: torch.zeros(s, dtype=dt, device=dev)
+    c, hs, ist, rst, ierr = c0.clone(), z(n), z(20, n, dt=torch.int32), z(20, n), z(n, dt=torch.int32)
+
+    def steps(stream=None):
+        for _ in range(2):
+            solver.fullchem_step_learned(cp.handle, 600.0, met, ph, c, at, rt, ic, rc, hs, ist, rst, ierr,
+                                         stream=stream)
+
+    steps()
+    torch.cuda.synchronize()
+    ref = [x.cpu().numpy() for x in (c, hs, ist, rst, ierr)]
+    solver.set(async_steps=True)
+    c.copy_(c0)
+    hs.zero_()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g):
+        steps(stream=torch.cuda.current_stream().cuda_stream)
+    c.copy_(c0)
+    hs.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    for a, b in zip([x.cpu().numpy() for x in (c, hs, ist, rst, ierr)], ref):
+        assert np.array_equal(a, b)
+    solver.set(async_steps=False, evict_after=0)
+    cp.close()
