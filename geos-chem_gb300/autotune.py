@@ -52,7 +52,7 @@ def tune(solver, case, hs0, order=None, nblock=0, sweeps=2, reps=2, axes=None, l
     import torch
 
     axes = axes or AXES
-    best = dict(DEFAULTS)
+    best = {k: (DEFAULTS[k] if DEFAULTS[k] in axes[k] else axes[k][0]) for k in DEFAULTS}
     _, ref = time_step(solver, best, case, hs0, order, nblock)
     seen = {}
 

@@ -20,6 +20,7 @@
 #include "kpp_rates.h"
 #include "kpp_launch.h"
 #include "kpp_util.h"
+#include "kpp_block.cuh"
 #include "kpp_rosenbrock.cuh"
 #include "ros_methods.h"
 
@@ -349,6 +350,7 @@ struct DevArgs {
   int nblock;        // the first nblock cells of order run block-per-cell
   const int* nblock_dev;  // or: that count in device memory (no host synchronisation)
   const int* qrange;      // or: device {begin, end} of the order positions to integrate
+  int block_only;         // every cell of the range block-per-cell (no queue kernel)
   const double* c_in;
   double* c_out;
   long long ldc;
@@ -411,7 +413,9 @@ int block_grid(gc_kpp_ctx* c, const Resolved& R, int autonomous, long long want,
   long long g = (long long)c->nsm * c->bocc_value;
   if (want > 0 && want < g) g = want;
   *grid = (int)g;
-  GC_CUDA(c->bws.ensure((size_t)g * T::LU_NONZERO * sizeof(double)));
+  const BlockLayout bl = block_layout(T::NAUX, T::NSPEC, T::NVAR, T::NREACT, T::NB, T::LU_NONZERO, R.meth.S,
+                                      autonomous);
+  GC_CUDA(c->bws.ensure((size_t)g * bl.slot * sizeof(double)));
   *ws = (double*)c->bws.p;
   return GC_KPP_OK;
 }
@@ -545,6 +549,25 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     if (eb != cudaSuccess) return cuda_fail(eb, "block-per-cell kernel launch");
     GC_CUDA(cudaEventRecord(c->join, c->side));
     if (launches) *launches += 1;
+  }
+  if (a.block_only) {
+    if (c->arith > 1 || c->lu_form != 0 || !a.qrange)
+      return fail(GC_KPP_EINVAL, "block-only launches need a device range, ARITH 0 or 1 and the row-wise LU");
+    RosParams pb = p;
+    pb.queue_counter = (int*)c->counter.p + 1;
+    pb.evict_after = 0;
+    pb.nslot = 0;
+    int bgrid = 0;
+    GC_TRY(block_grid(c, R, p.autonomous, 0, &bgrid, &pb.ws));
+    cudaError_t eb = c->arith == 1 ? gckpp_launch_block_strict(bgrid, c->cell_block, c->mech, R.meth, pb, s)
+                                   : gckpp_launch_block_fast(bgrid, c->cell_block, c->mech, R.meth, pb, s);
+    if (eb != cudaSuccess) return cuda_fail(eb, "block-per-cell kernel launch");
+    if (launches) *launches += 1;
+    if (timed) {
+      GC_CUDA(cudaEventRecord(c->ev[2 * c->ntimed + 1], s));
+      c->ntimed += 1;
+    }
+    return GC_KPP_OK;
   }
   if (nthread > 0) {
     cudaError_t e = variant_launch(c->arith, queue, grid, block, c->mech, R.meth, p, s);
@@ -783,6 +806,7 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
       b.qrange = ranges + 4;
       b.nblock = 0;
       b.nblock_dev = nullptr;
+      b.block_only = (c->arith <= 1 && c->lu_form == 0) ? 1 : 0;  // retries are few: latency form
       b.cell_limit = ncell;
       b.c_in = dcb;
       b.hstart = nullptr;
@@ -809,7 +833,9 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
       b.ncell = (int)failed.size();
       b.order = dord;
       b.cell_limit = ncell;
-      b.nblock = 0;
+      // a few cells integrate faster one per block than on the queue kernel
+      b.nblock = (c->arith <= 1 && c->lu_form == 0 && (long long)failed.size() <= 4LL * c->nsm)
+                     ? (int)failed.size() : 0;
       b.nblock_dev = nullptr;
       b.qrange = nullptr;
       b.c_in = dcb;

@@ -1,7 +1,8 @@
 // Block-per-cell Rosenbrock: all threads of one block integrate one cell,
 // whose working set (rates, Y, stage vectors, A/B products and the LU
-// factors, about 96 KB for Rodas3) sits in shared memory; Jac0, read once per
-// decomposition, stays in a per-block global slot (L2-resident).  Two cells
+// factors, about 71 KB for Rodas3) sits in shared memory; Jac0, the rate
+// constants and the A/B products, which are read in parallel loops off the
+// critical path, stay in a per-block global slot (L2-resident).  Three cells
 // fit on an SM.
 //
 // This is the latency form of the solver, for the few stiff cells that need
@@ -25,25 +26,29 @@ namespace gckpp {
 // Shared-memory layout of one cell (offsets in doubles) for a method with
 // `stages` stages; dFdT only for non-autonomous problems.
 struct BlockLayout {
-  int aux, y0, y1, fcn0, fcn, dfdt, k, a, b, g, e, total;
+  int y0, y1, fcn0, fcn, dfdt, k, g, e, total;  // shared memory
+  int j0, aux, a, b, slot;                      // global slot of the block
 };
 
 __host__ __device__ inline BlockLayout block_layout(int naux, int nspec, int nvar, int nreact, int nb, int lunz,
                                                     int stages, int autonomous) {
   BlockLayout l{};
   int o = 0;
-  l.aux = o; o += naux;
   l.y0 = o; o += nspec;
   l.y1 = o; o += nspec;
   l.fcn0 = o; o += nvar;
   l.fcn = o; o += nvar;
   l.dfdt = o; o += autonomous ? 0 : nvar;
   l.k = o; o += stages * nvar;
-  l.a = o; o += nreact;
-  l.b = o; o += nb;
   l.g = o; o += lunz;
   l.e = o; o += nvar;
   l.total = o;
+  o = 0;
+  l.j0 = o; o += lunz;
+  l.aux = o; o += naux;
+  l.a = o; o += nreact;
+  l.b = o; o += nb;
+  l.slot = o;
   return l;
 }
 
@@ -203,23 +208,24 @@ struct BlockShared {
 
 // One block integrates cells order[0..ncell) (or 0..ncell) taken from a
 // per-launch queue (p.queue_counter), one at a time.  Dynamic shared memory:
-// block_layout(...).total doubles; p.ws holds LU_NONZERO doubles (Jac0) per
-// block of the grid.
+// block_layout(...).total doubles; p.ws holds block_layout(...).slot doubles
+// per block of the grid.
 template <bool STRICT>
 __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const RosParams& p) {
   extern __shared__ double sm[];
   __shared__ BlockShared sh;
   const BlockLayout lay = block_layout(m.naux, m.nspec, m.nvar, m.nreact, m.nb, m.lu_nonzero, r.S, p.autonomous);
-  double* aux = sm + lay.aux;
+  double* slot = p.ws + (long long)blockIdx.x * lay.slot;
+  double* aux = slot + lay.aux;
   double* Y = sm + lay.y0;
   double* Ynew = sm + lay.y1;
   double* F0 = sm + lay.fcn0;
   double* F = sm + lay.fcn;
   double* dfdt = sm + lay.dfdt;
   double* K = sm + lay.k;
-  double* A = sm + lay.a;
-  double* B = sm + lay.b;
-  double* J0 = p.ws + (long long)blockIdx.x * m.lu_nonzero;
+  double* A = slot + lay.a;
+  double* B = slot + lay.b;
+  double* J0 = slot + lay.j0;
   double* G = sm + lay.g;
   double* E = sm + lay.e;
   const int nvar = m.nvar;
