@@ -169,6 +169,15 @@ int gc_kpp_ctx_create(gc_kpp_ctx** out, int device) {
     return cuda_fail(e, "cudaGetDeviceProperties");
   }
   c->nsm = prop.multiProcessorCount;
+  // side stream and events of block-per-cell launches, made here so that no
+  // later call (possibly inside a stream capture) has to create them
+  e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    gc_kpp_ctx_destroy(c);
+    return cuda_fail(e, "stream/event creation");
+  }
   MechDev& m = c->mech;
   m.nvar = T::NVAR; m.nfix = T::NFIX; m.nreact = T::NREACT; m.nspec = T::NSPEC;
   m.lu_nonzero = T::LU_NONZERO; m.nb = T::NB; m.lit0 = T::LIT0;
@@ -724,6 +733,13 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
   }
   const size_t n = (size_t)ncell, ntol = R.vector_tol ? T::NVAR : 1;
   GC_CUDA(c->ord_buf.ensure(n * sizeof(int)));  // retry list, sized before any capture
+  if (c->arith <= 1 && c->lu_form == 0 && !R.code) {
+    // the block-per-cell kernel's attributes and slots (asynchronous retries
+    // use it), set up by synchronous calls so that a capture never allocates
+    int g = 0;
+    double* w = nullptr;
+    GC_TRY(block_grid(c, R, R.autonomous, 0, &g, &w));
+  }
   const double *dmet, *dph, *dat, *drt;
   double *dc, *dhs = nullptr, *drs;
   int *dis, *die;
