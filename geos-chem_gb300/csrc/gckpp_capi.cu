@@ -450,7 +450,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   if (dev_split && (!a.order || nb != 0)) return fail(GC_KPP_EINVAL, "device block-per-cell count needs an order");
   // with counts on the device, size for every cell; the kernels read the ranges
   const long long nthread = (dev_split || a.qrange) ? (long long)a.ncell : (long long)a.ncell - nb;
-  long long nslot;
+  long long nslot, ws_slots = 0;
   int grid;
   if (queue) {
     int per_sm = c->blocks_per_sm;
@@ -470,13 +470,20 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     if (c->max_slots > 0 && (long long)grid * per_block > c->max_slots)
       grid = (int)std::max(1LL, c->max_slots / per_block);
     nslot = (long long)grid * per_block;
+    // the workspace is sized for every cell of the call on the queue kernel,
+    // whatever share goes block-per-cell, so that an asynchronous call of the
+    // same batch (possibly inside a capture) never has to grow it
+    long long all = std::min<long long>((long long)c->nsm * per_sm,
+                                        std::max(1LL, ((long long)a.ncell + per_block - 1) / per_block));
+    if (c->max_slots > 0 && all * per_block > c->max_slots) all = std::max(1LL, c->max_slots / per_block);
+    ws_slots = std::max(nslot, all * per_block);
   } else {
     grid = (int)std::max(1LL, (nthread + per_block - 1) / per_block);
     nslot = (long long)grid * per_block;
     if (c->max_slots > 0 && nslot > c->max_slots)
       return fail(GC_KPP_EINVAL, "plain schedule needs one workspace slot per cell; raise MAX_SLOTS or use the queue");
   }
-  const size_t ws_bytes = (size_t)nslot * (size_t)c->lay.total * sizeof(double);
+  const size_t ws_bytes = (size_t)std::max(nslot, ws_slots) * (size_t)c->lay.total * sizeof(double);
   GC_CUDA(c->ws.ensure(ws_bytes));
   GC_CUDA(c->counter.ensure(2 * sizeof(int)));
   GC_CUDA(cudaMemsetAsync(c->counter.p, 0, 2 * sizeof(int), s));
