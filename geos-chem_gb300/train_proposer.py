@@ -22,6 +22,8 @@ def main(argv=None):
     ap.add_argument("--grid", default="72x46x72", help="NLONxNLATxNLEV of the training grids")
     ap.add_argument("--train-seeds", default="11,12,13", help="grid seeds used for training")
     ap.add_argument("--test-seed", type=int, default=14, help="held-out grid seed")
+    ap.add_argument("--extra-grid", default=None, help="a second grid (e.g. 144x91x72, NOx-seeded) for more rows")
+    ap.add_argument("--extra-seeds", default="", help="seeds of the second grid")
     ap.add_argument("--nsteps", type=int, default=2, help="1200 s steps recorded per grid after spin-up")
     ap.add_argument("--spinup", type=float, default=86400.0)
     ap.add_argument("--epochs", type=int, default=6)
@@ -51,6 +53,13 @@ def main(argv=None):
             cells = inputs.grid_cells(nlon, nlat, nlev, seed=s, nox_boundary_layer=nox)
             parts.append(learned.collect(solver, prop, cells, nsteps=args.nsteps, spinup=args.spinup, log=log))
             log("seed %d nox %s collected (%.0f s)" % (s, nox, time.time() - t0))
+    if args.extra_grid:
+        elon, elat, elev = (int(v) for v in args.extra_grid.split("x"))
+        for s in (int(v) for v in args.extra_seeds.split(",") if v):
+            cells = inputs.grid_cells(elon, elat, elev, seed=s, nox_boundary_layer=True)
+            parts.append(learned.collect(solver, prop, cells, nsteps=args.nsteps, spinup=args.spinup, log=log))
+            del cells
+            log("extra grid seed %d collected (%.0f s)" % (s, time.time() - t0))
     data = {k: torch.cat([p[k] for p in parts]) for k in parts[0]}
     log("training rows: %d" % data["x"].shape[0])
     hist = learned.fit(prop, data, epochs=args.epochs, log=log)
@@ -64,6 +73,7 @@ def main(argv=None):
         with open(args.report, "w") as f:
             json.dump({"loss_history": hist, "held_out": score, "rows": int(data["x"].shape[0]),
                        "train_seeds": args.train_seeds, "test_seed": args.test_seed, "grid": args.grid,
+                       "extra_grid": args.extra_grid, "extra_seeds": args.extra_seeds,
                        "seconds": time.time() - t0}, f, indent=1)
 
 
