@@ -37,7 +37,7 @@ GRID = (72, 46, 72)
 DT = 1200.0
 SPINUP_S = 86400.0
 EVICT_LEARNED = 2  # hand-over after 2 steps in the learned arms (best of the sweep)
-WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "geos-chem_gb300", "weights", "proposer_4x5.npz")
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "geos-chem_gb300", "weights", "proposer_fullchem.npz")
 
 
 def parse():

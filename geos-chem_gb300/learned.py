@@ -26,7 +26,7 @@ import numpy as np
 from . import capi, inputs, mechanism
 
 NFEAT, HID, NOUT, NJ, NSPC, NBIN = 56, 128, 5, 20, 32, 4
-WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "proposer_4x5.npz")
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "proposer_fullchem.npz")
 BIN_EDGES = (2, 4, 16)  # Rosenbrock steps per chemistry step: 1 | 2-3 | 4-15 | >= 16
 
 J_SPECIES = ["NO2", "O3", "O3", "HNO2", "H2O2", "HNO3", "HNO4", "NO3", "NO3", "N2O5", "CH2O", "CH2O", "MP",

@@ -1,7 +1,7 @@
 """A small, self-contained chemistry case for profiling the kernels.
 
     python geos-chem_gb300/profile_case.py --cells 4096 --tout 60 --arith fast [--probe]
-    python geos-chem_gb300/profile_case.py --grid 72x46x8 --step --binned 64
+    python geos-chem_gb300/profile_case.py --grid 72x46x8 --binned 64
 
 Box cells (``inputs.box_cells``) are integrated once from 0 to TOUT with
 ``Solver.integrate``; ``--grid`` instead spins up a grid and runs one 1200 s
@@ -23,6 +23,7 @@ def main(argv=None):
     ap.add_argument("--arith", default="fast", choices=["fast", "strict", "fast2", "fast4"])
     ap.add_argument("--schedule", default="queue", choices=["plain", "queue"])
     ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--max-slots", type=int, default=0, help="cap on cells in flight (0: all resident threads)")
     ap.add_argument("--grid", default=None, help="NLONxNLATxNLEV: grid step instead of box cells")
     ap.add_argument("--binned", type=int, default=0, help="grid step: cells sent block-per-cell")
     ap.add_argument("--probe", action="store_true")
@@ -44,7 +45,7 @@ def main(argv=None):
 
     dev = torch.device("cuda", 0)
     T = lambda x: torch.tensor(x, device=dev).contiguous()
-    s = capi.Solver(0, arith=args.arith, schedule=args.schedule, block=args.block)
+    s = capi.Solver(0, arith=args.arith, schedule=args.schedule, block=args.block, max_slots=args.max_slots)
     atol, rtol = inputs.tolerances()
     ic, rc = inputs.default_controls()
     at, rt = T(atol), T(rtol)
