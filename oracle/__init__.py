@@ -2,8 +2,8 @@
 
 ctypes binding of the C restatement in this directory (kpp_oracle.c and the
 generated mechanism/rate code).  Imported only by the tests, by the smoke
-check and by the CPU-baseline leg of bench.py, always as the checker, never
-as the thing measured or shipped.
+check and by the CPU-baseline leg of bench.py, always to check or time
+against, never as the thing measured or shipped.
 
 Two builds of the same sources:
   "strict"  -O2 -ffp-contract=off  (reference arithmetic, parity oracle)

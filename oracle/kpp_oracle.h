@@ -2,8 +2,9 @@
  *
  * A plain-C restatement of the reference's per-cell integration
  * (KPP/fullchem/gckpp_Integrator.F90, gckpp_LinearAlgebra.F90) used only by
- * the tests, the smoke check and the CPU-baseline leg of the benchmark as the
- * checker.  It is never linked into, or called by, the product library.
+ * the tests, the smoke check and the CPU-baseline leg of the benchmark, to
+ * check or time against.  It is never linked into, or called by, the product
+ * library.
  */
 #ifndef KPP_ORACLE_H
 #define KPP_ORACLE_H

@@ -62,7 +62,7 @@ def test_integrate_matches_oracle(solver, case, arith):
     same = np.all(ist[:8] == ist_ref[:8], axis=0)
     big = np.abs(c_ref[:NVAR]) > 1e4
     rel = _rel(c[:NVAR], c_ref[:NVAR])
-    # tolerance of the spec parity bar: 1e-9 relative on species > 1e4 molec/cm3,
+    # the parity bar: 1e-9 relative on species > 1e4 molec/cm3,
     # on every cell whose step sequence matches the oracle's
     assert same.mean() >= 0.99, same.mean()
     assert np.max(np.where(big, rel, 0.0)[:, same]) < 1e-9
