@@ -1,9 +1,13 @@
-"""Build the CUDA library ``libgckpp_gb300.so`` in-tree for sm_103a.
+"""Build the CUDA libraries in-tree for sm_103a.
 
-Steps: lower the mechanism IR to device tables (``csrc/_gen``), compile the
-Rosenbrock kernels twice (strict: ``-fmad=false``; fast: default contraction),
-compile the C ABI, link a shared library into ``lib/``.  Translation units are
-compiled in parallel; nothing here needs CMake.
+Steps: lower each mechanism's IR (``mechanism/<name>.json``) to device tables
+(``csrc/_gen/<name>``), compile the Rosenbrock kernels once per arithmetic
+variant (strict: ``-fmad=false``; fast: default contraction; 1, 2 and 4 cells
+per thread), the rate, utility and MLP kernels once, the C ABI once per
+mechanism, and link ``lib/libgckpp_gb300.so`` (fullchem) and
+``lib/libgckpp_gb300_<name>.so`` (the other mechanisms).  The kernels are
+table-driven, so every mechanism shares them.  Translation units are compiled
+in parallel; nothing here needs CMake.
 """
 import os
 import shutil
@@ -30,8 +34,12 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
-def lib_path():
-    return os.path.join(LIBDIR, LIBNAME)
+MECHANISMS = ("fullchem", "Hg")  # KPP mechanisms with a library each (mechanism/<name>.json)
+
+
+def lib_path(mech="fullchem"):
+    """libgckpp_gb300.so (fullchem) or libgckpp_gb300_<mech>.so."""
+    return os.path.join(LIBDIR, LIBNAME if mech == "fullchem" else "libgckpp_gb300_%s.so" % mech)
 
 
 def _units():
@@ -45,7 +53,6 @@ def _units():
         (os.path.join(CSRC, "kpp_util.cu"), "kpp_util.o", []),
         (os.path.join(CSRC, "kpp_mlp.cu"), "kpp_mlp.o", []),
         (os.path.join(CSRC, "gckpp_mlp_capi.cu"), "gckpp_mlp_capi.o", []),
-        (os.path.join(CSRC, "gckpp_capi.cu"), "gckpp_capi.o", []),
         (os.path.join(CSRC, "gckpp_learned_capi.cu"), "gckpp_learned_capi.o", []),
     ]
 
@@ -60,18 +67,33 @@ def _stale(obj, deps):
 def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    tables.write_generated(GEN)
-    rates_program.write_generated(GEN)
+    from . import mechanism
+
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
-    deps += [os.path.join(GEN, f) for f in os.listdir(GEN)]
     deps += [os.path.join(PKG, "..", "include", f) for f in ("gckpp_gb300.h", "gckpp_gb300_mlp.h")]
+    units = list(_units())
+    # the mechanism enters only through the tables that gckpp_capi.cu uploads:
+    # one C ABI object (and library) per mechanism, every kernel object shared
+    mech_objs = {}
+    for mech in MECHANISMS:
+        gen = os.path.join(GEN, mech)
+        ir = mechanism.load_ir(mech)
+        tables.write_generated(gen, ir)
+        rates_program.write_generated(gen, ir)
+        obj = "gckpp_capi_%s.o" % mech
+        units.append((os.path.join(CSRC, "gckpp_capi.cu"), obj, ["-I", gen], [os.path.join(gen, f)
+                                                                          for f in os.listdir(gen)]))
+        mech_objs[mech] = obj
     exe = nvcc()
     procs = []
-    objs = []
-    for src, obj, extra in _units():
+    shared = []
+    for unit in units:
+        src, obj, extra = unit[:3]
+        extra_deps = unit[3] if len(unit) > 3 else []
         obj = os.path.join(BUILD, obj)
-        objs.append(obj)
-        if force or _stale(obj, deps):
+        if os.path.basename(obj) not in mech_objs.values():
+            shared.append(obj)
+        if force or _stale(obj, deps + extra_deps):
             cmd = [exe] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
             if verbose:
                 print(" ".join(cmd), flush=True)
@@ -82,12 +104,18 @@ def build(verbose=False, force=False):
             raise RuntimeError("nvcc failed: %s\n%s" % (" ".join(cmd), out.decode()))
         if verbose and out:
             print(out.decode())
+    links = []
+    for mech, obj in mech_objs.items():
+        lib = lib_path(mech)
+        objs = shared + [os.path.join(BUILD, obj)]
+        if force or procs or not os.path.exists(lib):
+            cmd = [exe] + ARCH + ["-shared", "-cudart", "shared", "-o", lib] + objs
+            links.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    for cmd, p in links:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), out.decode()))
     lib = lib_path()
-    if force or procs or not os.path.exists(lib):
-        cmd = [exe] + ARCH + ["-shared", "-cudart", "shared", "-o", lib] + objs
-        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
-        if r.returncode != 0:
-            raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), r.stdout.decode()))
     probe = probe_path()
     src = os.path.join(CSRC, "fp64_probe.cu")
     if force or not os.path.exists(probe) or os.path.getmtime(src) > os.path.getmtime(probe):

@@ -56,7 +56,7 @@ EXPORTED = [
     "gc_kpp_last_kernel_ms",
 ]
 
-_lib = None
+_libs = {}
 
 
 class GcKppError(RuntimeError):
@@ -65,12 +65,12 @@ class GcKppError(RuntimeError):
         self.code = code
 
 
-def load_library(path=None):
-    """Load libgckpp_gb300.so (raises OSError if it has not been built)."""
-    global _lib
-    if _lib is not None and path is None:
-        return _lib
-    path = path or _build.lib_path()
+def load_library(path=None, mech="fullchem"):
+    """Load the library of a mechanism, libgckpp_gb300.so for fullchem
+    (raises OSError if it has not been built)."""
+    if path is None and mech in _libs:
+        return _libs[mech]
+    path = path or _build.lib_path(mech)
     if not os.path.exists(path):
         raise OSError("CUDA library %s is not built; run gcchem.build.build()" % path)
     lib = ctypes.CDLL(path)
@@ -83,13 +83,13 @@ def load_library(path=None):
     lib.gc_kpp_integrate_batch.argtypes = [vp, i32, f64, f64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64,
                                            vp, i32, vp]
     lib.gc_kpp_update_rconst_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, vp, i64, i32, vp]
-    if path == _build.lib_path():
-        _lib = lib
+    if path == _build.lib_path(mech):
+        _libs[mech] = lib
     return lib
 
 
-def dims():
-    lib = load_library()
+def dims(mech="fullchem"):
+    lib = load_library(mech=mech)
     out = [ctypes.c_int() for _ in range(5)]
     lib.gc_kpp_mechanism_dims(*[ctypes.byref(o) for o in out])
     return dict(zip(["nspec", "nvar", "nfix", "nreact", "lu_nonzero"], [o.value for o in out]))
@@ -118,8 +118,10 @@ def _ld(x, ncell):
 class Solver:
     """A solver context on one CUDA device (gc_kpp_ctx)."""
 
-    def __init__(self, device=0, arith="fast", schedule="plain", block=0, blocks_per_sm=0, max_slots=0):
-        self.lib = load_library()
+    def __init__(self, device=0, arith="fast", schedule="plain", block=0, blocks_per_sm=0, max_slots=0,
+                 mech="fullchem"):
+        self.lib = load_library(mech=mech)
+        self.mech = mech
         self.ctx = ctypes.c_void_p()
         self._check(self.lib.gc_kpp_ctx_create(ctypes.byref(self.ctx), device))
         self.set(arith=arith, schedule=schedule, block=block, blocks_per_sm=blocks_per_sm, max_slots=max_slots)

@@ -15,8 +15,8 @@
 #include <vector>
 
 #include "../../include/gckpp_gb300.h"
-#include "_gen/mech_tables.inc"
-#include "_gen/rates_program.inc"
+#include "mech_tables.inc"  // generated per mechanism (csrc/_gen/<mechanism>/)
+#include "rates_program.inc"
 #include "kpp_rates.h"
 #include "kpp_launch.h"
 #include "kpp_util.h"

@@ -80,7 +80,8 @@ def _fill_concentrations(rng, ir, numden, n):
     c = _log_uniform(rng, 1e2, 1e12, (d["nspec"], n))
     fixed = {"O2": 0.2095, "N2": 0.7808, "H2": 5.0e-7}
     for name, frac in fixed.items():
-        c[sp.index(name)] = frac * numden
+        if name in sp:
+            c[sp.index(name)] = frac * numden
     for fam in ir["families"]:
         c[sp.index(fam)] = 0.0
     return c

@@ -32,11 +32,11 @@ import os
 import re
 import sys
 
-KPP = os.path.join("KPP", "fullchem")
+MECH = ["fullchem"]  # the KPP mechanism directory being read (KPP/<mech>)
 
 
 def _read(root, name):
-    with open(os.path.join(root, KPP, name)) as fh:
+    with open(os.path.join(root, "KPP", MECH[0], name)) as fh:
         return fh.read()
 
 
@@ -206,12 +206,21 @@ def parse_fun(root, dims):
             A[idx - 1] = _product(rhs)
             _check(rhs, _render_product(A[idx - 1]), "A(%d)" % idx)
         elif name == "P_VAR":
-            P[idx - 1] = _coef_ref_terms(rhs, "A")
-            _check(rhs, _render_coef_ref(P[idx - 1], "A"), "P_VAR(%d)" % idx)
+            P[idx - 1] = [] if rhs.strip() == "0" else _coef_ref_terms(rhs, "A")
+            if P[idx - 1]:
+                _check(rhs, _render_coef_ref(P[idx - 1], "A"), "P_VAR(%d)" % idx)
         else:
-            D[idx - 1] = _prod_terms(rhs)
-            _check(rhs, _render_prod_terms(D[idx - 1]), "D_VAR(%d)" % idx)
-    assert all(x is not None for x in A + P + D)
+            D[idx - 1] = [] if rhs.strip() == "0" else _prod_terms(rhs)
+            if D[idx - 1]:
+                _check(rhs, _render_prod_terms(D[idx - 1]), "D_VAR(%d)" % idx)
+    assert all(x is not None for x in P + D)
+    # KPP leaves out A(r) of reactions that change no variable species; such
+    # a rate is never referenced, and is kept as an empty product
+    used = {t[2] for terms in P for t in terms}
+    for r, a in enumerate(A):
+        if a is None:
+            assert r not in used, "A(%d) referenced but not computed" % (r + 1)
+            A[r] = []
     assert "Vdot = P_VAR - D_VAR*V" in body
     return {"A": A, "P": P, "D": D}
 
@@ -354,7 +363,9 @@ def parse_families(root):
     """Prod/loss family dummy species (KPP/fullchem/fullchem.kpp:13-20); their
     concentrations are zeroed before each integration
     (GeosCore/fullchem_mod.F90:943-946)."""
-    txt = _read(root, "fullchem.kpp")
+    txt = _read(root, MECH[0] + ".kpp")
+    if "#FAMILIES" not in txt:
+        return []
     block = txt.split("#FAMILIES", 1)[1].split("#INLINE", 1)[0]
     return re.findall(r"^\s*(\w+)\s*:", block, re.M)
 
@@ -378,10 +389,11 @@ def parse_tolerances(root, species):
     return {"atol_default": 1.0e-2, "rtol_default": 0.5e-2, "atol": atol, "rtol": rtol}
 
 
-def extract(root):
+def extract(root, mech="fullchem"):
+    MECH[0] = mech
     dims, species = parse_parameters(root)
     ir = {
-        "mechanism": "fullchem",
+        "mechanism": mech,
         "generator": "KPP-3.2.0",
         "dims": dims,
         "species": species,
@@ -399,8 +411,9 @@ def extract(root):
 
 def main(argv):
     root = argv[1]
-    out = argv[2] if len(argv) > 2 else os.path.join(os.path.dirname(os.path.abspath(__file__)), "fullchem.json")
-    ir = extract(root)
+    mech = argv[3] if len(argv) > 3 else "fullchem"
+    out = argv[2] if len(argv) > 2 else os.path.join(os.path.dirname(os.path.abspath(__file__)), mech + ".json")
+    ir = extract(root, mech)
     with open(out, "w") as fh:
         json.dump(ir, fh, separators=(",", ":"))
         fh.write("\n")

@@ -2,11 +2,12 @@
 
     python geos-chem_gb300/profile_case.py --cells 4096 --tout 60 --arith fast [--probe]
     python geos-chem_gb300/profile_case.py --grid 72x46x8 --binned 64
+    python geos-chem_gb300/profile_case.py --grid 72x46x24 --learned
 
 Box cells (``inputs.box_cells``) are integrated once from 0 to TOUT with
 ``Solver.integrate``; ``--grid`` instead spins up a grid and runs one 1200 s
 chemistry step (``--binned N``: the N cells with the most steps go
-block-per-cell).  It prints the ISTATUS sums and the algorithmic FP64
+block-per-cell; ``--learned``: the learned form from a cold start).  It prints the ISTATUS sums and the algorithmic FP64
 operations of the reference routines for them; ``--probe`` also runs the FP64
 throughput probe.  Meant to run under ncu on one GPU with few launches.
 """
@@ -26,6 +27,8 @@ def main(argv=None):
     ap.add_argument("--max-slots", type=int, default=0, help="cap on cells in flight (0: all resident threads)")
     ap.add_argument("--grid", default=None, help="NLONxNLATxNLEV: grid step instead of box cells")
     ap.add_argument("--binned", type=int, default=0, help="grid step: cells sent block-per-cell")
+    ap.add_argument("--learned", action="store_true",
+                    help="grid step: the learned form (cold start, H0 proposals, bins, hand-over after 2 steps)")
     ap.add_argument("--probe", action="store_true")
     args = ap.parse_args(argv)
 
@@ -63,7 +66,16 @@ def main(argv=None):
         hs = torch.zeros(n, dtype=torch.float64, device=dev)
         s.fullchem_step(86400.0, met, ph, c, at, rt, ic, rc, hs, ist, rst, ierr)
         order, nb = None, 0
-        if args.binned:
+        if args.learned:
+            import gcchem.learned as learned
+
+            prop = learned.Proposer(0)
+            prop.load_state(dict(np.load(learned.WEIGHTS)))
+            hs.zero_()
+            _, _, order = learned.plan(prop, met, ph, c, hstart=hs, hmax=1200.0)
+            nb = int(prop.last_counts[learned.NBIN - 1].item())
+            s.set(evict_after=2)
+        elif args.binned:
             s.fullchem_step(1200.0, met, ph, c.clone(), at, rt, ic, rc, hs.clone(), ist, rst, ierr)
             order = torch.argsort(ist[2], descending=True, stable=True).int()
             nb = args.binned

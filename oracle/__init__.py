@@ -18,21 +18,28 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 _libs = {}
 
 
-def build(verbose=False):
+def _builder():
     import importlib.util
 
     spec = importlib.util.spec_from_file_location("_oracle_build", os.path.join(HERE, "build_oracle.py"))
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
-    return mod.build(verbose=verbose)
+    return mod
 
 
-def load(variant="strict"):
-    if variant in _libs:
-        return _libs[variant]
-    path = os.path.join(HERE, "_build", "liboracle_%s.so" % variant)
+def build(verbose=False):
+    return _builder().build(verbose=verbose)
+
+
+def load(variant="strict", mech="fullchem"):
+    """The oracle library of one mechanism (KPP/<mech>) and arithmetic variant."""
+    key = (mech, variant)
+    if key in _libs:
+        return _libs[key]
+    b = _builder()
+    path = b.lib_path(variant, mech)
     if not os.path.exists(path):
-        build()
+        b.build(mechs=(mech,))
     lib = ctypes.CDLL(path)
     vp, i32, i64, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
     lib.oracle_integrate_batch.argtypes = [i32, f64, f64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64, vp, i32]
@@ -43,8 +50,15 @@ def load(variant="strict"):
     lib.oracle_kpp_decomp.argtypes = [vp]
     lib.oracle_kpp_decomp.restype = i32
     lib.oracle_max_threads.restype = i32
-    _libs[variant] = lib
+    _libs[key] = lib
     return lib
+
+
+def _dims(mech):
+    import json
+
+    with open(os.path.join(HERE, "..", "geos-chem_gb300", "mechanism", mech + ".json")) as fh:
+        return json.load(fh)["dims"]
 
 
 def _p(a):
@@ -56,10 +70,10 @@ def _c(a, dt):
 
 
 def integrate(c, rconst, atol, rtol, tin, tout, icntrl=None, rcntrl=None, hstart=None, variant="strict",
-              nthreads=0):
+              nthreads=0, mech="fullchem"):
     """Batched INTEGRATE on the CPU.  c [NSPEC, n] (copied), rconst [NREACT, n].
     Returns (c_out, istatus [20, n], rstatus [20, n], ierr [n])."""
-    lib = load(variant)
+    lib = load(variant, mech)
     c = np.array(c, dtype=np.float64, order="C", copy=True)
     rconst = _c(rconst, np.float64)
     n = c.shape[1]
@@ -75,43 +89,44 @@ def integrate(c, rconst, atol, rtol, tin, tout, icntrl=None, rcntrl=None, hstart
     return c, ist, rst, ierr
 
 
-def update_rconst(met, photol, c, variant="strict"):
-    lib = load(variant)
+def update_rconst(met, photol, c, variant="strict", mech="fullchem"):
+    lib = load(variant, mech)
     met = _c(met, np.float64)
     photol = _c(photol, np.float64)
     c = _c(c, np.float64)
     n = met.shape[1]
-    nreact = 1058
+    nreact = _dims(mech)["nreact"]
     out = np.zeros((nreact, n), np.float64)
     lib.oracle_update_rconst_batch(n, _p(met), n, _p(photol), n, _p(c), n, _p(out), n)
     return out
 
 
-def fun_split(v, f, rct):
-    lib = load("strict")
+def fun_split(v, f, rct, mech="fullchem"):
+    lib = load("strict", mech)
     v, f, rct = _c(v, np.float64), _c(f, np.float64), _c(rct, np.float64)
     out = np.zeros_like(v)
     lib.oracle_fun_split(_p(v), _p(f), _p(rct), _p(out))
     return out
 
 
-def jac_sp(v, f, rct, lu_nonzero=5683):
-    lib = load("strict")
+def jac_sp(v, f, rct, lu_nonzero=None, mech="fullchem"):
+    lib = load("strict", mech)
+    lu_nonzero = lu_nonzero or _dims(mech)["lu_nonzero"]
     v, f, rct = _c(v, np.float64), _c(f, np.float64), _c(rct, np.float64)
     out = np.zeros(lu_nonzero, np.float64)
     lib.oracle_jac_sp(_p(v), _p(f), _p(rct), _p(out))
     return out
 
 
-def decomp(jvs):
-    lib = load("strict")
+def decomp(jvs, mech="fullchem"):
+    lib = load("strict", mech)
     jvs = np.array(jvs, dtype=np.float64, copy=True)
     ier = lib.oracle_kpp_decomp(_p(jvs))
     return jvs, ier
 
 
-def solve(jvs, x):
-    lib = load("strict")
+def solve(jvs, x, mech="fullchem"):
+    lib = load("strict", mech)
     jvs = _c(jvs, np.float64)
     x = np.array(x, dtype=np.float64, copy=True)
     lib.oracle_kpp_solve(_p(jvs), _p(x))

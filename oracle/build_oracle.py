@@ -21,33 +21,46 @@ VARIANTS = {
 }
 
 
-def lib_path(variant="strict"):
-    return os.path.join(BUILD, "liboracle_%s.so" % variant)
+MECHANISMS = ("fullchem", "Hg")
 
 
-def build(verbose=False):
+def lib_path(variant="strict", mech="fullchem"):
+    name = "liboracle_%s.so" % variant if mech == "fullchem" else "liboracle_%s_%s.so" % (mech, variant)
+    return os.path.join(BUILD, name)
+
+
+def build(verbose=False, mechs=MECHANISMS):
     sys.path.insert(0, HERE)
     import gen_oracle  # noqa: E402
 
-    gen_oracle.write(GEN)
     os.makedirs(BUILD, exist_ok=True)
-    srcs = [os.path.join(HERE, "kpp_oracle.c"), os.path.join(GEN, "kpp_mech_oracle.c"),
-            os.path.join(GEN, "kpp_rates_oracle.c")]
-    deps = srcs + [os.path.join(HERE, f) for f in ("kpp_oracle.h", "rate_laws.h")] + [os.path.join(GEN, "kpp_dims.h")]
     procs = []
-    for variant, flags in VARIANTS.items():
-        out = lib_path(variant)
-        if os.path.exists(out) and all(os.path.getmtime(d) <= os.path.getmtime(out) for d in deps):
-            continue
-        cmd = ["gcc", "-shared", "-fPIC", "-fopenmp", "-std=gnu11", "-I", HERE] + flags + srcs + ["-o", out, "-lm"]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    for mech in mechs:
+        gen = os.path.join(GEN, mech)
+        gen_oracle.write(gen, mech)
+        procs += _compile(gen, mech, verbose)
     for cmd, p in procs:
         out, _ = p.communicate()
         if p.returncode != 0:
             raise RuntimeError("oracle build failed: %s\n%s" % (" ".join(cmd), out.decode()))
-    return {v: lib_path(v) for v in VARIANTS}
+    return {(m, v): lib_path(v, m) for m in mechs for v in VARIANTS}
+
+
+def _compile(gen, mech, verbose):
+    srcs = [os.path.join(HERE, "kpp_oracle.c"), os.path.join(gen, "kpp_mech_oracle.c"),
+            os.path.join(gen, "kpp_rates_oracle.c")]
+    deps = srcs + [os.path.join(HERE, f) for f in ("kpp_oracle.h", "rate_laws.h")] + [os.path.join(gen, "kpp_dims.h")]
+    procs = []
+    for variant, flags in VARIANTS.items():
+        out = lib_path(variant, mech)
+        if os.path.exists(out) and all(os.path.getmtime(d) <= os.path.getmtime(out) for d in deps):
+            continue
+        cmd = ["gcc", "-shared", "-fPIC", "-fopenmp", "-std=gnu11", "-I", HERE, "-I", gen] + flags + srcs + \
+            ["-o", out, "-lm"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    return procs
 
 
 if __name__ == "__main__":

@@ -24,7 +24,12 @@ import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-IR_PATH = os.path.join(HERE, "..", "geos-chem_gb300", "mechanism", "fullchem.json")
+MECH_DIR = os.path.join(HERE, "..", "geos-chem_gb300", "mechanism")
+
+
+def _ir(mech):
+    with open(os.path.join(MECH_DIR, mech + ".json")) as fh:
+        return json.load(fh)
 
 
 def _lit(tok):
@@ -40,7 +45,8 @@ def _fac(tok):
 
 
 def _prod(toks):
-    return "*".join(_fac(t) for t in toks)
+    # an empty product is a reaction KPP leaves uncomputed (never referenced)
+    return "*".join(_fac(t) for t in toks) if toks else "0.0"
 
 
 def _signed(terms, render):
@@ -107,9 +113,8 @@ def generate(ir):
                                  "nspec": d["nspec"], "nfix": d["nfix"]}
 
 
-def write(outdir):
-    with open(IR_PATH) as fh:
-        ir = json.load(fh)
+def write(outdir, mech="fullchem"):
+    ir = _ir(mech)
     text, dims = generate(ir)
     os.makedirs(outdir, exist_ok=True)
     path = os.path.join(outdir, "kpp_mech_oracle.c")
@@ -123,7 +128,7 @@ def write(outdir):
     if old != htxt:
         with open(hdr, "w") as fh:
             fh.write(htxt)
-    write_rates(outdir)
+    write_rates(outdir, mech)
     return path
 
 
@@ -203,10 +208,8 @@ def generate_rates(ir):
     return "\n".join(L) + "\n", sorted(het)
 
 
-def write_rates(outdir):
-    with open(IR_PATH) as fh:
-        ir = json.load(fh)
-    text, het = generate_rates(ir)
+def write_rates(outdir, mech="fullchem"):
+    text, het = generate_rates(_ir(mech))
     path = os.path.join(outdir, "kpp_rates_oracle.c")
     old = open(path).read() if os.path.exists(path) else None
     if old != text:
@@ -216,4 +219,5 @@ def write_rates(outdir):
 
 
 if __name__ == "__main__":
-    print(write(sys.argv[1] if len(sys.argv) > 1 else os.path.join(HERE, "_gen")))
+    mech = sys.argv[2] if len(sys.argv) > 2 else "fullchem"
+    print(write(sys.argv[1] if len(sys.argv) > 1 else os.path.join(HERE, "_gen", mech), mech))

@@ -8,7 +8,7 @@
  */
 #ifndef KPP_ORACLE_H
 #define KPP_ORACLE_H
-#include "_gen/kpp_dims.h"
+#include "kpp_dims.h" /* generated per mechanism (oracle/_gen/<mechanism>/) */
 
 extern const int ORACLE_LU_CROW[];
 extern const int ORACLE_LU_DIAG[];

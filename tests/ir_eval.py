@@ -21,6 +21,8 @@ def _val(tok, V, F, RCT, lit=float):
 
 
 def _prod(toks, V, F, RCT):
+    if not toks:  # a rate KPP leaves uncomputed (never referenced)
+        return 0.0
     acc = _val(toks[0], V, F, RCT)
     for t in toks[1:]:
         acc = acc * _val(t, V, F, RCT)
