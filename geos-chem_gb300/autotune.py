@@ -5,12 +5,16 @@ each candidate of
 
 * threads per block of the thread-per-cell queue kernel (32, 64, 128, 256),
 * cells per thread (the layout: 1 or 2 cells per thread share a table walk),
-* threads per block of the block-per-cell kernel (128, 256; 32 = warp per cell),
+* the block-per-cell form (split sums, or the level form with 128 or 256
+  threads per block; 32 = warp per cell),
 * the hand-over point k (steps after which a cell moves to the block kernel),
 
 one axis at a time from the defaults (coordinate descent, two sweeps), and
-returns the fastest settings.  Every candidate gives bit-identical results
-(the schedule never changes a cell's arithmetic), which `tune` checks.  The
+returns the fastest settings.  Candidates without the split form give
+bit-identical results (the schedule never changes a cell's arithmetic); the
+split form regroups sums, so its candidates must agree to rounding (same IERR,
+1e-8 relative on species above 1e4 molec/cm3 for 99 % of the cells); `tune`
+checks both.  The
 queue hands out one cell per lane through warp-aggregated claims: its "chunk"
 is a warp of 32 cells and is not a tuning axis.
 
@@ -26,9 +30,10 @@ AXES = {
     "block": [32, 64, 128, 256],
     "arith": ["fast", "fast2"],
     "cell_block": [128, 256],
+    "block_split": [True, False],
     "evict_after": [0, 2, 4, 8, 16],
 }
-DEFAULTS = {"block": 128, "arith": "fast", "cell_block": 256, "evict_after": 0}
+DEFAULTS = {"block": 128, "arith": "fast", "cell_block": 256, "block_split": True, "evict_after": 0}
 
 
 def time_step(solver, cfg, case, hs0, order=None, nblock=0):
@@ -36,7 +41,7 @@ def time_step(solver, cfg, case, hs0, order=None, nblock=0):
     import torch
 
     solver.set(arith=cfg["arith"], schedule="queue", block=cfg["block"], cell_block=cfg["cell_block"],
-               evict_after=cfg["evict_after"])
+               evict_after=cfg["evict_after"], block_split=cfg.get("block_split", True))
     c = case["c"].clone()
     hs = hs0.clone()
     torch.cuda.synchronize()
@@ -44,15 +49,31 @@ def time_step(solver, cfg, case, hs0, order=None, nblock=0):
     solver.fullchem_step(case["dt"], case["met"], case["ph"], c, case["at"], case["rt"], case["ic"], case["rc"],
                          hs, case["ist"], case["rst"], case["ierr"], order=order, nblock=nblock)
     torch.cuda.synchronize()
-    return time.perf_counter() - t, c
+    return time.perf_counter() - t, (c, case["ierr"].clone())
+
+
+def _agrees(cfg, got, ref, nvar):
+    """Bit for bit, or (split block-per-cell form) to rounding."""
+    import torch
+
+    if torch.equal(got[0], ref[0]) and torch.equal(got[1], ref[1]):
+        return True
+    if not cfg.get("block_split", True) or not torch.equal(got[1], ref[1]):
+        return False
+    a, b = got[0][:nvar], ref[0][:nvar]
+    rel = torch.where(b.abs() > 1e4, (a - b).abs() / b.abs().clamp_min(1e-300), torch.zeros_like(b))
+    return (rel.max(dim=0).values <= 1e-8).double().mean().item() >= 0.99
 
 
 def tune(solver, case, hs0, order=None, nblock=0, sweeps=2, reps=2, axes=None, log=None):
     """Coordinate descent over the axes; returns (best config, seconds, table)."""
     import torch
 
+    import gcchem.capi as capi
+
     axes = axes or AXES
-    best = {k: (DEFAULTS[k] if DEFAULTS[k] in axes[k] else axes[k][0]) for k in DEFAULTS}
+    best = {k: (DEFAULTS[k] if k not in axes or DEFAULTS[k] in axes[k] else axes[k][0]) for k in DEFAULTS}
+    nvar = capi.dims(getattr(solver, "mech", "fullchem"))["nvar"]
     _, ref = time_step(solver, best, case, hs0, order, nblock)
     seen = {}
 
@@ -62,7 +83,7 @@ def tune(solver, case, hs0, order=None, nblock=0, sweeps=2, reps=2, axes=None, l
             ts = []
             for _ in range(reps):
                 t, c = time_step(solver, cfg, case, hs0, order, nblock)
-                if not torch.equal(c, ref):
+                if not _agrees(cfg, c, ref, nvar):
                     raise RuntimeError("configuration %s changed the results" % key)
                 ts.append(t)
             seen[key] = min(ts)

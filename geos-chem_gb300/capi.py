@@ -36,6 +36,7 @@ OPT_CELL_BLOCK = 8
 OPT_ASYNC = 9
 OPT_EVICT_AFTER = 10
 OPT_EVICT_DRAINED = 11
+OPT_BLOCK_SPLIT = 12
 
 EXPORTED = [
     "gc_kpp_mechanism_dims",
@@ -131,7 +132,7 @@ class Solver:
             raise GcKppError(rc, self.lib.gc_kpp_last_error().decode())
 
     def set(self, arith=None, schedule=None, block=None, blocks_per_sm=None, max_slots=None, cell_block=None,
-            async_steps=None, evict_after=None, evict_drained=None):
+            async_steps=None, evict_after=None, evict_drained=None, block_split=None):
         if arith is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1, "fast2": 2, "fast4": 3}[arith]))
         if schedule is not None:
@@ -150,6 +151,8 @@ class Solver:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_EVICT_DRAINED, 1 if evict_drained else 0))
         if async_steps is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ASYNC, 1 if async_steps else 0))
+        if block_split is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_BLOCK_SPLIT, 1 if block_split else 0))
 
     def close(self):
         if self.ctx:

@@ -137,6 +137,7 @@ struct gc_kpp_ctx {
   int schedule = 0;  // 0 plain, 1 queue
   int block = 128;
   int cell_block = 256;  // threads of the block-per-cell kernel
+  int block_split = 1;   // fast arithmetic: the split block-per-cell form
   cudaStream_t side = nullptr;  // block-per-cell launches run beside the queue kernel
   cudaEvent_t fork = nullptr, join = nullptr;
   int blocks_per_sm = 0;
@@ -198,6 +199,17 @@ int gc_kpp_ctx_create(gc_kpp_ctx** out, int device) {
   UP(bs_lvl_row, bs_lvl_row) UP(fun_rows_by_len, fun_rows_by_len) UP(jac_by_len, jac_by_len)
   m.lu_nlvl = T::LU_NLVL; m.fs_nlvl = T::FS_NLVL; m.bs_nlvl = T::BS_NLVL;
 #undef UP
+#define UPSPLIT(ph, name, NAME)                                                                                \
+  e = upload(reinterpret_cast<const uint4*>(T::split_##name##_task), sizeof(T::split_##name##_task) / 16,    \
+             &m.sp_task[ph], c->owned);                                                                      \
+  if (e == cudaSuccess)                                                                                      \
+    e = upload(T::split_##name##_pass, sizeof(T::split_##name##_pass) / 4, &m.sp_pass[ph], c->owned);        \
+  if (e != cudaSuccess) { gc_kpp_ctx_destroy(c); return cuda_fail(e, "upload split schedule " #name); }      \
+  m.sp_npass[ph] = T::SPLIT_##NAME##_NPASS;                                                                   \
+  m.sp_nt[ph] = T::SPLIT_##NAME##_NT;
+  UPSPLIT(gckpp::SP_LU, lu, LU) UPSPLIT(gckpp::SP_FS, fs, FS) UPSPLIT(gckpp::SP_BS, bs, BS)
+  UPSPLIT(gckpp::SP_FUN, fun, FUN) UPSPLIT(gckpp::SP_JAC, jac, JAC)
+#undef UPSPLIT
   gcrates::RatesDev& rp = c->rates;
   rp.nreact = T::NREACT;
   rp.nmet = RT::NMET;
@@ -276,6 +288,10 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
       if (v < 32 || v > 1024 || v % 32)
         return fail(GC_KPP_EINVAL, "block-per-cell threads must be a multiple of 32 in [32,1024]");
       c->cell_block = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_BLOCK_SPLIT:
+      if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "block-split must be 0 or 1");
+      c->block_split = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_MAX_SLOTS:
       if (v < 0) return fail(GC_KPP_EINVAL, "max slots must be >= 0");
@@ -409,10 +425,13 @@ int variant_cells_per_thread(int arith) {
 int block_grid(gc_kpp_ctx* c, const Resolved& R, int autonomous, long long want, int* grid, double** ws) {
   const size_t smem = c->arith == 1 ? gckpp_block_smem_strict(c->mech, R.meth, autonomous)
                                     : gckpp_block_smem_fast(c->mech, R.meth, autonomous);
-  const int key = (int)smem + (c->arith << 18) + ((c->cell_block / 32) << 20);  // smem < 2^18 bytes
+  const bool split = c->arith != 1 && c->block_split;
+  // smem < 2^18 bytes, arith < 4, cell_block / 32 <= 32
+  const int key = (int)smem + (c->arith << 18) + ((c->cell_block / 32) << 20) + ((split ? 1 : 0) << 26);
   if (c->bocc_key != key) {
     int occ = 0;
     cudaError_t e = c->arith == 1 ? gckpp_block_occupancy_strict(c->cell_block, smem, &occ)
+                    : split       ? gckpp_block_occupancy_split(smem, &occ)
                                   : gckpp_block_occupancy_fast(c->cell_block, smem, &occ);
     if (e != cudaSuccess) return cuda_fail(e, "block-per-cell occupancy");
     if (occ < 1) return fail(GC_KPP_EUNSUPPORTED, "block-per-cell kernel does not fit an SM");
@@ -427,6 +446,13 @@ int block_grid(gc_kpp_ctx* c, const Resolved& R, int autonomous, long long want,
   GC_CUDA(c->bws.ensure((size_t)g * bl.slot * sizeof(double)));
   *ws = (double*)c->bws.p;
   return GC_KPP_OK;
+}
+
+// Launch of the block-per-cell kernel of the context's arithmetic.
+cudaError_t launch_block(gc_kpp_ctx* c, int grid, const Resolved& R, const RosParams& p, cudaStream_t s) {
+  if (c->arith == 1) return gckpp_launch_block_strict(grid, c->cell_block, c->mech, R.meth, p, s);
+  if (c->block_split) return gckpp_launch_block_split(grid, c->mech, R.meth, p, s);
+  return gckpp_launch_block_fast(grid, c->cell_block, c->mech, R.meth, p, s);
 }
 
 // Launch the Rosenbrock kernel over device arrays.  A thread holds `nc`
@@ -560,8 +586,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     pb.nslot = 0;
     int bgrid = 0;
     GC_TRY(block_grid(c, R, p.autonomous, dev_split ? 0 : nb, &bgrid, &pb.ws));
-    cudaError_t eb = c->arith == 1 ? gckpp_launch_block_strict(bgrid, c->cell_block, c->mech, R.meth, pb, c->side)
-                                   : gckpp_launch_block_fast(bgrid, c->cell_block, c->mech, R.meth, pb, c->side);
+    cudaError_t eb = launch_block(c, bgrid, R, pb, c->side);
     if (eb != cudaSuccess) return cuda_fail(eb, "block-per-cell kernel launch");
     GC_CUDA(cudaEventRecord(c->join, c->side));
     if (launches) *launches += 1;
@@ -575,8 +600,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     pb.nslot = 0;
     int bgrid = 0;
     GC_TRY(block_grid(c, R, p.autonomous, 0, &bgrid, &pb.ws));
-    cudaError_t eb = c->arith == 1 ? gckpp_launch_block_strict(bgrid, c->cell_block, c->mech, R.meth, pb, s)
-                                   : gckpp_launch_block_fast(bgrid, c->cell_block, c->mech, R.meth, pb, s);
+    cudaError_t eb = launch_block(c, bgrid, R, pb, s);
     if (eb != cudaSuccess) return cuda_fail(eb, "block-per-cell kernel launch");
     if (launches) *launches += 1;
     if (timed) {
@@ -606,8 +630,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     int rgrid = 0;
     GC_TRY(block_grid(c, R, p.autonomous, 0, &rgrid, &pr.ws));
     GC_CUDA(cudaMemsetAsync(pr.queue_counter, 0, sizeof(int), s));
-    cudaError_t er = c->arith == 1 ? gckpp_launch_block_strict(rgrid, c->cell_block, c->mech, R.meth, pr, s)
-                                   : gckpp_launch_block_fast(rgrid, c->cell_block, c->mech, R.meth, pr, s);
+    cudaError_t er = launch_block(c, rgrid, R, pr, s);
     if (er != cudaSuccess) return cuda_fail(er, "block-per-cell continuation launch");
     if (launches) *launches += 1;
   }

@@ -200,18 +200,206 @@ __device__ void bk_solve(const MechDev& m, const double* G, double* X) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Split form (fast arithmetic only).  The level-by-level form above keeps
+// each sum in one thread, so one long LU dot product or substitution row
+// (up to ~260 terms) sets a level's time.  Here every sum is cut into chunks
+// of at most SPLIT_MAXCH terms, summed by the lanes of an aligned segment of
+// one warp and combined by a shuffle butterfly; the static pass schedule
+// (tables.py _split_schedules) says which chunk each lane takes in each pass.
+// The next pass's task word and term indices are loaded before the current
+// pass computes, so the table reads overlap the arithmetic.  The sums are
+// regrouped, so the split form agrees with the thread-per-cell form to
+// rounding, not bit for bit.
+constexpr int SPLIT_MAXCH = 16;
+
+// Each phase is a functor: terms(item) is the term array of the item,
+// pre(item, z) a value loaded together with the task of the next pass (it
+// may only depend on data that the phase does not change), base(item, z,
+// pre) the starting value of the sum, term(...) one multiply-add, and
+// finish(item, z, v) stores the item.  z is the task's third word.
+//
+// LU entry e of Ghimj = -Jac0 + diag(ghinv) (J0 holds -JVS), L entries times
+// the reciprocal pivot (z = its position), the diagonal stored inverted
+// (z = SPLIT_DIAG), U entries as they are (z = SPLIT_UPPER).
+constexpr unsigned SPLIT_DIAG = 0xffffffffu, SPLIT_UPPER = 0xfffffffeu;
+
+struct SplitLu {
+  const MechDev& m;
+  const double* J0;
+  double ghinv;
+  double* G;
+  __device__ const unsigned* terms(int) const { return m.dot_term; }
+  __device__ double pre(int e, unsigned) const { return J0[e]; }
+  __device__ double base(int, unsigned z, double j) const { return z == SPLIT_DIAG ? j + ghinv : j; }
+  __device__ double term(int, int, unsigned w, double acc) const { return fma(-G[w >> 16], G[w & 0xffffu], acc); }
+  __device__ void finish(int e, unsigned z, double v) const {
+    if (z == SPLIT_DIAG)
+      v = 1.0 / v;
+    else if (z != SPLIT_UPPER)
+      v = v * G[z];
+    G[e] = v;
+  }
+};
+
+// Substitution row i: X(i) - sum G(kk) X(icol(kk)); BACK multiplies by the
+// stored reciprocal pivot G(z).  The term index kk is the position in G.
+template <bool BACK>
+struct SplitSolve {
+  const MechDev& m;
+  const double* G;
+  double* X;
+  __device__ const unsigned* terms(int) const { return reinterpret_cast<const unsigned*>(m.lu_icol); }
+  __device__ double pre(int, unsigned) const { return 0.0; }
+  __device__ double base(int i, unsigned, double) const { return X[i]; }
+  __device__ double term(int, int kk, unsigned w, double acc) const { return fma(-G[kk], X[w], acc); }
+  __device__ void finish(int i, unsigned z, double v) const { X[i] = BACK ? v * G[z] : v; }
+};
+
+// Fun_SPLIT sums: items [0, NVAR) are P_VAR rows over A (into Vdot), items
+// [NVAR, 2 NVAR) D_VAR rows over B (into D).
+struct SplitFun {
+  const MechDev& m;
+  const double* A;
+  const double* B;
+  double* Vdot;
+  double* D;
+  __device__ const unsigned* terms(int item) const { return item < m.nvar ? m.p_sterm : m.d_sterm; }
+  __device__ double pre(int, unsigned) const { return 0.0; }
+  __device__ double base(int, unsigned, double) const { return 0.0; }
+  __device__ double term(int item, int, unsigned w, double acc) const {
+    const double* X = item < m.nvar ? A : B;
+    return fma(__ldg(m.slit + (w >> 20)), X[w & 0xfffffu], acc);
+  }
+  __device__ void finish(int item, unsigned, double v) const {
+    if (item < m.nvar)
+      Vdot[item] = v;
+    else
+      D[item - m.nvar] = v;
+  }
+};
+
+// Jac_SP entries, stored negated (-JVS) as the fast form keeps them.
+struct SplitJac {
+  const MechDev& m;
+  const double* B;
+  double* J;
+  __device__ const unsigned* terms(int) const { return m.j_sterm; }
+  __device__ double pre(int, unsigned) const { return 0.0; }
+  __device__ double base(int, unsigned, double) const { return 0.0; }
+  __device__ double term(int, int, unsigned w, double acc) const {
+    return fma(-__ldg(m.slit + (w >> 20)), B[w & 0xfffffu], acc);
+  }
+  __device__ void finish(int e, unsigned, double v) const { J[e] = v; }
+};
+
+// Task of one lane in one pass: x = item | seglog << 16 | nterms << 19,
+// y = first term, z = the phase's finish word; item 0xFFFF is an idle lane.
+struct SplitTask {
+  uint4 t;
+  double pre;
+  unsigned w[SPLIT_MAXCH];
+};
+
+template <class PH>
+__device__ __forceinline__ void split_fetch(const PH& f, const uint4* task, int idx, bool valid, SplitTask& s) {
+  s.t = valid ? __ldg(task + idx) : make_uint4(0xffffu, 0u, 0u, 0u);
+  const int item = s.t.x & 0xffff;
+  const int n = (s.t.x >> 19) & 31;
+  const unsigned* t = f.terms(item) + s.t.y;
+#pragma unroll
+  for (int k = 0; k < SPLIT_MAXCH; ++k) s.w[k] = k < n ? __ldg(t + k) : 0u;
+  s.pre = item != 0xffff ? f.pre(item, s.t.z) : 0.0;
+}
+
+// Runs the passes of one phase on the first sp_nt[ph] threads (32 or the
+// whole block; the host checks this).  A pass whose word has bit 3 set ends
+// with a barrier over those threads.  The caller adds the block barrier when
+// the phase used fewer threads than the block.
+template <class PH>
+__device__ __forceinline__ void split_run(const MechDev& m, int ph, const PH& f) {
+  const int nt = m.sp_nt[ph];
+  const int np = m.sp_npass[ph];
+  const int tid = threadIdx.x;
+  if (tid >= nt || np == 0) return;
+  const uint4* task = m.sp_task[ph];
+  const unsigned* pw = m.sp_pass[ph];
+  SplitTask cur, nxt;
+  split_fetch(f, task, tid, true, cur);
+  for (int p = 0; p < np; ++p) {
+    split_fetch(f, task, (p + 1) * nt + tid, p + 1 < np, nxt);
+    const unsigned info = __ldg(pw + p);
+    const int item = cur.t.x & 0xffff;
+    const int seg = 1 << ((cur.t.x >> 16) & 7);
+    const int n = (cur.t.x >> 19) & 31;
+    const bool lead = item != 0xffff && (tid & (seg - 1)) == 0;
+    double acc = lead ? f.base(item, cur.t.z, cur.pre) : 0.0;
+#pragma unroll
+    for (int k = 0; k < SPLIT_MAXCH; ++k)
+      if (k < n) acc = f.term(item, (int)cur.t.y + k, cur.w[k], acc);
+    for (int o = (1 << (info & 7)) >> 1; o > 0; o >>= 1) {
+      const double v = __shfl_xor_sync(0xffffffffu, acc, o);
+      if (o < seg) acc += v;
+    }
+    if (lead) f.finish(item, cur.t.z, acc);
+    if (info & 8u) {
+      if (nt == 32)
+        __syncwarp();
+      else
+        __syncthreads();
+    }
+    cur = nxt;
+  }
+}
+
+// Fun_SPLIT at V in the split form; B must hold the B products at V.  D is a
+// scratch vector of NVAR.  Ends with a barrier.
+__device__ inline void bk_fun_split(const MechDev& m, const double* V, const double* aux, double* A, const double* B,
+                             double* Vdot, double* D) {
+  for (int r = threadIdx.x; r < m.nreact; r += blockDim.x) A[r] = bk_product(m, r, V, aux);
+  __syncthreads();
+  split_run(m, SP_FUN, SplitFun{m, A, B, Vdot, D});
+  if (m.sp_nt[SP_FUN] < (int)blockDim.x) __syncthreads();
+  for (int i = threadIdx.x; i < m.nvar; i += blockDim.x) Vdot[i] = fma(-D[i], V[i], Vdot[i]);
+  __syncthreads();
+}
+
+// Singular check and LU factors in the split form.  Ends with a barrier.
+__device__ inline void bk_decomp_split(const MechDev& m, const double* J0, double ghinv, double* G, int* ier) {
+  if (threadIdx.x == 0) *ier = INT_MAX;
+  __syncthreads();
+  for (int i = threadIdx.x; i < m.nvar; i += blockDim.x) {
+    const double g = J0[__ldg(m.lu_diag + i)] + ghinv;
+    if (tiny_abs(g)) atomicMin(ier, i + 1);
+  }
+  split_run(m, SP_LU, SplitLu{m, J0, ghinv, G});
+  __syncthreads();
+  if (threadIdx.x == 0 && *ier == INT_MAX) *ier = 0;
+  __syncthreads();
+}
+
+// Forward and backward substitution in the split form.  Ends with a barrier.
+__device__ inline void bk_solve_split(const MechDev& m, const double* G, double* X) {
+  split_run(m, SP_FS, SplitSolve<false>{m, G, X});
+  if (m.sp_nt[SP_FS] != m.sp_nt[SP_BS]) __syncthreads();
+  split_run(m, SP_BS, SplitSolve<true>{m, G, X});
+  __syncthreads();
+}
+
 // Shared scalars of the block's cell.
 struct BlockShared {
   Lane L;
   int ier, flag, next, nconsec;
+  double red[32];
 };
 
 // One block integrates cells order[0..ncell) (or 0..ncell) taken from a
 // per-launch queue (p.queue_counter), one at a time.  Dynamic shared memory:
 // block_layout(...).total doubles; p.ws holds block_layout(...).slot doubles
 // per block of the grid.
-template <bool STRICT>
+template <bool STRICT, bool SPLIT = false>
 __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const RosParams& p) {
+  static_assert(!(STRICT && SPLIT), "the split form is fast arithmetic only");
   extern __shared__ double sm[];
   __shared__ BlockShared sh;
   const BlockLayout lay = block_layout(m.naux, m.nspec, m.nvar, m.nreact, m.nb, m.lu_nonzero, r.S, p.autonomous);
@@ -270,10 +458,19 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
       // Fun0 and Jac0 (B products shared)
       bk_b_products(m, Y, aux, B);
       __syncthreads();
-      bk_jac<STRICT>(m, B, J0);
-      bk_fun<STRICT>(m, Y, aux, A, B, F0);
+      if constexpr (SPLIT) {
+        split_run(m, SP_JAC, SplitJac{m, B, J0});
+        if (m.sp_nt[SP_JAC] < nt) __syncthreads();
+        bk_fun_split(m, Y, aux, A, B, F0, E);
+      } else {
+        bk_jac<STRICT>(m, B, J0);
+        bk_fun<STRICT>(m, Y, aux, A, B, F0);
+      }
       if (!p.autonomous) {
-        bk_fun<STRICT>(m, Y, aux, A, B, dfdt);
+        if constexpr (SPLIT)
+          bk_fun_split(m, Y, aux, A, B, dfdt, E);
+        else
+          bk_fun<STRICT>(m, Y, aux, A, B, dfdt);
         const double delta = sqrt(p.roundoff) * fmax(1.0e-6, fabs(sh.L.T));
         const double rd = 1.0 / delta;
         for (int i = tid; i < nvar; i += nt) {
@@ -295,7 +492,10 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
         __syncthreads();
         while (true) {
           const double ghinv = 1.0 / (dir * sh.L.H * r.Gamma[0]);
-          bk_decomp<STRICT>(m, J0, ghinv, G, &sh.ier);
+          if constexpr (SPLIT)
+            bk_decomp_split(m, J0, ghinv, G, &sh.ier);
+          else
+            bk_decomp<STRICT>(m, J0, ghinv, G, &sh.ier);
           if (tid == 0) sh.flag = ros.singular_retry(sh.L, sh.ier, sh.nconsec) ? 1 : 0;
           __syncthreads();
           if (!sh.flag) break;
@@ -316,7 +516,10 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
             __syncthreads();
             bk_b_products(m, Ynew, aux, B);
             __syncthreads();
-            bk_fun<STRICT>(m, Ynew, aux, A, B, F);
+            if constexpr (SPLIT)
+              bk_fun_split(m, Ynew, aux, A, B, F, E);
+            else
+              bk_fun<STRICT>(m, Ynew, aux, A, B, F);
             if (tid == 0) sh.L.nfun += 1;
             fcn = F;
           }
@@ -338,7 +541,10 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
             Ks[i] = k;
           }
           __syncthreads();
-          bk_solve<STRICT>(m, G, Ks);
+          if constexpr (SPLIT)
+            bk_solve_split(m, G, Ks);
+          else
+            bk_solve<STRICT>(m, G, Ks);
           if (tid == 0) sh.L.nsol += 1;
         }
         // new solution, error estimate, scaled errors
@@ -359,8 +565,20 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
           E[i] = yerr / scale;
         }
         __syncthreads();
-        // error norm summed in species order, then the step size control
-        if (tid == 0) {
+        // error norm (summed in species order, or in the split form by a
+        // block reduction), then the step size control
+        if constexpr (SPLIT) {
+          double s = 0.0;
+          for (int i = tid; i < nvar; i += nt) s = fma(E[i], E[i], s);
+          for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+          if ((tid & 31) == 0) sh.red[tid >> 5] = s;
+          __syncthreads();
+          if (tid == 0) {
+            double err = 0.0;
+            for (int w = 0; w < (nt >> 5); ++w) err += sh.red[w];
+            sh.flag = ros.control(sh.L, err, dir) ? 1 : 0;
+          }
+        } else if (tid == 0) {
           double err = 0.0;
           for (int i = 0; i < nvar; ++i) {
             const double e = E[i];

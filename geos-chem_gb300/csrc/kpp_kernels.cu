@@ -15,6 +15,9 @@
 #ifndef GCKPP_NC
 #define GCKPP_NC 1  // cells per thread
 #endif
+#ifndef GCKPP_SPLIT_NT
+#define GCKPP_SPLIT_NT 256  // threads of the split block-per-cell kernel (tables.py SPLIT_NT)
+#endif
 #ifndef GCKPP_VARIANT
 #define GCKPP_VARIANT fast
 #endif
@@ -82,6 +85,39 @@ cudaError_t GCKPP_CAT(gckpp_launch_block_, GCKPP_VARIANT)(int grid, int block, c
   if (e != cudaSuccess) return e;
   if (nblk < 1) return cudaErrorInvalidConfiguration;
   ros_block_kernel<GCKPP_STRICT != 0><<<grid, block, smem, s>>>(m, r, p);
+  return cudaGetLastError();
+}
+#endif
+
+#if GCKPP_NC == 1 && GCKPP_STRICT == 0
+// Split block-per-cell form: SPLIT_NT threads, sums cut across warp lanes.
+__global__ void __launch_bounds__(GCKPP_SPLIT_NT, 3) ros_block_split_kernel(MechDev m, RosMethod r, RosParams p) {
+  ros_block_driver<false, true>(m, r, p);
+}
+
+cudaError_t gckpp_block_occupancy_split(size_t smem, int* nblocks) {
+  static int smem_set[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64 || smem_set[dev] < (int)smem) {
+    e = cudaFuncSetAttribute(ros_block_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64) smem_set[dev] = (int)smem;
+  }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_block_split_kernel, GCKPP_SPLIT_NT, smem);
+}
+
+cudaError_t gckpp_launch_block_split(int grid, const MechDev& m, const RosMethod& r, const RosParams& p,
+                                     cudaStream_t s) {
+  for (int ph = 0; ph < 5; ++ph)  // each phase runs on one warp or on the whole block
+    if (m.sp_nt[ph] != 32 && m.sp_nt[ph] != GCKPP_SPLIT_NT) return cudaErrorInvalidConfiguration;
+  const size_t smem = gckpp_block_smem_fast(m, r, p.autonomous);
+  int nblk = 0;  // also sets the shared-memory attribute
+  cudaError_t e = gckpp_block_occupancy_split(smem, &nblk);
+  if (e != cudaSuccess) return e;
+  if (nblk < 1) return cudaErrorInvalidConfiguration;
+  ros_block_split_kernel<<<grid, GCKPP_SPLIT_NT, smem, s>>>(m, r, p);
   return cudaGetLastError();
 }
 #endif

@@ -29,4 +29,8 @@ size_t gckpp_block_smem_strict(const MechDev& m, const RosMethod& r, int autonom
 size_t gckpp_block_smem_fast(const MechDev& m, const RosMethod& r, int autonomous);
 cudaError_t gckpp_block_occupancy_strict(int block, size_t smem, int* nblocks);
 cudaError_t gckpp_block_occupancy_fast(int block, size_t smem, int* nblocks);
+// split form (fast arithmetic, SPLIT_NT threads per block)
+cudaError_t gckpp_launch_block_split(int grid, const MechDev& m, const RosMethod& r, const RosParams& p,
+                                     cudaStream_t s);
+cudaError_t gckpp_block_occupancy_split(size_t smem, int* nblocks);
 }  // namespace gckpp

@@ -60,7 +60,15 @@ struct MechDev {
   const int* fun_rows_by_len;
   const int* jac_by_len;
   int lu_nlvl, fs_nlvl, bs_nlvl;
+  // pass schedules of the split block-per-cell kernel (tables.py
+  // _split_schedules), indexed by SplitPhase
+  const uint4* sp_task[5];  // x, y, z, 0 per lane per pass
+  const unsigned* sp_pass[5];
+  int sp_npass[5];
+  int sp_nt[5];
 };
+
+enum SplitPhase : int { SP_LU = 0, SP_FS = 1, SP_BS = 2, SP_FUN = 3, SP_JAC = 4 };
 
 __device__ __forceinline__ int ldi(const int* p) { return __ldg(p); }
 __device__ __forceinline__ unsigned ldu(const unsigned* p) { return __ldg(p); }

@@ -29,6 +29,8 @@ def main(argv=None):
     ap.add_argument("--binned", type=int, default=0, help="grid step: cells sent block-per-cell")
     ap.add_argument("--learned", action="store_true",
                     help="grid step: the learned form (cold start, H0 proposals, bins, hand-over after 2 steps)")
+    ap.add_argument("--block-form", default="split", choices=["split", "level"],
+                    help="block-per-cell kernel form (GC_KPP_OPT_BLOCK_SPLIT 1 or 0)")
     ap.add_argument("--probe", action="store_true")
     args = ap.parse_args(argv)
 
@@ -49,6 +51,7 @@ def main(argv=None):
     dev = torch.device("cuda", 0)
     T = lambda x: torch.tensor(x, device=dev).contiguous()
     s = capi.Solver(0, arith=args.arith, schedule=args.schedule, block=args.block, max_slots=args.max_slots)
+    s.set(block_split=args.block_form == "split")
     atol, rtol = inputs.tolerances()
     ic, rc = inputs.default_controls()
     at, rt = T(atol), T(rtol)

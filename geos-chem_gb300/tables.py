@@ -37,6 +37,14 @@ import numpy as np
 from . import mechanism
 
 NOCOEF = 0x7FF
+# threads of the split block-per-cell kernel, the lanes each phase's passes
+# use (the substitutions run on the first warp alone, with warp barriers), and
+# the largest number of terms a lane sums before a segment combines its
+# partial sums
+SPLIT_NT = 256
+SPLIT_PHASE_NT = {"lu": 256, "fs": 32, "bs": 32, "fun": 256, "jac": 256}
+SPLIT_CHUNK = 8
+SPLIT_MAXCH = 16  # register slots of a lane's chunk in the kernel
 
 
 def _hexfloat(x):
@@ -260,6 +268,91 @@ class Tables:
         self.fun_rows_by_len = np.array(sorted(range(nvar), key=lambda i: (-flen[i], i)), np.int32)
         jlen = np.diff(self.j_start)
         self.jac_by_len = np.array(sorted(range(nz), key=lambda e: (-jlen[e], e)), np.int32)
+        self._split_schedules(crow, diag)
+
+    def _split_schedules(self, crow, diag):
+        """Pass schedules of the split block-per-cell kernel.
+
+        Every sum of the block phases (an LU entry's dot product, a
+        substitution row, a Fun_SPLIT P or D row, a Jac_SP entry) is one item;
+        an item of L terms gets a segment of s lanes (s a power of two, the
+        smallest with ceil(L/s) <= SPLIT_CHUNK, at most 32), each lane sums a
+        contiguous chunk of the terms and the segment adds its partial sums
+        with a butterfly of warp shuffles.  Within a dependency level the
+        segments are placed largest first, so each starts at a multiple of its
+        size and none crosses a warp; the level is cut into passes of
+        SPLIT_PHASE_NT[phase] lanes and only its last pass ends with a barrier.
+
+        task (four uint32 per lane): x = item | seglog << 16 | nterms << 19,
+        y = index of the lane's first term in the phase's term array, z =
+        the phase's finish word (LU: position of the pivot of an L entry,
+        0xFFFFFFFF for a diagonal entry, 0xFFFFFFFE for a U entry; backward
+        substitution: position of the row's diagonal), 0; item 0xFFFF is an
+        idle lane.  pass word: max seglog of the pass | barrier << 3."""
+        nvar, nz = self.nvar, self.lu_nonzero
+        CH = SPLIT_CHUNK
+
+        def passes(levels, NT):
+            task, info = [], []
+            for items in levels:
+                segs = []
+                for it, t0, n, z in items:
+                    s = 1
+                    while s < 32 and -(-n // s) > CH:
+                        s *= 2
+                    segs.append((s, n, it, t0, z))
+                if not segs:
+                    continue
+                segs.sort(key=lambda x: (-x[0], -x[1], x[2]))
+                lanes = []
+                for s, n, it, t0, z in segs:
+                    ch = -(-n // s)
+                    assert ch <= SPLIT_MAXCH and it < 0xFFFF
+                    for j in range(s):
+                        a, b = min(n, j * ch), min(n, (j + 1) * ch)
+                        lanes.append((it | (s.bit_length() - 1) << 16 | (b - a) << 19, t0 + a, z))
+                npass = -(-len(lanes) // NT)
+                lanes += [(0xFFFF, 0, 0)] * (npass * NT - len(lanes))
+                for p in range(npass):
+                    blk = lanes[p * NT:(p + 1) * NT]
+                    maxlog = max((x >> 16) & 7 for x, _, _ in blk)
+                    info.append(maxlog | (8 if p == npass - 1 else 0))
+                    for x, y, z in blk:
+                        task += [x, y, z, 0]
+            return np.array(task, np.uint32), np.array(info, np.uint32)
+
+        def levels_of(order, start, item):
+            return [[item(int(i)) for i in order[start[l]:start[l + 1]]] for l in range(len(start) - 1)]
+
+        irow = np.repeat(np.arange(nvar), np.diff(crow))
+
+        def lu_z(e):
+            k = int(irow[e])
+            if e == diag[k]:
+                return 0xFFFFFFFF
+            return int(diag[self.icol[e]]) if e < diag[k] else 0xFFFFFFFE
+
+        self.split = {}
+        self.split["lu"] = passes(levels_of(
+            self.lu_lvl_entry, self.lu_lvl_start,
+            lambda e: (e, int(self.dot_start[e]), int(self.dot_start[e + 1] - self.dot_start[e]), lu_z(e))),
+            SPLIT_PHASE_NT["lu"])
+        # substitution terms are positions kk of the LU pattern (G[kk] times
+        # X[icol[kk]]); forward rows without terms are left out
+        fs = levels_of(self.fs_lvl_row, self.fs_lvl_start,
+                       lambda i: (i, int(crow[i]), int(diag[i] - crow[i]), 0))
+        self.split["fs"] = passes([[x for x in lv if x[2] > 0] for lv in fs], SPLIT_PHASE_NT["fs"])
+        self.split["bs"] = passes(levels_of(self.bs_lvl_row, self.bs_lvl_start,
+                                            lambda i: (i, int(diag[i]) + 1, int(crow[i + 1] - diag[i] - 1),
+                                                       int(diag[i]))),
+                                  SPLIT_PHASE_NT["bs"])
+        # Fun_SPLIT: items [0, NVAR) are P rows (p_sterm), [NVAR, 2 NVAR) D rows (d_sterm)
+        self.split["fun"] = passes([
+            [(i, int(self.p_start[i]), int(self.p_start[i + 1] - self.p_start[i]), 0) for i in range(nvar)] +
+            [(nvar + i, int(self.d_start[i]), int(self.d_start[i + 1] - self.d_start[i]), 0) for i in range(nvar)]],
+            SPLIT_PHASE_NT["fun"])
+        self.split["jac"] = passes([[(e, int(self.j_start[e]), int(self.j_start[e + 1] - self.j_start[e]), 0)
+                                     for e in range(nz)]], SPLIT_PHASE_NT["jac"])
 
     # flop bookkeeping used by the roofline accounting (FP64 operations per
     # call, counting a multiply-add as 2, a division as 1, in STRICT form)
@@ -337,6 +430,13 @@ class Tables:
         arr("jac_by_len", self.jac_by_len)
         out.append("constexpr int LU_NLVL = %d, FS_NLVL = %d, BS_NLVL = %d;" % (
             len(self.lu_lvl_start) - 1, len(self.fs_lvl_start) - 1, len(self.bs_lvl_start) - 1))
+        out.append("constexpr int SPLIT_NT = %d;" % SPLIT_NT)
+        for ph in ("lu", "fs", "bs", "fun", "jac"):
+            task, info = self.split[ph]
+            out.append("constexpr int SPLIT_%s_NT = %d, SPLIT_%s_NPASS = %d;" % (
+                ph.upper(), SPLIT_PHASE_NT[ph], ph.upper(), len(info)))
+            arr("split_%s_task" % ph, task if len(task) else np.zeros(4, np.uint32), "unsigned")
+            arr("split_%s_pass" % ph, info if len(info) else np.zeros(1, np.uint32), "unsigned")
         out.append("static const double lit[%d] = {%s};" % (
             len(self.literals), ",".join(_hexfloat(v) for v in self.literals)))
         out.append("}  // namespace gcmech_tables")

@@ -59,12 +59,21 @@ extern "C" {
 #define GC_KPP_OPT_EVICT_AFTER 10 /* > 0: a cell of the thread-per-cell queue that still runs after
                                      this many steps is handed over, at a step boundary, to the
                                      block-per-cell kernel, which finishes it with the same
-                                     arithmetic (same results); 0 = off (default).  Needs the queue
+                                     arithmetic (same results with GC_KPP_OPT_BLOCK_SPLIT 0);
+                                     0 = off (default).  Needs the queue
                                      schedule, ARITH 0 or 1, the row-wise LU and ISTATUS/RSTATUS
                                      arrays (the fullchem step always has them). */
 #define GC_KPP_OPT_EVICT_DRAINED 11 /* 1 = hand a cell over only once the work queue has no
                                        unclaimed cell left (the tail of the launch); 0 = as soon
                                        as it has taken GC_KPP_OPT_EVICT_AFTER steps (default) */
+#define GC_KPP_OPT_BLOCK_SPLIT 12 /* fast arithmetic (ARITH 0, 2, 3): 1 = the block-per-cell kernel
+                                     runs the split form (default): 256 threads, every sum of the
+                                     LU, the substitutions, Fun_SPLIT and Jac_SP cut into chunks
+                                     that the lanes of a warp segment add in a shuffle tree, which
+                                     shortens the serial chains of a stiff cell's step; results
+                                     agree with the thread-per-cell form to rounding.  0 = the
+                                     level form (GC_KPP_OPT_CELL_BLOCK threads, each sum in one
+                                     thread, results identical to the thread-per-cell form). */
 #define GC_KPP_OPT_ASYNC 9        /* 1 = chemistry steps never synchronise the host, so that a
                                      caller can capture them in a CUDA graph: the retry list and
                                      the block-per-cell count stay on the device, *nretry (and
@@ -200,7 +209,8 @@ int gc_kpp_fullchem_step_ordered(gc_kpp_ctx* ctx, int ncell, double dt, const do
  * shared memory, on a second stream beside the thread-per-cell queue that
  * takes the other cells.  Meant for the few stiff cells that need tens of
  * steps while most need one or two; each cell gets the same arithmetic in
- * either form.  Needs GC_KPP_OPT_ARITH 0 or 1 and the row-wise LU
+ * either form (to rounding in the split form, GC_KPP_OPT_BLOCK_SPLIT).
+ * Needs GC_KPP_OPT_ARITH 0 or 1 and the row-wise LU
  * (GC_KPP_EUNSUPPORTED otherwise).  No counterpart in the reference. */
 int gc_kpp_fullchem_step_binned(gc_kpp_ctx* ctx, int ncell, double dt, const double* met, long long ldm,
                                 const double* photol, long long ldp, double* c, long long ldc,

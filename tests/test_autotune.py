@@ -1,5 +1,6 @@
 """The autotuner's candidates all give the default configuration's results
-bit for bit, and it returns the fastest one it timed."""
+(bit for bit, or to rounding where the split block-per-cell form takes
+cells), and it returns the fastest one it timed."""
 import numpy as np
 import pytest
 
