@@ -46,6 +46,7 @@ EXPORTED = [
     "gc_kpp_last_error",
     "gc_kpp_integrate_batch",
     "gc_kpp_update_rconst_batch",
+    "gc_kpp_update_rconst_het_batch",
     "gc_kpp_fullchem_step",
     "gc_kpp_fullchem_step_ordered",
     "gc_kpp_fullchem_step_binned",
@@ -84,6 +85,7 @@ def load_library(path=None, mech="fullchem"):
     lib.gc_kpp_integrate_batch.argtypes = [vp, i32, f64, f64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64,
                                            vp, i32, vp]
     lib.gc_kpp_update_rconst_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, vp, i64, i32, vp]
+    lib.gc_kpp_update_rconst_het_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64, i32, vp]
     if path == _build.lib_path(mech):
         _libs[mech] = lib
     return lib
@@ -257,13 +259,23 @@ class Solver:
         self._check(rc)
         return nretry.value, nblock.value
 
-    def update_rconst(self, met, photol, c, rconst, stream=None):
+    def update_rconst(self, met, photol, c, rconst, stream=None, het=None):
         """Batched Update_RCONST.  met: [NMET, ncell]; photol: [200, ncell];
-        c: [NSPEC, ncell]; rconst: [NREACT, ncell] output."""
+        c: [NSPEC, ncell]; rconst: [NREACT, ncell] output; het: the cells'
+        HetState rows [168, ncell] (gcchem.hetstate) or None (heterogeneous
+        rates 0)."""
         dev = _is_torch(rconst) and rconst.is_cuda
         ncell = rconst.shape[1]
         s = ctypes.c_void_p(stream) if stream else None
-        rc = self.lib.gc_kpp_update_rconst_batch(
-            self.ctx, ncell, _ptr(met), _ld(met, ncell), _ptr(photol), _ld(photol, ncell), _ptr(c), _ld(c, ncell),
-            _ptr(rconst), _ld(rconst, ncell), MEM_DEVICE if dev else MEM_HOST, s)
+        mem = MEM_DEVICE if dev else MEM_HOST
+        if het is None:
+            rc = self.lib.gc_kpp_update_rconst_batch(
+                self.ctx, ncell, _ptr(met), _ld(met, ncell), _ptr(photol), _ld(photol, ncell), _ptr(c),
+                _ld(c, ncell), _ptr(rconst), _ld(rconst, ncell), mem, s)
+        else:
+            if not _is_torch(het):
+                het = np.ascontiguousarray(het, dtype=np.float64)
+            rc = self.lib.gc_kpp_update_rconst_het_batch(
+                self.ctx, ncell, _ptr(met), _ld(met, ncell), _ptr(photol), _ld(photol, ncell), _ptr(c),
+                _ld(c, ncell), _ptr(het), _ld(het, ncell), _ptr(rconst), _ld(rconst, ncell), mem, s)
         self._check(rc)

@@ -17,6 +17,7 @@
 #include "../../include/gckpp_gb300.h"
 #include "mech_tables.inc"  // generated per mechanism (csrc/_gen/<mechanism>/)
 #include "rates_program.inc"
+#include "het_layout.h"
 #include "kpp_rates.h"
 #include "kpp_launch.h"
 #include "kpp_util.h"
@@ -113,7 +114,7 @@ struct gc_kpp_ctx {
   WsLayout lay{};
   DevBuf ws, counter;
   DevBuf h_c, h_r, h_at, h_rt, h_hs, h_is, h_rs, h_ie;  // staging for host-memory calls
-  DevBuf h_met, h_ph, h_ord;
+  DevBuf h_met, h_ph, h_ord, h_het;
   DevBuf rc_buf, cb_buf, ord_buf;  // chemistry-step scratch: RCONST, C_before, retry list
   int last_launches = 0;
   // optional CUDA-event timing of the Rosenbrock launches (GC_KPP_OPT_TIMING)
@@ -217,6 +218,12 @@ int gc_kpp_ctx_create(gc_kpp_ctx** out, int device) {
   if (e == cudaSuccess) e = upload(RT::start, sizeof(RT::start) / sizeof(int), &rp.start, c->owned);
   if (e == cudaSuccess) e = upload(RT::consts, sizeof(RT::consts) / sizeof(double), &rp.consts, c->owned);
   if (e == cudaSuccess) e = upload(RT::law_nargs, sizeof(RT::law_nargs) / sizeof(int), &rp.law_nargs, c->owned);
+  if (e == cudaSuccess) e = upload(RT::het_nargs, sizeof(RT::het_nargs) / sizeof(int), &rp.het_nargs, c->owned);
+  if (e == cudaSuccess) e = upload(RT::hs_ind, sizeof(RT::hs_ind) / sizeof(int), &rp.hs_ind, c->owned);
+  if (e == cudaSuccess) e = upload(RT::hs_mw, sizeof(RT::hs_mw) / sizeof(double), &rp.hs_mw, c->owned);
+  if (e == cudaSuccess) e = upload(RT::hs_srmw, sizeof(RT::hs_srmw) / sizeof(double), &rp.hs_srmw, c->owned);
+  if (e == cudaSuccess) e = upload(RT::hs_hk0, sizeof(RT::hs_hk0) / sizeof(double), &rp.hs_hk0, c->owned);
+  if (e == cudaSuccess) e = upload(RT::hs_hcr, sizeof(RT::hs_hcr) / sizeof(double), &rp.hs_hcr, c->owned);
   if (e != cudaSuccess) {
     gc_kpp_ctx_destroy(c);
     return cuda_fail(e, "upload rate program");
@@ -237,7 +244,8 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
   if (c->side) cudaStreamDestroy(c->side);
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
                     &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
-                    &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges, &c->evict_buf, &c->bws};
+                    &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges, &c->evict_buf, &c->bws,
+                    &c->h_het};
   for (DevBuf* b : bufs) b->release();
   delete c;
   return GC_KPP_OK;
@@ -960,11 +968,18 @@ int gc_kpp_last_kernel_ms(gc_kpp_ctx* c, double* ms, int* nlaunch) {
 int gc_kpp_update_rconst_batch(gc_kpp_ctx* c, int ncell, const double* met, long long ldm, const double* photol,
                                long long ldp, const double* conc, long long ldc, double* rconst, long long ldr, int mem,
                                void* stream) {
+  return gc_kpp_update_rconst_het_batch(c, ncell, met, ldm, photol, ldp, conc, ldc, nullptr, 0, rconst, ldr, mem,
+                                        stream);
+}
+
+int gc_kpp_update_rconst_het_batch(gc_kpp_ctx* c, int ncell, const double* met, long long ldm, const double* photol,
+                                   long long ldp, const double* conc, long long ldc, const double* het, long long ldh,
+                                   double* rconst, long long ldr, int mem, void* stream) {
   if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
   if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
   if (ncell == 0) return GC_KPP_OK;
   if (!met || !photol || !conc || !rconst) return fail(GC_KPP_EINVAL, "required array is NULL");
-  if (ldm < ncell || ldp < ncell || ldc < ncell || ldr < ncell)
+  if (ldm < ncell || ldp < ncell || ldc < ncell || ldr < ncell || (het && ldh < ncell))
     return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
   if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
   GC_CUDA(cudaSetDevice(c->device));
@@ -988,7 +1003,16 @@ int gc_kpp_update_rconst_batch(gc_kpp_ctx* c, int ncell, const double* met, long
     a.c = (const double*)c->h_c.p;
     a.rconst = (double*)c->h_r.p;
     a.ldm = a.ldp = a.ldc = a.ldr = ncell;
+    if (het) {
+      GC_CUDA(c->h_het.ensure((size_t)HET_NFIELD * n * sizeof(double)));
+      GC_CUDA(cudaMemcpy2DAsync(c->h_het.p, n * sizeof(double), het, ldh * sizeof(double), n * sizeof(double),
+                                HET_NFIELD, cudaMemcpyHostToDevice, s));
+      a.het = (const double*)c->h_het.p;
+      a.ldh = ncell;
+    }
   } else {
+    a.het = het;
+    a.ldh = ldh;
     a.met = met;
     a.ldm = ldm;
     a.photol = photol;

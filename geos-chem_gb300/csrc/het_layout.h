@@ -1,0 +1,95 @@
+// Generated by gcchem.hetstate (emit_c). Do not edit.
+#pragma once
+// rows of the cell-interleaved HetState array (order of the Fortran type)
+#define HET_NFIELD 168
+#define HET_AVO 0
+#define HET_natSurface 1
+#define HET_pscBox 2
+#define HET_stratBox 3
+#define HET_NAEROTYPE 4
+#define HET_aClArea 5
+#define HET_aClRadi 6
+#define HET_aClVol 7
+#define HET_aIce 8
+#define HET_aLiq 9
+#define HET_aWater 10  /* 2 rows */
+#define HET_Br_conc_CldA 12
+#define HET_Br_conc_CldC 13
+#define HET_Br_conc_CldG 14
+#define HET_Br_conc_Cld 15
+#define HET_Br_conc_SSA 16
+#define HET_Br_conc_SSC 17
+#define HET_Br_over_Cl_Cld 18
+#define HET_Br_over_Cl_SSA 19
+#define HET_Br_over_Cl_SSC 20
+#define HET_Cl_conc_CldA 21
+#define HET_Cl_conc_CldC 22
+#define HET_Cl_conc_CldG 23
+#define HET_Cl_conc_Cld 24
+#define HET_Cl_conc_SSA 25
+#define HET_Cl_conc_SSC 26
+#define HET_cldFr 27
+#define HET_clearFr 28
+#define HET_frac_Br_CldA 29
+#define HET_frac_Br_CldC 30
+#define HET_frac_Br_CldG 31
+#define HET_frac_Cl_CldA 32
+#define HET_frac_Cl_CldC 33
+#define HET_frac_Cl_CldG 34
+#define HET_frac_HSO3_aq 35
+#define HET_frac_SALACL 36
+#define HET_frac_SO3_aq 37
+#define HET_fupdateHOBr 38
+#define HET_fupdateHOCl 39
+#define HET_gamma_HO2 40
+#define HET_H2O 41
+#define HET_HBr_theta 42
+#define HET_HCl_theta 43
+#define HET_H_conc_ICl 44
+#define HET_H_conc_LCl 45
+#define HET_H_conc_SSA 46
+#define HET_H_conc_SSC 47
+#define HET_H_conc_Sul 48
+#define HET_HNO3_theta 49
+#define HET_HSO3_aq 50
+#define HET_SO3_aq 51
+#define HET_HSO3m 52
+#define HET_SO3mm 53
+#define HET_TSO3_aq 54
+#define HET_H_plus 55
+#define HET_KHETI_SLA 56  /* 11 rows */
+#define HET_HSO4_molal 67
+#define HET_NO3_molal 68
+#define HET_SO4_molal 69
+#define HET_NIT_conc_SSA 70
+#define HET_NIT_conc_SSC 71
+#define HET_PI 72
+#define HET_pHCloud 73
+#define HET_pHSSA 74  /* 2 rows */
+#define HET_OMOC_POA 76
+#define HET_OMOC_OPOA 77
+#define HET_qIce 78
+#define HET_qLiq 79
+#define HET_rIce 80
+#define HET_rLiq 81
+#define HET_f_Acid_SSA 82
+#define HET_f_Acid_SSC 83
+#define HET_f_Alk_SSA 84
+#define HET_f_Alk_SSC 85
+#define HET_SSA_is_Alk 86
+#define HET_SSA_is_Acid 87
+#define HET_SSC_is_Alk 88
+#define HET_SSC_is_Acid 89
+#define HET_vAir 90
+#define HET_vIce 91
+#define HET_vLiq 92
+#define HET_wetArea 93  /* 14 rows */
+#define HET_xArea 107  /* 14 rows */
+#define HET_xH2O 121  /* 14 rows */
+#define HET_xRadi 135  /* 14 rows */
+#define HET_xVol 149  /* 14 rows */
+#define HET_cloudBox 163
+#define HET_fracOrgAer 164
+#define HET_fracInorgAer 165
+#define HET_TurnOffHetRates 166
+#define HET_SUNCOS 167

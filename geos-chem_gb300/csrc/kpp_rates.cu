@@ -1,13 +1,16 @@
 // Update_RCONST on the GPU (KPP/fullchem/gckpp_Rates.F90:408-1503): one
 // thread per cell runs the postfix program of all 1058 rate expressions
 // (lowered by gcchem.rates_program); the opcode stream is warp-uniform.
+// Heterogeneous laws (het_rates.cuh) read the cell's HetState rows; without
+// a HetState array they are 0 (no aerosol surface, no cloud).
+#include "het_rates.cuh"
 #include "kpp_rates.h"
 #include "rate_laws.cuh"
 
 namespace gcrates {
 
 enum : int { OP_END = 0, OP_CONST, OP_VAR, OP_PHOTOL, OP_CONC, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_EXP,
-             OP_LOG10, OP_CALL, OP_HETZERO };
+             OP_LOG10, OP_CALL, OP_HETZERO, OP_HET };
 
 constexpr int NMET_MAX = 32;
 constexpr int STACK = 24;
@@ -19,6 +22,14 @@ __global__ void __launch_bounds__(128) rates_kernel(RatesDev rp, RatesArgs a) {
   for (int f = 0; f < rp.nmet; ++f) v[f] = a.met[(long long)f * a.ldm + cell];
   Env E;
   env_init(E, v[0], v[1], v[2], v[3], v[4], v[5]);
+  HetCell X;
+  X.H = a.het;
+  X.ldh = a.ldh;
+  X.C = a.c;
+  X.ldc = a.ldc;
+  X.cell = cell;
+  X.sp = HetSpecies{rp.hs_ind, rp.hs_mw, rp.hs_srmw, rp.hs_hk0, rp.hs_hcr};
+  if (a.het) het_cell_init(X, E);
   double st[STACK];
   for (int r = 0; r < rp.nreact; ++r) {
     int pc = __ldg(rp.start + r);
@@ -48,6 +59,14 @@ __global__ void __launch_bounds__(128) rates_kernel(RatesDev rp, RatesArgs a) {
           break;
         }
         case OP_HETZERO: st[sp++] = 0.0; break;
+        case OP_HET: {
+          const int id = __ldg(rp.code + pc++);
+          const int n = __ldg(rp.het_nargs + id);
+          sp -= n;
+          st[sp] = a.het ? het_law(id, st + sp, X) : 0.0;
+          ++sp;
+          break;
+        }
         default: bad = true; break;
       }
       if (bad || sp > STACK - 8 || sp < 0) {

@@ -6,11 +6,16 @@ parsed with ordinary precedence and left associativity (the Fortran
 evaluation order) and emitted as postfix code for ``csrc/kpp_rates.cu``:
 every lane of a warp runs the same opcode for its own cell.
 
-Heterogeneous rate functions (those taking the HetState ``H``) are emitted as
-HETZERO: the rate kernel evaluates the zeroed HetState of the synthetic
-cells, for which each of them is a sum of Ars_L1k/CloudHet terms that vanish
-with zero aerosol area and radius and zero cloud fraction
-(KPP/fullchem/rateLawUtilFuncs.F90:77-96, :141-230).
+Heterogeneous rate functions (those taking the HetState ``H``) of
+KPP/fullchem/fullchem_RateLawFuncs.F90 are emitted as HET calls of the laws
+in csrc/het_rates.cuh (HET_LAWS order), their numeric arguments first
+(``SR_MW[i]`` becomes the constant SQRT(MW) of the species database, as
+GeosCore/fullchem_mod.F90:2915 sets it).  Without a HetState array the
+heterogeneous rates are 0 (no aerosol surface, no cloud: the sums of
+Ars_L1k/CloudHet terms vanish, KPP/fullchem/rateLawUtilFuncs.F90:77-96,
+:141-230; evaluating the laws on an all-zero HetState gives the same zeros
+except N2O5 uptake, which the Fortran arithmetic turns into NaN there).
+Heterogeneous functions of other mechanisms stay HETZERO.
 """
 import os
 import re
@@ -18,7 +23,7 @@ import re
 from . import mechanism
 
 OPS = ["END", "CONST", "VAR", "PHOTOL", "CONC", "ADD", "SUB", "MUL", "DIV", "NEG", "EXP", "LOG10", "CALL",
-       "HETZERO"]
+       "HETZERO", "HET"]
 OP = {n: i for i, n in enumerate(OPS)}
 
 # Per-cell met/state fields, in the order of GC_KPP_MET_* in the C ABI.
@@ -36,6 +41,30 @@ LAWS = [
     ("GCJPLPR_aa", 3), ("GCJPLPR_aba", 4), ("GCJPLPR_abab", 5), ("GCJPLPR_abcabc", 7), ("GCJPLAC_ababac", 7),
 ]
 LAW_ID = {n: (i, k) for i, (n, k) in enumerate(LAWS)}
+
+# Heterogeneous rate laws of csrc/het_rates.cuh (het_law switch order):
+# name -> number of numeric arguments (the HetState argument H is implicit)
+HET_LAWS = [
+    ("BrNO3uptkByH2O", 0), ("BrNO3uptkByHCl", 0), ("ClNO2uptkByBrSALA", 0), ("ClNO2uptkByBrSALC", 0),
+    ("ClNO2uptkByHBr", 0), ("ClNO2uptkBySALACL", 0), ("ClNO2uptkBySALCCL", 0), ("ClNO2uptkByHCl", 0),
+    ("ClNO3uptkByH2O", 0), ("ClNO3uptkByHCl", 0), ("ClNO3uptkByHBr", 0), ("ClNO3uptkByBrSALA", 0),
+    ("ClNO3uptkByBrSALC", 0), ("ClNO3uptkBySALACL", 0), ("ClNO3uptkBySALCCL", 0), ("HBrUptkBySALA", 0),
+    ("HBrUptkBySALC", 0), ("HO2uptk1stOrd", 0), ("HOBrUptkByHBr", 0), ("HOBrUptkByHCl", 0),
+    ("HOBrUptkByBrSALA", 0), ("HOBrUptkByBrSALC", 0), ("HOBrUptkBySALACL", 0), ("HOBrUptkBySALCCL", 0),
+    ("HOBrUptkByHSO3m", 0), ("HOBrUptkBySO3mm", 0), ("HOClUptkByHCl", 0), ("HOClUptkByHBr", 0),
+    ("HOClUptkBySALACL", 0), ("HOClUptkBySALCCL", 0), ("HOClUptkByHSO3m", 0), ("HOClUptkBySO3mm", 0),
+    ("IuptkBySulf1stOrd", 2), ("IuptkBySALA1stOrd", 2), ("IuptkByAlkSALA1stOrd", 2), ("IuptkBySALC1stOrd", 2),
+    ("IuptkByAlkSALC1stOrd", 2), ("IbrkdnByAcidBrSALA", 3), ("IbrkdnByAcidBrSALC", 3), ("IbrkdnByAcidSALACl", 3),
+    ("IbrkdnByAcidSALCCl", 3), ("IONO2uptkByH2O", 0), ("N2O5uptkByH2O", 0), ("N2O5uptkBySALACl", 0),
+    ("N2O5uptkBySALCCl", 0), ("N2O5uptkByCloud", 0), ("N2O5uptkByStratHCl", 0), ("NO2uptk1stOrdAndCloud", 0),
+    ("NO3uptk1stOrdAndCloud", 0), ("NO3hypsisClonSALA", 0), ("NO3hypsisClonSALC", 0), ("O3uptkByHBr", 0),
+    ("O3uptkByBrSALA", 0), ("O3uptkByBrSALC", 0), ("OHuptkBySALACl", 0), ("OHuptkBySALCCl", 0),
+    ("GLYXuptk1stOrd", 1), ("IEPOXuptk1stOrd", 2), ("MGLYuptk1stOrd", 1), ("VOCuptk1stOrd", 2),
+]
+HET_ID = {n: (i, k) for i, (n, k) in enumerate(HET_LAWS)}
+# species the heterogeneous laws reference (csrc/het_rates.cuh HetSpc order)
+HET_SPECIES = ["BrNO3", "H2O", "HCl", "ClNO2", "BrSALA", "BrSALC", "HBr", "SALACL", "SALCCL", "ClNO3", "HOBr",
+               "SO2", "HOCl", "HO2", "IONO2", "N2O5", "NIT", "NITs", "NO2", "NO3", "O3", "OH"]
 
 _TOKEN = re.compile(r"\s*(?:(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|\d+(?:[eE][+-]?\d+)?)|"
                     r"([A-Za-z_][A-Za-z_0-9]*)|(.))")
@@ -57,12 +86,14 @@ def _tokens(s):
 
 
 class _Parser:
-    def __init__(self, text, consts):
+    def __init__(self, text, consts, srmw=None, het_laws=True):
         self.t = _tokens(text)
         self.i = 0
         self.code = []
         self.consts = consts
         self.het = 0
+        self.srmw = srmw
+        self.het_laws = het_laws
 
     def peek(self):
         return self.t[self.i] if self.i < len(self.t) else (None, None)
@@ -118,6 +149,23 @@ class _Parser:
         self.take(")")
         return n
 
+    def _het_args(self):
+        """Numeric arguments of a heterogeneous law; the HetState H is implicit."""
+        self.take("(")
+        n = 0
+        while True:
+            if self.peek() == ("id", "H") and self.t[self.i + 1][1] in (",", ")"):
+                self.take()
+            else:
+                self.expr()
+                n += 1
+            if self.peek()[1] == ",":
+                self.take()
+                continue
+            break
+        self.take(")")
+        return n
+
     def _skip_call(self):
         depth = 0
         while True:
@@ -153,6 +201,8 @@ class _Parser:
                     self.code += [OP["VAR"], MET_FIELDS.index("K_CLD%d" % idx)]
                 elif val == "C":
                     self.code += [OP["CONC"], idx]
+                elif val == "SR_MW" and self.srmw is not None:
+                    self.const(self.srmw[idx])
                 else:
                     raise ValueError("array %s" % val)
             elif nxt == "(":
@@ -165,6 +215,12 @@ class _Parser:
                     n = self._args()
                     assert n == k, (val, n, k)
                     self.code += [OP["CALL"], lid]
+                elif val in HET_ID and self.het_laws:
+                    hid, k = HET_ID[val]
+                    n = self._het_args()
+                    assert n == k, (val, n, k)
+                    self.code += [OP["HET"], hid]
+                    self.het += 1
                 else:
                     self._skip_call()
                     self.code.append(OP["HETZERO"])
@@ -178,13 +234,22 @@ class _Parser:
 
 
 def build_program(ir=None):
+    import math
+
+    from .mechanism import species_db
+
     ir = ir or mechanism.load_ir()
+    mech = ir.get("mechanism", "fullchem")
+    spc = species_db.load(mech)
+    assert spc["species"] == ir["species"], "species constants out of date for %s" % mech
+    srmw = [math.sqrt(m) for m in spc["mw"]]
+    het_laws = mech == "fullchem"
     consts = {}
     code = []
     start = [0]
     nhet = 0
     for e in ir["rconst"]:
-        p = _Parser(e, consts)
+        p = _Parser(e, consts, srmw, het_laws)
         p.expr()
         assert p.i == len(p.t), e
         code += p.code + [OP["END"]]
@@ -193,11 +258,15 @@ def build_program(ir=None):
     pool = [0.0] * len(consts)
     for v, i in consts.items():
         pool[i] = v
-    return {"code": code, "start": start, "consts": pool, "nhet": nhet}
+    # species table of the heterogeneous laws (KPP index or -1, MW, SR_MW, HENRY_K0, HENRY_CR)
+    ind = [ir["species"].index(n) if n in ir["species"] else -1 for n in HET_SPECIES]
+    pick = lambda arr: [arr[i] if i >= 0 else 0.0 for i in ind]
+    return {"code": code, "start": start, "consts": pool, "nhet": nhet, "hs_ind": ind, "hs_mw": pick(spc["mw"]),
+            "hs_srmw": pick(srmw), "hs_hk0": pick(spc["henry_k0"]), "hs_hcr": pick(spc["henry_cr"])}
 
 
 def emit_c(prog):
-    lines = ["// Generated by gcchem.rates_program from mechanism/fullchem.json. Do not edit.",
+    lines = ["// Generated by gcchem.rates_program from the mechanism IR. Do not edit.",
              "#pragma once",
              "namespace gcrates_tables {",
              "constexpr int NMET = %d;" % len(MET_FIELDS),
@@ -206,7 +275,12 @@ def emit_c(prog):
              "static const double consts[%d] = {%s};" % (len(prog["consts"]),
                                                        ",".join(float(v).hex() for v in prog["consts"])),
              "static const int law_nargs[%d] = {%s};" % (len(LAWS), ",".join(str(k) for _, k in LAWS)),
-             "}  // namespace gcrates_tables"]
+             "static const int het_nargs[%d] = {%s};" % (len(HET_LAWS), ",".join(str(k) for _, k in HET_LAWS)),
+             "static const int hs_ind[%d] = {%s};" % (len(HET_SPECIES), ",".join(map(str, prog["hs_ind"])))]
+    for key in ("hs_mw", "hs_srmw", "hs_hk0", "hs_hcr"):
+        lines.append("static const double %s[%d] = {%s};" % (key, len(HET_SPECIES),
+                                                            ",".join(float(v).hex() for v in prog[key])))
+    lines.append("}  // namespace gcrates_tables")
     return "\n".join(lines) + "\n"
 
 

@@ -157,11 +157,37 @@ int gc_kpp_integrate_batch(gc_kpp_ctx* ctx, int ncell, double tin, double tout,
  *   rconst  [NREACT][ldr]         out  RCONST
  *
  * Gas-phase, photolysis, K_MT/K_CLD and constant rates are evaluated as the
- * reference does.  Heterogeneous rates are evaluated for a zeroed HetState
- * (no aerosol surface, no cloud), for which every one of them is 0. */
+ * reference does.  Heterogeneous rates are 0 (no aerosol surface, no cloud);
+ * gc_kpp_update_rconst_het_batch evaluates them from a HetState. */
 int gc_kpp_update_rconst_batch(gc_kpp_ctx* ctx, int ncell, const double* met, long long ldm,
                                const double* photol, long long ldp, const double* c, long long ldc,
                                double* rconst, long long ldr, int mem, void* stream);
+
+/* Rows of the HetState array of gc_kpp_update_rconst_het_batch: the fields
+ * of the reference's HetState type (KPP/fullchem/commonIncludeVars.H:111-201)
+ * in declaration order, one row per scalar and one per array element
+ * (aWater 2, KHETI_SLA 11, pHSSA 2, wetArea/xArea/xH2O/xRadi/xVol 14 each,
+ * logicals as 0.0/1.0), then SUNCOS; 168 rows.  Row offsets: the HET_*
+ * macros of geos-chem_gb300/csrc/het_layout.h. */
+#define GC_KPP_NHET 168
+
+/* gc_kpp_update_rconst_batch with the cells' HetState (replaces the
+ * State_Het that fullchem_SetStateHet fills before Update_RCONST,
+ * GeosCore/fullchem_mod.F90:861-936):
+ *
+ *   het     [GC_KPP_NHET][ldh]    in   HetState rows (NULL: heterogeneous rates 0)
+ *
+ * The heterogeneous rates are the fullchem rate laws of
+ * KPP/fullchem/fullchem_RateLawFuncs.F90:795-3460 (uptake on aerosol types,
+ * cloud droplets and ice, with kIIR1Ltd's limiting-reactant form and
+ * CloudHet's entrainment limit), reading C, MW/SR_MW/HENRY_K0/HENRY_CR of the
+ * species database and RELHUM from TEMP and H2O as Set_Kpp_GridBox_Values
+ * computes it.  Mechanisms other than fullchem keep their heterogeneous
+ * rates at 0. */
+int gc_kpp_update_rconst_het_batch(gc_kpp_ctx* ctx, int ncell, const double* met, long long ldm,
+                                   const double* photol, long long ldp, const double* c, long long ldc,
+                                   const double* het, long long ldh, double* rconst, long long ldr, int mem,
+                                   void* stream);
 
 /* One chemistry step of Do_FullChem's cell loop for a batch of cells
  * (GeosCore/fullchem_mod.F90:528-1551, the loop body from :817 to :1350):

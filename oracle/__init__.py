@@ -44,6 +44,7 @@ def load(variant="strict", mech="fullchem"):
     vp, i32, i64, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
     lib.oracle_integrate_batch.argtypes = [i32, f64, f64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64, vp, i32]
     lib.oracle_update_rconst_batch.argtypes = [i32, vp, i64, vp, i64, vp, i64, vp, i64]
+    lib.oracle_update_rconst_het_batch.argtypes = [i32, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64]
     lib.oracle_fun_split.argtypes = [vp, vp, vp, vp]
     lib.oracle_jac_sp.argtypes = [vp, vp, vp, vp]
     lib.oracle_kpp_solve.argtypes = [vp, vp]
@@ -89,7 +90,8 @@ def integrate(c, rconst, atol, rtol, tin, tout, icntrl=None, rcntrl=None, hstart
     return c, ist, rst, ierr
 
 
-def update_rconst(met, photol, c, variant="strict", mech="fullchem"):
+def update_rconst(met, photol, c, variant="strict", mech="fullchem", het=None):
+    """Batched Update_RCONST; het [168, n] HetState rows or None (zeroed)."""
     lib = load(variant, mech)
     met = _c(met, np.float64)
     photol = _c(photol, np.float64)
@@ -97,7 +99,11 @@ def update_rconst(met, photol, c, variant="strict", mech="fullchem"):
     n = met.shape[1]
     nreact = _dims(mech)["nreact"]
     out = np.zeros((nreact, n), np.float64)
-    lib.oracle_update_rconst_batch(n, _p(met), n, _p(photol), n, _p(c), n, _p(out), n)
+    if het is None:
+        lib.oracle_update_rconst_batch(n, _p(met), n, _p(photol), n, _p(c), n, _p(out), n)
+    else:
+        het = _c(het, np.float64)
+        lib.oracle_update_rconst_het_batch(n, _p(met), n, _p(photol), n, _p(c), n, _p(het), n, _p(out), n)
     return out
 
 

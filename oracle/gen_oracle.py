@@ -148,7 +148,42 @@ MET_FIELDS = ["TEMP", "NUMDEN", "H2O", "PRESS", "SRHOCl", "SRHOBr"] + \
     ["K_MT%d" % i for i in range(6)] + ["K_CLD%d" % i for i in range(6)]
 
 
-def _rate_c(expr, het_calls):
+# heterogeneous rate functions restated in het_laws.h (o_<name>), with the
+# number of numeric arguments before the HetState argument H
+HET_FUNCS = {
+    "IuptkBySulf1stOrd": 2, "IuptkBySALA1stOrd": 2, "IuptkByAlkSALA1stOrd": 2, "IuptkBySALC1stOrd": 2,
+    "IuptkByAlkSALC1stOrd": 2, "IbrkdnByAcidBrSALA": 3, "IbrkdnByAcidBrSALC": 3, "IbrkdnByAcidSALACl": 3,
+    "IbrkdnByAcidSALCCl": 3, "GLYXuptk1stOrd": 1, "IEPOXuptk1stOrd": 2, "MGLYuptk1stOrd": 1, "VOCuptk1stOrd": 2,
+}
+for _n in ("BrNO3uptkByH2O BrNO3uptkByHCl ClNO2uptkByBrSALA ClNO2uptkByBrSALC ClNO2uptkByHBr ClNO2uptkBySALACL "
+           "ClNO2uptkBySALCCL ClNO2uptkByHCl ClNO3uptkByH2O ClNO3uptkByHCl ClNO3uptkByHBr ClNO3uptkByBrSALA "
+           "ClNO3uptkByBrSALC ClNO3uptkBySALACL ClNO3uptkBySALCCL HBrUptkBySALA HBrUptkBySALC HO2uptk1stOrd "
+           "HOBrUptkByHBr HOBrUptkByHCl HOBrUptkByBrSALA HOBrUptkByBrSALC HOBrUptkBySALACL HOBrUptkBySALCCL "
+           "HOBrUptkByHSO3m HOBrUptkBySO3mm HOClUptkByHCl HOClUptkByHBr HOClUptkBySALACL HOClUptkBySALCCL "
+           "HOClUptkByHSO3m HOClUptkBySO3mm IONO2uptkByH2O N2O5uptkByH2O N2O5uptkBySALACl N2O5uptkBySALCCl "
+           "N2O5uptkByCloud N2O5uptkByStratHCl NO2uptk1stOrdAndCloud NO3uptk1stOrdAndCloud NO3hypsisClonSALA "
+           "NO3hypsisClonSALC O3uptkByHBr O3uptkByBrSALA O3uptkByBrSALC OHuptkBySALACl OHuptkBySALCCl").split():
+    HET_FUNCS[_n] = 0
+HET_SPECIES = ["BrNO3", "H2O", "HCl", "ClNO2", "BrSALA", "BrSALC", "HBr", "SALACL", "SALCCL", "ClNO3", "HOBr",
+               "SO2", "HOCl", "HO2", "IONO2", "N2O5", "NIT", "NITs", "NO2", "NO3", "O3", "OH"]
+
+
+def _split_args(text):
+    out, depth, cur = [], 0, ""
+    for ch in text:
+        if ch == "," and depth == 0:
+            out.append(cur.strip())
+            cur = ""
+            continue
+        depth += ch == "("
+        depth -= ch == ")"
+        cur += ch
+    if cur.strip():
+        out.append(cur.strip())
+    return out
+
+
+def _rate_c(expr, het_calls, het_laws=False):
     """Rate expression (C-like IR text) -> oracle C text."""
     out = ""
     i = 0
@@ -170,7 +205,12 @@ def _rate_c(expr, het_calls):
                     k += 1
                 args = expr[j + 1:k]
                 if name in GAS_LAWS:
-                    out += "%s(&E, %s)" % (name, _rate_c(args, het_calls))
+                    out += "%s(&E, %s)" % (name, _rate_c(args, het_calls, het_laws))
+                elif het_laws and name in HET_FUNCS:
+                    parts = _split_args(args)
+                    assert parts[-1] == "H" and len(parts) == HET_FUNCS[name] + 1, (name, parts)
+                    num = "".join(", " + _rate_c(a, het_calls, het_laws) for a in parts[:-1])
+                    out += "(het ? o_%s(&X%s) : 0.0)" % (name, num)
                 else:
                     het_calls.add(name)
                     out += "HET_ZERO"
@@ -187,28 +227,79 @@ def _rate_c(expr, het_calls):
     return out
 
 
+def _species_consts(ir):
+    """SR_MW of every species and the MW/SR_MW/HENRY table of HET_SPECIES
+    (species database values, mechanism/<mech>_species.json)."""
+    import math
+
+    path = os.path.join(MECH_DIR, ir.get("mechanism", "fullchem") + "_species.json")
+    with open(path) as fh:
+        spc = json.load(fh)
+    assert spc["species"] == ir["species"]
+    L = ["static const double SR_MW[%d] = {%s};" % (len(spc["mw"]),
+                                                   ",".join(math.sqrt(m).hex() for m in spc["mw"]))]
+    ind = [ir["species"].index(n) if n in ir["species"] else -1 for n in HET_SPECIES]
+    for k, (n, i) in enumerate(zip(HET_SPECIES, ind)):
+        L.append("#define OHS_%s %d" % (n, i))
+        L.append("#define OHSI_%s %d" % (n, k))
+    for name, key in (("O_MW", "mw"), ("O_HK0", "henry_k0"), ("O_HCR", "henry_cr")):
+        L.append("static const double %s[%d] = {%s};" % (name, len(ind), ",".join(
+            (spc[key][i] if i >= 0 else 0.0).hex() for i in ind)))
+    L.append("static const double O_SRMW[%d] = {%s};" % (len(ind), ",".join(
+        (math.sqrt(spc["mw"][i]) if i >= 0 else 0.0).hex() for i in ind)))
+    return L
+
+
 def generate_rates(ir):
+    het_laws = ir.get("mechanism", "fullchem") == "fullchem"
     L = ["/* Generated by oracle/gen_oracle.py: Update_RCONST (KPP/fullchem/gckpp_Rates.F90:408-1503). */",
          "#include \"kpp_oracle.h\"",
-         "#include \"rate_laws.h\"",
-         "/* Heterogeneous rates with the zeroed HetState of the synthetic cells: every het",
-         " * rate function of fullchem_RateLawFuncs.F90 sums Ars_L1k/CloudHet terms that are 0",
-         " * for zero aerosol area/radius and zero cloud fraction. */",
-         "#define HET_ZERO 0.0",
-         "void oracle_update_rconst(const double* met, const double* PHOTOL, const double* C, double* RCONST) {",
-         "  rate_env_t E;",
-         "  rate_env_init(&E, met[0], met[1], met[2], met[3], met[4], met[5]);",
-         "  const double* K_MT = met + 6;",
-         "  const double* K_CLD = met + 12;",
-         "  (void)C;"]
+         "#include \"rate_laws.h\""]
+    L += _species_consts(ir)
+    L += ["#include \"het_laws.h\"",
+          "/* Heterogeneous rates without a HetState, and those that het_laws.h does not",
+          " * restate (other mechanisms), are 0: no aerosol surface and no cloud, where the",
+          " * Ars_L1k/CloudHet terms vanish. */",
+          "#define HET_ZERO 0.0",
+          "void oracle_update_rconst_het(const double* met, const double* PHOTOL, const double* C, const double* het,",
+          "                              long long ldh, double* RCONST) {",
+          "  rate_env_t E;",
+          "  rate_env_init(&E, met[0], met[1], met[2], met[3], met[4], met[5]);",
+          "  const double* K_MT = met + 6;",
+          "  const double* K_CLD = met + 12;",
+          "  het_cell_t X;",
+          "  if (het) het_cell_load(&X, &E, het, ldh, C);",
+          "  (void)C;",
+          "  (void)X;"]
     het = set()
     for i, e in enumerate(ir["rconst"]):
-        L.append("  RCONST[%d] = %s;" % (i, _rate_c(e, het)))
+        L.append("  RCONST[%d] = %s;" % (i, _rate_c(e, het, het_laws)))
+    L.append("}")
+    L.append("void oracle_update_rconst(const double* met, const double* PHOTOL, const double* C, double* RCONST) {")
+    L.append("  oracle_update_rconst_het(met, PHOTOL, C, 0, 0, RCONST);")
     L.append("}")
     return "\n".join(L) + "\n", sorted(het)
 
 
+def write_het_layout(outdir):
+    """oracle_het_layout.h: OHET_* row offsets of the HetState array."""
+    sys.path.insert(0, os.path.join(HERE, "..", "geos-chem_gb300"))
+    import hetstate  # the field list of the batch interface (data only)
+
+    lines = ["/* Generated by oracle/gen_oracle.py from the HetState field list. */", "#pragma once"]
+    for name, n in hetstate.FIELDS:
+        lines.append("#define OHET_%s %d" % (name, hetstate.OFFSET[name]))
+    text = "\n".join(lines) + "\n"
+    path = os.path.join(outdir, "oracle_het_layout.h")
+    old = open(path).read() if os.path.exists(path) else None
+    if old != text:
+        with open(path, "w") as fh:
+            fh.write(text)
+    return path
+
+
 def write_rates(outdir, mech="fullchem"):
+    write_het_layout(outdir)
     text, het = generate_rates(_ir(mech))
     path = os.path.join(outdir, "kpp_rates_oracle.c")
     old = open(path).read() if os.path.exists(path) else None

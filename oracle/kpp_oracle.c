@@ -410,8 +410,9 @@ void oracle_integrate_batch(int ncell, double tin, double tout, double* c, long 
   (void)nthreads;
 }
 
-void oracle_update_rconst_batch(int ncell, const double* met, long long ldm, const double* photol, long long ldp,
-                                const double* c, long long ldc, double* rconst, long long ldr) {
+void oracle_update_rconst_het_batch(int ncell, const double* met, long long ldm, const double* photol,
+                                    long long ldp, const double* c, long long ldc, const double* het, long long ldh,
+                                    double* rconst, long long ldr) {
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -420,7 +421,12 @@ void oracle_update_rconst_batch(int ncell, const double* met, long long ldm, con
     for (int k = 0; k < 18; ++k) M[k] = met[(long long)k * ldm + cell];
     for (int k = 0; k < 200; ++k) P[k] = photol[(long long)k * ldp + cell];
     for (int k = 0; k < NSPEC; ++k) C[k] = c[(long long)k * ldc + cell];
-    oracle_update_rconst(M, P, C, R);
+    oracle_update_rconst_het(M, P, C, het ? het + cell : 0, ldh, R);
     for (int k = 0; k < NREACT; ++k) rconst[(long long)k * ldr + cell] = R[k];
   }
+}
+
+void oracle_update_rconst_batch(int ncell, const double* met, long long ldm, const double* photol, long long ldp,
+                                const double* c, long long ldc, double* rconst, long long ldr) {
+  oracle_update_rconst_het_batch(ncell, met, ldm, photol, ldp, c, ldc, 0, 0, rconst, ldr);
 }

@@ -24,6 +24,13 @@ int oracle_kpp_decomp(double* JVS);
 void oracle_update_rconst(const double* met, const double* PHOTOL, const double* C, double* RCONST);
 void oracle_update_rconst_batch(int ncell, const double* met, long long ldm, const double* photol, long long ldp,
                                 const double* c, long long ldc, double* rconst, long long ldr);
+/* The same with the cells' HetState rows het[f * ldh + cell] (NULL: zeroed
+ * HetState), for the heterogeneous rate laws of het_laws.h. */
+void oracle_update_rconst_het(const double* met, const double* PHOTOL, const double* C, const double* het,
+                              long long ldh, double* RCONST);
+void oracle_update_rconst_het_batch(int ncell, const double* met, long long ldm, const double* photol,
+                                    long long ldp, const double* c, long long ldc, const double* het, long long ldh,
+                                    double* rconst, long long ldr);
 
 /* One cell: INTEGRATE(TIN, TOUT, ICNTRL_U, RCNTRL_U, ISTATUS, RSTATUS, IERR)
  * on C[NSPEC] (in/out) with RCONST[NREACT]. */

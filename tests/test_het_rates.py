@@ -1,0 +1,189 @@
+"""Heterogeneous rates of Update_RCONST with a real HetState
+(gc_kpp_update_rconst_het_batch): the GPU rate laws of csrc/het_rates.cuh
+against the oracle's restatement (oracle/het_laws.h) of
+KPP/fullchem/fullchem_RateLawFuncs.F90:795-3460, on seeded synthetic
+HetStates; plus the interface tables and a few laws recomputed here from
+their Fortran formulas."""
+import math
+import os
+import re
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "geos-chem_gb300", "csrc")
+
+
+def test_het_layout_header_matches_field_list():
+    import gcchem.hetstate as hs
+
+    with open(os.path.join(CSRC, "het_layout.h")) as fh:
+        assert fh.read() == hs.emit_c()
+    assert hs.NFIELD == 168
+    with open(os.path.join(ROOT, "include", "gckpp_gb300.h")) as fh:
+        assert "#define GC_KPP_NHET %d" % hs.NFIELD in fh.read()
+
+
+def test_het_law_tables_agree():
+    """rates_program.HET_LAWS is the het_law switch of het_rates.cuh, its
+    HET_SPECIES the HetSpc enum, and the oracle generator knows every law."""
+    import gcchem.rates_program as rp
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gen_oracle
+
+    src = open(os.path.join(CSRC, "het_rates.cuh")).read()
+    cases = re.findall(r"case (\d+): return .*;  // (\w+)", src)
+    assert [(int(i), n) for i, n in cases] == [(i, n) for i, (n, _) in enumerate(rp.HET_LAWS)]
+    enum = re.search(r"enum HetSpc : int \{([^}]*)\}", src).group(1)
+    names = [x.strip().split("=")[0].strip()[3:] for x in enum.split(",") if x.strip()]
+    assert names[:-1] == rp.HET_SPECIES and names[-1] == "N"
+    assert rp.HET_SPECIES == gen_oracle.HET_SPECIES
+    assert {n: k for n, k in rp.HET_LAWS} == gen_oracle.HET_FUNCS
+    # every heterogeneous call of the fullchem Update_RCONST is one of them
+    from gcchem.mechanism import load_ir
+
+    calls = set()
+    for e in load_ir()["rconst"]:
+        calls |= {m for m in re.findall(r"([A-Za-z_]\w*)\(", e) if "(H)" in e or ",H)" in e}
+    het_calls = {c for c in calls if c not in {n for n, _ in rp.LAWS} and c not in ("exp", "log10")}
+    assert het_calls <= set(gen_oracle.HET_FUNCS)
+    assert len(het_calls) == 60
+
+
+def test_species_database_constants():
+    from gcchem.mechanism import species_db
+
+    d = species_db.load("fullchem")
+    i = d["species"].index
+    assert d["mw"][i("BrNO3")] == 141.91 and d["mw"][i("NO")] == 30.01
+    assert d["henry_k0"][i("HOBr")] == 1300.0 and d["henry_cr"][i("HOCl")] == 5900.0
+    assert all(m > 0 for m in d["mw"])
+
+
+def _oracle_rates(n, seed):
+    import gcchem.hetstate as hs
+    import gcchem.inputs as inputs
+    import oracle
+
+    cells = inputs.box_cells(n, seed=seed)
+    h = hs.het_cells(n, seed=seed + 100)
+    r = oracle.update_rconst(cells["met"], cells["photol"], cells["c"], het=h)
+    r0 = oracle.update_rconst(cells["met"], cells["photol"], cells["c"])
+    return cells, h, r, r0
+
+
+def test_oracle_het_rates_are_finite_and_switch_on():
+    from gcchem.mechanism import load_ir
+
+    ir = load_ir()
+    cells, h, r, r0 = _oracle_rates(256, 1)
+    het_rows = [i for i, e in enumerate(ir["rconst"]) if "H)" in e]
+    other = np.setdiff1d(np.arange(len(ir["rconst"])), het_rows)
+    assert np.array_equal(r[other], r0[other])  # gas-phase rates do not see the HetState
+    assert np.all(np.isfinite(r)) and np.all(r[het_rows] >= 0.0)
+    assert np.all(r0[het_rows] == 0.0)
+    on = (r[het_rows] > 0).mean(axis=1)
+    assert (on > 0).mean() > 0.9  # nearly every heterogeneous reaction is active somewhere
+
+
+def test_oracle_laws_against_fortran_formulas():
+    """A few laws recomputed here from the Fortran text (Ars_L1k,
+    kIIR1Ltd without its minimum-lifetime clamp, HBrUptkBySALA,
+    VOCuptk1stOrd, MGLYuptk1stOrd)."""
+    import gcchem.hetstate as hs
+    from gcchem.mechanism import load_ir, species_db
+
+    ir = load_ir()
+    cells, h, r, _ = _oracle_rates(64, 2)
+    sp = species_db.load("fullchem")
+    T = cells["met"][0]
+    nd = cells["met"][1]
+    h2o = cells["met"][2]
+    o = hs.OFFSET
+    srt = np.sqrt(T)
+
+    def ars(area, radius, gamma, srmw):
+        dfkg = (9.45e17 / nd) * srt * math.sqrt(3.472e-2 + 1.0 / (srmw * srmw))
+        k = area / ((radius / dfkg) + 2.749064e-4 * srmw / (gamma * srt))
+        return np.where((gamma < 1e-30) | (radius < 1e-30), 0.0, k)
+
+    def row(expr):
+        return ir["rconst"].index(expr)
+
+    strat = h[o["stratBox"]] != 0
+    srmw_hbr = math.sqrt(sp["mw"][sp["species"].index("HBr")])
+    area = h[o["clearFr"]] * h[o["aClArea"]]
+    ref = np.where(strat, 0.0, ars(area, h[o["aClRadi"]], 1.3e-8 * np.exp(4290.0 / T), srmw_hbr))
+    got = r[[i for i, e in enumerate(ir["rconst"]) if e == "(HBrUptkBySALA(H))"][0]]
+    assert np.allclose(got, ref, rtol=1e-13, atol=0)
+    # RELHUM of Set_Kpp_GridBox_Values
+    consvap = 6.1078e3 / (1.38064852e-23 * 1e7)
+    relhum = h2o / (consvap * np.exp(17.2693882 * (T - 273.16) / (T - 35.86)) / T) * 100.0
+    for i, e in enumerate(ir["rconst"]):
+        m = re.fullmatch(r"\(VOCuptk1stOrd\(SR_MW\[(\d+)\],([0-9.eE+-]+),H\)\)", e)
+        if m:
+            srmw = math.sqrt(sp["mw"][int(m.group(1))])
+            g = float(m.group(2))
+            k = sum(ars(h[o["xArea"] + t - 1], h[o["xRadi"] + t - 1], g, srmw) for t in (8, 9, 10, 11, 12, 13, 14))
+            assert np.allclose(r[i], np.where(relhum >= 35.0, k, 0.0), rtol=1e-12, atol=0), e
+        m = re.fullmatch(r"\(MGLYuptk1stOrd\(SR_MW\[(\d+)\],H\)\)", e)
+        if m:
+            srmw = math.sqrt(sp["mw"][int(m.group(1))])
+            k = ars(h[o["xArea"] + 7], h[o["xRadi"] + 7], 3.6e-7, srmw)
+            assert np.allclose(r[i], np.where(relhum >= 35.0, k, 0.0), rtol=1e-13, atol=0), e
+
+
+@pytest.mark.gpu
+def test_gpu_het_rates_match_oracle():
+    import gcchem.capi as capi
+
+    n = 4096
+    cells, h, r_ref, _ = _oracle_rates(n, 3)
+    s = capi.Solver(0, arith="fast")
+    r = np.zeros_like(r_ref)
+    s.update_rconst(cells["met"], cells["photol"], cells["c"], r, het=h)
+    assert np.array_equal(r == 0, r_ref == 0)
+    rel = np.abs(r - r_ref) / np.maximum(np.abs(r_ref), 1e-300)
+    assert np.max(rel) < 1e-12, np.max(rel)
+    # NULL HetState: the heterogeneous rates are 0, the rest unchanged
+    r0 = np.zeros_like(r_ref)
+    s.update_rconst(cells["met"], cells["photol"], cells["c"], r0)
+    from gcchem.mechanism import load_ir
+
+    het_rows = [i for i, e in enumerate(load_ir()["rconst"]) if "H)" in e]
+    assert np.all(r0[het_rows] == 0.0)
+    other = np.setdiff1d(np.arange(r.shape[0]), het_rows)
+    assert np.array_equal(r0[other], r[other])
+    s.close()
+
+
+@pytest.mark.gpu
+def test_gpu_step_with_het_rates_matches_oracle():
+    """Integration with the heterogeneous rates switched on: GPU (fast
+    arithmetic) against the oracle at the parity bar of the gas-phase case."""
+    import gcchem.capi as capi
+    import gcchem.inputs as inputs
+    import oracle
+
+    n = 256
+    cells, h, r_ref, _ = _oracle_rates(n, 4)
+    atol, rtol = inputs.tolerances()
+    ic, rc = inputs.default_controls()
+    c_ref, ist_ref, _, ierr_ref = oracle.integrate(cells["c"], r_ref, atol, rtol, 0.0, 600.0, ic, rc)
+    s = capi.Solver(0, arith="fast", schedule="queue")
+    r = np.zeros_like(r_ref)
+    s.update_rconst(cells["met"], cells["photol"], cells["c"], r, het=h)
+    c = cells["c"].copy()
+    ist = np.zeros((20, n), np.int32)
+    ierr = np.zeros(n, np.int32)
+    s.integrate(c, r, atol, rtol, 0.0, 600.0, ic, rc, istatus=ist, ierr=ierr)
+    assert np.array_equal(ierr, ierr_ref)
+    same = np.all(ist[:8] == ist_ref[:8], axis=0)
+    assert same.mean() >= 0.97
+    big = np.abs(c_ref[:353]) > 1e4
+    rel = np.abs(c[:353] - c_ref[:353]) / np.maximum(np.abs(c_ref[:353]), 1e-300)
+    assert np.max(np.where(big, rel, 0.0)[:, same]) < 1e-8
+    s.close()
