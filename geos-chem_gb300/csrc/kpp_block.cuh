@@ -211,7 +211,7 @@ __device__ void bk_solve(const MechDev& m, const double* G, double* X) {
 // pass computes, so the table reads overlap the arithmetic.  The sums are
 // regrouped, so the split form agrees with the thread-per-cell form to
 // rounding, not bit for bit.
-constexpr int SPLIT_MAXCH = 16;
+constexpr int SPLIT_MAXCH = 12;
 
 // Each phase is a functor: terms(item) is the term array of the item,
 // pre(item, z) a value loaded together with the task of the next pass (it
@@ -295,15 +295,18 @@ struct SplitJac {
 
 // Task of one lane in one pass: x = item | seglog << 16 | nterms << 19,
 // y = first term, z = the phase's finish word; item 0xFFFF is an idle lane.
+// With it travel the lane's term words, the functor's pre value and the
+// pass word.
 struct SplitTask {
   uint4 t;
   double pre;
+  unsigned info;
   unsigned w[SPLIT_MAXCH];
 };
 
+// Loads the term words and pre value of s.t (whose task word is known).
 template <class PH>
-__device__ __forceinline__ void split_fetch(const PH& f, const uint4* task, int idx, bool valid, SplitTask& s) {
-  s.t = valid ? __ldg(task + idx) : make_uint4(0xffffu, 0u, 0u, 0u);
+__device__ __forceinline__ void split_terms(const PH& f, SplitTask& s) {
   const int item = s.t.x & 0xffff;
   const int n = (s.t.x >> 19) & 31;
   const unsigned* t = f.terms(item) + s.t.y;
@@ -315,7 +318,9 @@ __device__ __forceinline__ void split_fetch(const PH& f, const uint4* task, int 
 // Runs the passes of one phase on the first sp_nt[ph] threads (32 or the
 // whole block; the host checks this).  A pass whose word has bit 3 set ends
 // with a barrier over those threads.  The caller adds the block barrier when
-// the phase used fewer threads than the block.
+// the phase used fewer threads than the block.  Loads run two passes ahead
+// for the task word and one pass ahead for what it points to, so a pass
+// waits on no chain of dependent loads.
 template <class PH>
 __device__ __forceinline__ void split_run(const MechDev& m, int ph, const PH& f) {
   const int nt = m.sp_nt[ph];
@@ -324,11 +329,17 @@ __device__ __forceinline__ void split_run(const MechDev& m, int ph, const PH& f)
   if (tid >= nt || np == 0) return;
   const uint4* task = m.sp_task[ph];
   const unsigned* pw = m.sp_pass[ph];
+  const uint4 idle = make_uint4(0xffffu, 0u, 0u, 0u);
   SplitTask cur, nxt;
-  split_fetch(f, task, tid, true, cur);
+  cur.t = __ldg(task + tid);
+  uint4 ahead = np > 1 ? __ldg(task + nt + tid) : idle;
+  split_terms(f, cur);
+  cur.info = __ldg(pw);
   for (int p = 0; p < np; ++p) {
-    split_fetch(f, task, (p + 1) * nt + tid, p + 1 < np, nxt);
-    const unsigned info = __ldg(pw + p);
+    nxt.t = ahead;
+    ahead = p + 2 < np ? __ldg(task + (p + 2) * nt + tid) : idle;
+    split_terms(f, nxt);
+    nxt.info = p + 1 < np ? __ldg(pw + p + 1) : 0u;
     const int item = cur.t.x & 0xffff;
     const int seg = 1 << ((cur.t.x >> 16) & 7);
     const int n = (cur.t.x >> 19) & 31;
@@ -337,12 +348,12 @@ __device__ __forceinline__ void split_run(const MechDev& m, int ph, const PH& f)
 #pragma unroll
     for (int k = 0; k < SPLIT_MAXCH; ++k)
       if (k < n) acc = f.term(item, (int)cur.t.y + k, cur.w[k], acc);
-    for (int o = (1 << (info & 7)) >> 1; o > 0; o >>= 1) {
+    for (int o = (1 << (cur.info & 7)) >> 1; o > 0; o >>= 1) {
       const double v = __shfl_xor_sync(0xffffffffu, acc, o);
       if (o < seg) acc += v;
     }
     if (lead) f.finish(item, cur.t.z, acc);
-    if (info & 8u) {
+    if (cur.info & 8u) {
       if (nt == 32)
         __syncwarp();
       else

@@ -44,7 +44,7 @@ NOCOEF = 0x7FF
 SPLIT_NT = 256
 SPLIT_PHASE_NT = {"lu": 256, "fs": 32, "bs": 32, "fun": 256, "jac": 256}
 SPLIT_CHUNK = 8
-SPLIT_MAXCH = 16  # register slots of a lane's chunk in the kernel
+SPLIT_MAXCH = 12  # register slots of a lane's chunk in the kernel
 
 
 def _hexfloat(x):
