@@ -47,6 +47,7 @@ EXPORTED = [
     "gc_kpp_integrate_batch",
     "gc_kpp_update_rconst_batch",
     "gc_kpp_update_rconst_het_batch",
+    "gc_kpp_ctx_set_hetstate",
     "gc_kpp_fullchem_step",
     "gc_kpp_fullchem_step_ordered",
     "gc_kpp_fullchem_step_binned",
@@ -86,6 +87,7 @@ def load_library(path=None, mech="fullchem"):
                                            vp, i32, vp]
     lib.gc_kpp_update_rconst_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, vp, i64, i32, vp]
     lib.gc_kpp_update_rconst_het_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64, i32, vp]
+    lib.gc_kpp_ctx_set_hetstate.argtypes = [vp, i32, vp, i64, i32]
     if path == _build.lib_path(mech):
         _libs[mech] = lib
     return lib
@@ -258,6 +260,21 @@ class Solver:
             ctypes.byref(nretry), ctypes.byref(nblock), MEM_DEVICE if dev else MEM_HOST, s)
         self._check(rc)
         return nretry.value, nblock.value
+
+    def set_hetstate(self, het):
+        """HetState rows [168, ncell] (numpy: copied; torch CUDA: kept by
+        pointer) used by the following chemistry steps; None clears it."""
+        if het is None:
+            self._check(self.lib.gc_kpp_ctx_set_hetstate(self.ctx, 0, None, 0, MEM_HOST))
+            self._het = None
+            return
+        dev = _is_torch(het) and het.is_cuda
+        if not dev:
+            het = np.ascontiguousarray(het, dtype=np.float64)
+        n = het.shape[1]
+        self._check(self.lib.gc_kpp_ctx_set_hetstate(self.ctx, n, _ptr(het), _ld(het, n),
+                                                     MEM_DEVICE if dev else MEM_HOST))
+        self._het = het if dev else None
 
     def update_rconst(self, met, photol, c, rconst, stream=None, het=None):
         """Batched Update_RCONST.  met: [NMET, ncell]; photol: [200, ncell];

@@ -115,6 +115,11 @@ struct gc_kpp_ctx {
   DevBuf ws, counter;
   DevBuf h_c, h_r, h_at, h_rt, h_hs, h_is, h_rs, h_ie;  // staging for host-memory calls
   DevBuf h_met, h_ph, h_ord, h_het;
+  // HetState of the chemistry steps (gc_kpp_ctx_set_hetstate): device rows
+  DevBuf step_het;
+  const double* het = nullptr;
+  long long het_ld = 0;
+  int het_ncell = 0;
   DevBuf rc_buf, cb_buf, ord_buf;  // chemistry-step scratch: RCONST, C_before, retry list
   int last_launches = 0;
   // optional CUDA-event timing of the Rosenbrock launches (GC_KPP_OPT_TIMING)
@@ -245,7 +250,7 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
                     &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
                     &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges, &c->evict_buf, &c->bws,
-                    &c->h_het};
+                    &c->h_het, &c->step_het};
   for (DevBuf* b : bufs) b->release();
   delete c;
   return GC_KPP_OK;
@@ -830,6 +835,11 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
   gcrates::RatesArgs ra{};
   ra.ncell = ncell; ra.met = dmet; ra.ldm = lm; ra.photol = dph; ra.ldp = lp; ra.c = dc; ra.ldc = lc;
   ra.rconst = drc; ra.ldr = ncell;
+  if (c->het) {
+    if (c->het_ncell != ncell) return fail(GC_KPP_EINVAL, "HetState was set for a different number of cells");
+    ra.het = c->het;
+    ra.ldh = c->het_ld;
+  }
   cudaError_t e = gcrates::launch_rates(c->rates, ra, s);
   if (e != cudaSuccess) return cuda_fail(e, "rates kernel launch");
   c->last_launches = 1;
@@ -962,6 +972,31 @@ int gc_kpp_last_kernel_ms(gc_kpp_ctx* c, double* ms, int* nlaunch) {
   *ms = total;
   if (nlaunch) *nlaunch = c->ntimed;
   c->ntimed = 0;
+  return GC_KPP_OK;
+}
+
+int gc_kpp_ctx_set_hetstate(gc_kpp_ctx* c, int ncell, const double* het, long long ldh, int mem) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  if (!het) {
+    c->het = nullptr;
+    c->het_ncell = 0;
+    return GC_KPP_OK;
+  }
+  if (ncell <= 0 || ldh < ncell) return fail(GC_KPP_EINVAL, "bad ncell or leading dimension");
+  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  GC_CUDA(cudaSetDevice(c->device));
+  if (mem == GC_KPP_MEM_DEVICE) {
+    c->het = het;
+    c->het_ld = ldh;
+  } else {
+    const size_t n = (size_t)ncell;
+    GC_CUDA(c->step_het.ensure((size_t)HET_NFIELD * n * sizeof(double)));
+    GC_CUDA(cudaMemcpy2D(c->step_het.p, n * sizeof(double), het, ldh * sizeof(double), n * sizeof(double),
+                         HET_NFIELD, cudaMemcpyHostToDevice));
+    c->het = (const double*)c->step_het.p;
+    c->het_ld = ncell;
+  }
+  c->het_ncell = ncell;
   return GC_KPP_OK;
 }
 

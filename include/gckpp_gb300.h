@@ -184,6 +184,14 @@ int gc_kpp_update_rconst_batch(gc_kpp_ctx* ctx, int ncell, const double* met, lo
  * species database and RELHUM from TEMP and H2O as Set_Kpp_GridBox_Values
  * computes it.  Mechanisms other than fullchem keep their heterogeneous
  * rates at 0. */
+/* HetState of the cells of the following chemistry steps on this context
+ * (gc_kpp_fullchem_step and its ordered/binned/learned forms evaluate the
+ * heterogeneous rates from it): het [GC_KPP_NHET][ldh] for `ncell` cells, in
+ * device memory (kept by pointer: the caller keeps it alive and up to date)
+ * or host memory (copied now).  het = NULL clears it (heterogeneous rates 0).
+ * A step over a different number of cells fails with GC_KPP_EINVAL. */
+int gc_kpp_ctx_set_hetstate(gc_kpp_ctx* ctx, int ncell, const double* het, long long ldh, int mem);
+
 int gc_kpp_update_rconst_het_batch(gc_kpp_ctx* ctx, int ncell, const double* met, long long ldm,
                                    const double* photol, long long ldp, const double* c, long long ldc,
                                    const double* het, long long ldh, double* rconst, long long ldr, int mem,

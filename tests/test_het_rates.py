@@ -136,6 +136,85 @@ def test_oracle_laws_against_fortran_formulas():
             assert np.allclose(r[i], np.where(relhum >= 35.0, k, 0.0), rtol=1e-13, atol=0), e
 
 
+def _het_calls(ir):
+    """(rconst row, law id, numeric arguments) of every heterogeneous call; a
+    concentration argument C(i) is encoded as -1-i."""
+    import gcchem.rates_program as rp
+    from gcchem.mechanism import species_db
+
+    sp = species_db.load(ir.get("mechanism", "fullchem"))
+    out = []
+    for i, e in enumerate(ir["rconst"]):
+        for m in re.finditer(r"(\w+)\(([^()]*)\)", e):
+            if m.group(1) not in rp.HET_ID:
+                continue
+            vals = []
+            for a in m.group(2).split(",")[:-1]:
+                mm = re.fullmatch(r"SR_MW\[(\d+)\]", a)
+                mc = re.fullmatch(r"C\[(\d+)\]", a)
+                vals.append(math.sqrt(sp["mw"][int(mm.group(1))]) if mm else
+                            -1.0 - int(mc.group(1)) if mc else float(a))
+            out.append((i, rp.HET_ID[m.group(1)][0], vals + [0.0] * (3 - len(vals))))
+    return out
+
+
+def test_gpu_laws_equal_oracle_on_the_same_libm(tmp_path):
+    """The GPU laws of csrc/het_rates.cuh, built for the host (g++, glibc's
+    math), give the oracle's rates bit for bit: the two restatements perform
+    the same arithmetic, so every GPU/oracle difference comes from CUDA's
+    libm (checked on the GPU below)."""
+    import shutil
+    import subprocess
+
+    import gcchem.rates_program as rp
+    from gcchem.mechanism import load_ir
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    ir = load_ir()
+    n = 1024
+    cells, h, r_ref, _ = _oracle_rates(n, 3)
+    prog = rp.build_program(ir)
+    (tmp_path / "fake").mkdir()
+    (tmp_path / "fake" / "cuda_runtime.h").write_text("#pragma once\n")
+    exe = str(tmp_path / "harness")
+    subprocess.check_call([gxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", str(tmp_path / "fake"), "-I", CSRC,
+                           os.path.join(ROOT, "tests", "host", "het_laws_host.cpp"), "-o", exe])
+    for name, arr in (("met", cells["met"]), ("c", cells["c"]), ("het", h)):
+        np.ascontiguousarray(arr, np.float64).tofile(str(tmp_path / (name + ".bin")))
+    for name, key in (("hsind", "hs_ind"), ("hsmw", "hs_mw"), ("hssr", "hs_srmw"), ("hsk0", "hs_hk0"),
+                      ("hscr", "hs_hcr")):
+        np.array(prog[key], np.float64).tofile(str(tmp_path / (name + ".bin")))
+    calls = _het_calls(ir)
+    np.array([[k] + v for _, k, v in calls], np.float64).tofile(str(tmp_path / "calls.bin"))
+    subprocess.check_call([exe, str(n), str(len(ir["species"])), str(len(calls))], cwd=str(tmp_path))
+    out = np.fromfile(str(tmp_path / "out.bin")).reshape(len(calls), n)
+    met = cells["met"]
+    for k, (i, _, _) in enumerate(calls):
+        e = ir["rconst"][i]
+        if "+" in e:  # (HOClUptkByHSO3m(H)+HOClUptkBySO3mm(H)+SRHOCl): check the sum
+            ks = [q for q, c in enumerate(calls) if c[0] == i]
+            if k != ks[0]:
+                continue
+            extra = met[4] if "SRHOCl" in e else met[5]
+            got = out[ks[0]] + out[ks[1]] + extra
+        else:
+            got = out[k]
+        assert np.array_equal(got, r_ref[i]), e
+
+
+def _ulp_sensitivity(cells, h, r_ref):
+    """How much the oracle's rates move when TEMP moves by 2 ulp: the
+    conditioning of the reference's formulas at each cell."""
+    import oracle
+
+    met = cells["met"].copy()
+    met[0] *= 1.0 + 4.4e-16
+    r2 = oracle.update_rconst(met, cells["photol"], cells["c"], het=h)
+    return np.abs(r2 - r_ref) / np.maximum(np.abs(r_ref), 1e-300)
+
+
 @pytest.mark.gpu
 def test_gpu_het_rates_match_oracle():
     import gcchem.capi as capi
@@ -147,7 +226,14 @@ def test_gpu_het_rates_match_oracle():
     s.update_rconst(cells["met"], cells["photol"], cells["c"], r, het=h)
     assert np.array_equal(r == 0, r_ref == 0)
     rel = np.abs(r - r_ref) / np.maximum(np.abs(r_ref), 1e-300)
-    assert np.max(rel) < 1e-12, np.max(rel)
+    # CUDA's exp/log10/pow differ from glibc's in the last bit; a few rates
+    # are ill-conditioned in the reference's own formulas (CloudHet's
+    # (ff-kk-1)/2 + sqrt(...)/2 cancels when kk >> ff), where those bits grow
+    # to ~1e-3 -- the same spread a 2-ulp change of TEMP gives the oracle
+    sens = _ulp_sensitivity(cells, h, r_ref)
+    loose = rel > 1e-12
+    assert loose.mean() < 1e-3, loose.mean()
+    assert np.all(rel[loose] <= np.maximum(100.0 * sens[loose], 1e-9)), np.max(rel)
     # NULL HetState: the heterogeneous rates are 0, the rest unchanged
     r0 = np.zeros_like(r_ref)
     s.update_rconst(cells["met"], cells["photol"], cells["c"], r0)
@@ -172,10 +258,11 @@ def test_gpu_step_with_het_rates_matches_oracle():
     cells, h, r_ref, _ = _oracle_rates(n, 4)
     atol, rtol = inputs.tolerances()
     ic, rc = inputs.default_controls()
-    c_ref, ist_ref, _, ierr_ref = oracle.integrate(cells["c"], r_ref, atol, rtol, 0.0, 600.0, ic, rc)
     s = capi.Solver(0, arith="fast", schedule="queue")
     r = np.zeros_like(r_ref)
     s.update_rconst(cells["met"], cells["photol"], cells["c"], r, het=h)
+    # the same rates on both sides (the rates' own parity is the test above)
+    c_ref, ist_ref, _, ierr_ref = oracle.integrate(cells["c"], r, atol, rtol, 0.0, 600.0, ic, rc)
     c = cells["c"].copy()
     ist = np.zeros((20, n), np.int32)
     ierr = np.zeros(n, np.int32)
@@ -186,4 +273,59 @@ def test_gpu_step_with_het_rates_matches_oracle():
     big = np.abs(c_ref[:353]) > 1e4
     rel = np.abs(c[:353] - c_ref[:353]) / np.maximum(np.abs(c_ref[:353]), 1e-300)
     assert np.max(np.where(big, rel, 0.0)[:, same]) < 1e-8
+    s.close()
+
+
+@pytest.mark.gpu
+def test_gpu_chemistry_step_with_hetstate_matches_oracle():
+    """gc_kpp_ctx_set_hetstate: the one-call chemistry step (family zeroing,
+    rates with the HetState, integration, retry, clamp) against the oracle's
+    Do_FullChem loop body with the same heterogeneous rates (strict
+    arithmetic: the parity bar of the gas-phase step)."""
+    import gcchem.capi as capi
+    import gcchem.hetstate as hs
+    import gcchem.inputs as inputs
+    import oracle
+    from gcchem.mechanism import load_ir
+
+    ir = load_ir()
+    n = 192
+    cells = inputs.box_cells(n, seed=21)
+    h = hs.het_cells(n, seed=22)
+    atol, rtol = inputs.tolerances()
+    ic, rc = inputs.default_controls()
+    c = cells["c"].copy()
+    for fam in ir["families"]:
+        c[ir["species"].index(fam)] = 0.0
+    s = capi.Solver(0, arith="strict", schedule="queue")
+    # the step's rates are the GPU's (compared with the oracle's above); the
+    # oracle integrates with the same rates
+    r = np.zeros((len(ir["rconst"]), n))
+    s.update_rconst(cells["met"], cells["photol"], c, r, het=h)
+    r_o = oracle.update_rconst(cells["met"], cells["photol"], c, het=h)
+    assert np.allclose(r, r_o, rtol=1e-2, atol=0)
+    c_ref, ist_ref, _, ierr_ref = oracle.integrate(c, r, atol, rtol, 0.0, 600.0, ic, rc)
+    bad = ierr_ref < 0
+    if bad.any():
+        c2, ist2, _, ierr2 = oracle.integrate(c[:, bad], r[:, bad], atol, rtol, 0.0, 600.0, ic, rc)
+        c_ref[:, bad], ist_ref[:, bad], ierr_ref[bad] = c2, ist2, ierr2
+    c_ref = np.maximum(c_ref, 0.0)
+
+    s.set_hetstate(h)
+    cg = cells["c"].copy()
+    ist = np.zeros((20, n), np.int32)
+    rst = np.zeros((20, n))
+    ierr = np.zeros(n, np.int32)
+    s.fullchem_step(600.0, cells["met"], cells["photol"], cg, atol, rtol, ic, rc, None, ist, rst, ierr)
+    assert np.array_equal(ierr, ierr_ref)
+    same = np.all(ist[:8] == ist_ref[:8], axis=0)
+    assert same.mean() >= 0.99
+    big = np.abs(c_ref) > 1e4
+    rel = np.abs(cg - c_ref) / np.maximum(np.abs(c_ref), 1e-300)
+    assert np.max(np.where(big, rel, 0.0)[:, same]) < 1e-9
+    # a step over another number of cells is refused while the HetState is set
+    with pytest.raises(capi.GcKppError):
+        s.fullchem_step(600.0, cells["met"][:, :8].copy(), cells["photol"][:, :8].copy(), cg[:, :8].copy(),
+                        atol, rtol, ic, rc)
+    s.set_hetstate(None)
     s.close()
