@@ -205,14 +205,18 @@ def test_gpu_laws_equal_oracle_on_the_same_libm(tmp_path):
 
 
 def _ulp_sensitivity(cells, h, r_ref):
-    """How much the oracle's rates move when TEMP moves by 2 ulp: the
-    conditioning of the reference's formulas at each cell."""
+    """How much the oracle's rates move when TEMP or NUMDEN move by a few
+    ulp (the largest of three such changes): the conditioning of the
+    reference's formulas at each cell."""
     import oracle
 
-    met = cells["met"].copy()
-    met[0] *= 1.0 + 4.4e-16
-    r2 = oracle.update_rconst(met, cells["photol"], cells["c"], het=h)
-    return np.abs(r2 - r_ref) / np.maximum(np.abs(r_ref), 1e-300)
+    out = np.zeros_like(r_ref)
+    for row, fac in ((0, 1.0 + 4.4e-16), (0, 1.0 - 4.4e-16), (1, 1.0 + 4.4e-16)):
+        met = cells["met"].copy()
+        met[row] *= fac
+        r2 = oracle.update_rconst(met, cells["photol"], cells["c"], het=h)
+        out = np.maximum(out, np.abs(r2 - r_ref) / np.maximum(np.abs(r_ref), 1e-300))
+    return out
 
 
 @pytest.mark.gpu
@@ -226,14 +230,16 @@ def test_gpu_het_rates_match_oracle():
     s.update_rconst(cells["met"], cells["photol"], cells["c"], r, het=h)
     assert np.array_equal(r == 0, r_ref == 0)
     rel = np.abs(r - r_ref) / np.maximum(np.abs(r_ref), 1e-300)
-    # CUDA's exp/log10/pow differ from glibc's in the last bit; a few rates
-    # are ill-conditioned in the reference's own formulas (CloudHet's
+    # CUDA's exp/log10/pow differ from glibc's in the last bit (the host
+    # build of these laws equals the oracle bit for bit, test above).  A few
+    # rates are ill-conditioned in the reference's own formulas (CloudHet's
     # (ff-kk-1)/2 + sqrt(...)/2 cancels when kk >> ff), where those bits grow
-    # to ~1e-3 -- the same spread a 2-ulp change of TEMP gives the oracle
+    # to ~1e-3: the GPU's spread must stay within what a few-ulp change of
+    # TEMP or NUMDEN does to the oracle itself.
     sens = _ulp_sensitivity(cells, h, r_ref)
-    loose = rel > 1e-12
-    assert loose.mean() < 1e-3, loose.mean()
-    assert np.all(rel[loose] <= np.maximum(100.0 * sens[loose], 1e-9)), np.max(rel)
+    for thr in (1e-12, 1e-9, 1e-6):
+        assert (rel > thr).mean() <= 3.0 * (sens > thr).mean() + 1e-5, (thr, (rel > thr).mean(), (sens > thr).mean())
+    assert rel.max() <= 10.0 * sens.max() + 1e-9, (rel.max(), sens.max())
     # NULL HetState: the heterogeneous rates are 0, the rest unchanged
     r0 = np.zeros_like(r_ref)
     s.update_rconst(cells["met"], cells["photol"], cells["c"], r0)
