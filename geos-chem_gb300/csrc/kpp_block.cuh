@@ -12,10 +12,13 @@
 // each phase run in parallel (products, Fun_SPLIT rows, Jac_SP entries, the
 // stage vectors), and the LU factorization and the two substitutions run in
 // dependency levels (tables.py _level_schedules) with a barrier between
-// levels.  Every item is evaluated by one thread with exactly the operations
-// and order of the thread-per-cell engine (kpp_mech.cuh), and the error norm
-// is summed by one thread in species order, so both forms give the same
-// numbers for a cell.  A block of 32 threads is the warp-per-cell layout.
+// levels.  In this level form every item is evaluated by one thread with
+// exactly the operations and order of the thread-per-cell engine
+// (kpp_mech.cuh), and the error norm is summed by one thread in species
+// order, so both engines give the same numbers for a cell.  A block of 32
+// threads is the warp-per-cell layout.  The split form (SPLIT = true, fast
+// arithmetic, 256 threads; below) cuts each sum across the lanes of a warp
+// segment instead and agrees with the thread-per-cell engine to rounding.
 #pragma once
 #include <climits>
 
