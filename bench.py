@@ -36,7 +36,11 @@ METRIC = "fullchem cells/s per 1200 s step, learned-binned vs plain GPU, at RTOL
 GRID = (72, 46, 72)
 DT = 1200.0
 SPINUP_S = 86400.0
-EVICT_LEARNED = 2  # hand-over after 2 steps in the learned arms (best of the sweep)
+# hand-over point of the learned arms, best of a sweep over k = 1-4 on this
+# grid: from a cold start k = 2 (762k cells/s; k = 1 468k, k = 3 747k), on the
+# KPPHvalue chain k = 1 (1.15M cells/s; k = 2 964k, k = 3 855k)
+EVICT_LEARNED = 2
+EVICT_LEARNED_CHAINED = 1
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "geos-chem_gb300", "weights", "proposer_fullchem.npz")
 
 
@@ -282,11 +286,11 @@ def run_ours(args):
             step(w, hs)
         return arm
 
-    def learned_arm(w, hs, met_=met, ph_=ph, tt=dev_t):
+    def learned_arm(w, hs, met_=met, ph_=ph, tt=dev_t, evict=EVICT_LEARNED):
         # H0 proposals seed RCNTRL(3) where the cell has no KPPHvalue yet;
         # stiffness bins order the queue and the top bin goes block-per-cell;
-        # cells the network missed are handed over after EVICT_LEARNED steps
-        solver.set(evict_after=EVICT_LEARNED)
+        # cells the network missed are handed over after `evict` steps
+        solver.set(evict_after=evict)
         _, _, order = learned.plan(prop, met_, ph_, w, stream=sp, hstart=hs, hmax=DT)
         nheavy = int(prop.last_counts[learned.NBIN - 1].item())
         last["nblock"] = nheavy
@@ -299,7 +303,8 @@ def run_ours(args):
     arms = {"plain": (plain_arm, 0, cold0), "handover": (handover_arm(16), 0, cold0),
             "learned": (learned_arm, learned.PLAN_LAUNCHES, cold0),
             "plain_chained": (plain_arm, 0, hs_spun), "handover_chained": (handover_arm(2), 0, hs_spun),
-            "learned_chained": (learned_arm, learned.PLAN_LAUNCHES, hs_spun)}
+            "learned_chained": (lambda w, hs: learned_arm(w, hs, evict=EVICT_LEARNED_CHAINED),
+                                learned.PLAN_LAUNCHES, hs_spun)}
 
     def time_arm(name):
         fn, extra, hs0 = arms[name]

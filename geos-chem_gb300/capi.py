@@ -37,6 +37,7 @@ OPT_ASYNC = 9
 OPT_EVICT_AFTER = 10
 OPT_EVICT_DRAINED = 11
 OPT_BLOCK_SPLIT = 12
+OPT_RATES_DIRECT = 13
 
 EXPORTED = [
     "gc_kpp_mechanism_dims",
@@ -136,7 +137,7 @@ class Solver:
             raise GcKppError(rc, self.lib.gc_kpp_last_error().decode())
 
     def set(self, arith=None, schedule=None, block=None, blocks_per_sm=None, max_slots=None, cell_block=None,
-            async_steps=None, evict_after=None, evict_drained=None, block_split=None):
+            async_steps=None, evict_after=None, evict_drained=None, block_split=None, rates_direct=None):
         if arith is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1, "fast2": 2, "fast4": 3}[arith]))
         if schedule is not None:
@@ -157,6 +158,8 @@ class Solver:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ASYNC, 1 if async_steps else 0))
         if block_split is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_BLOCK_SPLIT, 1 if block_split else 0))
+        if rates_direct is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_RATES_DIRECT, 1 if rates_direct else 0))
 
     def close(self):
         if self.ctx:

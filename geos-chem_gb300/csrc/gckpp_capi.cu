@@ -18,7 +18,9 @@
 #include "mech_tables.inc"  // generated per mechanism (csrc/_gen/<mechanism>/)
 #include "rates_program.inc"
 #include "het_layout.h"
+#include "het_rates.cuh"
 #include "kpp_rates.h"
+#include "rate_laws.cuh"
 #include "kpp_launch.h"
 #include "kpp_util.h"
 #include "kpp_block.cuh"
@@ -28,6 +30,56 @@
 using namespace gckpp;
 namespace T = gcmech_tables;
 namespace RT = gcrates_tables;
+
+// Update_RCONST as straight-line code of this mechanism's rate program
+// (rates_direct.inc, gcchem.rates_program emit_direct): the operations of
+// gcrates::rates_kernel in the same order, without its opcode dispatch and
+// local-memory stack; same results bit for bit.
+namespace gcrates {
+template <typename... A>
+__device__ __forceinline__ double lawv(int id, const Env& E, A... v) {
+  const double t[] = {double(v)...};
+  return law(id, t, E);
+}
+template <typename... A>
+__device__ __forceinline__ double hetv(int id, bool has_het, const HetCell& X, A... v) {
+  if (!has_het) return 0.0;
+  const double t[] = {double(v)..., 0.0};
+  return het_law(id, t, X);
+}
+
+__global__ void __launch_bounds__(128) rates_direct_kernel(RatesDev rp, RatesArgs a) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= a.ncell) return;
+#define M(f) a.met[(long long)(f) * a.ldm + cell]
+#define PH(j) a.photol[(long long)(j) * a.ldp + cell]
+#define CC(i) a.c[(long long)(i) * a.ldc + cell]
+#define OUT(r) a.rconst[(long long)(r) * a.ldr + cell]
+  Env E;
+  env_init(E, M(0), M(1), M(2), M(3), M(4), M(5));
+  const bool has_het = a.het != nullptr;
+  HetCell X;
+  X.H = a.het;
+  X.ldh = a.ldh;
+  X.C = a.c;
+  X.ldc = a.ldc;
+  X.cell = cell;
+  X.sp = HetSpecies{rp.hs_ind, rp.hs_mw, rp.hs_srmw, rp.hs_hk0, rp.hs_hcr};
+  if (has_het) het_cell_init(X, E);
+#include "rates_direct.inc"
+#undef M
+#undef PH
+#undef CC
+#undef OUT
+}
+
+cudaError_t launch_rates_direct(const RatesDev& rp, const RatesArgs& a, cudaStream_t s) {
+  const int block = 128;
+  const int grid = (a.ncell + block - 1) / block;
+  if (grid > 0) rates_direct_kernel<<<grid, block, 0, s>>>(rp, a);
+  return cudaGetLastError();
+}
+}  // namespace gcrates
 
 namespace {
 
@@ -144,6 +196,7 @@ struct gc_kpp_ctx {
   int block = 128;
   int cell_block = 256;  // threads of the block-per-cell kernel
   int block_split = 1;   // fast arithmetic: the split block-per-cell form
+  int rates_direct = 1;  // Update_RCONST as straight-line code (0: the interpreter)
   cudaStream_t side = nullptr;  // block-per-cell launches run beside the queue kernel
   cudaEvent_t fork = nullptr, join = nullptr;
   int blocks_per_sm = 0;
@@ -301,6 +354,10 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
       if (v < 32 || v > 1024 || v % 32)
         return fail(GC_KPP_EINVAL, "block-per-cell threads must be a multiple of 32 in [32,1024]");
       c->cell_block = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_RATES_DIRECT:
+      if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "rates-direct must be 0 or 1");
+      c->rates_direct = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_BLOCK_SPLIT:
       if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "block-split must be 0 or 1");
@@ -840,7 +897,7 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
     ra.het = c->het;
     ra.ldh = c->het_ld;
   }
-  cudaError_t e = gcrates::launch_rates(c->rates, ra, s);
+  cudaError_t e = c->rates_direct ? gcrates::launch_rates_direct(c->rates, ra, s) : gcrates::launch_rates(c->rates, ra, s);
   if (e != cudaSuccess) return cuda_fail(e, "rates kernel launch");
   c->last_launches = 1;
   if (R.code && async) {
@@ -1057,7 +1114,7 @@ int gc_kpp_update_rconst_het_batch(gc_kpp_ctx* c, int ncell, const double* met, 
     a.rconst = rconst;
     a.ldr = ldr;
   }
-  cudaError_t e = gcrates::launch_rates(c->rates, a, s);
+  cudaError_t e = c->rates_direct ? gcrates::launch_rates_direct(c->rates, a, s) : gcrates::launch_rates(c->rates, a, s);
   if (e != cudaSuccess) return cuda_fail(e, "rates kernel launch");
   if (mem == GC_KPP_MEM_HOST) {
     GC_CUDA(cudaMemcpy2DAsync(rconst, ldr * sizeof(double), a.rconst, n * sizeof(double), n * sizeof(double),

@@ -1122,7 +1122,7 @@ __device__ __forceinline__ double VOCuptk1stOrd(const HetCell& X, double srMw, d
 
 // Heterogeneous rate law `id` (gcchem.rates_program HET_LAWS order) with its
 // numeric arguments a[] (the HetState argument H is implicit).
-__device__ __noinline__ double het_law(int id, const double* a, const HetCell& X) {
+static __device__ __noinline__ double het_law(int id, const double* a, const HetCell& X) {
   switch (id) {
     case 0: return BrNO3uptkByH2O(X);  // BrNO3uptkByH2O
     case 1: return BrNO3uptkByHCl(X);  // BrNO3uptkByHCl

@@ -73,7 +73,7 @@ __device__ __forceinline__ double pan(double k0, double k1, const Env& E, double
 
 // Evaluate law `id` (index into the law list of gcchem.rates_program) on
 // arguments a[0..nargs).
-__device__ double law(int id, const double* a, const Env& E) {
+__device__ __forceinline__ double law(int id, const double* a, const Env& E) {
   const double T = E.TEMP;
   switch (id) {
     case 0: return a[0] * pow(E.K300_OVER_TEMP, a[1]);                                   // GCARR_ab

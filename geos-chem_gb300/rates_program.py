@@ -287,10 +287,82 @@ def emit_c(prog):
 def write_generated(outdir, ir=None):
     prog = build_program(ir)
     os.makedirs(outdir, exist_ok=True)
-    path = os.path.join(outdir, "rates_program.inc")
-    text = emit_c(prog)
-    old = open(path).read() if os.path.exists(path) else None
-    if old != text:
-        with open(path, "w") as fh:
-            fh.write(text)
-    return path
+    for name, text in (("rates_program.inc", emit_c(prog)), ("rates_direct.inc", emit_direct(prog))):
+        path = os.path.join(outdir, name)
+        old = open(path).read() if os.path.exists(path) else None
+        if old != text:
+            with open(path, "w") as fh:
+                fh.write(text)
+    return os.path.join(outdir, "rates_program.inc")
+
+
+def emit_direct(prog):
+    """Straight-line CUDA statements of the same postfix program (one
+    expression per rate, operations in the program's order, additions and
+    multiplications through the round-to-nearest intrinsics so that nothing
+    is contracted): the body of the per-mechanism rates_direct_kernel
+    (gckpp_capi.cu), which gives the interpreter's results bit for bit
+    without its dispatch and local-memory stack.  Uses the kernel's macros
+    M(f) (met row), PH(j), CC(i), OUT(r) and the functions lawv/hetv."""
+    code, start, consts = prog["code"], prog["start"], prog["consts"]
+    nargs = {i: k for i, (_, k) in enumerate(LAWS)}
+    hnargs = {i: k for i, (_, k) in enumerate(HET_LAWS)}
+    lines = ["// Generated by gcchem.rates_program (emit_direct). Do not edit."]
+    ntmp = 0
+    for r in range(len(start) - 1):
+        st = []
+        pc = start[r]
+        while True:
+            op = OPS[code[pc]]
+            pc += 1
+            if op == "END":
+                break
+            if op == "CONST":
+                st.append(float(consts[code[pc]]).hex())
+                pc += 1
+            elif op == "VAR":
+                st.append("M(%d)" % code[pc])
+                pc += 1
+            elif op == "PHOTOL":
+                st.append("PH(%d)" % code[pc])
+                pc += 1
+            elif op == "CONC":
+                st.append("CC(%d)" % code[pc])
+                pc += 1
+            elif op in ("ADD", "SUB", "MUL", "DIV"):
+                b, a = st.pop(), st.pop()
+                if op == "DIV":
+                    st.append("(%s / %s)" % (a, b))
+                else:
+                    st.append("__d%s_rn(%s, %s)" % ({"ADD": "add", "SUB": "sub", "MUL": "mul"}[op], a, b))
+            elif op == "NEG":
+                st.append("(-%s)" % st.pop())
+            elif op in ("EXP", "LOG10"):
+                st.append("%s(%s)" % (op.lower(), st.pop()))
+            elif op == "CALL":
+                lid = code[pc]
+                pc += 1
+                k = nargs[lid]
+                args = st[len(st) - k:]
+                del st[len(st) - k:]
+                lines.append("  const double x%d = lawv(%d, E, %s);" % (ntmp, lid, ", ".join(args)))
+                st.append("x%d" % ntmp)
+                ntmp += 1
+            elif op == "HETZERO":
+                st.append("0.0")
+            elif op == "HET":
+                hid = code[pc]
+                pc += 1
+                k = hnargs[hid]
+                args = st[len(st) - k:] if k else []
+                if k:
+                    del st[len(st) - k:]
+                lines.append("  const double x%d = hetv(%d, has_het, X%s);" % (
+                    ntmp, hid, "".join(", " + a for a in args)))
+                st.append("x%d" % ntmp)
+                ntmp += 1
+            else:
+                raise ValueError(op)
+        assert len(st) == 1, r
+        lines.append("  OUT(%d) = %s;" % (r, st[0]))
+    return "\n".join(lines) + "\n"

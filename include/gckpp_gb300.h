@@ -74,6 +74,9 @@ extern "C" {
                                      agree with the thread-per-cell form to rounding.  0 = the
                                      level form (GC_KPP_OPT_CELL_BLOCK threads, each sum in one
                                      thread, results identical to the thread-per-cell form). */
+#define GC_KPP_OPT_RATES_DIRECT 13 /* 1 = Update_RCONST runs as straight-line code generated
+                                      from the mechanism's rate program (default); 0 = the
+                                      rate-program interpreter.  Same results bit for bit. */
 #define GC_KPP_OPT_ASYNC 9        /* 1 = chemistry steps never synchronise the host, so that a
                                      caller can capture them in a CUDA graph: the retry list and
                                      the block-per-cell count stay on the device, *nretry (and

@@ -335,3 +335,25 @@ def test_gpu_chemistry_step_with_hetstate_matches_oracle():
                         atol, rtol, ic, rc)
     s.set_hetstate(None)
     s.close()
+
+
+@pytest.mark.gpu
+def test_direct_rates_kernel_equals_interpreter():
+    """GC_KPP_OPT_RATES_DIRECT: the generated straight-line Update_RCONST
+    gives the rate-program interpreter's results bit for bit, with and
+    without a HetState."""
+    import gcchem.capi as capi
+
+    n = 2048
+    cells, h, _, _ = _oracle_rates(n, 5)
+    s = capi.Solver(0, arith="fast")
+    out = {}
+    for direct in (False, True):
+        s.set(rates_direct=direct)
+        for het in (None, h):
+            r = np.zeros((1058, n))
+            s.update_rconst(cells["met"], cells["photol"], cells["c"], r, het=het)
+            out[(direct, het is None)] = r
+    assert np.array_equal(out[(True, True)], out[(False, True)])
+    assert np.array_equal(out[(True, False)], out[(False, False)])
+    s.close()
