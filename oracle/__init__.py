@@ -46,6 +46,7 @@ def load(variant="strict", mech="fullchem"):
     lib.oracle_update_rconst_batch.argtypes = [i32, vp, i64, vp, i64, vp, i64, vp, i64]
     lib.oracle_update_rconst_het_batch.argtypes = [i32, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64]
     lib.oracle_fun_split.argtypes = [vp, vp, vp, vp]
+    lib.oracle_fun_pd.argtypes = [vp, vp, vp, vp, vp]
     lib.oracle_jac_sp.argtypes = [vp, vp, vp, vp]
     lib.oracle_kpp_solve.argtypes = [vp, vp]
     lib.oracle_kpp_decomp.argtypes = [vp]
@@ -113,6 +114,16 @@ def fun_split(v, f, rct, mech="fullchem"):
     out = np.zeros_like(v)
     lib.oracle_fun_split(_p(v), _p(f), _p(rct), _p(out))
     return out
+
+
+def fun_pd(v, f, rct, mech="fullchem"):
+    """Fun_SPLITF: production P_VAR and destruction D_VAR (Vdot = P - D*V)."""
+    lib = load("strict", mech)
+    v, f, rct = _c(v, np.float64), _c(f, np.float64), _c(rct, np.float64)
+    p = np.zeros_like(v)
+    d = np.zeros_like(v)
+    lib.oracle_fun_pd(_p(v), _p(f), _p(rct), _p(p), _p(d))
+    return p, d
 
 
 def jac_sp(v, f, rct, lu_nonzero=None, mech="fullchem"):

@@ -77,7 +77,7 @@ def generate(ir):
          "#include \"kpp_oracle.h\"",
          ""]
     lu = ir["lu"]
-    for name in ("crow", "diag", "icol"):
+    for name in ("crow", "diag", "icol", "irow"):
         vals = lu[name]
         L.append("const int ORACLE_LU_%s[%d] = {%s};" % (name.upper(), len(vals), ",".join(map(str, vals))))
     L.append("")
@@ -92,6 +92,18 @@ def generate(ir):
     L.append("  for (int i = 0; i < %d; ++i) Vdot[i] = P_VAR[i] - D_VAR[i]*V[i];" % nvar)
     L.append("}")
     L.append("")
+    # Fun_SPLITF (gckpp_Function.F90:5081-7260) has the same A, P_VAR and D_VAR
+    # statements as Fun_SPLIT and returns P_VAR and D_VAR themselves
+    L.append("void oracle_fun_pd(const double* V, const double* F, const double* RCT, double* P, double* D) {")
+    L.append("  double A[%d];" % nreact)
+    for r, f in enumerate(ir["fun"]["A"]):
+        L.append("  A[%d] = %s;" % (r, _prod(f)))
+    for i, terms in enumerate(ir["fun"]["P"]):
+        L.append("  P[%d] = %s;" % (i, _signed([(s_, (c, a_)) for s_, c, a_ in terms], _coef_ref("A"))))
+    for i, terms in enumerate(ir["fun"]["D"]):
+        L.append("  D[%d] = %s;" % (i, _signed([(s_, f) for s_, f in terms], _prod)))
+    L.append("}")
+    L.append("")
     L.append("void oracle_jac_sp(const double* V, const double* F, const double* RCT, double* JVS) {")
     L.append("  double B[%d];" % nb)
     for b, f in enumerate(ir["jac"]["B"]):
@@ -101,14 +113,18 @@ def generate(ir):
         L.append("  JVS[%d] = %s;" % (k, _signed([(s, (c, b)) for s, c, b in terms], _coef_ref("B"))))
     L.append("}")
     L.append("")
-    L.append("void oracle_kpp_solve(const double* JVS, double* X) {")
-    for st in ir["solve"]:
-        i = st["row"]
-        e = "X[%d]" % i + "".join(" - JVS[%d]*X[%d]" % (k, j) for k, j in st["terms"])
-        if st["kind"] == "B":
-            e = "(%s)/(JVS[%d])" % (e, st["diag"]) if st["terms"] else "X[%d]/JVS[%d]" % (i, st["diag"])
-        L.append("  X[%d] = %s;" % (i, e))
-    L.append("}")
+    for name, guarded in (("oracle_kpp_solve", False), ("oracle_kpp_solve_slv", True)):
+        # the guarded form is KppSolve's IF (DO_SLV(i)) statements
+        # (gckpp_LinearAlgebra.F90:644-2309) under auto-reduction
+        L.append("void %s(const double* JVS, double* X%s) {" % (name, ", const unsigned char* DO_SLV" if guarded else ""))
+        for st in ir["solve"]:
+            i = st["row"]
+            e = "X[%d]" % i + "".join(" - JVS[%d]*X[%d]" % (k, j) for k, j in st["terms"])
+            if st["kind"] == "B":
+                e = "(%s)/(JVS[%d])" % (e, st["diag"]) if st["terms"] else "X[%d]/JVS[%d]" % (i, st["diag"])
+            L.append("  %sX[%d] = %s;" % ("if (DO_SLV[%d]) " % i if guarded else "", i, e))
+        L.append("}")
+        L.append("")
     return "\n".join(L) + "\n", {"nvar": nvar, "nreact": nreact, "lu_nonzero": lunz, "nb": nb,
                                  "nspec": d["nspec"], "nfix": d["nfix"]}
 

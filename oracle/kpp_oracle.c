@@ -323,6 +323,252 @@ static void ros_integrator(cellctx_t* cx, const method_t* m, double* Y, double T
   *IERR = 1;
 }
 
+/* ---- auto-reduce (gckpp_Integrator.F90:789-1237, 1702-1712, 2624-2661) ----
+ * ros_yIntegrator: at the first step the species whose production and loss
+ * (Fun_SPLITF's P_VAR and D_VAR*y) are both below the threshold are frozen
+ * (DO_SLV false); the others are integrated with the Jacobian restricted to
+ * them (compressed pattern cLU_*, cKppDecomp) and KppSolve's DO_SLV-guarded
+ * statements; at the end each frozen species takes the first-order
+ * solution y = P/k + (y - P/k) exp(-k dt) (AutoReduce_1stOrder). */
+typedef struct {
+  unsigned char DO_SLV[NVAR];
+  int SPC_MAP[NVAR], iSPC_MAP[NVAR];
+  int rNVAR, cNONZERO;
+  int JVS_MAP[LU_NONZERO], cLU_IROW[LU_NONZERO], cLU_ICOL[LU_NONZERO];
+  int cLU_CROW[NVAR + 1], cLU_DIAG[NVAR + 1];
+} ar_map_t;
+
+/* the reduction set-up of ros_yIntegrator (:917-1000), 0-based; keep[i]
+ * marks species kept active (keepSpcActive) when keep is not NULL */
+static void ar_build(ar_map_t* R, const double* Prod, const double* LossY, double AR_thr,
+                     const unsigned char* keep) {
+  int NRMV = 0, S = 0;
+  for (int i = 0; i < NVAR; ++i) {
+    R->DO_SLV[i] = 1;
+    R->iSPC_MAP[i] = -1;
+  }
+  for (int i = 0; i < NVAR; ++i) {
+    if ((!keep || !keep[i]) && fabs(LossY[i]) < AR_thr && fabs(Prod[i]) < AR_thr) {
+      NRMV = NRMV + 1;
+      R->DO_SLV[i] = 0;
+      continue;
+    }
+    R->SPC_MAP[S] = i;
+    R->iSPC_MAP[i] = S;
+    S = S + 1;
+  }
+  R->rNVAR = NVAR - NRMV;
+  int II = 0, III = 0, idx = 0, i = 0;
+  for (; i < LU_NONZERO; ++i) { /* ScanFirstNonZero */
+    if (R->DO_SLV[ORACLE_LU_IROW[i]] && R->DO_SLV[ORACLE_LU_ICOL[i]]) {
+      idx = 1;
+      R->cLU_IROW[0] = R->iSPC_MAP[ORACLE_LU_IROW[i]];
+      R->cLU_ICOL[0] = R->iSPC_MAP[ORACLE_LU_ICOL[i]];
+      R->JVS_MAP[0] = i;
+      break;
+    }
+  }
+  for (i = i + 1; i < LU_NONZERO; ++i) {
+    if (R->DO_SLV[ORACLE_LU_IROW[i]] && R->DO_SLV[ORACLE_LU_ICOL[i]]) {
+      idx = idx + 1;
+      R->cLU_IROW[idx - 1] = R->iSPC_MAP[ORACLE_LU_IROW[i]];
+      R->cLU_ICOL[idx - 1] = R->iSPC_MAP[ORACLE_LU_ICOL[i]];
+      R->JVS_MAP[idx - 1] = i;
+      if (R->cLU_IROW[idx - 1] != R->cLU_IROW[idx - 2]) {
+        II = II + 1;
+        R->cLU_CROW[II] = idx - 1;
+      }
+      if (R->cLU_IROW[idx - 1] == R->cLU_ICOL[idx - 1]) {
+        III = III + 1;
+        R->cLU_DIAG[III] = idx - 1;
+      }
+    }
+  }
+  R->cNONZERO = idx;
+  R->cLU_CROW[0] = 0;
+  R->cLU_DIAG[0] = 0;
+  if (R->rNVAR > 0) {
+    R->cLU_CROW[R->rNVAR] = R->cNONZERO;
+    R->cLU_DIAG[R->rNVAR] = R->cLU_DIAG[R->rNVAR - 1] + 1;
+  }
+}
+
+/* cKppDecomp (gckpp_Integrator.F90:2624-2661) on the compressed pattern */
+static int ckpp_decomp(const ar_map_t* R, double* JVS) {
+  double W[NVAR], a;
+  for (int k = 0; k < R->rNVAR; ++k) {
+    if (fabs(JVS[R->cLU_DIAG[k]]) < DBL_MIN) return k + 1;
+    for (int kk = R->cLU_CROW[k]; kk < R->cLU_CROW[k + 1]; ++kk) W[R->cLU_ICOL[kk]] = JVS[kk];
+    for (int kk = R->cLU_CROW[k]; kk < R->cLU_DIAG[k]; ++kk) {
+      int j = R->cLU_ICOL[kk];
+      a = -W[j] / JVS[R->cLU_DIAG[j]];
+      W[j] = -a;
+      for (int jj = R->cLU_DIAG[j] + 1; jj < R->cLU_CROW[j + 1]; ++jj) W[R->cLU_ICOL[jj]] = W[R->cLU_ICOL[jj]] + a * JVS[jj];
+    }
+    for (int kk = R->cLU_CROW[k]; kk < R->cLU_CROW[k + 1]; ++kk) JVS[kk] = W[R->cLU_ICOL[kk]];
+  }
+  return 0;
+}
+
+/* ros_cPrepareMatrix (:1773-1851) */
+static void c_prepare_matrix(cellctx_t* cx, const ar_map_t* R, double* H, int Direction, double gam,
+                             const double* Jac0, double* cGhimj, int* Singular) {
+  int Nconsecutive = 0;
+  *Singular = 1;
+  while (*Singular) {
+    for (int i = 0; i < R->cNONZERO; ++i) cGhimj[i] = -Jac0[R->JVS_MAP[i]];
+    double ghinv = 1.0 / (Direction * (*H) * gam);
+    for (int i = 0; i < R->rNVAR; ++i) cGhimj[R->cLU_DIAG[i]] = cGhimj[R->cLU_DIAG[i]] + ghinv;
+    int ising = ckpp_decomp(R, cGhimj);
+    cx->istatus[Ndec] += 1;
+    if (ising == 0) {
+      *Singular = 0;
+    } else {
+      cx->istatus[Nsng] += 1;
+      Nconsecutive += 1;
+      *Singular = 1;
+      if (Nconsecutive <= 5) *H = (*H) * 0.5;
+      else return;
+    }
+  }
+}
+
+static void ros_yintegrator(cellctx_t* cx, const method_t* m, double* Y, double Tstart, double Tend, double* Tout,
+                            const double* AbsTol, const double* RelTol, int Autonomous, int VectorTol,
+                            int Max_no_steps, double Roundoff, double Hmin, double Hmax, double Hstart,
+                            double FacMin, double FacMax, double FacRej, double FacSafe, double threshold,
+                            int AR_target_spc, double AR_thr_ratio, const unsigned char* keep, int* IERR) {
+  double Ynew[NVAR], Fcn0[NVAR], Fcn[NVAR], Prod[NVAR], Loss[NVAR], LossY[NVAR], K[6 * NVAR], dFdT[NVAR];
+  double Yerr[NVAR];
+  static __thread double Jac0[LU_NONZERO], Ghimj[LU_NONZERO], cGhimj[LU_NONZERO];
+  static __thread ar_map_t R;
+  double H, Hnew, HC, HG, Fac, Err, alpha_factor, AR_thr;
+  int Direction, ioffset, j, istage, RejectLastH, RejectMoreH, Singular, reduced = 0;
+  const double DeltaMin = 1.0e-5;
+  double T = Tstart;
+  cx->rstatus[Nhexit] = 0.0;
+  H = fmin(fmax(fabs(Hmin), fabs(Hstart)), fabs(Hmax));
+  if (fabs(H) <= 10.0 * Roundoff) H = DeltaMin;
+  Direction = (Tend >= Tstart) ? +1 : -1;
+  H = Direction * H;
+  RejectLastH = 0;
+  RejectMoreH = 0;
+  memset(K, 0, sizeof(K));
+  memset(Ghimj, 0, sizeof(Ghimj));
+  memset(dFdT, 0, sizeof(dFdT));
+  memset(Prod, 0, sizeof(Prod));
+  memset(Loss, 0, sizeof(Loss));
+
+  while ((Direction > 0 && ((T - Tend) + Roundoff <= 0.0)) || (Direction < 0 && ((Tend - T) + Roundoff <= 0.0))) {
+    if (cx->istatus[Nstp] > Max_no_steps) { *IERR = -6; *Tout = T; return; }
+    if (((T + 0.1 * H) == T) || (H <= Roundoff)) { *IERR = -7; *Tout = T; return; }
+    H = fmin(H, fabs(Tend - T));
+    if (T == Tstart) { /* FunSplitF: production and loss as well */
+      oracle_fun_pd(Y, cx->fix, cx->rct, Prod, Loss);
+      for (int i = 0; i < NVAR; ++i) {
+        LossY[i] = Loss[i] * Y[i];
+        Fcn0[i] = Prod[i] - LossY[i];
+      }
+    } else {
+      fun_template(cx, Y, Fcn0);
+    }
+    cx->istatus[Nfun] += 1;
+    if (!reduced) {
+      AR_thr = threshold;
+      if (AR_target_spc > 0) {
+        AR_thr = AR_thr_ratio * fmax(LossY[AR_target_spc - 1], Prod[AR_target_spc - 1]);
+        cx->rstatus[3] = AR_thr; /* RSTATUS(NARthr) */
+      }
+      ar_build(&R, Prod, LossY, AR_thr, keep);
+      reduced = 1;
+    }
+    if (!Autonomous) fun_time_derivative(cx, T, Roundoff, Y, Fcn0, dFdT);
+    jac_template(cx, Y, Jac0);
+    cx->istatus[Njac] += 1;
+    for (;;) { /* UntilAccepted */
+      c_prepare_matrix(cx, &R, &H, Direction, m->Gamma[0], Jac0, cGhimj, &Singular);
+      if (Singular) { *IERR = -8; *Tout = T; return; }
+      for (int i = 0; i < R.cNONZERO; ++i) Ghimj[R.JVS_MAP[i]] = cGhimj[i];
+      for (istage = 1; istage <= m->S; ++istage) {
+        ioffset = NVAR * (istage - 1);
+        if (istage == 1) {
+          memcpy(Fcn, Fcn0, sizeof(Fcn));
+        } else if (m->NewF[istage - 1]) {
+          memcpy(Ynew, Y, sizeof(Ynew));
+          for (j = 1; j <= istage - 1; ++j) {
+            alpha_factor = m->A[(istage - 1) * (istage - 2) / 2 + j - 1];
+            for (int i = 0; i < R.rNVAR; ++i)
+              Ynew[R.SPC_MAP[i]] = Ynew[R.SPC_MAP[i]] + alpha_factor * K[NVAR * (j - 1) + R.SPC_MAP[i]];
+          }
+          fun_template(cx, Ynew, Fcn);
+          cx->istatus[Nfun] += 1;
+        }
+        if (istage > 1) {
+          HC = m->C[(istage - 1) * (istage - 2) / 2] / (Direction * H);
+          for (int i = 0; i < R.rNVAR; ++i) K[ioffset + R.SPC_MAP[i]] = Fcn[R.SPC_MAP[i]] + HC * K[R.SPC_MAP[i]];
+        }
+        if (istage == 1)
+          for (int i = 0; i < R.rNVAR; ++i) K[ioffset + R.SPC_MAP[i]] = Fcn[R.SPC_MAP[i]];
+        for (j = 2; j <= istage - 1; ++j) {
+          HC = m->C[(istage - 1) * (istage - 2) / 2 + j - 1] / (Direction * H);
+          for (int i = 0; i < R.rNVAR; ++i)
+            K[ioffset + R.SPC_MAP[i]] = K[ioffset + R.SPC_MAP[i]] + HC * K[NVAR * (j - 1) + R.SPC_MAP[i]];
+        }
+        if (!Autonomous && m->Gamma[istage - 1] != 0.0) {
+          HG = Direction * H * m->Gamma[istage - 1];
+          for (int i = 0; i < R.rNVAR; ++i)
+            K[ioffset + R.SPC_MAP[i]] = K[ioffset + R.SPC_MAP[i]] + HG * dFdT[R.SPC_MAP[i]];
+        }
+        oracle_kpp_solve_slv(Ghimj, K + ioffset, R.DO_SLV);
+        cx->istatus[Nsol] += 1;
+      }
+      memcpy(Ynew, Y, sizeof(Ynew));
+      memset(Yerr, 0, sizeof(Yerr));
+      for (j = 1; j <= m->S; ++j)
+        for (int i = 0; i < R.rNVAR; ++i) {
+          Ynew[R.SPC_MAP[i]] = Ynew[R.SPC_MAP[i]] + m->M[j - 1] * K[NVAR * (j - 1) + R.SPC_MAP[i]];
+          Yerr[R.SPC_MAP[i]] = Yerr[R.SPC_MAP[i]] + m->E[j - 1] * K[NVAR * (j - 1) + R.SPC_MAP[i]];
+        }
+      Err = error_norm(Y, Ynew, Yerr, AbsTol, RelTol, VectorTol);
+      Fac = fmin(FacMax, fmax(FacMin, FacSafe / pow(Err, 1.0 / m->ELO)));
+      Hnew = H * Fac;
+      cx->istatus[Nstp] += 1;
+      if ((Err <= 1.0) || (H <= Hmin)) {
+        cx->istatus[Nacc] += 1;
+        memcpy(Y, Ynew, sizeof(Ynew));
+        T = T + Direction * H;
+        Hnew = fmax(Hmin, fmin(Hnew, Hmax));
+        if (RejectLastH) Hnew = fmin(Hnew, H);
+        cx->rstatus[Nhexit] = H;
+        cx->rstatus[Nhnew] = Hnew;
+        cx->rstatus[Ntexit] = T;
+        RejectLastH = 0;
+        RejectMoreH = 0;
+        H = Hnew;
+        break;
+      } else {
+        if (RejectMoreH) Hnew = H * FacRej;
+        RejectMoreH = RejectLastH;
+        RejectLastH = 1;
+        H = Hnew;
+        if (cx->istatus[Nacc] >= 1) cx->istatus[Nrej] += 1;
+      }
+    }
+  }
+  /* AutoReduce_1stOrder (:1702-1712) for the frozen species */
+  for (int i = 0; i < NVAR; ++i) {
+    if (!R.DO_SLV[i]) {
+      const double k = Loss[i];
+      if (k <= 1.0e-30) continue;
+      if (Y[i] <= 1.0e-30) continue;
+      const double term = Prod[i] / k;
+      Y[i] = term + (Y[i] - term) * exp(-k * (Tend - Tstart));
+    }
+  }
+  *Tout = T;
+  *IERR = 1;
+}
+
 void oracle_integrate(double* C, const double* RCONST, const double* atol, const double* rtol, double tin,
                       double tout, const int* icntrl_u, const double* rcntrl_u, int* istatus_u, double* rstatus_u,
                       int* ierr_u) {
@@ -369,8 +615,25 @@ void oracle_integrate(double* C, const double* RCONST, const double* atol, const
     if ((atol[i] <= 0.0) || (rtol[i] <= 10.0 * Roundoff) || (rtol[i] >= 1.0)) { IERR = -5; goto done; }
   {
     double Texit;
-    ros_integrator(&cx, &m, C, tin, tout, &Texit, atol, rtol, Autonomous, VectorTol, Max_no_steps, Roundoff, Hmin,
-                   Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, ICNTRL[15] == 1, &IERR);
+    /* auto-reduction (gckpp_Integrator.F90:388-394, 478-520): ICNTRL(12) = 1
+     * selects ros_yIntegrator with threshold RCNTRL(12) (default 100) or, with
+     * ICNTRL(14) = target species, RCNTRL(14) x max(P, L*y) of that species;
+     * keepActive is off.  The append form (ICNTRL(13) = 1, ros_yIntegratorA)
+     * is not restated: IERR = -100. */
+    const int Autoreduce = ICNTRL[11] == 1;
+    if (Autoreduce && ICNTRL[12] == 1) {
+      IERR = -100;
+      goto done;
+    }
+    if (Autoreduce) {
+      const double threshold = RCNTRL[11] > 0.0 ? RCNTRL[11] : 1.0e2;
+      ros_yintegrator(&cx, &m, C, tin, tout, &Texit, atol, rtol, Autonomous, VectorTol, Max_no_steps, Roundoff,
+                      Hmin, Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, threshold, ICNTRL[13], RCNTRL[13], 0,
+                      &IERR);
+    } else {
+      ros_integrator(&cx, &m, C, tin, tout, &Texit, atol, rtol, Autonomous, VectorTol, Max_no_steps, Roundoff,
+                     Hmin, Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, ICNTRL[15] == 1, &IERR);
+    }
   }
 done:
   if (istatus_u) memcpy(istatus_u, cx.istatus, sizeof(cx.istatus));

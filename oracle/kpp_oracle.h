@@ -13,10 +13,13 @@
 extern const int ORACLE_LU_CROW[];
 extern const int ORACLE_LU_DIAG[];
 extern const int ORACLE_LU_ICOL[];
+extern const int ORACLE_LU_IROW[];
 
 void oracle_fun_split(const double* V, const double* F, const double* RCT, double* Vdot);
 void oracle_jac_sp(const double* V, const double* F, const double* RCT, double* JVS);
 void oracle_kpp_solve(const double* JVS, double* X);
+void oracle_kpp_solve_slv(const double* JVS, double* X, const unsigned char* DO_SLV);
+void oracle_fun_pd(const double* V, const double* F, const double* RCT, double* P, double* D);
 int oracle_kpp_decomp(double* JVS);
 
 /* Update_RCONST for one cell.  met[18] = TEMP, NUMDEN, H2O, PRESS, SRHOCl,
