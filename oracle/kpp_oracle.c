@@ -433,11 +433,42 @@ static void c_prepare_matrix(cellctx_t* cx, const ar_map_t* R, double* H, int Di
   }
 }
 
+/* The masked form of the same decomposition, for the GPU design: the full
+ * Ghimj with every frozen row and column zeroed and a frozen diagonal set to
+ * 1, factored by the full KppDecomp.  Frozen entries only ever contribute
+ * exact zeros, so the kept entries come out as cKppDecomp leaves them. */
+static void masked_prepare_matrix(cellctx_t* cx, const ar_map_t* R, double* H, int Direction, double gam,
+                                  const double* Jac0, double* Ghimj, int* Singular) {
+  int Nconsecutive = 0;
+  *Singular = 1;
+  while (*Singular) {
+    for (int i = 0; i < LU_NONZERO; ++i) {
+      const int kr = R->DO_SLV[ORACLE_LU_IROW[i]], kc = R->DO_SLV[ORACLE_LU_ICOL[i]];
+      Ghimj[i] = (kr && kc) ? -Jac0[i] : 0.0;
+    }
+    double ghinv = 1.0 / (Direction * (*H) * gam);
+    for (int i = 0; i < NVAR; ++i)
+      Ghimj[ORACLE_LU_DIAG[i]] = R->DO_SLV[i] ? Ghimj[ORACLE_LU_DIAG[i]] + ghinv : 1.0;
+    int ising = oracle_kpp_decomp(Ghimj);
+    cx->istatus[Ndec] += 1;
+    if (ising == 0) {
+      *Singular = 0;
+    } else {
+      cx->istatus[Nsng] += 1;
+      Nconsecutive += 1;
+      *Singular = 1;
+      if (Nconsecutive <= 5) *H = (*H) * 0.5;
+      else return;
+    }
+  }
+}
+
 static void ros_yintegrator(cellctx_t* cx, const method_t* m, double* Y, double Tstart, double Tend, double* Tout,
                             const double* AbsTol, const double* RelTol, int Autonomous, int VectorTol,
                             int Max_no_steps, double Roundoff, double Hmin, double Hmax, double Hstart,
                             double FacMin, double FacMax, double FacRej, double FacSafe, double threshold,
-                            int AR_target_spc, double AR_thr_ratio, const unsigned char* keep, int* IERR) {
+                            int AR_target_spc, double AR_thr_ratio, const unsigned char* keep, int masked,
+                            int* IERR) {
   double Ynew[NVAR], Fcn0[NVAR], Fcn[NVAR], Prod[NVAR], Loss[NVAR], LossY[NVAR], K[6 * NVAR], dFdT[NVAR];
   double Yerr[NVAR];
   static __thread double Jac0[LU_NONZERO], Ghimj[LU_NONZERO], cGhimj[LU_NONZERO];
@@ -486,9 +517,14 @@ static void ros_yintegrator(cellctx_t* cx, const method_t* m, double* Y, double 
     jac_template(cx, Y, Jac0);
     cx->istatus[Njac] += 1;
     for (;;) { /* UntilAccepted */
-      c_prepare_matrix(cx, &R, &H, Direction, m->Gamma[0], Jac0, cGhimj, &Singular);
+      if (masked) {
+        masked_prepare_matrix(cx, &R, &H, Direction, m->Gamma[0], Jac0, Ghimj, &Singular);
+      } else {
+        c_prepare_matrix(cx, &R, &H, Direction, m->Gamma[0], Jac0, cGhimj, &Singular);
+      }
       if (Singular) { *IERR = -8; *Tout = T; return; }
-      for (int i = 0; i < R.cNONZERO; ++i) Ghimj[R.JVS_MAP[i]] = cGhimj[i];
+      if (!masked)
+        for (int i = 0; i < R.cNONZERO; ++i) Ghimj[R.JVS_MAP[i]] = cGhimj[i];
       for (istage = 1; istage <= m->S; ++istage) {
         ioffset = NVAR * (istage - 1);
         if (istage == 1) {
@@ -519,7 +555,10 @@ static void ros_yintegrator(cellctx_t* cx, const method_t* m, double* Y, double 
           for (int i = 0; i < R.rNVAR; ++i)
             K[ioffset + R.SPC_MAP[i]] = K[ioffset + R.SPC_MAP[i]] + HG * dFdT[R.SPC_MAP[i]];
         }
-        oracle_kpp_solve_slv(Ghimj, K + ioffset, R.DO_SLV);
+        if (masked) /* frozen right-hand sides are 0, the full KppSolve keeps them 0 */
+          oracle_kpp_solve(Ghimj, K + ioffset);
+        else
+          oracle_kpp_solve_slv(Ghimj, K + ioffset, R.DO_SLV);
         cx->istatus[Nsol] += 1;
       }
       memcpy(Ynew, Y, sizeof(Ynew));
@@ -619,7 +658,9 @@ void oracle_integrate(double* C, const double* RCONST, const double* atol, const
      * selects ros_yIntegrator with threshold RCNTRL(12) (default 100) or, with
      * ICNTRL(14) = target species, RCNTRL(14) x max(P, L*y) of that species;
      * keepActive is off.  The append form (ICNTRL(13) = 1, ros_yIntegratorA)
-     * is not restated: IERR = -100. */
+     * is not restated: IERR = -100.  ICNTRL(20) = 7 (unused by the reference)
+     * selects the masked-full decomposition of the GPU design instead of the
+     * compressed one (tests only). */
     const int Autoreduce = ICNTRL[11] == 1;
     if (Autoreduce && ICNTRL[12] == 1) {
       IERR = -100;
@@ -629,7 +670,7 @@ void oracle_integrate(double* C, const double* RCONST, const double* atol, const
       const double threshold = RCNTRL[11] > 0.0 ? RCNTRL[11] : 1.0e2;
       ros_yintegrator(&cx, &m, C, tin, tout, &Texit, atol, rtol, Autonomous, VectorTol, Max_no_steps, Roundoff,
                       Hmin, Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, threshold, ICNTRL[13], RCNTRL[13], 0,
-                      &IERR);
+                      ICNTRL[19] == 7, &IERR);
     } else {
       ros_integrator(&cx, &m, C, tin, tout, &Texit, atol, rtol, Autonomous, VectorTol, Max_no_steps, Roundoff,
                      Hmin, Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, ICNTRL[15] == 1, &IERR);
