@@ -80,10 +80,11 @@ def build(verbose=False, force=False):
         ir = mechanism.load_ir(mech)
         tables.write_generated(gen, ir)
         rates_program.write_generated(gen, ir)
-        obj = "gckpp_capi_%s.o" % mech
-        units.append((os.path.join(CSRC, "gckpp_capi.cu"), obj, ["-I", gen], [os.path.join(gen, f)
-                                                                          for f in os.listdir(gen)]))
-        mech_objs[mech] = obj
+        gen_deps = [os.path.join(gen, f) for f in os.listdir(gen)]
+        objs = ["gckpp_capi_%s.o" % mech, "rates_direct_%s.o" % mech]
+        units.append((os.path.join(CSRC, "gckpp_capi.cu"), objs[0], ["-I", gen], gen_deps))
+        units.append((os.path.join(CSRC, "rates_direct.cu"), objs[1], ["-I", gen], gen_deps))
+        mech_objs[mech] = objs
     exe = nvcc()
     procs = []
     shared = []
@@ -91,7 +92,7 @@ def build(verbose=False, force=False):
         src, obj, extra = unit[:3]
         extra_deps = unit[3] if len(unit) > 3 else []
         obj = os.path.join(BUILD, obj)
-        if os.path.basename(obj) not in mech_objs.values():
+        if not any(os.path.basename(obj) in objs for objs in mech_objs.values()):
             shared.append(obj)
         if force or _stale(obj, deps + extra_deps):
             cmd = [exe] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
@@ -105,9 +106,9 @@ def build(verbose=False, force=False):
         if verbose and out:
             print(out.decode())
     links = []
-    for mech, obj in mech_objs.items():
+    for mech, own in mech_objs.items():
         lib = lib_path(mech)
-        objs = shared + [os.path.join(BUILD, obj)]
+        objs = shared + [os.path.join(BUILD, o) for o in own]
         if force or procs or not os.path.exists(lib):
             cmd = [exe] + ARCH + ["-shared", "-cudart", "shared", "-o", lib] + objs
             links.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

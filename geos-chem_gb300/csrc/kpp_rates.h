@@ -31,4 +31,6 @@ struct RatesArgs {
   long long ldh;
 };
 cudaError_t launch_rates(const RatesDev& rp, const RatesArgs& a, cudaStream_t s);
+// the generated straight-line form (rates_direct.cu, one object per mechanism)
+cudaError_t launch_rates_direct(const RatesDev& rp, const RatesArgs& a, cudaStream_t s);
 }  // namespace gcrates
