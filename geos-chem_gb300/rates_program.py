@@ -301,7 +301,7 @@ def emit_direct(prog):
     expression per rate, operations in the program's order, additions and
     multiplications through the round-to-nearest intrinsics so that nothing
     is contracted): the body of the per-mechanism rates_direct_kernel
-    (gckpp_capi.cu), which gives the interpreter's results bit for bit
+    (rates_direct.cu), which gives the interpreter's results to rounding
     without its dispatch and local-memory stack.  Uses the kernel's macros
     M(f) (met row), PH(j), CC(i), OUT(r) and the functions lawv/hetv."""
     code, start, consts = prog["code"], prog["start"], prog["consts"]

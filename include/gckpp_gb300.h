@@ -76,7 +76,10 @@ extern "C" {
                                      thread, results identical to the thread-per-cell form). */
 #define GC_KPP_OPT_RATES_DIRECT 13 /* 1 = Update_RCONST runs as straight-line code generated
                                       from the mechanism's rate program (default); 0 = the
-                                      rate-program interpreter.  Same results bit for bit. */
+                                      rate-program interpreter.  The same operations in the
+                                      same order; results agree to rounding (within 1e-13
+                                      relative: compile-time constants let the compiler
+                                      specialise a few libm calls). */
 #define GC_KPP_OPT_ASYNC 9        /* 1 = chemistry steps never synchronise the host, so that a
                                      caller can capture them in a CUDA graph: the retry list and
                                      the block-per-cell count stay on the device, *nretry (and
