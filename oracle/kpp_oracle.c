@@ -433,10 +433,12 @@ static void c_prepare_matrix(cellctx_t* cx, const ar_map_t* R, double* H, int Di
   }
 }
 
-/* The masked form of the same decomposition, for the GPU design: the full
- * Ghimj with every frozen row and column zeroed and a frozen diagonal set to
- * 1, factored by the full KppDecomp.  Frozen entries only ever contribute
- * exact zeros, so the kept entries come out as cKppDecomp leaves them. */
+/* The masked form of the same decomposition, for the GPU design: Jac0 with
+ * every entry in a frozen row or column zeroed, so that Ghimj = -Jac0 +
+ * ghinv I decouples the frozen species (a frozen row is ghinv on the
+ * diagonal, 0 elsewhere), factored by the full KppDecomp.  Frozen entries
+ * only ever contribute exact zeros, so the kept entries come out as
+ * cKppDecomp leaves them. */
 static void masked_prepare_matrix(cellctx_t* cx, const ar_map_t* R, double* H, int Direction, double gam,
                                   const double* Jac0, double* Ghimj, int* Singular) {
   int Nconsecutive = 0;
@@ -444,11 +446,10 @@ static void masked_prepare_matrix(cellctx_t* cx, const ar_map_t* R, double* H, i
   while (*Singular) {
     for (int i = 0; i < LU_NONZERO; ++i) {
       const int kr = R->DO_SLV[ORACLE_LU_IROW[i]], kc = R->DO_SLV[ORACLE_LU_ICOL[i]];
-      Ghimj[i] = (kr && kc) ? -Jac0[i] : 0.0;
+      Ghimj[i] = -((kr && kc) ? Jac0[i] : 0.0);
     }
     double ghinv = 1.0 / (Direction * (*H) * gam);
-    for (int i = 0; i < NVAR; ++i)
-      Ghimj[ORACLE_LU_DIAG[i]] = R->DO_SLV[i] ? Ghimj[ORACLE_LU_DIAG[i]] + ghinv : 1.0;
+    for (int i = 0; i < NVAR; ++i) Ghimj[ORACLE_LU_DIAG[i]] = Ghimj[ORACLE_LU_DIAG[i]] + ghinv;
     int ising = oracle_kpp_decomp(Ghimj);
     cx->istatus[Ndec] += 1;
     if (ising == 0) {

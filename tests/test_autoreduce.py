@@ -90,10 +90,11 @@ def test_append_form_is_not_restated(case):
 
 @pytest.mark.parametrize("thr", [1e2, 1e5])
 def test_masked_full_decomposition_equals_the_compressed_one(case, thr):
-    """The design of the GPU form: factoring the full Ghimj with the frozen
-    rows and columns masked to the identity (ICNTRL(20) = 7 selects it in
-    the oracle) gives the compressed cKppDecomp path's integration bit for
-    bit -- frozen entries only ever contribute exact zeros."""
+    """The design of the GPU form: zeroing every Jac0 entry in a frozen row
+    or column and factoring the full Ghimj = -Jac0 + ghinv I (ICNTRL(20) = 7
+    selects it in the oracle) gives the compressed cKppDecomp path's
+    integration bit for bit -- frozen entries only ever contribute exact
+    zeros."""
     import oracle
 
     ic = case["ic"].copy()
