@@ -49,6 +49,7 @@ EXPORTED = [
     "gc_kpp_update_rconst_batch",
     "gc_kpp_update_rconst_het_batch",
     "gc_kpp_ctx_set_hetstate",
+    "gc_kpp_ctx_set_autoreduce",
     "gc_kpp_fullchem_step",
     "gc_kpp_fullchem_step_ordered",
     "gc_kpp_fullchem_step_binned",
@@ -89,6 +90,7 @@ def load_library(path=None, mech="fullchem"):
     lib.gc_kpp_update_rconst_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, vp, i64, i32, vp]
     lib.gc_kpp_update_rconst_het_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64, i32, vp]
     lib.gc_kpp_ctx_set_hetstate.argtypes = [vp, i32, vp, i64, i32]
+    lib.gc_kpp_ctx_set_autoreduce.argtypes = [vp, i32, vp, vp, vp, vp, i32]
     if path == _build.lib_path(mech):
         _libs[mech] = lib
     return lib
@@ -263,6 +265,37 @@ class Solver:
             ctypes.byref(nretry), ctypes.byref(nblock), MEM_DEVICE if dev else MEM_HOST, s)
         self._check(rc)
         return nretry.value, nblock.value
+
+    def set_autoreduce(self, thr=None, target=None, ratio=None, keep=None):
+        """Auto-reduce controls of the following integrations with
+        ICNTRL(12) = 1: per-cell RCNTRL(12) / ICNTRL(14) / RCNTRL(14) arrays
+        [ncell] (numpy or torch CUDA; copied) and the keepSpcActive mask
+        [NVAR] (host).  Each call replaces every earlier setting; no
+        arguments clear them (see gcchem.autoreduce for the arrays Do_FullChem
+        would pass)."""
+        cells = [a for a in (thr, target, ratio) if a is not None]
+        n = int(cells[0].shape[0]) if cells else 0
+        if any(int(a.shape[0]) != n for a in cells):
+            raise ValueError("per-cell arrays of different lengths")
+        dev = bool(cells) and _is_torch(cells[0]) and cells[0].is_cuda
+        if any((_is_torch(a) and a.is_cuda) != dev for a in cells):
+            raise ValueError("per-cell arrays must all be host or all be device arrays")
+
+        def conv(a, dt):
+            if a is None:
+                return a
+            if dev:
+                if not a.is_contiguous() or a.element_size() != np.dtype(dt).itemsize or a.dtype.is_floating_point \
+                        != (np.dtype(dt).kind == "f"):
+                    raise ValueError("device arrays must be contiguous float64 (thr, ratio) / int32 (target)")
+                return a
+            return np.ascontiguousarray(a, dtype=dt)
+
+        thr, target, ratio = conv(thr, np.float64), conv(target, np.int32), conv(ratio, np.float64)
+        k = None if keep is None else np.ascontiguousarray(np.asarray(keep) != 0, dtype=np.uint8)
+        self._ar_keep = (thr, target, ratio, k)
+        self._check(self.lib.gc_kpp_ctx_set_autoreduce(self.ctx, n, _ptr(thr), _ptr(target), _ptr(ratio), _ptr(k),
+                                                       MEM_DEVICE if dev else MEM_HOST))
 
     def set_hetstate(self, het):
         """HetState rows [168, ncell] (numpy: copied; torch CUDA: kept by

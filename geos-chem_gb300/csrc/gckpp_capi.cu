@@ -67,7 +67,9 @@ cudaError_t upload(const X* host, size_t n, const X** dev, std::vector<void*>& o
   return e;
 }
 
-WsLayout make_layout() {
+// Workspace layout of one cell of the thread-per-cell kernel; ar adds the
+// auto-reduction arrays (frozen mask, P_VAR and D_VAR at Tstart).
+WsLayout make_layout(bool ar = false) {
   WsLayout l;
   int o = 0;
   l.aux = o; o += T::NAUX;
@@ -81,6 +83,12 @@ WsLayout make_layout() {
   l.b = o; o += T::NB;
   l.j0 = o; o += T::LU_NONZERO;
   l.g = o; o += T::LU_NONZERO;
+  l.slv = l.prod = l.loss = -1;
+  if (ar) {
+    l.slv = o; o += T::NVAR;
+    l.prod = o; o += T::NVAR;
+    l.loss = o; o += T::NVAR;
+  }
   l.total = o;
   return l;
 }
@@ -122,6 +130,10 @@ struct gc_kpp_ctx {
   long long het_ld = 0;
   int het_ncell = 0;
   DevBuf rc_buf, cb_buf, ord_buf;  // chemistry-step scratch: RCONST, C_before, retry list
+  // auto-reduction controls (gc_kpp_ctx_set_autoreduce): per-cell RCNTRL(12),
+  // ICNTRL(14), RCNTRL(14) for ar_ncell cells, and keepSpcActive
+  DevBuf ar_thr, ar_tgt, ar_ratio, ar_keep;
+  int ar_ncell = 0, ar_has_thr = 0, ar_has_tgt = 0, ar_has_ratio = 0, ar_keep_on = 0;
   int last_launches = 0;
   // optional CUDA-event timing of the Rosenbrock launches (GC_KPP_OPT_TIMING)
   int timing = 0;
@@ -252,7 +264,7 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
                     &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
                     &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges, &c->evict_buf, &c->bws,
-                    &c->h_het, &c->step_het};
+                    &c->h_het, &c->step_het, &c->ar_thr, &c->ar_tgt, &c->ar_ratio, &c->ar_keep};
   for (DevBuf* b : bufs) b->release();
   delete c;
   return GC_KPP_OK;
@@ -334,6 +346,9 @@ struct Resolved {
   int max_steps = 200000;
   double hmin = 0, hmax = 0, hstart_default = 0, facmin = 0, facmax = 0, facrej = 0, facsafe = 0;
   int autonomous = 1, clamp = 0;
+  // auto-reduction (Rosenbrock :388-394, :478-487): ICNTRL(12) = 1
+  int autoreduce = 0, ar_target = 0;
+  double ar_thr = 1.0e2, ar_ratio = 0.0;
 };
 
 int resolve(const int* icntrl_u, const double* rcntrl_u, double tin, double tout, Resolved& R) {
@@ -350,7 +365,16 @@ int resolve(const int* icntrl_u, const double* rcntrl_u, double tin, double tout
   // inside the integrator need the met state, which this path does not take.
   if (icntrl[14] != -1 && (icntrl[14] & 5))
     return fail(GC_KPP_EUNSUPPORTED, "ICNTRL(15) requests Update_RCONST/Update_SUN inside the integrator");
-  if (icntrl[11] == 1) return fail(GC_KPP_EUNSUPPORTED, "auto-reduce (ICNTRL(12)=1) is not implemented");
+  if (icntrl[11] == 1) {
+    if (icntrl[12] == 1)
+      return fail(GC_KPP_EUNSUPPORTED, "auto-reduce with append (ICNTRL(13)=1, ros_yIntegratorA) is not implemented");
+    if (icntrl[13] < 0 || icntrl[13] > T::NVAR)
+      return fail(GC_KPP_EUNSUPPORTED, "auto-reduce target species ICNTRL(14) out of range");
+    R.autoreduce = 1;
+    R.ar_target = icntrl[13];
+    if (rcntrl[11] > 0.0) R.ar_thr = rcntrl[11];
+    R.ar_ratio = rcntrl[13];
+  }
   R.vector_tol = icntrl[1] == 0;
   if (!method_table(icntrl[2], R.meth)) R.code = -2;
   if (!R.code) {
@@ -412,12 +436,12 @@ struct DevArgs {
 // Kernel variant by GC_KPP_OPT_ARITH: 0 fast, 1 strict (both 1 cell per
 // thread), 2 fast with 2 cells per thread, 3 fast with 4.
 cudaError_t variant_launch(int arith, int queue, int grid, int block, const MechDev& m, const RosMethod& r,
-                           const RosParams& p, cudaStream_t s) {
+                           const RosParams& p, cudaStream_t s, int ar = 0) {
   switch (arith) {
-    case 1: return gckpp_launch_ros_strict(queue, grid, block, m, r, p, s);
-    case 2: return gckpp_launch_ros_fast2(queue, grid, block, m, r, p, s);
-    case 3: return gckpp_launch_ros_fast4(queue, grid, block, m, r, p, s);
-    default: return gckpp_launch_ros_fast(queue, grid, block, m, r, p, s);
+    case 1: return gckpp_launch_ros_strict(queue, grid, block, m, r, p, s, ar);
+    case 2: return gckpp_launch_ros_fast2(queue, grid, block, m, r, p, s, ar);
+    case 3: return gckpp_launch_ros_fast4(queue, grid, block, m, r, p, s, ar);
+    default: return gckpp_launch_ros_fast(queue, grid, block, m, r, p, s, ar);
   }
 }
 
@@ -492,6 +516,14 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     return fail(GC_KPP_EUNSUPPORTED, "block-per-cell cells need ARITH 0 or 1 and the row-wise LU");
   if ((dev_split || a.qrange) && !queue)
     return fail(GC_KPP_EINVAL, "cell counts held on the device need the queue schedule");
+  // auto-reduction runs on the thread-per-cell kernel alone (1 cell per
+  // thread, row-wise LU): no block-per-cell routing, no hand-over
+  if (R.autoreduce && (nb > 0 || dev_split || a.block_only || c->arith > 1 || c->lu_form != 0))
+    return fail(GC_KPP_EUNSUPPORTED,
+                "auto-reduce needs ARITH 0 or 1, the row-wise LU and no block-per-cell cells");
+  if (R.autoreduce && c->ar_ncell > 0 && (a.cell_limit > 0 ? a.cell_limit : a.ncell) != c->ar_ncell)
+    return fail(GC_KPP_EINVAL, "auto-reduce controls were set for a different number of cells");
+  const WsLayout lay = make_layout(R.autoreduce != 0);
   if (dev_split && (!a.order || nb != 0)) return fail(GC_KPP_EINVAL, "device block-per-cell count needs an order");
   // with counts on the device, size for every cell; the kernels read the ranges
   const long long nthread = (dev_split || a.qrange) ? (long long)a.ncell : (long long)a.ncell - nb;
@@ -528,7 +560,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     if (c->max_slots > 0 && nslot > c->max_slots)
       return fail(GC_KPP_EINVAL, "plain schedule needs one workspace slot per cell; raise MAX_SLOTS or use the queue");
   }
-  const size_t ws_bytes = (size_t)std::max(nslot, ws_slots) * (size_t)c->lay.total * sizeof(double);
+  const size_t ws_bytes = (size_t)std::max(nslot, ws_slots) * (size_t)lay.total * sizeof(double);
   GC_CUDA(c->ws.ensure(ws_bytes));
   GC_CUDA(c->counter.ensure(2 * sizeof(int)));
   GC_CUDA(cudaMemsetAsync(c->counter.p, 0, 2 * sizeof(int), s));
@@ -544,7 +576,8 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   p.order = a.order ? a.order + nb : nullptr;
   p.qrange = dev_split ? ranges + 2 : a.qrange;
   // hand-over of long-running cells (needs the status rows to carry their state)
-  const bool evict = c->evict_after > 0 && queue && c->arith <= 1 && c->lu_form == 0 && a.istatus && a.rstatus;
+  const bool evict = c->evict_after > 0 && queue && c->arith <= 1 && c->lu_form == 0 && a.istatus && a.rstatus &&
+                     !R.autoreduce;
   if (evict) {
     GC_CUDA(c->evict_buf.ensure((size_t)std::max(a.ncell, 1) * sizeof(int)));
     GC_CUDA(cudaMemsetAsync(ranges + 6, 0, 2 * sizeof(int), s));
@@ -582,8 +615,17 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   p.max_steps = R.max_steps;
   p.clamp_negative = R.clamp;
   p.lu_form = c->lu_form;
+  p.ar_target = R.ar_target;
+  p.ar_thr = R.ar_thr;
+  p.ar_ratio = R.ar_ratio;
+  if (R.autoreduce) {
+    p.ar_thr_cell = c->ar_has_thr ? (const double*)c->ar_thr.p : nullptr;
+    p.ar_target_cell = c->ar_has_tgt ? (const int*)c->ar_tgt.p : nullptr;
+    p.ar_ratio_cell = c->ar_has_ratio ? (const double*)c->ar_ratio.p : nullptr;
+    p.ar_keep = c->ar_keep_on ? (const unsigned char*)c->ar_keep.p : nullptr;
+  }
   p.ws = (double*)c->ws.p;
-  p.lay = c->lay;
+  p.lay = lay;
   p.nslot = nslot;
   const bool timed = c->timing && !c->async && c->ntimed < 4;
   if (timed) {
@@ -629,7 +671,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
     return GC_KPP_OK;
   }
   if (nthread > 0) {
-    cudaError_t e = variant_launch(c->arith, queue, grid, block, c->mech, R.meth, p, s);
+    cudaError_t e = variant_launch(c->arith, queue, grid, block, c->mech, R.meth, p, s, R.autoreduce);
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     if (launches) *launches += 1;
   }
@@ -876,7 +918,8 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
       b.qrange = ranges + 4;
       b.nblock = 0;
       b.nblock_dev = nullptr;
-      b.block_only = (c->arith <= 1 && c->lu_form == 0) ? 1 : 0;  // retries are few: latency form
+      // retries are few: latency form (auto-reduction runs on the thread kernel)
+      b.block_only = (c->arith <= 1 && c->lu_form == 0 && !R.autoreduce) ? 1 : 0;
       b.cell_limit = ncell;
       b.c_in = dcb;
       b.hstart = nullptr;
@@ -904,7 +947,7 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
       b.order = dord;
       b.cell_limit = ncell;
       // a few cells integrate faster one per block than on the queue kernel
-      b.nblock = (c->arith <= 1 && c->lu_form == 0 && (long long)failed.size() <= 4LL * c->nsm)
+      b.nblock = (c->arith <= 1 && c->lu_form == 0 && !R.autoreduce && (long long)failed.size() <= 4LL * c->nsm)
                      ? (int)failed.size() : 0;
       b.nblock_dev = nullptr;
       b.qrange = nullptr;
@@ -1003,6 +1046,47 @@ int gc_kpp_ctx_set_hetstate(gc_kpp_ctx* c, int ncell, const double* het, long lo
     c->het_ld = ncell;
   }
   c->het_ncell = ncell;
+  return GC_KPP_OK;
+}
+
+int gc_kpp_ctx_set_autoreduce(gc_kpp_ctx* c, int ncell, const double* thr, const int* target, const double* ratio,
+                              const unsigned char* keep, int mem) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  const bool cells = thr || target || ratio;
+  if (cells && ncell <= 0) return fail(GC_KPP_EINVAL, "per-cell controls need ncell > 0");
+  if (cells && mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  GC_CUDA(cudaSetDevice(c->device));
+  const size_t n = cells ? (size_t)ncell : 0;
+  const cudaMemcpyKind kind = mem == GC_KPP_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (target) {
+    // ICNTRL(14) must name a variable species (or be 0) in every cell
+    std::vector<int> t(n);
+    GC_CUDA(cudaMemcpy(t.data(), target, n * sizeof(int),
+                       mem == GC_KPP_MEM_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+    for (size_t i = 0; i < n; ++i)
+      if (t[i] < 0 || t[i] > T::NVAR) return fail(GC_KPP_EUNSUPPORTED, "auto-reduce target species out of range");
+    GC_CUDA(c->ar_tgt.ensure(n * sizeof(int)));
+    GC_CUDA(cudaMemcpy(c->ar_tgt.p, t.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (thr) {
+    GC_CUDA(c->ar_thr.ensure(n * sizeof(double)));
+    GC_CUDA(cudaMemcpy(c->ar_thr.p, thr, n * sizeof(double), kind));
+  }
+  if (ratio) {
+    GC_CUDA(c->ar_ratio.ensure(n * sizeof(double)));
+    GC_CUDA(cudaMemcpy(c->ar_ratio.p, ratio, n * sizeof(double), kind));
+  }
+  if (keep) {
+    unsigned char k[T::NVAR];
+    for (int i = 0; i < T::NVAR; ++i) k[i] = keep[i] ? 1 : 0;
+    GC_CUDA(c->ar_keep.ensure(sizeof(k)));
+    GC_CUDA(cudaMemcpy(c->ar_keep.p, k, sizeof(k), cudaMemcpyHostToDevice));
+  }
+  c->ar_ncell = (int)n;
+  c->ar_has_thr = thr != nullptr;
+  c->ar_has_tgt = target != nullptr;
+  c->ar_has_ratio = ratio != nullptr;
+  c->ar_keep_on = keep != nullptr;
   return GC_KPP_OK;
 }
 
@@ -1250,7 +1334,7 @@ int gc_kpp_integrate_batch_noalloc(int ncell, double tin, double tout, double* c
   p.lay = make_layout();
   p.nslot = (long long)grid * NOALLOC_BLOCK * nc;
   if (p.nslot > NOALLOC_MAX_CELLS) return fail(GC_KPP_EINVAL, "no-allocation workspace too small");
-  cudaError_t e = gckpp_launch_ros_fast(0, grid, NOALLOC_BLOCK, d->mech, R.meth, p, s);
+  cudaError_t e = gckpp_launch_ros_fast(0, grid, NOALLOC_BLOCK, d->mech, R.meth, p, s, 0);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
   return GC_KPP_OK;
 }

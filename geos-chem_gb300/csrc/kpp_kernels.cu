@@ -26,26 +26,39 @@
 
 namespace gckpp {
 
-template <bool QUEUE>
+template <bool QUEUE, bool AR>
 __global__ void __launch_bounds__(GCKPP_MAX_THREADS, 1) ros_kernel(MechDev m, RosMethod r, RosParams p) {
-  ros_driver<GCKPP_STRICT != 0, QUEUE, GCKPP_NC>(m, r, p);
+  ros_driver<GCKPP_STRICT != 0, QUEUE, GCKPP_NC, AR>(m, r, p);
 }
 
+// ar = 1: the auto-reducing integrator (one cell per thread only)
 cudaError_t GCKPP_CAT(gckpp_launch_ros_, GCKPP_VARIANT)(int queue, int grid, int block, const MechDev& m,
-                                                        const RosMethod& r, const RosParams& p, cudaStream_t s) {
+                                                        const RosMethod& r, const RosParams& p, cudaStream_t s,
+                                                        int ar) {
   if (block > GCKPP_MAX_THREADS) return cudaErrorInvalidConfiguration;
+#if GCKPP_NC == 1
+  if (ar) {
+    if (queue)
+      ros_kernel<true, true><<<grid, block, 0, s>>>(m, r, p);
+    else
+      ros_kernel<false, true><<<grid, block, 0, s>>>(m, r, p);
+    return cudaGetLastError();
+  }
+#else
+  if (ar) return cudaErrorInvalidConfiguration;
+#endif
   if (queue)
-    ros_kernel<true><<<grid, block, 0, s>>>(m, r, p);
+    ros_kernel<true, false><<<grid, block, 0, s>>>(m, r, p);
   else
-    ros_kernel<false><<<grid, block, 0, s>>>(m, r, p);
+    ros_kernel<false, false><<<grid, block, 0, s>>>(m, r, p);
   return cudaGetLastError();
 }
 
 int GCKPP_CAT(gckpp_cells_per_thread_, GCKPP_VARIANT)() { return GCKPP_NC; }
 
 cudaError_t GCKPP_CAT(gckpp_occupancy_, GCKPP_VARIANT)(int queue, int block, int* nblocks) {
-  if (queue) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_kernel<true>, block, 0);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_kernel<false>, block, 0);
+  if (queue) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_kernel<true, false>, block, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nblocks, ros_kernel<false, false>, block, 0);
 }
 
 #if GCKPP_NC == 1

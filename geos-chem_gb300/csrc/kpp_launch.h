@@ -10,7 +10,7 @@ struct RosParams;
 
 #define GCKPP_DECLARE_VARIANT(name)                                                                        \
   cudaError_t gckpp_launch_ros_##name(int queue, int grid, int block, const MechDev& m, const RosMethod& r, \
-                                      const RosParams& p, cudaStream_t s);                                 \
+                                      const RosParams& p, cudaStream_t s, int ar);                         \
   cudaError_t gckpp_occupancy_##name(int queue, int block, int* nblocks);                                    \
   int gckpp_cells_per_thread_##name();
 

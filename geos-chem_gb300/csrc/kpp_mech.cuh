@@ -164,10 +164,13 @@ __device__ __forceinline__ void b_products(const MechDev& m, const double* __res
 }
 
 // Fun_SPLIT: Vdot = P_VAR - D_VAR*V at point Y = [V | F] (aux = RCT).
-// B must hold the B products at Y (b_products).
-template <bool STRICT, int NC>
+// B must hold the B products at Y (b_products).  With PD, P_VAR and D_VAR
+// are stored too (Fun_SPLITF, gckpp_Function.F90:5081-7260: the same
+// statements).
+template <bool STRICT, int NC, bool PD = false>
 __device__ void fun_split(const MechDev& m, const double* __restrict__ V, const double* __restrict__ aux,
-                          double* __restrict__ A, const double* __restrict__ B, double* __restrict__ Vdot) {
+                          double* __restrict__ A, const double* __restrict__ B, double* __restrict__ Vdot,
+                          double* __restrict__ P = nullptr, double* __restrict__ D = nullptr) {
   constexpr int TSN = TS * NC;
 #pragma unroll 2
   for (int r = 0; r < m.nreact; ++r) {
@@ -184,6 +187,10 @@ __device__ void fun_split(const MechDev& m, const double* __restrict__ V, const 
     for (int q = 0; q < NC; ++q) {
       const double v = V[i * TSN + q * TS];
       Vdot[i * TSN + q * TS] = STRICT ? p[q] - d[q] * v : fma(-d[q], v, p[q]);
+      if (PD) {
+        P[i * TSN + q * TS] = p[q];
+        D[i * TSN + q * TS] = d[q];
+      }
     }
   }
 }

@@ -33,7 +33,9 @@ struct RosMethod {
 };
 
 struct WsLayout {
-  int aux, y0, y1, fcn0, fcn, dfdt, k, a, b, j0, g, total;
+  int aux, y0, y1, fcn0, fcn, dfdt, k, a, b, j0, g;
+  int slv, prod, loss;  // auto-reduction only (else -1): DO_SLV mask, P_VAR and D_VAR at Tstart
+  int total;
 };
 
 struct RosParams {
@@ -64,6 +66,22 @@ struct RosParams {
   double hmin, hmax, hstart_default, facmin, facmax, facrej, facsafe, roundoff;
   int autonomous, max_steps, clamp_negative;
   int lu_form;  // 0 decomp_rows, 1 decomp (KppDecomp order)
+  // auto-reduction (ros_yIntegrator, gckpp_Integrator.F90:789-1237): at the
+  // first step, species with |P_VAR| and |D_VAR*y| below the threshold are
+  // frozen -- their Jac0 rows and columns are zeroed, their stage vectors
+  // kept 0 -- and take the first-order solution at the end.  The threshold
+  // is ar_thr, or with ar_target > 0 (1-based species) ar_ratio * max(P, L*y)
+  // of that species, reported in RSTATUS(4).  Kernels built with AR only.
+  // Per-cell arrays, when set, replace the three scalars cell by cell
+  // (fullchem_AutoReduceFuncs.F90:293-343 sets them per grid box; a
+  // threshold <= 0 means the default 100, a ratio <= 0 means 0), and
+  // ar_keep [nvar] marks species never frozen (keepActive/keepSpcActive).
+  int ar_target;
+  double ar_thr, ar_ratio;
+  const double* ar_thr_cell;
+  const int* ar_target_cell;
+  const double* ar_ratio_cell;
+  const unsigned char* ar_keep;
   // hand-over of long-running cells to the block-per-cell kernel: a cell
   // about to start step evict_after + 1 leaves its state (Y in c_out, T and H
   // in RSTATUS(4:5), counters in ISTATUS(1:8)) and its id at
@@ -90,10 +108,14 @@ struct Lane {
   int nfun, njac, nstp, nacc, nrej, ndec, nsol, nsng;
   double texit, hexit, hnew_out;
   int ierr;
+  int ar_built;   // auto-reduction: the frozen set is chosen
+  int ar_report;  // auto-reduction: threshold from a target species (RSTATUS(4))
+  double ar_thr;  // auto-reduction: the threshold used
 };
 
-template <bool STRICT, int NC>
+template <bool STRICT, int NC, bool AR = false>
 struct Rosenbrock {
+  static_assert(!AR || NC == 1, "auto-reduction runs one cell per thread");
   static constexpr int TSN = TS * NC;
   const MechDev& m;
   const RosMethod& r;
@@ -162,6 +184,9 @@ struct Rosenbrock {
     L.hexit = 0.0;
     L.hnew_out = 0.0;
     L.ierr = 0;
+    L.ar_built = 0;
+    L.ar_report = 0;
+    L.ar_thr = 0.0;
     // Hstart (Rosenbrock :420-428; INTEGRATE keeps only RCNTRL > 0, :115-117)
     double hs = p.hstart_default;
     if (p.hstart) {
@@ -230,6 +255,25 @@ struct Rosenbrock {
     const int nvar = m.nvar;
     const double* y = arr(w, p.lay.y0, q);
     const int cell = L.cell;
+    if constexpr (AR) {
+      // AutoReduce_1stOrder (:1702-1712) for every frozen species, after a
+      // successful integration (:1226-1232)
+      if (L.ierr == 1 && L.ar_built) {
+        double* yw = arr(w, p.lay.y0, q);
+        const double* slv = arr(w, p.lay.slv, q);
+        const double* pr = arr(w, p.lay.prod, q);
+        const double* lo = arr(w, p.lay.loss, q);
+        const double dt = p.tend - p.tstart;
+        for (int i = 0; i < nvar; ++i) {
+          if (slv[i * TSN] != 0.0) continue;
+          const double k = lo[i * TSN];
+          const double yi = yw[i * TSN];
+          if (k <= 1.0e-30 || yi <= 1.0e-30) continue;
+          const double term = pr[i * TSN] / k;
+          yw[i * TSN] = term + (yi - term) * exp(-k * dt);
+        }
+      }
+    }
     for (int i = 0; i < nvar; ++i) p.c_out[(long long)i * p.ldc + cell] = y[i * TSN];
     if (p.c_out != p.c_in)
       for (int f = 0; f < m.nfix; ++f)
@@ -244,6 +288,7 @@ struct Rosenbrock {
         if (k == 0) v = L.texit;
         if (k == 1) v = L.hexit;
         if (k == 2) v = L.hnew_out;
+        if (AR && k == 3 && L.ar_report) v = L.ar_thr;  // RSTATUS(NARthr)
         p.rstatus[(long long)k * p.ldo + cell] = v;
       }
     }
@@ -273,14 +318,59 @@ struct Rosenbrock {
   // time derivative for non-autonomous problems (:1748-1769; rates are frozen
   // for the step, ICNTRL(15)=-1, so FunTemplate(T+Delta) evaluates the same
   // point).
-  __device__ void fun0_jac0(double* w, const Lane* L) {
+  __device__ void fun0_jac0(double* w, Lane* L) {
     const double* aux = arr(w, p.lay.aux, 0);
     const double* Y = arr(w, p.lay.y0, 0);
     double* B = arr(w, p.lay.b, 0);
     // B products once for both Jac_SP and Fun0's D_VAR terms.
     b_products<NC>(m, Y, aux, B);
-    jac_sp<STRICT, NC>(m, B, arr(w, p.lay.j0, 0));
-    fun_split<STRICT, NC>(m, Y, aux, arr(w, p.lay.a, 0), B, arr(w, p.lay.fcn0, 0));
+    if constexpr (AR) {
+      double* J0 = arr(w, p.lay.j0, 0);
+      double* slv = arr(w, p.lay.slv, 0);
+      if (!L[0].ar_built && L[0].T == p.tstart) {
+        // FunSplitF at T = Tstart and the frozen set (:900-930)
+        double* pr = arr(w, p.lay.prod, 0);
+        double* lo = arr(w, p.lay.loss, 0);
+        fun_split<STRICT, NC, true>(m, Y, aux, arr(w, p.lay.a, 0), B, arr(w, p.lay.fcn0, 0), pr, lo);
+        const int cell = L[0].cell;
+        double thr = p.ar_thr, ratio = p.ar_ratio;
+        int tgt = p.ar_target;
+        if (p.ar_thr_cell) {
+          const double v = p.ar_thr_cell[cell];
+          thr = v > 0.0 ? v : 1.0e2;
+        }
+        if (p.ar_target_cell) tgt = p.ar_target_cell[cell];
+        if (p.ar_ratio_cell) {
+          const double v = p.ar_ratio_cell[cell];
+          ratio = v > 0.0 ? v : 0.0;
+        }
+        if (tgt > 0) {  // 1..nvar, checked on the host
+          const int t = tgt - 1;
+          thr = ratio * fmax(lo[t * TSN] * Y[t * TSN], pr[t * TSN]);
+        }
+        for (int i = 0; i < m.nvar; ++i) {
+          const double lossy = lo[i * TSN] * Y[i * TSN];
+          const bool keep = p.ar_keep && p.ar_keep[i];
+          slv[i * TSN] = (!keep && fabs(lossy) < thr && fabs(pr[i * TSN]) < thr) ? 0.0 : 1.0;
+        }
+        L[0].ar_thr = thr;
+        L[0].ar_report = tgt > 0;
+        L[0].ar_built = 1;
+      } else {
+        fun_split<STRICT, NC>(m, Y, aux, arr(w, p.lay.a, 0), B, arr(w, p.lay.fcn0, 0));
+      }
+      jac_sp<STRICT, NC>(m, B, J0);
+      // frozen rows and columns of Jac0 to 0: Ghimj = -Jac0 + ghinv I then
+      // factors like cKppDecomp's compressed matrix (the frozen species only
+      // meet exact zeros)
+      for (int e = 0; e < m.lu_nonzero; ++e) {
+        const int ir = ldi(m.lu_irow + e), ic = ldi(m.lu_icol + e);
+        if (slv[ir * TSN] == 0.0 || slv[ic * TSN] == 0.0) J0[e * TSN] = 0.0;
+      }
+    } else {
+      jac_sp<STRICT, NC>(m, B, arr(w, p.lay.j0, 0));
+      fun_split<STRICT, NC>(m, Y, aux, arr(w, p.lay.a, 0), B, arr(w, p.lay.fcn0, 0));
+    }
     if (!p.autonomous) {
       double* dfdt = arr(w, p.lay.dfdt, 0);
       const double* f0 = arr(w, p.lay.fcn0, 0);
@@ -392,6 +482,10 @@ struct Rosenbrock {
             const double dd = dfdt[i * TSN + q * TS];
             k = STRICT ? k + hg[q] * dd : fma(hg[q], dd, k);
           }
+          if constexpr (AR) {
+            // a frozen species' stage vector stays 0 (:704-728 loop over kept ones)
+            if (arr(w, p.lay.slv, q)[i * TSN] == 0.0) k = 0.0;
+          }
           Ks[i * TSN + q * TS] = k;
         }
       }
@@ -433,7 +527,7 @@ struct Rosenbrock {
         const double* ynq = arr(w, p.lay.y1, q);
         for (int i = 0; i < nvar; ++i) {
           const double v = ynq[i * TSN];
-          yq[i * TSN] = p.clamp_negative ? fmax(v, 0.0) : v;
+          yq[i * TSN] = (!AR && p.clamp_negative) ? fmax(v, 0.0) : v;  // ros_yIntegrator does not clamp
         }
       }
     }
@@ -454,13 +548,13 @@ __device__ __forceinline__ int queue_claim(int* counter) {
   return base + __popc(lt);
 }
 
-template <bool STRICT, bool QUEUE, int NC>
+template <bool STRICT, bool QUEUE, int NC, bool AR = false>
 __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams& p) {
   constexpr int TSN = TS * NC;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long warp = tid / TS;
   const int lane = (int)(tid % TS);
-  Rosenbrock<STRICT, NC> ros(m, r, p);
+  Rosenbrock<STRICT, NC, AR> ros(m, r, p);
   double* w = p.ws + warp * (long long)p.lay.total * TSN + lane;
   Lane L[NC];
   bool has[NC];

@@ -133,7 +133,9 @@ const char* gc_kpp_last_error(void);
  *   hstart   [ncell] or NULL       per-cell RCNTRL(3) (the KPPHvalue chain,
  *                                  fullchem_AutoReduceFuncs.F90:287)
  *   istatus  [20][ldo] out or NULL ISTATUS(1:8) counters, rest zero
- *   rstatus  [20][ldo] out or NULL RSTATUS(1:3) = Texit, Hexit, Hnew
+ *   rstatus  [20][ldo] out or NULL RSTATUS(1:3) = Texit, Hexit, Hnew;
+ *                                  RSTATUS(4) = auto-reduce threshold
+ *                                  with a target species, rest zero
  *   ierr     [ncell]   out         IERR per cell
  *   mem      GC_KPP_MEM_HOST or GC_KPP_MEM_DEVICE for all arrays above
  *   stream   cudaStream_t (NULL = default stream); with device memory the
@@ -142,9 +144,15 @@ const char* gc_kpp_last_error(void);
  *
  * Supported: Rosenbrock methods ICNTRL(3) = 0..6, autonomous or not,
  * vector or scalar tolerances, ICNTRL(4) step cap, ICNTRL(16) clamping,
- * RCNTRL(1:7).  ICNTRL(15) must disable in-integrator rate updates (-1, 0
- * after merging, or 2) and ICNTRL(12) (auto-reduce) must be off; otherwise
- * GC_KPP_EUNSUPPORTED. */
+ * RCNTRL(1:7), and auto-reduction (ICNTRL(12) = 1: ros_yIntegrator,
+ * :789-1237) with threshold RCNTRL(12) (default 100 molec/cm3/s) or a
+ * target species ICNTRL(14) in 1..NVAR with ratio RCNTRL(14), the
+ * threshold then reported in RSTATUS(4).  Auto-reduction runs on the
+ * thread-per-cell kernel with GC_KPP_OPT_ARITH 0 or 1 and the row-wise LU.
+ * GC_KPP_EUNSUPPORTED for: in-integrator rate updates (ICNTRL(15) must be
+ * -1, 0 after merging, or 2), the append form of auto-reduction
+ * (ICNTRL(13) = 1, ros_yIntegratorA), a target species outside VAR, and
+ * auto-reduction with more cells per thread or the KppDecomp-order LU. */
 int gc_kpp_integrate_batch(gc_kpp_ctx* ctx, int ncell, double tin, double tout,
                            double* c, long long ldc,
                            const double* rconst, long long ldr,
@@ -197,6 +205,28 @@ int gc_kpp_update_rconst_batch(gc_kpp_ctx* ctx, int ncell, const double* met, lo
  * or host memory (copied now).  het = NULL clears it (heterogeneous rates 0).
  * A step over a different number of cells fails with GC_KPP_EINVAL. */
 int gc_kpp_ctx_set_hetstate(gc_kpp_ctx* ctx, int ncell, const double* het, long long ldh, int mem);
+
+/* Auto-reduction controls of the following integrations with ICNTRL(12) = 1
+ * on this context, as Do_FullChem sets them per grid box
+ * (KPP/fullchem/fullchem_AutoReduceFuncs.F90:274-343, GeosCore/
+ * fullchem_mod.F90:510-515 and :585-587):
+ *
+ *   thr    [ncell] or NULL  RCNTRL(12) of each cell (<= 0: the default 100)
+ *   target [ncell] or NULL  ICNTRL(14) of each cell, 0..NVAR (1-based
+ *                           species; 0 = threshold mode)
+ *   ratio  [ncell] or NULL  RCNTRL(14) of each cell (<= 0: 0)
+ *   keep   [NVAR]  or NULL  keepSpcActive in HOST memory: nonzero species
+ *                           are never frozen (keepActive on); NULL = off
+ *   mem    GC_KPP_MEM_HOST or GC_KPP_MEM_DEVICE for thr/target/ratio
+ *
+ * The arrays are copied.  A NULL per-cell array leaves that control to the
+ * call's ICNTRL/RCNTRL.  Each call replaces every earlier setting; all NULL
+ * clears them.  An integration over a different number of cells (the cell
+ * count, or cell_limit of the ordered forms) fails with GC_KPP_EINVAL; a
+ * target outside 0..NVAR fails here with GC_KPP_EUNSUPPORTED.  Integrations
+ * without ICNTRL(12) = 1 ignore these controls. */
+int gc_kpp_ctx_set_autoreduce(gc_kpp_ctx* ctx, int ncell, const double* thr, const int* target,
+                              const double* ratio, const unsigned char* keep, int mem);
 
 int gc_kpp_update_rconst_het_batch(gc_kpp_ctx* ctx, int ncell, const double* met, long long ldm,
                                    const double* photol, long long ldp, const double* c, long long ldc,

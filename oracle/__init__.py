@@ -43,6 +43,9 @@ def load(variant="strict", mech="fullchem"):
     lib = ctypes.CDLL(path)
     vp, i32, i64, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
     lib.oracle_integrate_batch.argtypes = [i32, f64, f64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64, vp, i32]
+    lib.oracle_integrate_batch_ar.argtypes = [i32, f64, f64, vp, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, i64, vp,
+                                              i32, vp, vp, vp]
+    lib.oracle_set_keep.argtypes = [vp]
     lib.oracle_update_rconst_batch.argtypes = [i32, vp, i64, vp, i64, vp, i64, vp, i64]
     lib.oracle_update_rconst_het_batch.argtypes = [i32, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64]
     lib.oracle_fun_split.argtypes = [vp, vp, vp, vp]
@@ -72,8 +75,10 @@ def _c(a, dt):
 
 
 def integrate(c, rconst, atol, rtol, tin, tout, icntrl=None, rcntrl=None, hstart=None, variant="strict",
-              nthreads=0, mech="fullchem"):
+              nthreads=0, mech="fullchem", ar_thr=None, ar_target=None, ar_ratio=None):
     """Batched INTEGRATE on the CPU.  c [NSPEC, n] (copied), rconst [NREACT, n].
+    ar_thr/ar_target/ar_ratio [n]: per-cell RCNTRL(12), ICNTRL(14),
+    RCNTRL(14) of auto-reduction (optional).
     Returns (c_out, istatus [20, n], rstatus [20, n], ierr [n])."""
     lib = load(variant, mech)
     c = np.array(c, dtype=np.float64, order="C", copy=True)
@@ -85,10 +90,21 @@ def integrate(c, rconst, atol, rtol, tin, tout, icntrl=None, rcntrl=None, hstart
     ic = _c(icntrl, np.int32) if icntrl is not None else None
     rc = _c(rcntrl, np.float64) if rcntrl is not None else None
     hs = _c(hstart, np.float64) if hstart is not None else None
-    lib.oracle_integrate_batch(n, float(tin), float(tout), _p(c), n, _p(rconst), n, _p(_c(atol, np.float64)),
-                               _p(_c(rtol, np.float64)), _p(ic), _p(rc), _p(hs), _p(ist), _p(rst), n, _p(ierr),
-                               int(nthreads))
+    at = _c(ar_thr, np.float64) if ar_thr is not None else None
+    ag = _c(ar_target, np.int32) if ar_target is not None else None
+    ar = _c(ar_ratio, np.float64) if ar_ratio is not None else None
+    lib.oracle_integrate_batch_ar(n, float(tin), float(tout), _p(c), n, _p(rconst), n, _p(_c(atol, np.float64)),
+                                  _p(_c(rtol, np.float64)), _p(ic), _p(rc), _p(hs), _p(ist), _p(rst), n, _p(ierr),
+                                  int(nthreads), _p(at), _p(ag), _p(ar))
     return c, ist, rst, ierr
+
+
+def set_keep(keep, variant="strict", mech="fullchem"):
+    """keepSpcActive of auto-reduction: a [NVAR] boolean mask of species that
+    are never frozen (keepActive on), or None (keepActive off)."""
+    lib = load(variant, mech)
+    k = None if keep is None else _c(np.asarray(keep) != 0, np.uint8)
+    lib.oracle_set_keep(_p(k))
 
 
 def update_rconst(met, photol, c, variant="strict", mech="fullchem", het=None):

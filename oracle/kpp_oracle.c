@@ -609,6 +609,17 @@ static void ros_yintegrator(cellctx_t* cx, const method_t* m, double* Y, double 
   *IERR = 1;
 }
 
+/* keepActive and keepSpcActive (gckpp_Global; fullchem_mod.F90:510-515 and
+ * :585-587 set them through fullchem_AutoReduceFuncs.F90:47-110, 128-140):
+ * species of the mask are never frozen by the reduction.  Off by default. */
+static unsigned char g_keep[NVAR];
+static int g_keep_on = 0;
+
+void oracle_set_keep(const unsigned char* keep) {
+  g_keep_on = keep != 0;
+  for (int i = 0; i < NVAR; ++i) g_keep[i] = keep ? (keep[i] != 0) : 0;
+}
+
 void oracle_integrate(double* C, const double* RCONST, const double* atol, const double* rtol, double tin,
                       double tout, const int* icntrl_u, const double* rcntrl_u, int* istatus_u, double* rstatus_u,
                       int* ierr_u) {
@@ -658,8 +669,8 @@ void oracle_integrate(double* C, const double* RCONST, const double* atol, const
     /* auto-reduction (gckpp_Integrator.F90:388-394, 478-520): ICNTRL(12) = 1
      * selects ros_yIntegrator with threshold RCNTRL(12) (default 100) or, with
      * ICNTRL(14) = target species, RCNTRL(14) x max(P, L*y) of that species;
-     * keepActive is off.  The append form (ICNTRL(13) = 1, ros_yIntegratorA)
-     * is not restated: IERR = -100.  ICNTRL(20) = 7 (unused by the reference)
+     * keepActive with the mask of oracle_set_keep.  The append form
+     * (ICNTRL(13) = 1, ros_yIntegratorA) is not restated: IERR = -100.  ICNTRL(20) = 7 (unused by the reference)
      * selects the masked-full decomposition of the GPU design instead of the
      * compressed one (tests only). */
     const int Autoreduce = ICNTRL[11] == 1;
@@ -670,8 +681,8 @@ void oracle_integrate(double* C, const double* RCONST, const double* atol, const
     if (Autoreduce) {
       const double threshold = RCNTRL[11] > 0.0 ? RCNTRL[11] : 1.0e2;
       ros_yintegrator(&cx, &m, C, tin, tout, &Texit, atol, rtol, Autonomous, VectorTol, Max_no_steps, Roundoff,
-                      Hmin, Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, threshold, ICNTRL[13], RCNTRL[13], 0,
-                      ICNTRL[19] == 7, &IERR);
+                      Hmin, Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, threshold, ICNTRL[13], RCNTRL[13],
+                      g_keep_on ? g_keep : 0, ICNTRL[19] == 7, &IERR);
     } else {
       ros_integrator(&cx, &m, C, tin, tout, &Texit, atol, rtol, Autonomous, VectorTol, Max_no_steps, Roundoff,
                      Hmin, Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, ICNTRL[15] == 1, &IERR);
@@ -691,10 +702,14 @@ int oracle_max_threads(void) {
 #endif
 }
 
-void oracle_integrate_batch(int ncell, double tin, double tout, double* c, long long ldc, const double* rconst,
-                            long long ldr, const double* atol, const double* rtol, const int* icntrl_u,
-                            const double* rcntrl_u, const double* hstart, int* istatus, double* rstatus,
-                            long long ldo, int* ierr, int nthreads) {
+/* The batch over cells; ar_thr/ar_target/ar_ratio, when given, are each
+ * cell's RCNTRL(12), ICNTRL(14) and RCNTRL(14) (fullchem_AutoReduceFuncs.F90:
+ * 293-343 sets them per grid box). */
+void oracle_integrate_batch_ar(int ncell, double tin, double tout, double* c, long long ldc, const double* rconst,
+                               long long ldr, const double* atol, const double* rtol, const int* icntrl_u,
+                               const double* rcntrl_u, const double* hstart, int* istatus, double* rstatus,
+                               long long ldo, int* ierr, int nthreads, const double* ar_thr, const int* ar_target,
+                               const double* ar_ratio) {
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 24) num_threads(nthreads)
@@ -704,15 +719,28 @@ void oracle_integrate_batch(int ncell, double tin, double tout, double* c, long 
     int is[20], ie;
     for (int k = 0; k < NSPEC; ++k) C[k] = c[(long long)k * ldc + cell];
     for (int k = 0; k < NREACT; ++k) R[k] = rconst[(long long)k * ldr + cell];
+    int ic[20];
     for (int k = 0; k < 20; ++k) rc[k] = rcntrl_u ? rcntrl_u[k] : 0.0;
+    for (int k = 0; k < 20; ++k) ic[k] = icntrl_u ? icntrl_u[k] : 0;
     if (hstart) rc[2] = hstart[cell];
-    oracle_integrate(C, R, atol, rtol, tin, tout, icntrl_u, rc, is, rs, &ie);
+    if (ar_thr) rc[11] = ar_thr[cell];
+    if (ar_target) ic[13] = ar_target[cell];
+    if (ar_ratio) rc[13] = ar_ratio[cell];
+    oracle_integrate(C, R, atol, rtol, tin, tout, ic, rc, is, rs, &ie);
     for (int k = 0; k < NVAR; ++k) c[(long long)k * ldc + cell] = C[k];
     if (istatus) for (int k = 0; k < 20; ++k) istatus[(long long)k * ldo + cell] = is[k];
     if (rstatus) for (int k = 0; k < 20; ++k) rstatus[(long long)k * ldo + cell] = rs[k];
     ierr[cell] = ie;
   }
   (void)nthreads;
+}
+
+void oracle_integrate_batch(int ncell, double tin, double tout, double* c, long long ldc, const double* rconst,
+                            long long ldr, const double* atol, const double* rtol, const int* icntrl_u,
+                            const double* rcntrl_u, const double* hstart, int* istatus, double* rstatus,
+                            long long ldo, int* ierr, int nthreads) {
+  oracle_integrate_batch_ar(ncell, tin, tout, c, ldc, rconst, ldr, atol, rtol, icntrl_u, rcntrl_u, hstart, istatus,
+                            rstatus, ldo, ierr, nthreads, 0, 0, 0);
 }
 
 void oracle_update_rconst_het_batch(int ncell, const double* met, long long ldm, const double* photol,

@@ -48,5 +48,14 @@ void oracle_integrate_batch(int ncell, double tin, double tout, double* c, long 
                             const double* rconst, long long ldr, const double* atol, const double* rtol,
                             const int* icntrl_u, const double* rcntrl_u, const double* hstart,
                             int* istatus, double* rstatus, long long ldo, int* ierr, int nthreads);
+/* The same with per-cell RCNTRL(12), ICNTRL(14), RCNTRL(14) (each optional). */
+void oracle_integrate_batch_ar(int ncell, double tin, double tout, double* c, long long ldc,
+                               const double* rconst, long long ldr, const double* atol, const double* rtol,
+                               const int* icntrl_u, const double* rcntrl_u, const double* hstart,
+                               int* istatus, double* rstatus, long long ldo, int* ierr, int nthreads,
+                               const double* ar_thr, const int* ar_target, const double* ar_ratio);
+/* keepSpcActive [NVAR] (nonzero = never frozen) with keepActive on; NULL
+ * turns keepActive off. */
+void oracle_set_keep(const unsigned char* keep);
 int oracle_max_threads(void);
 #endif

@@ -1,8 +1,8 @@
-"""Auto-reduction (SURVEY §8 f3), the CPU restatement: ros_yIntegrator of
+"""Auto-reduction, the CPU restatement: ros_yIntegrator of
 KPP/fullchem/gckpp_Integrator.F90:789-1237 with cKppDecomp (:2624-2661),
 the DO_SLV-guarded KppSolve and AutoReduce_1stOrder (:1702-1712), selected by
-ICNTRL(12) = 1 as INTEGRATE does (:388-394, :478-520).  The GPU solver does
-not run it yet (ICNTRL(12) = 1 is refused with GC_KPP_EUNSUPPORTED)."""
+ICNTRL(12) = 1 as INTEGRATE does (:388-394, :478-520).  The GPU form is
+tested against it in test_zzz_autoreduce_gpu.py."""
 import numpy as np
 import pytest
 
@@ -106,3 +106,89 @@ def test_masked_full_decomposition_equals_the_compressed_one(case, thr):
     b = oracle.integrate(case["cells"]["c"], case["r"], case["atol"], case["rtol"], 0.0, 600.0, ic, rc)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+@pytest.fixture
+def keep_off():
+    import oracle
+
+    yield
+    oracle.set_keep(None)
+
+
+def test_keep_every_species_is_the_full_integrator(case, keep_off):
+    """keepActive with every species in keepSpcActive freezes nothing."""
+    import oracle
+
+    oracle.set_keep(np.ones(353, np.uint8))
+    c, ist, rst, ierr = _ar(case, thr=1e5)
+    c0, ist0, rst0, ierr0 = case["full"]
+    assert np.array_equal(c, c0) and np.array_equal(ist[:8], ist0[:8])
+
+
+def test_halogens_kept_active(case, keep_off, ir):
+    """fullchem_AR_KeepHalogensActive's 40 species stay in the solve: with a
+    threshold that freezes some of them, keeping them changes their result
+    and brings it back towards the full integration."""
+    import gcchem.autoreduce as ar
+    import oracle
+
+    mask = ar.keep_mask(ir)
+    assert mask.sum() == 40
+    free = _ar(case, thr=1e5)[0]
+    oracle.set_keep(mask)
+    kept = _ar(case, thr=1e5)[0]
+    full = case["full"][0]
+    hal = np.nonzero(mask)[0]
+    assert not np.array_equal(free[hal], kept[hal])
+    err_free = np.abs(free[hal] - full[hal]).sum()
+    err_kept = np.abs(kept[hal] - full[hal]).sum()
+    assert err_kept < err_free
+
+
+def test_per_cell_controls_equal_per_cell_calls(case, ir):
+    """The batch entry with per-cell RCNTRL(12)/ICNTRL(14)/RCNTRL(14) gives
+    each cell what a call with those scalars gives it."""
+    import gcchem.autoreduce as ar
+    import oracle
+
+    n = case["cells"]["c"].shape[1]
+    rng = np.random.default_rng(5)
+    thr, target, ratio = ar.integrator_options(ir, n, threshold=1e3, pmid=rng.uniform(100, 1000, n),
+                                               pmid_sfc=np.full(n, 1000.0), is_prs_threshold=True)
+    # half of the cells in key-species mode
+    t2, g2, r2 = ar.integrator_options(ir, n, is_key_threshold=True, suncos_mid=rng.uniform(-1, 1, n),
+                                       tuning_oh=1e-3, tuning_no2=5e-5)
+    half = np.arange(n) % 2 == 1
+    thr[half], target[half], ratio[half] = t2[half], g2[half], r2[half]
+    ic = case["ic"].copy()
+    ic[11] = 1
+    got = oracle.integrate(case["cells"]["c"], case["r"], case["atol"], case["rtol"], 0.0, 600.0, ic, case["rc"],
+                           ar_thr=thr, ar_target=target, ar_ratio=ratio)
+    for k in range(0, n, 7):
+        ick, rck = ic.copy(), case["rc"].copy()
+        rck[11], ick[13], rck[13] = thr[k], target[k], ratio[k]
+        one = oracle.integrate(case["cells"]["c"][:, k:k + 1], case["r"][:, k:k + 1], case["atol"], case["rtol"],
+                               0.0, 600.0, ick, rck)
+        for x, y in zip(got, one):
+            assert np.array_equal(x[..., k], y[..., 0])
+    assert np.all(got[3] == 1)
+    # key-species cells report their threshold
+    assert np.all(got[2][3, half] > 0) and np.all(got[2][3, ~half] == 0)
+
+
+def test_integrator_options_follow_the_driver(ir):
+    import gcchem.autoreduce as ar
+
+    oh = ir["species"].index("OH") + 1
+    no2 = ir["species"].index("NO2") + 1
+    thr, target, ratio = ar.integrator_options(ir, 3, threshold=50.0)
+    assert np.all(thr == 50.0) and np.all(target == 0) and np.all(ratio == 0)
+    thr, _, _ = ar.integrator_options(ir, 2, threshold=50.0, pmid=np.array([500.0, 1000.0]),
+                                      pmid_sfc=np.array([1000.0, 1000.0]), is_prs_threshold=True)
+    assert np.array_equal(thr, [25.0, 50.0])
+    sc = np.array([0.5, -0.1391731, -0.2, -0.1])
+    thr, target, ratio = ar.integrator_options(ir, 4, is_key_threshold=True, suncos_mid=sc, tuning_oh=1e-3,
+                                               tuning_no2=5e-5)
+    assert list(target) == [oh, no2, no2, oh]
+    assert list(ratio) == [1e-3, 5e-5, 5e-5, 1e-3]

@@ -3,8 +3,8 @@ cudaMalloc (a host application that owns all device memory, or code that runs
 while its allocator must not be touched), gives the same results as the
 regular entry point, through the C ABI, on two calls in a row.
 
-Collected last (file name), so a run that stops at its first failure has run
-every other test before this one."""
+Collected near the end (file name), so a run that stops at its first failure
+has run the parity tests of the regular entry points before this one."""
 import ctypes
 
 import numpy as np
