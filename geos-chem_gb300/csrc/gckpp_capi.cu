@@ -68,7 +68,8 @@ cudaError_t upload(const X* host, size_t n, const X** dev, std::vector<void*>& o
 }
 
 // Workspace layout of one cell of the thread-per-cell kernel; ar adds the
-// auto-reduction arrays (frozen mask, P_VAR and D_VAR at Tstart).
+// auto-reduction arrays (order of entry, P_VAR and D_VAR at Tstart and at
+// the current step).
 WsLayout make_layout(bool ar = false) {
   WsLayout l;
   int o = 0;
@@ -83,11 +84,13 @@ WsLayout make_layout(bool ar = false) {
   l.b = o; o += T::NB;
   l.j0 = o; o += T::LU_NONZERO;
   l.g = o; o += T::LU_NONZERO;
-  l.slv = l.prod = l.loss = -1;
+  l.slv = l.prod = l.loss = l.pcur = l.dcur = -1;
   if (ar) {
     l.slv = o; o += T::NVAR;
     l.prod = o; o += T::NVAR;
     l.loss = o; o += T::NVAR;
+    l.pcur = o; o += T::NVAR;
+    l.dcur = o; o += T::NVAR;
   }
   l.total = o;
   return l;
@@ -347,7 +350,7 @@ struct Resolved {
   double hmin = 0, hmax = 0, hstart_default = 0, facmin = 0, facmax = 0, facrej = 0, facsafe = 0;
   int autonomous = 1, clamp = 0;
   // auto-reduction (Rosenbrock :388-394, :478-487): ICNTRL(12) = 1
-  int autoreduce = 0, ar_target = 0;
+  int autoreduce = 0, ar_target = 0, ar_append = 0;
   double ar_thr = 1.0e2, ar_ratio = 0.0;
 };
 
@@ -366,12 +369,11 @@ int resolve(const int* icntrl_u, const double* rcntrl_u, double tin, double tout
   if (icntrl[14] != -1 && (icntrl[14] & 5))
     return fail(GC_KPP_EUNSUPPORTED, "ICNTRL(15) requests Update_RCONST/Update_SUN inside the integrator");
   if (icntrl[11] == 1) {
-    if (icntrl[12] == 1)
-      return fail(GC_KPP_EUNSUPPORTED, "auto-reduce with append (ICNTRL(13)=1, ros_yIntegratorA) is not implemented");
     if (icntrl[13] < 0 || icntrl[13] > T::NVAR)
       return fail(GC_KPP_EUNSUPPORTED, "auto-reduce target species ICNTRL(14) out of range");
     R.autoreduce = 1;
     R.ar_target = icntrl[13];
+    R.ar_append = icntrl[12] == 1 ? 1 : 0;  // ros_yIntegratorA
     if (rcntrl[11] > 0.0) R.ar_thr = rcntrl[11];
     R.ar_ratio = rcntrl[13];
   }
@@ -616,6 +618,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   p.clamp_negative = R.clamp;
   p.lu_form = c->lu_form;
   p.ar_target = R.ar_target;
+  p.ar_append = R.ar_append;
   p.ar_thr = R.ar_thr;
   p.ar_ratio = R.ar_ratio;
   if (R.autoreduce) {

@@ -34,7 +34,10 @@ struct RosMethod {
 
 struct WsLayout {
   int aux, y0, y1, fcn0, fcn, dfdt, k, a, b, j0, g;
-  int slv, prod, loss;  // auto-reduction only (else -1): DO_SLV mask, P_VAR and D_VAR at Tstart
+  // auto-reduction only (else -1): the order of entry of each species into
+  // the solve (-1 frozen, 0 from the start, t the t-th appended one), P_VAR
+  // and D_VAR at Tstart, and P_VAR/D_VAR of the current step (append form)
+  int slv, prod, loss, pcur, dcur;
   int total;
 };
 
@@ -76,7 +79,10 @@ struct RosParams {
   // (fullchem_AutoReduceFuncs.F90:293-343 sets them per grid box; a
   // threshold <= 0 means the default 100, a ratio <= 0 means 0), and
   // ar_keep [nvar] marks species never frozen (keepActive/keepSpcActive).
-  int ar_target;
+  // ar_append selects the append form (ros_yIntegratorA, :1242-1700): at
+  // every step a frozen species whose |P| or |L*y| exceeds the RCNTRL(12)
+  // threshold re-enters the solve after the species already in it.
+  int ar_target, ar_append;
   double ar_thr, ar_ratio;
   const double* ar_thr_cell;
   const int* ar_target_cell;
@@ -110,7 +116,9 @@ struct Lane {
   int ierr;
   int ar_built;   // auto-reduction: the frozen set is chosen
   int ar_report;  // auto-reduction: threshold from a target species (RSTATUS(4))
+  int ar_napp;    // auto-reduction: species appended so far
   double ar_thr;  // auto-reduction: the threshold used
+  double ar_thr_app;  // auto-reduction: the RCNTRL(12) threshold of APPEND
 };
 
 template <bool STRICT, int NC, bool AR = false>
@@ -186,7 +194,9 @@ struct Rosenbrock {
     L.ierr = 0;
     L.ar_built = 0;
     L.ar_report = 0;
+    L.ar_napp = 0;
     L.ar_thr = 0.0;
+    L.ar_thr_app = 0.0;
     // Hstart (Rosenbrock :420-428; INTEGRATE keeps only RCNTRL > 0, :115-117)
     double hs = p.hstart_default;
     if (p.hstart) {
@@ -265,7 +275,7 @@ struct Rosenbrock {
         const double* lo = arr(w, p.lay.loss, q);
         const double dt = p.tend - p.tstart;
         for (int i = 0; i < nvar; ++i) {
-          if (slv[i * TSN] != 0.0) continue;
+          if (slv[i * TSN] >= 0.0) continue;  // in the solve
           const double k = lo[i * TSN];
           const double yi = yw[i * TSN];
           if (k <= 1.0e-30 || yi <= 1.0e-30) continue;
@@ -314,6 +324,36 @@ struct Rosenbrock {
     }
   }
 
+  // The frozen set of ros_yIntegrator (:917-958) from P_VAR/D_VAR at
+  // Tstart: order of entry -1 for the frozen species, 0 for the others.
+  __device__ void ar_build(Lane& L, const double* Y, const double* pr, const double* lo, double* slv) const {
+    const int cell = L.cell;
+    double thr = p.ar_thr, ratio = p.ar_ratio;
+    int tgt = p.ar_target;
+    if (p.ar_thr_cell) {
+      const double v = p.ar_thr_cell[cell];
+      thr = v > 0.0 ? v : 1.0e2;
+    }
+    L.ar_thr_app = thr;
+    if (p.ar_target_cell) tgt = p.ar_target_cell[cell];
+    if (p.ar_ratio_cell) {
+      const double v = p.ar_ratio_cell[cell];
+      ratio = v > 0.0 ? v : 0.0;
+    }
+    if (tgt > 0) {  // 1..nvar, checked on the host
+      const int t = tgt - 1;
+      thr = ratio * fmax(lo[t * TSN] * Y[t * TSN], pr[t * TSN]);
+    }
+    for (int i = 0; i < m.nvar; ++i) {
+      const double lossy = lo[i * TSN] * Y[i * TSN];
+      const bool keep = p.ar_keep && p.ar_keep[i];
+      slv[i * TSN] = (!keep && fabs(lossy) < thr && fabs(pr[i * TSN]) < thr) ? -1.0 : 0.0;
+    }
+    L.ar_thr = thr;
+    L.ar_report = tgt > 0;
+    L.ar_built = 1;
+  }
+
   // Fun0 and Jac0 at Y for all NC cells (ros_Integrator :667-677), and the
   // time derivative for non-autonomous problems (:1748-1769; rates are frozen
   // for the step, ICNTRL(15)=-1, so FunTemplate(T+Delta) evaluates the same
@@ -327,45 +367,34 @@ struct Rosenbrock {
     if constexpr (AR) {
       double* J0 = arr(w, p.lay.j0, 0);
       double* slv = arr(w, p.lay.slv, 0);
-      if (!L[0].ar_built && L[0].T == p.tstart) {
-        // FunSplitF at T = Tstart and the frozen set (:900-930)
-        double* pr = arr(w, p.lay.prod, 0);
-        double* lo = arr(w, p.lay.loss, 0);
+      const bool first = !L[0].ar_built && L[0].T == p.tstart;
+      if (first || p.ar_append) {
+        // FunSplitF: P_VAR and D_VAR as well, at T = Tstart (kept for
+        // AutoReduce_1stOrder) and, in the append form, at every step
+        double* pr = arr(w, first ? p.lay.prod : p.lay.pcur, 0);
+        double* lo = arr(w, first ? p.lay.loss : p.lay.dcur, 0);
         fun_split<STRICT, NC, true>(m, Y, aux, arr(w, p.lay.a, 0), B, arr(w, p.lay.fcn0, 0), pr, lo);
-        const int cell = L[0].cell;
-        double thr = p.ar_thr, ratio = p.ar_ratio;
-        int tgt = p.ar_target;
-        if (p.ar_thr_cell) {
-          const double v = p.ar_thr_cell[cell];
-          thr = v > 0.0 ? v : 1.0e2;
+        if (first) ar_build(L[0], Y, pr, lo, slv);
+        if (p.ar_append) {
+          // APPEND (:1460-1474, :2663-2700), in species order, against the
+          // RCNTRL(12) threshold
+          const double ta = L[0].ar_thr_app;
+          for (int i = 0; i < m.nvar; ++i)
+            if (slv[i * TSN] < 0.0 && (fabs(lo[i * TSN] * Y[i * TSN]) > ta || fabs(pr[i * TSN]) > ta))
+              slv[i * TSN] = (double)(++L[0].ar_napp);
         }
-        if (p.ar_target_cell) tgt = p.ar_target_cell[cell];
-        if (p.ar_ratio_cell) {
-          const double v = p.ar_ratio_cell[cell];
-          ratio = v > 0.0 ? v : 0.0;
-        }
-        if (tgt > 0) {  // 1..nvar, checked on the host
-          const int t = tgt - 1;
-          thr = ratio * fmax(lo[t * TSN] * Y[t * TSN], pr[t * TSN]);
-        }
-        for (int i = 0; i < m.nvar; ++i) {
-          const double lossy = lo[i * TSN] * Y[i * TSN];
-          const bool keep = p.ar_keep && p.ar_keep[i];
-          slv[i * TSN] = (!keep && fabs(lossy) < thr && fabs(pr[i * TSN]) < thr) ? 0.0 : 1.0;
-        }
-        L[0].ar_thr = thr;
-        L[0].ar_report = tgt > 0;
-        L[0].ar_built = 1;
       } else {
         fun_split<STRICT, NC>(m, Y, aux, arr(w, p.lay.a, 0), B, arr(w, p.lay.fcn0, 0));
       }
       jac_sp<STRICT, NC>(m, B, J0);
       // frozen rows and columns of Jac0 to 0: Ghimj = -Jac0 + ghinv I then
       // factors like cKppDecomp's compressed matrix (the frozen species only
-      // meet exact zeros)
+      // meet exact zeros).  An appended species' row keeps the columns that
+      // entered no later than it, its column is zeroed in earlier rows: the
+      // compressed pattern of APPEND, whose new row comes last.
       for (int e = 0; e < m.lu_nonzero; ++e) {
-        const int ir = ldi(m.lu_irow + e), ic = ldi(m.lu_icol + e);
-        if (slv[ir * TSN] == 0.0 || slv[ic * TSN] == 0.0) J0[e * TSN] = 0.0;
+        const double orr = slv[ldi(m.lu_irow + e) * TSN], oc = slv[ldi(m.lu_icol + e) * TSN];
+        if (orr < 0.0 || oc < 0.0 || oc > orr) J0[e * TSN] = 0.0;
       }
     } else {
       jac_sp<STRICT, NC>(m, B, arr(w, p.lay.j0, 0));
@@ -484,7 +513,7 @@ struct Rosenbrock {
           }
           if constexpr (AR) {
             // a frozen species' stage vector stays 0 (:704-728 loop over kept ones)
-            if (arr(w, p.lay.slv, q)[i * TSN] == 0.0) k = 0.0;
+            if (arr(w, p.lay.slv, q)[i * TSN] < 0.0) k = 0.0;
           }
           Ks[i * TSN + q * TS] = k;
         }

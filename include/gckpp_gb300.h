@@ -145,13 +145,13 @@ const char* gc_kpp_last_error(void);
  * Supported: Rosenbrock methods ICNTRL(3) = 0..6, autonomous or not,
  * vector or scalar tolerances, ICNTRL(4) step cap, ICNTRL(16) clamping,
  * RCNTRL(1:7), and auto-reduction (ICNTRL(12) = 1: ros_yIntegrator,
- * :789-1237) with threshold RCNTRL(12) (default 100 molec/cm3/s) or a
+ * :789-1237; with ICNTRL(13) = 1 the append form ros_yIntegratorA,
+ * :1242-1700) with threshold RCNTRL(12) (default 100 molec/cm3/s) or a
  * target species ICNTRL(14) in 1..NVAR with ratio RCNTRL(14), the
  * threshold then reported in RSTATUS(4).  Auto-reduction runs on the
  * thread-per-cell kernel with GC_KPP_OPT_ARITH 0 or 1 and the row-wise LU.
  * GC_KPP_EUNSUPPORTED for: in-integrator rate updates (ICNTRL(15) must be
- * -1, 0 after merging, or 2), the append form of auto-reduction
- * (ICNTRL(13) = 1, ros_yIntegratorA), a target species outside VAR, and
+ * -1, 0 after merging, or 2), a target species outside VAR, and
  * auto-reduction with more cells per thread or the KppDecomp-order LU. */
 int gc_kpp_integrate_batch(gc_kpp_ctx* ctx, int ncell, double tin, double tout,
                            double* c, long long ldc,

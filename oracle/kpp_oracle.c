@@ -329,9 +329,15 @@ static void ros_integrator(cellctx_t* cx, const method_t* m, double* Y, double T
  * (DO_SLV false); the others are integrated with the Jacobian restricted to
  * them (compressed pattern cLU_*, cKppDecomp) and KppSolve's DO_SLV-guarded
  * statements; at the end each frozen species takes the first-order
- * solution y = P/k + (y - P/k) exp(-k dt) (AutoReduce_1stOrder). */
+ * solution y = P/k + (y - P/k) exp(-k dt) (AutoReduce_1stOrder).
+ * ros_yIntegratorA (:1242-1700) adds APPEND (:2663-2700): at every step a
+ * frozen species whose |P| or |L*y| exceeds RCNTRL(12) re-enters the solve
+ * as the last row of the compressed pattern, with the columns active at that
+ * moment; ORD records the order of entry (-1 frozen, 0 active from the
+ * start, t the t-th appended species). */
 typedef struct {
   unsigned char DO_SLV[NVAR];
+  int ORD[NVAR], nappend;
   int SPC_MAP[NVAR], iSPC_MAP[NVAR];
   int rNVAR, cNONZERO;
   int JVS_MAP[LU_NONZERO], cLU_IROW[LU_NONZERO], cLU_ICOL[LU_NONZERO];
@@ -345,12 +351,15 @@ static void ar_build(ar_map_t* R, const double* Prod, const double* LossY, doubl
   int NRMV = 0, S = 0;
   for (int i = 0; i < NVAR; ++i) {
     R->DO_SLV[i] = 1;
+    R->ORD[i] = 0;
     R->iSPC_MAP[i] = -1;
   }
+  R->nappend = 0;
   for (int i = 0; i < NVAR; ++i) {
     if ((!keep || !keep[i]) && fabs(LossY[i]) < AR_thr && fabs(Prod[i]) < AR_thr) {
       NRMV = NRMV + 1;
       R->DO_SLV[i] = 0;
+      R->ORD[i] = -1;
       continue;
     }
     R->SPC_MAP[S] = i;
@@ -391,6 +400,31 @@ static void ar_build(ar_map_t* R, const double* Prod, const double* LossY, doubl
     R->cLU_CROW[R->rNVAR] = R->cNONZERO;
     R->cLU_DIAG[R->rNVAR] = R->cLU_DIAG[R->rNVAR - 1] + 1;
   }
+}
+
+/* APPEND (:2663-2700), 0-based: species idx becomes the last row of the
+ * compressed pattern, holding the entries of its row whose column is active
+ * now; no other row gains column idx. */
+static void ar_append(ar_map_t* R, int idx) {
+  R->DO_SLV[idx] = 1;
+  R->ORD[idx] = ++R->nappend;
+  R->rNVAR = R->rNVAR + 1;
+  const int r = R->rNVAR - 1;
+  R->SPC_MAP[r] = idx;
+  R->iSPC_MAP[idx] = r;
+  for (int i = 0; i < LU_NONZERO; ++i) {
+    if (ORACLE_LU_IROW[i] == idx && R->DO_SLV[ORACLE_LU_ICOL[i]]) {
+      const int e = R->cNONZERO;
+      R->cNONZERO = R->cNONZERO + 1;
+      R->cLU_IROW[e] = R->iSPC_MAP[ORACLE_LU_IROW[i]];
+      R->cLU_ICOL[e] = R->iSPC_MAP[ORACLE_LU_ICOL[i]];
+      R->JVS_MAP[e] = i;
+      if (e == 0 || R->cLU_IROW[e] != R->cLU_IROW[e - 1]) R->cLU_CROW[r] = e;
+      if (R->cLU_IROW[e] == R->cLU_ICOL[e]) R->cLU_DIAG[r] = e;
+    }
+  }
+  R->cLU_CROW[r + 1] = R->cNONZERO;
+  R->cLU_DIAG[r + 1] = R->cLU_DIAG[r] + 1;
 }
 
 /* cKppDecomp (gckpp_Integrator.F90:2624-2661) on the compressed pattern */
@@ -438,15 +472,20 @@ static void c_prepare_matrix(cellctx_t* cx, const ar_map_t* R, double* H, int Di
  * ghinv I decouples the frozen species (a frozen row is ghinv on the
  * diagonal, 0 elsewhere), factored by the full KppDecomp.  Frozen entries
  * only ever contribute exact zeros, so the kept entries come out as
- * cKppDecomp leaves them. */
+ * cKppDecomp leaves them.  An appended species' row keeps the columns that
+ * entered no later than it, and its column is zeroed in the rows that
+ * entered earlier: the compressed pattern with appended rows last, in the
+ * original order (the eliminations of an appended row only reach rows that
+ * precede it in both orders). */
 static void masked_prepare_matrix(cellctx_t* cx, const ar_map_t* R, double* H, int Direction, double gam,
                                   const double* Jac0, double* Ghimj, int* Singular) {
   int Nconsecutive = 0;
   *Singular = 1;
   while (*Singular) {
     for (int i = 0; i < LU_NONZERO; ++i) {
-      const int kr = R->DO_SLV[ORACLE_LU_IROW[i]], kc = R->DO_SLV[ORACLE_LU_ICOL[i]];
-      Ghimj[i] = -((kr && kc) ? Jac0[i] : 0.0);
+      /* with appends: row r holds column c if c entered no later than r */
+      const int orr = R->ORD[ORACLE_LU_IROW[i]], oc = R->ORD[ORACLE_LU_ICOL[i]];
+      Ghimj[i] = -((orr >= 0 && oc >= 0 && oc <= orr) ? Jac0[i] : 0.0);
     }
     double ghinv = 1.0 / (Direction * (*H) * gam);
     for (int i = 0; i < NVAR; ++i) Ghimj[ORACLE_LU_DIAG[i]] = Ghimj[ORACLE_LU_DIAG[i]] + ghinv;
@@ -469,8 +508,9 @@ static void ros_yintegrator(cellctx_t* cx, const method_t* m, double* Y, double 
                             int Max_no_steps, double Roundoff, double Hmin, double Hmax, double Hstart,
                             double FacMin, double FacMax, double FacRej, double FacSafe, double threshold,
                             int AR_target_spc, double AR_thr_ratio, const unsigned char* keep, int masked,
-                            int* IERR) {
+                            int append, int* IERR) {
   double Ynew[NVAR], Fcn0[NVAR], Fcn[NVAR], Prod[NVAR], Loss[NVAR], LossY[NVAR], K[6 * NVAR], dFdT[NVAR];
+  double Prd0[NVAR], Los0[NVAR];
   double Yerr[NVAR];
   static __thread double Jac0[LU_NONZERO], Ghimj[LU_NONZERO], cGhimj[LU_NONZERO];
   static __thread ar_map_t R;
@@ -495,7 +535,7 @@ static void ros_yintegrator(cellctx_t* cx, const method_t* m, double* Y, double 
     if (cx->istatus[Nstp] > Max_no_steps) { *IERR = -6; *Tout = T; return; }
     if (((T + 0.1 * H) == T) || (H <= Roundoff)) { *IERR = -7; *Tout = T; return; }
     H = fmin(H, fabs(Tend - T));
-    if (T == Tstart) { /* FunSplitF: production and loss as well */
+    if (append || T == Tstart) { /* FunSplitF: production and loss as well (every step in ros_yIntegratorA) */
       oracle_fun_pd(Y, cx->fix, cx->rct, Prod, Loss);
       for (int i = 0; i < NVAR; ++i) {
         LossY[i] = Loss[i] * Y[i];
@@ -512,8 +552,13 @@ static void ros_yintegrator(cellctx_t* cx, const method_t* m, double* Y, double 
         cx->rstatus[3] = AR_thr; /* RSTATUS(NARthr) */
       }
       ar_build(&R, Prod, LossY, AR_thr, keep);
+      memcpy(Prd0, Prod, sizeof(Prd0)); /* for AutoReduce_1stOrder */
+      memcpy(Los0, Loss, sizeof(Los0));
       reduced = 1;
     }
+    if (append) /* :1460-1474, against RCNTRL(12) itself, in species order */
+      for (int i = 0; i < NVAR; ++i)
+        if (!R.DO_SLV[i] && (fabs(LossY[i]) > threshold || fabs(Prod[i]) > threshold)) ar_append(&R, i);
     if (!Autonomous) fun_time_derivative(cx, T, Roundoff, Y, Fcn0, dFdT);
     jac_template(cx, Y, Jac0);
     cx->istatus[Njac] += 1;
@@ -598,10 +643,10 @@ static void ros_yintegrator(cellctx_t* cx, const method_t* m, double* Y, double 
   /* AutoReduce_1stOrder (:1702-1712) for the frozen species */
   for (int i = 0; i < NVAR; ++i) {
     if (!R.DO_SLV[i]) {
-      const double k = Loss[i];
+      const double k = Los0[i];
       if (k <= 1.0e-30) continue;
       if (Y[i] <= 1.0e-30) continue;
-      const double term = Prod[i] / k;
+      const double term = Prd0[i] / k;
       Y[i] = term + (Y[i] - term) * exp(-k * (Tend - Tstart));
     }
   }
@@ -669,20 +714,16 @@ void oracle_integrate(double* C, const double* RCONST, const double* atol, const
     /* auto-reduction (gckpp_Integrator.F90:388-394, 478-520): ICNTRL(12) = 1
      * selects ros_yIntegrator with threshold RCNTRL(12) (default 100) or, with
      * ICNTRL(14) = target species, RCNTRL(14) x max(P, L*y) of that species;
-     * keepActive with the mask of oracle_set_keep.  The append form
-     * (ICNTRL(13) = 1, ros_yIntegratorA) is not restated: IERR = -100.  ICNTRL(20) = 7 (unused by the reference)
+     * keepActive with the mask of oracle_set_keep; ICNTRL(13) = 1 selects
+     * the append form, ros_yIntegratorA.  ICNTRL(20) = 7 (unused by the reference)
      * selects the masked-full decomposition of the GPU design instead of the
      * compressed one (tests only). */
     const int Autoreduce = ICNTRL[11] == 1;
-    if (Autoreduce && ICNTRL[12] == 1) {
-      IERR = -100;
-      goto done;
-    }
     if (Autoreduce) {
       const double threshold = RCNTRL[11] > 0.0 ? RCNTRL[11] : 1.0e2;
       ros_yintegrator(&cx, &m, C, tin, tout, &Texit, atol, rtol, Autonomous, VectorTol, Max_no_steps, Roundoff,
                       Hmin, Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, threshold, ICNTRL[13], RCNTRL[13],
-                      g_keep_on ? g_keep : 0, ICNTRL[19] == 7, &IERR);
+                      g_keep_on ? g_keep : 0, ICNTRL[19] == 7, ICNTRL[12] == 1, &IERR);
     } else {
       ros_integrator(&cx, &m, C, tin, tout, &Texit, atol, rtol, Autonomous, VectorTol, Max_no_steps, Roundoff,
                      Hmin, Hmax, Hstart, FacMin, FacMax, FacRej, FacSafe, ICNTRL[15] == 1, &IERR);

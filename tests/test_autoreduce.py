@@ -1,8 +1,9 @@
 """Auto-reduction, the CPU restatement: ros_yIntegrator of
 KPP/fullchem/gckpp_Integrator.F90:789-1237 with cKppDecomp (:2624-2661),
 the DO_SLV-guarded KppSolve and AutoReduce_1stOrder (:1702-1712), selected by
-ICNTRL(12) = 1 as INTEGRATE does (:388-394, :478-520).  The GPU form is
-tested against it in test_zzz_autoreduce_gpu.py."""
+ICNTRL(12) = 1 as INTEGRATE does (:388-394, :478-520), and its append form
+ros_yIntegratorA (:1242-1700, APPEND :2663-2700) with ICNTRL(13) = 1.  The
+GPU form is tested against it in test_zzz_autoreduce_gpu.py."""
 import numpy as np
 import pytest
 
@@ -83,23 +84,50 @@ def test_target_species_threshold_is_reported(case):
         assert np.array_equal(vdot, p - d * v)  # Fun_SPLITF and Fun_SPLIT agree
 
 
-def test_append_form_is_not_restated(case):
-    c, ist, rst, ierr = _ar(case, append=True)
-    assert np.all(ierr == -100)
+def test_append_form_without_appends_is_ros_yintegrator(case, ir):
+    """ros_yIntegratorA (ICNTRL(13) = 1) with RCNTRL(12) above every rate can
+    append nothing: it is ros_yIntegrator bit for bit (here with the OH
+    target threshold, which does not involve RCNTRL(12))."""
+    oh = ir["species"].index("OH") + 1
+    a = _ar(case, thr=1e300, target=oh, ratio=1e-3)
+    b = _ar(case, thr=1e300, target=oh, ratio=1e-3, append=True)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("thr", [1e2, 1e4])
+def test_append_brings_species_back(case, thr):
+    """Species whose production or loss grows past RCNTRL(12) during the
+    integration re-enter the solve (APPEND): every cell succeeds and the
+    result moves towards the full integration."""
+    a = _ar(case, thr=thr)
+    b = _ar(case, thr=thr, append=True)
+    full = case["full"][0][:353]
+    assert np.all(b[3] == 1)
+    assert not np.array_equal(a[0], b[0])
+    big = np.abs(full) > 1e4
+
+    def err(x):
+        return np.median((np.abs(x[:353] - full) / np.maximum(np.abs(full), 1e-300))[big])
+
+    assert err(b[0]) < 0.2 * err(a[0])
+
+
+@pytest.mark.parametrize("append", [False, True])
 @pytest.mark.parametrize("thr", [1e2, 1e5])
-def test_masked_full_decomposition_equals_the_compressed_one(case, thr):
+def test_masked_full_decomposition_equals_the_compressed_one(case, thr, append):
     """The design of the GPU form: zeroing every Jac0 entry in a frozen row
     or column and factoring the full Ghimj = -Jac0 + ghinv I (ICNTRL(20) = 7
     selects it in the oracle) gives the compressed cKppDecomp path's
     integration bit for bit -- frozen entries only ever contribute exact
-    zeros."""
+    zeros.  With APPEND the appended species' row keeps the columns that
+    entered no later than it and its column is zeroed in earlier rows."""
     import oracle
 
     ic = case["ic"].copy()
     rc = case["rc"].copy()
     ic[11] = 1
+    ic[12] = 1 if append else 0
     rc[11] = thr
     a = oracle.integrate(case["cells"]["c"], case["r"], case["atol"], case["rtol"], 0.0, 600.0, ic, rc)
     ic[19] = 7

@@ -7,7 +7,8 @@ Jacobian rows and columns of the frozen species are zeroed, so that
 -Jac0 + ghinv I factors like the reference's compressed matrix (the oracle
 shows the two bit for bit, tests/test_autoreduce.py), the frozen stage
 vectors stay 0 and the frozen species take AutoReduce_1stOrder (:1702-1712)
-at the end.
+at the end.  The append form (ros_yIntegratorA, :1242-1700) masks an
+appended species' column in the rows that entered before it.
 
 Collected last (file name), after the allocation-free entry point."""
 import numpy as np
@@ -66,12 +67,14 @@ def _oracle(orc, case, ic, rc):
     return orc.integrate(case["cells"]["c"], case["rconst"], case["atol"], case["rtol"], 0.0, 600.0, ic, rc)
 
 
+@pytest.mark.parametrize("append", [False, True])
 @pytest.mark.parametrize("arith", ["strict", "fast"])
 @pytest.mark.parametrize("thr", [1e2, 1e5])
-def test_autoreduce_matches_oracle(solver, orc, case, arith, thr):
+def test_autoreduce_matches_oracle(solver, orc, case, arith, thr, append):
     """The parity bar of the full integrator: 1e-9 relative on species above
-    1e4 molec/cm3, on every cell whose step sequence matches the oracle's."""
-    ic, rc = _controls(case, thr=thr)
+    1e4 molec/cm3, on every cell whose step sequence matches the oracle's;
+    with append (ICNTRL(13) = 1, ros_yIntegratorA) too."""
+    ic, rc = _controls(case, thr=thr, append=append)
     c, ist, rst, ierr = _gpu(solver, case, ic, rc, arith=arith)
     c_ref, ist_ref, rst_ref, ierr_ref = _oracle(orc, case, ic, rc)
     assert np.all(ierr_ref == 1)
@@ -152,10 +155,6 @@ def test_fullchem_step_with_autoreduce(solver, orc, case, ir):
 
 
 def test_unsupported_forms_are_refused(solver, case):
-    # the append form (ros_yIntegratorA)
-    with pytest.raises(capi.GcKppError) as e:
-        _gpu(solver, case, *_controls(case, append=True))
-    assert e.value.code == capi.GC_KPP_EUNSUPPORTED
     # a target species outside VAR
     with pytest.raises(capi.GcKppError) as e:
         _gpu(solver, case, *_controls(case, target=NVAR + 1, ratio=1e-3))
@@ -172,7 +171,8 @@ def test_per_cell_controls_and_kept_halogens(solver, orc, case, ir, arith):
     """Do_FullChem's auto-reduce set-up: per-cell thresholds (pressure-scaled
     on half of the cells, OH/NO2 key species on the other half) and the
     halogens kept active, through gc_kpp_ctx_set_autoreduce, against the
-    oracle with the same per-cell controls and keepSpcActive."""
+    oracle with the same per-cell controls and keepSpcActive (the fast
+    arithmetic with the append form)."""
     import gcchem.autoreduce as ar
 
     n = case["n"]
@@ -184,7 +184,7 @@ def test_per_cell_controls_and_kept_halogens(solver, orc, case, ir, arith):
     half = np.arange(n) % 2 == 1
     thr[half], target[half], ratio[half] = t2[half], g2[half], r2[half]
     keep = ar.keep_mask(ir)
-    ic, rc = _controls(case)
+    ic, rc = _controls(case, append=(arith == "fast"))
     try:
         solver.set_autoreduce(thr=thr, target=target, ratio=ratio, keep=keep)
         c, ist, rst, ierr = _gpu(solver, case, ic, rc, arith=arith)
