@@ -63,8 +63,40 @@ def _gpu(solver, case, ic, rc, arith="strict", schedule="plain"):
     return c, ist, rst, ierr
 
 
-def _oracle(orc, case, ic, rc):
-    return orc.integrate(case["cells"]["c"], case["rconst"], case["atol"], case["rtol"], 0.0, 600.0, ic, rc)
+def _oracle(orc, case, ic, rc, rconst=None, **kw):
+    r = case["rconst"] if rconst is None else rconst
+    return orc.integrate(case["cells"]["c"], r, case["atol"], case["rtol"], 0.0, 600.0, ic, rc, **kw)
+
+
+def _check(orc, case, got, ref, ic, rc, scale=1e-15, c_in=None, rconst=None, clamp=False, **kw):
+    """The parity bar of the full integrator: 1e-9 relative on species above
+    1e4 molec/cm3, on every cell whose step sequence matches the oracle's
+    (at least 99 % of them).  A cell whose reduction or append decision sits
+    at its threshold amplifies rounding: there the bar is 10x the oracle's own
+    spread when its rate constants move by `scale` relative (two draws), so
+    that the GPU is held to the oracle's conditioning, not beyond it."""
+    c, ist, _, ierr = got
+    c_ref, ist_ref, _, ierr_ref = ref
+    assert np.array_equal(ierr, ierr_ref)
+    same = np.all(ist[:8] == ist_ref[:8], axis=0)
+    assert same.mean() >= 0.99, same.mean()
+    big = np.abs(c_ref[:NVAR]) > 1e4
+    c_in = case["cells"]["c"] if c_in is None else c_in
+    rconst = case["rconst"] if rconst is None else rconst
+    spread = np.zeros(case["n"])
+    for seed in (1, 2):
+        rng = np.random.default_rng(seed)
+        rp = rconst * (1.0 + rng.uniform(-scale, scale, rconst.shape))
+        x = orc.integrate(c_in, rp, case["atol"], case["rtol"], 0.0, 600.0, ic, rc, **kw)[0]
+        if clamp:
+            x = np.maximum(x, 0.0)
+        spread = np.maximum(spread, np.max(np.where(big, _rel(x[:NVAR], c_ref[:NVAR]), 0.0), axis=0))
+    bar = np.maximum(1e-9, 10.0 * spread)
+    dev = np.max(np.where(big, _rel(c[:NVAR], c_ref[:NVAR]), 0.0), axis=0)
+    bad = np.nonzero(same & (dev >= bar))[0]
+    assert bad.size == 0, (bad[:5], dev[bad][:5], bar[bad][:5])
+    assert np.mean(bar > 1e-9) <= 0.05  # the exception stays an exception
+    return same
 
 
 @pytest.mark.parametrize("append", [False, True])
@@ -75,20 +107,15 @@ def test_autoreduce_matches_oracle(solver, orc, case, arith, thr, append):
     1e4 molec/cm3, on every cell whose step sequence matches the oracle's;
     with append (ICNTRL(13) = 1, ros_yIntegratorA) too."""
     ic, rc = _controls(case, thr=thr, append=append)
-    c, ist, rst, ierr = _gpu(solver, case, ic, rc, arith=arith)
-    c_ref, ist_ref, rst_ref, ierr_ref = _oracle(orc, case, ic, rc)
-    assert np.all(ierr_ref == 1)
-    assert np.array_equal(ierr, ierr_ref)
-    same = np.all(ist[:8] == ist_ref[:8], axis=0)
-    assert same.mean() >= 0.99, same.mean()
+    got = _gpu(solver, case, ic, rc, arith=arith)
+    ref = _oracle(orc, case, ic, rc)
+    assert np.all(ref[3] == 1)
+    same = _check(orc, case, got, ref, ic, rc)
     if arith == "strict":
         assert same.all()
-    big = np.abs(c_ref[:NVAR]) > 1e4
-    rel = _rel(c[:NVAR], c_ref[:NVAR])
-    assert np.max(np.where(big, rel, 0.0)[:, same]) < 1e-9
     # and the reduction changed the answer (something was frozen)
     c_full = _oracle(orc, case, *_controls(case, on=False))[0]
-    assert not np.array_equal(c_ref, c_full)
+    assert not np.array_equal(ref[0], c_full)
 
 
 def test_target_species_threshold(solver, orc, case, ir):
@@ -96,14 +123,11 @@ def test_target_species_threshold(solver, orc, case, ir):
     L*y at Tstart, reported in RSTATUS(4)."""
     oh = ir["species"].index("OH")
     ic, rc = _controls(case, target=oh + 1, ratio=1e-3)
-    c, ist, rst, ierr = _gpu(solver, case, ic, rc)
-    c_ref, ist_ref, rst_ref, ierr_ref = _oracle(orc, case, ic, rc)
-    assert np.all(ierr == 1) and np.all(ierr_ref == 1)
-    assert np.max(_rel(rst[3], rst_ref[3])) < 1e-12
-    same = np.all(ist[:8] == ist_ref[:8], axis=0)
-    assert same.mean() >= 0.99
-    big = np.abs(c_ref[:NVAR]) > 1e4
-    assert np.max(np.where(big, _rel(c[:NVAR], c_ref[:NVAR]), 0.0)[:, same]) < 1e-9
+    got = _gpu(solver, case, ic, rc)
+    ref = _oracle(orc, case, ic, rc)
+    assert np.all(got[3] == 1) and np.all(ref[3] == 1)
+    assert np.max(_rel(got[2][3], ref[2][3])) < 1e-12
+    _check(orc, case, got, ref, ic, rc)
 
 
 @pytest.mark.parametrize("arith", ["strict", "fast"])
@@ -143,14 +167,13 @@ def test_fullchem_step_with_autoreduce(solver, orc, case, ir):
     for fam in ir["families"]:
         c0[ir["species"].index(fam)] = 0.0
     r = orc.update_rconst(cells["met"], cells["photol"], c0)
-    c_ref, ist_ref, _, ierr_ref = orc.integrate(c0, r, case["atol"], case["rtol"], 0.0, 600.0, ic, rc)
+    c_ref, ist_ref, rst_ref, ierr_ref = orc.integrate(c0, r, case["atol"], case["rtol"], 0.0, 600.0, ic, rc)
     assert nretry == 0 and np.all(ierr_ref == 1) and np.all(ierr == 1)
     c_ref = np.maximum(c_ref, 0.0)
-    same = np.all(ist[:8] == ist_ref[:8], axis=0)
-    assert same.mean() >= 0.99
-    big = np.abs(c_ref[:NVAR]) > 1e4
-    # the GPU step computes its own rates (CUDA libm): the bar of the step test
-    assert np.max(np.where(big, _rel(c[:NVAR], c_ref[:NVAR]), 0.0)[:, same]) < 1e-9
+    # the GPU step computes its own rates (CUDA libm, within 1e-12 of the
+    # oracle's): the conditioning bar at that scale
+    _check(orc, case, (c, ist, rst, ierr), (c_ref, ist_ref, rst_ref, ierr_ref), ic, rc, scale=1e-12, c_in=c0,
+           rconst=r, clamp=True)
     assert np.all(c >= 0.0)
 
 
@@ -185,23 +208,19 @@ def test_per_cell_controls_and_kept_halogens(solver, orc, case, ir, arith):
     thr[half], target[half], ratio[half] = t2[half], g2[half], r2[half]
     keep = ar.keep_mask(ir)
     ic, rc = _controls(case, append=(arith == "fast"))
+    kw = dict(ar_thr=thr, ar_target=target, ar_ratio=ratio)
     try:
         solver.set_autoreduce(thr=thr, target=target, ratio=ratio, keep=keep)
-        c, ist, rst, ierr = _gpu(solver, case, ic, rc, arith=arith)
+        got = _gpu(solver, case, ic, rc, arith=arith)
         orc.set_keep(keep)
-        c_ref, ist_ref, rst_ref, ierr_ref = orc.integrate(case["cells"]["c"], case["rconst"], case["atol"],
-                                                          case["rtol"], 0.0, 600.0, ic, rc, ar_thr=thr,
-                                                          ar_target=target, ar_ratio=ratio)
+        ref = _oracle(orc, case, ic, rc, **kw)
+        assert np.all(ref[3] == 1)
+        assert np.max(_rel(got[2][3], ref[2][3])) < 1e-12
+        assert np.all(got[2][3, ~half] == 0.0)
+        _check(orc, case, got, ref, ic, rc, **kw)
     finally:
         solver.set_autoreduce()
         orc.set_keep(None)
-    assert np.all(ierr_ref == 1) and np.array_equal(ierr, ierr_ref)
-    assert np.max(_rel(rst[3], rst_ref[3])) < 1e-12
-    assert np.all(rst[3, ~half] == 0.0)
-    same = np.all(ist[:8] == ist_ref[:8], axis=0)
-    assert same.mean() >= 0.99
-    big = np.abs(c_ref[:NVAR]) > 1e4
-    assert np.max(np.where(big, _rel(c[:NVAR], c_ref[:NVAR]), 0.0)[:, same]) < 1e-9
 
 
 def test_per_cell_controls_need_the_same_cell_count(solver, case):
