@@ -3,13 +3,17 @@
     python geos-chem_gb300/profile_case.py --cells 4096 --tout 60 --arith fast [--probe]
     python geos-chem_gb300/profile_case.py --grid 72x46x8 --binned 64
     python geos-chem_gb300/profile_case.py --grid 72x46x24 --learned
+    python geos-chem_gb300/profile_case.py --grid 72x46x24 --autoreduce 100 [--append]
 
 Box cells (``inputs.box_cells``) are integrated once from 0 to TOUT with
 ``Solver.integrate``; ``--grid`` instead spins up a grid and runs one 1200 s
 chemistry step (``--binned N``: the N cells with the most steps go
-block-per-cell; ``--learned``: the learned form from a cold start).  It prints the ISTATUS sums and the algorithmic FP64
-operations of the reference routines for them; ``--probe`` also runs the FP64
-throughput probe.  Meant to run under ncu on one GPU with few launches.
+block-per-cell; ``--learned``: the learned form from a cold start;
+``--autoreduce THR``: the timed step with auto-reduction).  It prints the
+time of the timed call (one cold run), the ISTATUS sums and the algorithmic
+FP64 operations of the reference routines for them; ``--probe`` also runs
+the FP64 throughput probe.  Meant to run under ncu on one GPU with few
+launches.
 """
 import argparse
 import ctypes
@@ -32,6 +36,10 @@ def main(argv=None):
     ap.add_argument("--block-form", default="split", choices=["split", "level"],
                     help="block-per-cell kernel form (GC_KPP_OPT_BLOCK_SPLIT 1 or 0)")
     ap.add_argument("--probe", action="store_true")
+    ap.add_argument("--autoreduce", type=float, default=0.0,
+                    help="> 0: the timed step or integration with auto-reduction (ICNTRL(12)=1) at this "
+                         "RCNTRL(12) threshold (thread-per-cell kernel; not with --learned/--binned)")
+    ap.add_argument("--append", action="store_true", help="with --autoreduce: the append form (ICNTRL(13)=1)")
     args = ap.parse_args(argv)
 
     here = os.path.dirname(os.path.abspath(__file__))
@@ -54,7 +62,13 @@ def main(argv=None):
     s.set(block_split=args.block_form == "split")
     atol, rtol = inputs.tolerances()
     ic, rc = inputs.default_controls()
+    ic_t, rc_t = ic.copy(), rc.copy()  # controls of the timed step
+    if args.autoreduce > 0:
+        ic_t[11] = 1
+        ic_t[12] = 1 if args.append else 0
+        rc_t[11] = args.autoreduce
     at, rt = T(atol), T(rtol)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if args.grid:
         nlon, nlat, nlev = (int(v) for v in args.grid.split("x"))
         cells = inputs.grid_cells(nlon, nlat, nlev, seed=0)
@@ -82,12 +96,19 @@ def main(argv=None):
             s.fullchem_step(1200.0, met, ph, c.clone(), at, rt, ic, rc, hs.clone(), ist, rst, ierr)
             order = torch.argsort(ist[2], descending=True, stable=True).int()
             nb = args.binned
-        s.fullchem_step(1200.0, met, ph, c, at, rt, ic, rc, hs, ist, rst, ierr, order=order, nblock=nb)
+        torch.cuda.synchronize()
+        t0.record()
+        s.fullchem_step(1200.0, met, ph, c, at, rt, ic_t, rc_t, hs, ist, rst, ierr, order=order, nblock=nb)
+        t1.record()
     else:
         r = torch.zeros((1058, n), dtype=torch.float64, device=dev)
         s.update_rconst(met, ph, c, r)
-        s.integrate(c, r, at, rt, 0.0, args.tout, ic, rc, istatus=ist, ierr=ierr)
+        torch.cuda.synchronize()
+        t0.record()
+        s.integrate(c, r, at, rt, 0.0, args.tout, ic_t, rc_t, istatus=ist, ierr=ierr)
+        t1.record()
     torch.cuda.synchronize()
+    print("timed call %.3f ms (one cold run, default stream)" % t0.elapsed_time(t1))
     ih = ist.cpu().numpy().astype(np.int64)
     t = Tables(load_ir())
     f = t.flops()
