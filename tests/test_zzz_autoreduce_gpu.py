@@ -130,11 +130,13 @@ def test_target_species_threshold(solver, orc, case, ir):
     _check(orc, case, got, ref, ic, rc)
 
 
+@pytest.mark.parametrize("append", [False, True])
 @pytest.mark.parametrize("arith", ["strict", "fast"])
-def test_nothing_frozen_is_the_full_integrator(solver, case, arith):
-    """A threshold below every rate freezes nothing: the auto-reduce kernel
-    then performs the regular kernel's arithmetic, bit for bit."""
-    a = _gpu(solver, case, *_controls(case, thr=1e-300), arith=arith)
+def test_nothing_frozen_is_the_full_integrator(solver, case, arith, append):
+    """A threshold below every rate freezes nothing (and leaves nothing to
+    append): the auto-reduce kernel then performs the regular kernel's
+    arithmetic, bit for bit."""
+    a = _gpu(solver, case, *_controls(case, thr=1e-300, append=append), arith=arith)
     b = _gpu(solver, case, *_controls(case, on=False), arith=arith)
     assert np.array_equal(a[0], b[0])
     assert np.array_equal(a[1][:8], b[1][:8])
