@@ -1,14 +1,17 @@
 // Host build of the thread-per-cell Rosenbrock driver (ros_driver of
-// geos-chem_gb300/csrc/kpp_rosenbrock.cuh, plain schedule, strict arithmetic)
-// for tests/test_ros_host.py: the CUDA qualifiers become plain C++, the
-// launch becomes a loop over the threads of the grid (in the plain schedule
-// a thread owns its cell and its lane of the workspace, so the threads are
-// independent), CUDA's math functions glibc's.  Built -ffp-contract=off, it
-// performs the kernel's strict arithmetic, so the kernel's integration logic
-// -- the step control, the auto-reduction mask, APPEND, the first-order
-// update -- can be checked against the oracle without a GPU.
+// geos-chem_gb300/csrc/kpp_rosenbrock.cuh, plain schedule, strict or fast
+// arithmetic) for tests/test_ros_host.py: the CUDA qualifiers become plain
+// C++, the launch becomes a loop over the threads of the grid (in the plain
+// schedule a thread owns its cell and its lane of the workspace, so the
+// threads are independent), CUDA's math functions glibc's.  Built
+// -ffp-contract=off, it performs the kernel's arithmetic operation for
+// operation, so the kernel's integration logic -- the step control, the
+// auto-reduction mask, APPEND, the first-order update -- can be checked
+// against the oracle without a GPU.
 //
-// argv: ncell tout ar append thr target ratio [percell] [keep]
+// argv: ncell tout ar append thr target ratio [percell] [keep] [strict]
+// (strict = 0: the fast arithmetic, FMA through std::fma, which rounds once
+// as the GPU's does)
 // Inputs (float64/int32, cell-interleaved): c.bin [nspec][n], r.bin
 // [nreact][n], atol.bin/rtol.bin [nvar]; with percell: pthr.bin [n],
 // ptgt.bin (int32) [n], pratio.bin [n]; with keep: keep.bin (uint8) [nvar].
@@ -96,6 +99,7 @@ int main(int argc, char** argv) {
   const double ratio = atof(argv[7]);
   const int percell = argc > 8 ? atoi(argv[8]) : 0;
   const int with_keep = argc > 9 ? atoi(argv[9]) : 0;
+  const int strict = argc > 10 ? atoi(argv[10]) : 1;
 
   gckpp::MechDev m{};
   m.nvar = T::NVAR;
@@ -219,10 +223,17 @@ int main(int argc, char** argv) {
   for (int t = 0; t < nthread; ++t) {
     blockIdx = HostDim{(unsigned)(t / block), 0, 0};
     threadIdx = HostDim{(unsigned)(t % block), 0, 0};
-    if (ar)
-      gckpp::ros_driver<true, false, 1, true>(m, meth, p);
-    else
-      gckpp::ros_driver<true, false, 1, false>(m, meth, p);
+    if (strict) {
+      if (ar)
+        gckpp::ros_driver<true, false, 1, true>(m, meth, p);
+      else
+        gckpp::ros_driver<true, false, 1, false>(m, meth, p);
+    } else {
+      if (ar)
+        gckpp::ros_driver<false, false, 1, true>(m, meth, p);
+      else
+        gckpp::ros_driver<false, false, 1, false>(m, meth, p);
+    }
   }
   wr("c_out.bin", c_out);
   wr("ist.bin", ist);

@@ -1,9 +1,9 @@
 """The GPU thread-per-cell integrator's own source (ros_driver of
-csrc/kpp_rosenbrock.cuh, plain schedule, strict arithmetic), built for the
-host with g++ (tests/host/ros_host.cpp), against the oracle: the kernel's
-integration logic -- step control, and auto-reduction with its Jacobian mask,
-APPEND, per-cell controls, keepActive and the first-order update -- checked
-without a GPU.  Same 1e-9 bar as the GPU parity tests (the LU runs row-wise
+csrc/kpp_rosenbrock.cuh, plain schedule), built for the host with g++
+(tests/host/ros_host.cpp) in the strict and the fast arithmetic (FMA through
+std::fma), against the oracle: the kernel's integration logic -- step
+control, and auto-reduction with its Jacobian mask, APPEND, per-cell
+controls, keepActive and the first-order update -- checked without a GPU.  Same 1e-9 bar as the GPU parity tests (the LU runs row-wise
 here and in KppDecomp's order in the oracle, so the two agree to rounding)."""
 import os
 import shutil
@@ -51,7 +51,7 @@ def case(orc):
     return dict(n=n, c=cells["c"], r=r, atol=atol, rtol=rtol, ic=ic, rc=rc)
 
 
-def _host(harness, case, ar=0, append=0, thr=0.0, target=0, ratio=0.0, percell=None, keep=None):
+def _host(harness, case, ar=0, append=0, thr=0.0, target=0, ratio=0.0, percell=None, keep=None, strict=True):
     tmp, exe = harness
     n = case["n"]
     for name, arr, dt in (("c", case["c"], np.float64), ("r", case["r"], np.float64),
@@ -64,7 +64,8 @@ def _host(harness, case, ar=0, append=0, thr=0.0, target=0, ratio=0.0, percell=N
     if keep is not None:
         np.ascontiguousarray(keep, np.uint8).tofile(str(tmp / "keep.bin"))
     subprocess.check_call([exe, str(n), "600", str(ar), str(append), repr(thr), str(target), repr(ratio),
-                           "1" if percell is not None else "0", "1" if keep is not None else "0"], cwd=str(tmp))
+                           "1" if percell is not None else "0", "1" if keep is not None else "0",
+                           "1" if strict else "0"], cwd=str(tmp))
     c = np.fromfile(str(tmp / "c_out.bin")).reshape(-1, n)
     ist = np.fromfile(str(tmp / "ist.bin"), np.int32).reshape(20, n)
     rst = np.fromfile(str(tmp / "rst.bin")).reshape(20, n)
@@ -99,14 +100,17 @@ def _agree(got, ref):
     assert np.max(np.abs(rst[3] - rst_ref[3]) / np.maximum(np.abs(rst_ref[3]), 1e-300)) < 1e-12
 
 
-def test_full_integrator(harness, orc, case):
-    _agree(_host(harness, case), _oracle(orc, case))
+@pytest.mark.parametrize("strict", [True, False])
+def test_full_integrator(harness, orc, case, strict):
+    _agree(_host(harness, case, strict=strict), _oracle(orc, case))
 
 
+@pytest.mark.parametrize("strict", [True, False])
 @pytest.mark.parametrize("append", [0, 1])
 @pytest.mark.parametrize("thr", [1e2, 1e5])
-def test_autoreduce(harness, orc, case, thr, append):
-    _agree(_host(harness, case, ar=1, append=append, thr=thr), _oracle(orc, case, ar=1, append=append, thr=thr))
+def test_autoreduce(harness, orc, case, thr, append, strict):
+    _agree(_host(harness, case, ar=1, append=append, thr=thr, strict=strict),
+           _oracle(orc, case, ar=1, append=append, thr=thr))
 
 
 def test_target_species(harness, orc, case, ir):
@@ -120,6 +124,7 @@ def test_target_species(harness, orc, case, ir):
 def test_per_cell_controls_and_keep(harness, orc, case, ir, append):
     import gcchem.autoreduce as ar
 
+    strict = append == 0  # the append form in the fast arithmetic
     n = case["n"]
     rng = np.random.default_rng(4)
     thr, tgt, ratio = ar.integrator_options(ir, n, threshold=1e3, pmid=rng.uniform(100, 1000, n),
@@ -130,14 +135,15 @@ def test_per_cell_controls_and_keep(harness, orc, case, ir, append):
     thr[half], tgt[half], ratio[half] = t2[half], g2[half], r2[half]
     pc = (thr, tgt, ratio)
     keep = ar.keep_mask(ir)
-    got = _host(harness, case, ar=1, append=append, percell=pc, keep=keep)
+    got = _host(harness, case, ar=1, append=append, percell=pc, keep=keep, strict=strict)
     _agree(got, _oracle(orc, case, ar=1, append=append, percell=pc, keep=keep))
     assert np.all(got[2][3, ~half] == 0.0) and np.all(got[2][3, half] > 0.0)
 
 
+@pytest.mark.parametrize("strict", [True, False])
 @pytest.mark.parametrize("append", [0, 1])
-def test_nothing_frozen_is_the_full_integrator(harness, case, append):
-    a = _host(harness, case, ar=1, append=append, thr=1e-300)
-    b = _host(harness, case)
+def test_nothing_frozen_is_the_full_integrator(harness, case, append, strict):
+    a = _host(harness, case, ar=1, append=append, thr=1e-300, strict=strict)
+    b = _host(harness, case, strict=strict)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
