@@ -9,9 +9,11 @@
 // auto-reduction mask, APPEND, the first-order update -- can be checked
 // against the oracle without a GPU.
 //
-// argv: ncell tout ar append thr target ratio [percell] [keep] [strict]
+// argv: ncell tout ar append thr target ratio [percell] [keep] [strict] [queue]
 // (strict = 0: the fast arithmetic, FMA through std::fma, which rounds once
-// as the GPU's does)
+// as the GPU's does; queue = 1: the work-queue schedule over the cells in
+// reverse order -- emulated one thread after the other, the first thread
+// claims every cell, so one workspace slot serves them all in turn)
 // Inputs (float64/int32, cell-interleaved): c.bin [nspec][n], r.bin
 // [nreact][n], atol.bin/rtol.bin [nvar]; with percell: pthr.bin [n],
 // ptgt.bin (int32) [n], pratio.bin [n]; with keep: keep.bin (uint8) [nvar].
@@ -48,7 +50,8 @@ static inline long long __double_as_longlong(double d) {
   memcpy(&v, &d, 8);
   return v;
 }
-static inline unsigned __activemask() { return 1u; }
+// one emulated thread runs at a time: it is the only active lane of its warp
+static inline unsigned __activemask() { return 1u << (threadIdx.x & 31u); }
 static inline int __ffs(unsigned x) { return __builtin_ffs((int)x); }
 static inline int __popc(unsigned x) { return __builtin_popcount(x); }
 static inline int __shfl_sync(unsigned, int v, int) { return v; }
@@ -100,6 +103,7 @@ int main(int argc, char** argv) {
   const int percell = argc > 8 ? atoi(argv[8]) : 0;
   const int with_keep = argc > 9 ? atoi(argv[9]) : 0;
   const int strict = argc > 10 ? atoi(argv[10]) : 1;
+  const int queue = argc > 11 ? atoi(argv[11]) : 0;
 
   gckpp::MechDev m{};
   m.nvar = T::NVAR;
@@ -174,6 +178,8 @@ int main(int argc, char** argv) {
   const int nthread = (n + block - 1) / block * block;
   std::vector<double> ws((size_t)nthread * l.total);
   int counter = 0;
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = n - 1 - i;
 
   gckpp::RosParams p{};
   p.ncell = n;
@@ -215,6 +221,7 @@ int main(int argc, char** argv) {
     p.ar_ratio_cell = pratio.data();
   }
   if (with_keep) p.ar_keep = keep.data();
+  if (queue) p.order = order.data();
   p.ws = ws.data();
   p.lay = l;
   p.nslot = nthread;
@@ -223,7 +230,19 @@ int main(int argc, char** argv) {
   for (int t = 0; t < nthread; ++t) {
     blockIdx = HostDim{(unsigned)(t / block), 0, 0};
     threadIdx = HostDim{(unsigned)(t % block), 0, 0};
-    if (strict) {
+    if (queue) {
+      if (strict) {
+        if (ar)
+          gckpp::ros_driver<true, true, 1, true>(m, meth, p);
+        else
+          gckpp::ros_driver<true, true, 1, false>(m, meth, p);
+      } else {
+        if (ar)
+          gckpp::ros_driver<false, true, 1, true>(m, meth, p);
+        else
+          gckpp::ros_driver<false, true, 1, false>(m, meth, p);
+      }
+    } else if (strict) {
       if (ar)
         gckpp::ros_driver<true, false, 1, true>(m, meth, p);
       else

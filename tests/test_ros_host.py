@@ -1,10 +1,11 @@
 """The GPU thread-per-cell integrator's own source (ros_driver of
-csrc/kpp_rosenbrock.cuh, plain schedule), built for the host with g++
-(tests/host/ros_host.cpp) in the strict and the fast arithmetic (FMA through
-std::fma), against the oracle: the kernel's integration logic -- step
-control, and auto-reduction with its Jacobian mask, APPEND, per-cell
-controls, keepActive and the first-order update -- checked without a GPU.  Same 1e-9 bar as the GPU parity tests (the LU runs row-wise
-here and in KppDecomp's order in the oracle, so the two agree to rounding)."""
+csrc/kpp_rosenbrock.cuh, plain and work-queue schedules), built for the host
+with g++ (tests/host/ros_host.cpp) in the strict and the fast arithmetic (FMA
+through std::fma), against the oracle: the kernel's integration logic --
+step control, and auto-reduction with its Jacobian mask, APPEND, per-cell
+controls, keepActive and the first-order update -- checked without a GPU.
+Same 1e-9 bar as the GPU parity tests (the LU runs row-wise here and in
+KppDecomp's order in the oracle, so the two agree to rounding)."""
 import os
 import shutil
 import subprocess
@@ -51,7 +52,8 @@ def case(orc):
     return dict(n=n, c=cells["c"], r=r, atol=atol, rtol=rtol, ic=ic, rc=rc)
 
 
-def _host(harness, case, ar=0, append=0, thr=0.0, target=0, ratio=0.0, percell=None, keep=None, strict=True):
+def _host(harness, case, ar=0, append=0, thr=0.0, target=0, ratio=0.0, percell=None, keep=None, strict=True,
+          queue=False):
     tmp, exe = harness
     n = case["n"]
     for name, arr, dt in (("c", case["c"], np.float64), ("r", case["r"], np.float64),
@@ -65,7 +67,7 @@ def _host(harness, case, ar=0, append=0, thr=0.0, target=0, ratio=0.0, percell=N
         np.ascontiguousarray(keep, np.uint8).tofile(str(tmp / "keep.bin"))
     subprocess.check_call([exe, str(n), "600", str(ar), str(append), repr(thr), str(target), repr(ratio),
                            "1" if percell is not None else "0", "1" if keep is not None else "0",
-                           "1" if strict else "0"], cwd=str(tmp))
+                           "1" if strict else "0", "1" if queue else "0"], cwd=str(tmp))
     c = np.fromfile(str(tmp / "c_out.bin")).reshape(-1, n)
     ist = np.fromfile(str(tmp / "ist.bin"), np.int32).reshape(20, n)
     rst = np.fromfile(str(tmp / "rst.bin")).reshape(20, n)
@@ -145,5 +147,16 @@ def test_per_cell_controls_and_keep(harness, orc, case, ir, append):
 def test_nothing_frozen_is_the_full_integrator(harness, case, append, strict):
     a = _host(harness, case, ar=1, append=append, thr=1e-300, strict=strict)
     b = _host(harness, case, strict=strict)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("ar", [0, 1])
+def test_queue_schedule_equals_plain(harness, case, ar):
+    """The work queue over a permuted cell order, one workspace slot reused
+    for every cell (the frozen set of one cell must not leak into the next):
+    the same results as the plain schedule, bit for bit."""
+    a = _host(harness, case, ar=ar, append=ar, thr=1e2, strict=False, queue=True)
+    b = _host(harness, case, ar=ar, append=ar, thr=1e2, strict=False)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
