@@ -18,17 +18,16 @@ CSRC = os.path.join(ROOT, "geos-chem_gb300", "csrc")
 NVAR = 353
 
 
-@pytest.fixture(scope="module")
-def harness(tmp_path_factory):
+def _build(tmp_path_factory, mech):
     import gcchem.tables as tables
     from gcchem.mechanism import load_ir
 
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("no g++")
-    tmp = tmp_path_factory.mktemp("ros_host")
+    tmp = tmp_path_factory.mktemp("ros_host_" + mech)
     gen = tmp / "gen"
-    tables.write_generated(str(gen), load_ir())
+    tables.write_generated(str(gen), load_ir(mech))
     (tmp / "fake").mkdir()
     (tmp / "fake" / "cuda_runtime.h").write_text(
         "#pragma once\ntypedef int cudaError_t;\ntypedef void* cudaStream_t;\n"
@@ -38,6 +37,11 @@ def harness(tmp_path_factory):
                            str(tmp / "fake"), "-I", CSRC, "-I", str(gen),
                            os.path.join(ROOT, "tests", "host", "ros_host.cpp"), "-o", exe])
     return tmp, exe
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    return _build(tmp_path_factory, "fullchem")
 
 
 @pytest.fixture(scope="module")
@@ -53,7 +57,7 @@ def case(orc):
 
 
 def _host(harness, case, ar=0, append=0, thr=0.0, target=0, ratio=0.0, percell=None, keep=None, strict=True,
-          queue=False):
+          queue=False, tout=600.0):
     tmp, exe = harness
     n = case["n"]
     for name, arr, dt in (("c", case["c"], np.float64), ("r", case["r"], np.float64),
@@ -65,7 +69,7 @@ def _host(harness, case, ar=0, append=0, thr=0.0, target=0, ratio=0.0, percell=N
         np.ascontiguousarray(percell[2], np.float64).tofile(str(tmp / "pratio.bin"))
     if keep is not None:
         np.ascontiguousarray(keep, np.uint8).tofile(str(tmp / "keep.bin"))
-    subprocess.check_call([exe, str(n), "600", str(ar), str(append), repr(thr), str(target), repr(ratio),
+    subprocess.check_call([exe, str(n), repr(tout), str(ar), str(append), repr(thr), str(target), repr(ratio),
                            "1" if percell is not None else "0", "1" if keep is not None else "0",
                            "1" if strict else "0", "1" if queue else "0"], cwd=str(tmp))
     c = np.fromfile(str(tmp / "c_out.bin")).reshape(-1, n)
@@ -90,14 +94,14 @@ def _oracle(orc, case, ar=0, append=0, thr=0.0, target=0, ratio=0.0, percell=Non
         orc.set_keep(None)
 
 
-def _agree(got, ref):
+def _agree(got, ref, nvar=NVAR):
     c, ist, rst, ierr = got
     c_ref, ist_ref, rst_ref, ierr_ref = ref
     assert np.all(ierr_ref == 1) and np.array_equal(ierr, ierr_ref)
     same = np.all(ist[:8] == ist_ref[:8], axis=0)
     assert same.mean() >= 0.95, same.mean()
-    big = np.abs(c_ref[:NVAR]) > 1e4
-    rel = np.abs(c[:NVAR] - c_ref[:NVAR]) / np.maximum(np.abs(c_ref[:NVAR]), 1e-300)
+    big = np.abs(c_ref[:nvar]) > 1e4
+    rel = np.abs(c[:nvar] - c_ref[:nvar]) / np.maximum(np.abs(c_ref[:nvar]), 1e-300)
     assert np.max(np.where(big, rel, 0.0)[:, same]) < 1e-9
     assert np.max(np.abs(rst[3] - rst_ref[3]) / np.maximum(np.abs(rst_ref[3]), 1e-300)) < 1e-12
 
@@ -160,3 +164,25 @@ def test_queue_schedule_equals_plain(harness, case, ar):
     b = _host(harness, case, ar=ar, append=ar, thr=1e2, strict=False)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("ar", [0, 1])
+@pytest.mark.parametrize("strict", [True, False])
+def test_hg_mechanism(tmp_path_factory, orc, strict, ar):
+    """The same source on the Hg mechanism's tables (KPP/Hg) against the
+    oracle's Hg build, 1 h, with and without auto-reduction."""
+    import gcchem.inputs as inputs
+    from gcchem.mechanism import load_ir
+
+    hg = load_ir("Hg")
+    h = _build(tmp_path_factory, "Hg")
+    n = 64
+    cells = inputs.box_cells(n, seed=4, ir=hg)
+    atol, rtol = inputs.tolerances(hg)
+    ic, rc = inputs.default_controls()
+    r = orc.update_rconst(cells["met"], cells["photol"], cells["c"], mech="Hg")
+    case = dict(n=n, c=cells["c"], r=r, atol=atol, rtol=rtol)
+    got = _host(h, case, ar=ar, thr=1e2, strict=strict, tout=3600.0)
+    ic[11] = ar
+    ref = orc.integrate(cells["c"], r, atol, rtol, 0.0, 3600.0, ic, rc, mech="Hg")
+    _agree(got, ref, nvar=hg["dims"]["nvar"])
