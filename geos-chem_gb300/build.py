@@ -51,6 +51,8 @@ def _units():
         (k, "kpp_kernels_fast4.o", ["-DGCKPP_STRICT=0", "-DGCKPP_VARIANT=fast4", "-DGCKPP_NC=4"]),
         (os.path.join(CSRC, "kpp_rates.cu"), "kpp_rates.o", []),
         (os.path.join(CSRC, "kpp_util.cu"), "kpp_util.o", []),
+        # no FMA contraction: the producer's arithmetic rounds as the Fortran's
+        (os.path.join(CSRC, "het_state.cu"), "het_state.o", ["-fmad=false"]),
         (os.path.join(CSRC, "kpp_mlp.cu"), "kpp_mlp.o", []),
         (os.path.join(CSRC, "gckpp_mlp_capi.cu"), "gckpp_mlp_capi.o", []),
         (os.path.join(CSRC, "gckpp_learned_capi.cu"), "gckpp_learned_capi.o", []),

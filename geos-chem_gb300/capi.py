@@ -48,6 +48,7 @@ EXPORTED = [
     "gc_kpp_integrate_batch",
     "gc_kpp_update_rconst_batch",
     "gc_kpp_update_rconst_het_batch",
+    "gc_kpp_set_state_het_batch",
     "gc_kpp_ctx_set_hetstate",
     "gc_kpp_ctx_set_autoreduce",
     "gc_kpp_fullchem_step",
@@ -91,6 +92,7 @@ def load_library(path=None, mech="fullchem"):
     lib.gc_kpp_update_rconst_het_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64, i32, vp]
     lib.gc_kpp_ctx_set_hetstate.argtypes = [vp, i32, vp, i64, i32]
     lib.gc_kpp_ctx_set_autoreduce.argtypes = [vp, i32, vp, vp, vp, vp, i32]
+    lib.gc_kpp_set_state_het_batch.argtypes = [vp, i32, vp, i64, vp, i64, f64, i32, i32, vp, i64, i32, vp]
     if path == _build.lib_path(mech):
         _libs[mech] = lib
     return lib
@@ -311,6 +313,23 @@ class Solver:
         self._check(self.lib.gc_kpp_ctx_set_hetstate(self.ctx, n, _ptr(het), _ld(het, n),
                                                      MEM_DEVICE if dev else MEM_HOST))
         self._het = het if dev else None
+
+    def set_state_het(self, hetin, c, het, gamma_ho2=0.2, lpscchem=1, turn_off_het_rates=0, stream=None):
+        """Batched fullchem_SetStateHet (gc_kpp_set_state_het_batch).
+        hetin: [NHETIN, ncell] grid-box fields (gcchem.hetstate.HETIN_FIELDS);
+        c: [NSPEC, ncell]; het: [168, ncell] output HetState rows.  numpy
+        arrays (host) or CUDA torch tensors (device), all of one kind."""
+        dev = _is_torch(het) and het.is_cuda
+        ncell = het.shape[1]
+        if not dev:
+            hetin = np.ascontiguousarray(hetin, dtype=np.float64)
+            c = np.ascontiguousarray(c, dtype=np.float64)
+        s = ctypes.c_void_p(stream) if stream else None
+        rc = self.lib.gc_kpp_set_state_het_batch(self.ctx, ncell, _ptr(hetin), _ld(hetin, ncell), _ptr(c),
+                                                 _ld(c, ncell), float(gamma_ho2), int(lpscchem),
+                                                 int(turn_off_het_rates), _ptr(het), _ld(het, ncell),
+                                                 MEM_DEVICE if dev else MEM_HOST, s)
+        self._check(rc)
 
     def update_rconst(self, met, photol, c, rconst, stream=None, het=None):
         """Batched Update_RCONST.  met: [NMET, ncell]; photol: [200, ncell];

@@ -21,6 +21,7 @@
 #include "kpp_rates.h"
 #include "kpp_launch.h"
 #include "kpp_util.h"
+#include "het_state.h"
 #include "kpp_block.cuh"
 #include "kpp_rosenbrock.cuh"
 #include "ros_methods.h"
@@ -127,6 +128,7 @@ struct gc_kpp_ctx {
   DevBuf ws, counter;
   DevBuf h_c, h_r, h_at, h_rt, h_hs, h_is, h_rs, h_ie;  // staging for host-memory calls
   DevBuf h_met, h_ph, h_ord, h_het;
+  DevBuf h_hetin;  // staging of fullchem_SetStateHet inputs for host-memory calls
   // HetState of the chemistry steps (gc_kpp_ctx_set_hetstate): device rows
   DevBuf step_het;
   const double* het = nullptr;
@@ -267,7 +269,8 @@ int gc_kpp_ctx_destroy(gc_kpp_ctx* c) {
   DevBuf* bufs[] = {&c->ws,   &c->counter, &c->h_c,  &c->h_r,  &c->h_at,  &c->h_rt,
                     &c->h_hs, &c->h_is,    &c->h_rs, &c->h_ie, &c->h_met, &c->h_ph,
                     &c->rc_buf, &c->cb_buf, &c->ord_buf, &c->h_ord, &c->ranges, &c->evict_buf, &c->bws,
-                    &c->h_het, &c->step_het, &c->ar_thr, &c->ar_tgt, &c->ar_ratio, &c->ar_keep};
+                    &c->h_het, &c->step_het, &c->ar_thr, &c->ar_tgt, &c->ar_ratio, &c->ar_keep,
+                    &c->h_hetin};
   for (DevBuf* b : bufs) b->release();
   delete c;
   return GC_KPP_OK;
@@ -1160,6 +1163,54 @@ int gc_kpp_update_rconst_het_batch(gc_kpp_ctx* c, int ncell, const double* met, 
   return GC_KPP_OK;
 }
 
+int gc_kpp_set_state_het_batch(gc_kpp_ctx* c, int ncell, const double* hetin, long long ldi, const double* conc,
+                               long long ldc, double gamma_ho2, int lpscchem, int turn_off_het_rates, double* het,
+                               long long ldh, int mem, void* stream) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
+  if (ncell == 0) return GC_KPP_OK;
+  if (!hetin || !conc || !het) return fail(GC_KPP_EINVAL, "required array is NULL");
+  if (ldi < ncell || ldc < ncell || ldh < ncell) return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
+  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  GC_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  gchet::SetStateArgs a{};
+  a.ncell = ncell;
+  for (int k = 0; k < HSS_N; ++k) a.ind[k] = RT::hss_ind[k];
+  a.gamma_ho2 = gamma_ho2;
+  a.lpscchem = lpscchem;
+  a.turn_off_het_rates = turn_off_het_rates;
+  const size_t n = (size_t)ncell;
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(c->h_hetin.ensure((size_t)HETIN_NFIELD * n * sizeof(double)));
+    GC_CUDA(c->h_c.ensure(T::NSPEC * n * sizeof(double)));
+    GC_CUDA(c->h_het.ensure((size_t)HET_NFIELD * n * sizeof(double)));
+    GC_CUDA(cudaMemcpy2DAsync(c->h_hetin.p, n * sizeof(double), hetin, ldi * sizeof(double), n * sizeof(double),
+                              HETIN_NFIELD, cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpy2DAsync(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
+                              T::NSPEC, cudaMemcpyHostToDevice, s));
+    a.in = (const double*)c->h_hetin.p;
+    a.c = (const double*)c->h_c.p;
+    a.het = (double*)c->h_het.p;
+    a.ldi = a.ldc = a.ldh = ncell;
+  } else {
+    a.in = hetin;
+    a.ldi = ldi;
+    a.c = conc;
+    a.ldc = ldc;
+    a.het = het;
+    a.ldh = ldh;
+  }
+  cudaError_t e = gchet::set_state_het(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "SetStateHet kernel launch");
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(cudaMemcpy2DAsync(het, ldh * sizeof(double), a.het, n * sizeof(double), n * sizeof(double), HET_NFIELD,
+                              cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+  }
+  return GC_KPP_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -1279,6 +1330,9 @@ int gc_kpp_integrate_batch_noalloc(int ncell, double tin, double tout, double* c
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   Resolved R;
   GC_TRY(resolve(icntrl_u, rcntrl_u, tin, tout, R));
+  // auto-reduction needs the per-cell mask rows of a context's workspace
+  if (R.autoreduce)
+    return fail(GC_KPP_EUNSUPPORTED, "the no-allocation entry point does not run auto-reduction (ICNTRL(12) = 1)");
   if (!R.code) {
     // Rosenbrock's tolerance check (:464-472) on host copies held on the stack
     const int ntol = R.vector_tol ? T::NVAR : 1;
@@ -1290,12 +1344,8 @@ int gc_kpp_integrate_batch_noalloc(int ncell, double tin, double tout, double* c
       if (!(at[i] > 0.0) || rt[i] <= 10.0 * DBL_EPSILON || rt[i] >= 1.0) R.code = -5;
   }
   if (R.code) {
-    int e[NOALLOC_MAX_CELLS];
-    for (int i = 0; i < ncell; ++i) e[i] = R.code;
-    GC_CUDA(cudaMemcpyAsync(ierr, e, ncell * sizeof(int), cudaMemcpyHostToDevice, s));
-    if (istatus) GC_CUDA(cudaMemset2DAsync(istatus, ldo * sizeof(int), 0, ncell * sizeof(int), 20, s));
-    if (rstatus) GC_CUDA(cudaMemset2DAsync(rstatus, ldo * sizeof(double), 0, ncell * sizeof(double), 20, s));
-    GC_CUDA(cudaStreamSynchronize(s));
+    // every cell gets the option error, ISTATUS/RSTATUS zeroed, on the device
+    GC_CUDA(gcutil::fill_error(R.code, ncell, ierr, istatus, rstatus, ldo, s));
     return GC_KPP_OK;
   }
   // One thread and one workspace slot per cell (plain schedule).  Every slot

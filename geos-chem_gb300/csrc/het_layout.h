@@ -93,3 +93,54 @@
 #define HET_fracInorgAer 165
 #define HET_TurnOffHetRates 166
 #define HET_SUNCOS 167
+// rows of the cell-interleaved fullchem_SetStateHet input array
+#define HETIN_NFIELD 100
+#define HETIN_T 0
+#define HETIN_CLDF 1
+#define HETIN_QI 2
+#define HETIN_QL 3
+#define HETIN_AIRVOL 4
+#define HETIN_AIRDEN 5
+#define HETIN_AD 6
+#define HETIN_FRLAND 7
+#define HETIN_FROCEAN 8
+#define HETIN_InStratosphere 9
+#define HETIN_aClArea 10
+#define HETIN_aClRadi 11
+#define HETIN_IsorropAeroH2O 12  /* 2 rows */
+#define HETIN_AeroArea 14  /* 14 rows */
+#define HETIN_AeroRadi 28  /* 14 rows */
+#define HETIN_WetAeroArea 42  /* 14 rows */
+#define HETIN_AeroH2O 56  /* 14 rows */
+#define HETIN_OMOC_POA 70
+#define HETIN_OMOC_OPOA 71
+#define HETIN_HSO3_aq 72
+#define HETIN_SO3_aq 73
+#define HETIN_IsorropBisulfate 74
+#define HETIN_IsorropNitrate 75
+#define HETIN_IsorropSulfate 76
+#define HETIN_IsorropHplus 77
+#define HETIN_pHCloud 78
+#define HETIN_IsorropAeropH 79  /* 2 rows */
+#define HETIN_SALA 81
+#define HETIN_SALAAL 82
+#define HETIN_SALC 83
+#define HETIN_SALCAL 84
+#define HETIN_fupdateHOBr 85
+#define HETIN_fupdateHOCl 86
+#define HETIN_KHETI_SLA 87  /* 11 rows */
+#define HETIN_STATE_PSC 98
+#define HETIN_SUNCOS 99
+// KPP species read by fullchem_SetStateHet, in the order of the index table
+#define HSS_SO2 0
+#define HSS_HNO3 1
+#define HSS_HCl 2
+#define HSS_HBr 3
+#define HSS_BrSALA 4
+#define HSS_BrSALC 5
+#define HSS_SALACL 6
+#define HSS_SALCCL 7
+#define HSS_NIT 8
+#define HSS_NITs 9
+#define HSS_SO4 10
+#define HSS_N 11

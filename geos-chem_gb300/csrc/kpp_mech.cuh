@@ -148,6 +148,29 @@ __device__ __forceinline__ void term_sum(const MechDev& m, const unsigned* __res
   }
 }
 
+// term_sum in the reference's arithmetic, whatever the translation unit's
+// contraction setting: every product and sum rounds on its own, as the
+// oracle's -ffp-contract=off build and the Fortran do.  The auto-reduction
+// decisions and AutoReduce_1stOrder read P_VAR/D_VAR through this form, so
+// the fast kernel freezes exactly the species the reference freezes.
+template <int NC>
+__device__ __forceinline__ void term_sum_exact(const MechDev& m, const unsigned* __restrict__ terms, int s, int e,
+                                               const double* __restrict__ X, double* acc) {
+  constexpr int TSN = TS * NC;
+#pragma unroll
+  for (int q = 0; q < NC; ++q) acc[q] = 0.0;
+  for (int i = s; i < e; ++i) {
+    const unsigned t = ldu(terms + i);
+    const double cf = __ldg(m.slit + (t >> 20));
+    const double* xp = X + (t & 0xfffffu) * TSN;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      const double v = __dmul_rn(cf, ldw(xp + q * TS));
+      acc[q] = (i == s) ? v : __dadd_rn(acc[q], v);
+    }
+  }
+}
+
 // B(b): the partial-derivative products of Jac_SP, which are also the
 // D_VAR products of Fun_SPLIT (same factor lists, same order).
 template <int NC>
@@ -166,7 +189,9 @@ __device__ __forceinline__ void b_products(const MechDev& m, const double* __res
 // Fun_SPLIT: Vdot = P_VAR - D_VAR*V at point Y = [V | F] (aux = RCT).
 // B must hold the B products at Y (b_products).  With PD, P_VAR and D_VAR
 // are stored too (Fun_SPLITF, gckpp_Function.F90:5081-7260: the same
-// statements).
+// statements), always in the reference's arithmetic (term_sum_exact); Vdot
+// keeps the variant's own arithmetic, so that it equals the Vdot of a call
+// without PD bit for bit.
 template <bool STRICT, int NC, bool PD = false>
 __device__ void fun_split(const MechDev& m, const double* __restrict__ V, const double* __restrict__ aux,
                           double* __restrict__ A, const double* __restrict__ B, double* __restrict__ Vdot,
@@ -187,7 +212,16 @@ __device__ void fun_split(const MechDev& m, const double* __restrict__ V, const 
     for (int q = 0; q < NC; ++q) {
       const double v = V[i * TSN + q * TS];
       Vdot[i * TSN + q * TS] = STRICT ? p[q] - d[q] * v : fma(-d[q], v, p[q]);
-      if (PD) {
+      if (PD && STRICT) {
+        P[i * TSN + q * TS] = p[q];
+        D[i * TSN + q * TS] = d[q];
+      }
+    }
+    if (PD && !STRICT) {
+      term_sum_exact<NC>(m, m.p_sterm, ldi(m.p_start + i), ldi(m.p_start + i + 1), A, p);
+      term_sum_exact<NC>(m, m.d_sterm, ldi(m.d_start + i), ldi(m.d_start + i + 1), B, d);
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
         P[i * TSN + q * TS] = p[q];
         D[i * TSN + q * TS] = d[q];
       }

@@ -57,12 +57,48 @@ NFIELD = _o
 DU1, SUL, BKC, ORC, SSA, SSC, SLA, IIC = 1, 8, 9, 10, 11, 12, 13, 14
 
 
+# Inputs of fullchem_SetStateHet (KPP/fullchem/fullchem_HetStateFuncs.F90:48-244)
+# per cell, as rows of a cell-interleaved array ``hetin[f * ldi + cell]``:
+# the State_Met and State_Chm fields it reads for the grid box, in its units
+# (State_Met: T [K], CLDF [1], QI/QL [kg/kg], AIRVOL [m3], AIRDEN [kg/m3],
+# AD [kg], FRLAND/FROCEAN [1], InStratosphere 0/1; State_Chm: aerosol areas
+# [cm2/cm3], radii [cm], AeroH2O [cm3/m3], ISORROPIA/HETP water, molalities,
+# H+ and pH, cloud pH, HSO3_aq/SO3_aq [mol/L], the sea-salt species SALA,
+# SALAAL, SALC, SALCAL (any one unit: only their ratios are used),
+# fupdateHOBr/HOCl, KHETI_SLA, STATE_PSC), and SUNCOS, which is copied to
+# the HetState array's last row.  The KPP species it reads come from C.
+HETIN_FIELDS = [
+    ("T", 1), ("CLDF", 1), ("QI", 1), ("QL", 1), ("AIRVOL", 1), ("AIRDEN", 1), ("AD", 1), ("FRLAND", 1),
+    ("FROCEAN", 1), ("InStratosphere", 1), ("aClArea", 1), ("aClRadi", 1), ("IsorropAeroH2O", 2),
+    ("AeroArea", 14), ("AeroRadi", 14), ("WetAeroArea", 14), ("AeroH2O", 14), ("OMOC_POA", 1), ("OMOC_OPOA", 1),
+    ("HSO3_aq", 1), ("SO3_aq", 1), ("IsorropBisulfate", 1), ("IsorropNitrate", 1), ("IsorropSulfate", 1),
+    ("IsorropHplus", 1), ("pHCloud", 1), ("IsorropAeropH", 2), ("SALA", 1), ("SALAAL", 1), ("SALC", 1),
+    ("SALCAL", 1), ("fupdateHOBr", 1), ("fupdateHOCl", 1), ("KHETI_SLA", 11), ("STATE_PSC", 1), ("SUNCOS", 1),
+]
+HETIN_OFFSET = {}
+_o = 0
+for _name, _len in HETIN_FIELDS:
+    HETIN_OFFSET[_name] = _o
+    _o += _len
+NHETIN = _o
+# KPP species that fullchem_SetStateHet reads through C(ind_X)
+SETSTATE_SPECIES = ["SO2", "HNO3", "HCl", "HBr", "BrSALA", "BrSALC", "SALACL", "SALCCL", "NIT", "NITs", "SO4"]
+
+
 def emit_c():
     lines = ["// Generated by gcchem.hetstate (emit_c). Do not edit.", "#pragma once",
              "// rows of the cell-interleaved HetState array (order of the Fortran type)",
              "#define HET_NFIELD %d" % NFIELD]
     for name, n in FIELDS:
         lines.append("#define HET_%s %d%s" % (name, OFFSET[name], "  /* %d rows */" % n if n > 1 else ""))
+    lines += ["// rows of the cell-interleaved fullchem_SetStateHet input array",
+              "#define HETIN_NFIELD %d" % NHETIN]
+    for name, n in HETIN_FIELDS:
+        lines.append("#define HETIN_%s %d%s" % (name, HETIN_OFFSET[name], "  /* %d rows */" % n if n > 1 else ""))
+    lines.append("// KPP species read by fullchem_SetStateHet, in the order of the index table")
+    for k, name in enumerate(SETSTATE_SPECIES):
+        lines.append("#define HSS_%s %d" % (name, k))
+    lines.append("#define HSS_N %d" % len(SETSTATE_SPECIES))
     return "\n".join(lines) + "\n"
 
 
@@ -171,4 +207,63 @@ def het_cells(n, seed=0, strat_fraction=0.15, cloud_fraction=0.5):
     h[o["fracOrgAer"]] = rng.uniform(0.0, 1.0, n)
     h[o["fracInorgAer"]] = 1.0 - h[o["fracOrgAer"]]
     h[o["SUNCOS"]] = np.where(rng.uniform(size=n) < 0.5, rng.uniform(0.0, 1.0, n), -rng.uniform(0.0, 1.0, n))
+    return h
+
+
+def hetin_cells(n, seed=0, strat_fraction=0.15, cloud_fraction=0.5):
+    """Seeded synthetic inputs of fullchem_SetStateHet for n cells
+    ([NHETIN, n]): grid-box air volume, density and mass of a 4x5 column,
+    cloud fraction and condensate where cloudy, land/ocean split, aerosol
+    areas/radii/water of the 14 types (the stratospheric liquid and ice
+    types only in the stratosphere), ISORROPIA/HETP water and molalities,
+    pH values, sulfite, sea-salt alkalinity, KHETI_SLA and the PSC state."""
+    rng = np.random.default_rng(seed)
+    h = np.zeros((NHETIN, n))
+    o = HETIN_OFFSET
+    lu = lambda lo, hi, size=n: np.exp(rng.uniform(np.log(lo), np.log(hi), size))
+    strat = rng.uniform(size=n) < strat_fraction
+    h[o["T"]] = np.where(strat, rng.uniform(185.0, 240.0, n), rng.uniform(200.0, 310.0, n))
+    cloudy = (rng.uniform(size=n) < cloud_fraction) & ~strat
+    h[o["CLDF"]] = np.where(cloudy, rng.uniform(1e-4, 1.0, n), 0.0)
+    h[o["QL"]] = np.where(cloudy & (rng.uniform(size=n) < 0.8), lu(1e-7, 1e-3), 0.0)
+    h[o["QI"]] = np.where(cloudy & (rng.uniform(size=n) < 0.5), lu(1e-8, 1e-4), 0.0)
+    h[o["AIRVOL"]] = lu(2e12, 3e14)
+    h[o["AIRDEN"]] = np.where(strat, lu(1e-3, 0.2), lu(0.1, 1.3))
+    h[o["AD"]] = h[o["AIRDEN"]] * h[o["AIRVOL"]]
+    land = rng.uniform(size=n)
+    h[o["FRLAND"]] = land
+    h[o["FROCEAN"]] = 1.0 - land
+    h[o["InStratosphere"]] = strat
+    for t in range(14):
+        area = lu(1e-9, 1e-5)
+        radi = lu(2e-6, 2e-4)
+        if t + 1 in (SLA, IIC):
+            area = area * strat
+        h[o["AeroArea"] + t] = area
+        h[o["WetAeroArea"] + t] = area * rng.uniform(1.0, 2.0, n)
+        h[o["AeroRadi"] + t] = radi
+        h[o["AeroH2O"] + t] = area * radi / 3.0 * 1e6 * rng.uniform(0.0, 0.8, n)
+    h[o["aClArea"]] = h[o["AeroArea"] + SUL - 1] + h[o["AeroArea"] + SSA - 1]
+    h[o["aClRadi"]] = lu(5e-6, 5e-5)
+    h[o["IsorropAeroH2O"]] = lu(1e-12, 1e-9)
+    h[o["IsorropAeroH2O"] + 1] = lu(1e-12, 1e-9)
+    h[o["OMOC_POA"]] = rng.uniform(1.4, 2.1, n)
+    h[o["OMOC_OPOA"]] = rng.uniform(1.4, 2.1, n)
+    h[o["HSO3_aq"]] = np.where(cloudy, lu(1e-9, 1e-4), 0.0)
+    h[o["SO3_aq"]] = np.where(cloudy, lu(1e-12, 1e-6), 0.0)
+    for f in ("IsorropBisulfate", "IsorropNitrate", "IsorropSulfate"):
+        h[o[f]] = lu(1e-4, 5.0)
+    h[o["IsorropHplus"]] = lu(1e-8, 1e-1)
+    h[o["pHCloud"]] = np.where(cloudy, rng.uniform(3.0, 6.5, n), 0.0)
+    h[o["IsorropAeropH"]] = rng.uniform(1.0, 8.0, n)
+    h[o["IsorropAeropH"] + 1] = rng.uniform(1.0, 8.0, n)
+    h[o["SALA"]] = lu(1e-3, 10.0)
+    h[o["SALAAL"]] = h[o["SALA"]] * np.where(rng.uniform(size=n) < 0.5, rng.uniform(0.0, 1.2, n), 0.0)
+    h[o["SALC"]] = np.where(rng.uniform(size=n) < 0.9, lu(1e-3, 10.0), 0.0)
+    h[o["SALCAL"]] = h[o["SALC"]] * rng.uniform(0.0, 0.05, n)
+    h[o["fupdateHOBr"]] = rng.uniform(0.5, 1.0, n)
+    h[o["fupdateHOCl"]] = rng.uniform(0.5, 1.0, n)
+    h[o["KHETI_SLA"]:o["KHETI_SLA"] + 11] = lu(1e-12, 1e-5, (11, n)) * strat
+    h[o["STATE_PSC"]] = np.where(strat, rng.integers(0, 4, n), 0)
+    h[o["SUNCOS"]] = rng.uniform(-1.0, 1.0, n)
     return h

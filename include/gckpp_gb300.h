@@ -198,6 +198,37 @@ int gc_kpp_update_rconst_batch(gc_kpp_ctx* ctx, int ncell, const double* met, lo
  * species database and RELHUM from TEMP and H2O as Set_Kpp_GridBox_Values
  * computes it.  Mechanisms other than fullchem keep their heterogeneous
  * rates at 0. */
+/* Rows of the input array of gc_kpp_set_state_het_batch: the State_Met and
+ * State_Chm fields of the grid box that fullchem_SetStateHet reads, in its
+ * units (T, CLDF, QI, QL, AIRVOL, AIRDEN, AD, FRLAND, FROCEAN,
+ * InStratosphere, aClArea, aClRadi, IsorropAeroH2O(2), AeroArea(14),
+ * AeroRadi(14), WetAeroArea(14), AeroH2O(14), OMOC_POA, OMOC_OPOA, HSO3_aq,
+ * SO3_aq, IsorropBisulfate, IsorropNitrate, IsorropSulfate, IsorropHplus,
+ * pHCloud, IsorropAeropH(2), the sea-salt species SALA, SALAAL, SALC,
+ * SALCAL, fupdateHOBr, fupdateHOCl, KHETI_SLA(11), STATE_PSC), then SUNCOS;
+ * 100 rows.  Row offsets: the HETIN_* macros of
+ * geos-chem_gb300/csrc/het_layout.h. */
+#define GC_KPP_NHETIN 100
+
+/* Batched fullChem_SetStateHet (KPP/fullchem/fullchem_HetStateFuncs.F90:
+ * 48-244, with Cld_Params, Get_Theta_Ice and Halide_Conc; called at
+ * GeosCore/fullchem_mod.F90:885): the HetState rows of each cell.
+ *
+ *   hetin  [GC_KPP_NHETIN][ldi]  in   grid-box fields (rows above)
+ *   c      [NSPEC][ldc]          in   KPP concentrations (SO2, HNO3, HCl, HBr,
+ *                                     BrSALA, BrSALC, SALACL, SALCCL, NIT,
+ *                                     NITs, SO4 are read)
+ *   gamma_ho2, lpscchem, turn_off_het_rates
+ *                                     Input_Opt%gamma_HO2, %LPSCCHEM (0/1),
+ *                                     %TurnOffHetRates (0/1)
+ *   het    [GC_KPP_NHET][ldh]    out  HetState rows, SUNCOS copied from hetin
+ *
+ * Fields the reference routine does not set (H2O, and the Hg-only cloudBox,
+ * fracOrgAer, fracInorgAer) are written as 0. */
+int gc_kpp_set_state_het_batch(gc_kpp_ctx* ctx, int ncell, const double* hetin, long long ldi,
+                               const double* c, long long ldc, double gamma_ho2, int lpscchem,
+                               int turn_off_het_rates, double* het, long long ldh, int mem, void* stream);
+
 /* HetState of the cells of the following chemistry steps on this context
  * (gc_kpp_fullchem_step and its ordered/binned/learned forms evaluate the
  * heterogeneous rates from it): het [GC_KPP_NHET][ldh] for `ncell` cells, in
@@ -316,12 +347,14 @@ int gc_kpp_fullchem_step_learned(gc_kpp_ctx* ctx, gc_kpp_proposer* proposer, int
                                  long long ldo, int* ierr, int* nretry, int* nblock, int mem, void* stream);
 
 /* Batched INTEGRATE that allocates nothing, for callers that cannot call
- * cudaMalloc: code running inside a host application's memory-pool or
- * graph-building phase, an embedding framework that owns all device memory,
- * or a process whose allocator must not be touched mid-step.  No counterpart
- * in the reference (whose state is module globals); arguments and results
- * are those of gc_kpp_integrate_batch, with every array in device memory and
- * the fast arithmetic with one thread per cell.
+ * cudaMalloc: an embedding framework or host model that owns all device
+ * memory through its own pool, or a process whose allocator must not be
+ * touched in the middle of a time step.  No counterpart in the reference
+ * (whose state is module globals); arguments and results are those of
+ * gc_kpp_integrate_batch, with every array in device memory and the fast
+ * arithmetic with one thread per cell.  Auto-reduction (ICNTRL(12) = 1) is
+ * refused with GC_KPP_EUNSUPPORTED.  The call reads ATOL/RTOL back to the
+ * host for the tolerance check and waits for that copy on the stream.
  *
  * It needs no context: its workspace for at most GC_KPP_NOALLOC_MAX_CELLS
  * cells (about 157 MB) and its copy of the mechanism tables are file-scope

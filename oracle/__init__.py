@@ -55,6 +55,7 @@ def load(variant="strict", mech="fullchem"):
     lib.oracle_kpp_decomp.argtypes = [vp]
     lib.oracle_kpp_decomp.restype = i32
     lib.oracle_max_threads.restype = i32
+    lib.oracle_set_state_het_batch.argtypes = [i32, vp, i64, vp, i64, f64, i32, i32, vp, i64]
     _libs[key] = lib
     return lib
 
@@ -121,6 +122,25 @@ def update_rconst(met, photol, c, variant="strict", mech="fullchem", het=None):
     else:
         het = _c(het, np.float64)
         lib.oracle_update_rconst_het_batch(n, _p(met), n, _p(photol), n, _p(c), n, _p(het), n, _p(out), n)
+    return out
+
+
+def set_state_het(hetin, c, gamma_ho2=0.2, lpscchem=1, turn_off_het_rates=0, mech="fullchem"):
+    """Batched fullchem_SetStateHet: hetin [NHETIN, n] grid-box fields and
+    c [NSPEC, n] -> HetState rows [168, n]."""
+    lib = load("strict", mech)
+    hetin = _c(hetin, np.float64)
+    c = _c(c, np.float64)
+    n = hetin.shape[1]
+    sys_path = os.path.join(HERE, "..", "geos-chem_gb300")
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("_oracle_hetstate", os.path.join(sys_path, "hetstate.py"))
+    hs = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(hs)
+    out = np.zeros((hs.NFIELD, n), np.float64)
+    lib.oracle_set_state_het_batch(n, _p(hetin), n, _p(c), n, float(gamma_ho2), int(lpscchem),
+                                   int(turn_off_het_rates), _p(out), n)
     return out
 
 

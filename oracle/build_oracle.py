@@ -48,9 +48,9 @@ def build(verbose=False, mechs=MECHANISMS):
 
 def _compile(gen, mech, verbose):
     srcs = [os.path.join(HERE, "kpp_oracle.c"), os.path.join(gen, "kpp_mech_oracle.c"),
-            os.path.join(gen, "kpp_rates_oracle.c")]
+            os.path.join(gen, "kpp_rates_oracle.c"), os.path.join(HERE, "het_state.c")]
     deps = srcs + [os.path.join(HERE, f) for f in ("kpp_oracle.h", "rate_laws.h", "het_laws.h")] + \
-        [os.path.join(gen, "kpp_dims.h")]
+        [os.path.join(gen, "kpp_dims.h"), os.path.join(gen, "oracle_het_layout.h")]
     procs = []
     for variant, flags in VARIANTS.items():
         out = lib_path(variant, mech)

@@ -297,14 +297,21 @@ def generate_rates(ir):
     return "\n".join(L) + "\n", sorted(het)
 
 
-def write_het_layout(outdir):
-    """oracle_het_layout.h: OHET_* row offsets of the HetState array."""
+def write_het_layout(outdir, mech="fullchem"):
+    """oracle_het_layout.h: OHET_* row offsets of the HetState array, OHIN_*
+    row offsets of fullchem_SetStateHet's inputs, and OSS_* the KPP indices
+    (-1 when absent) of the species fullchem_SetStateHet reads."""
     sys.path.insert(0, os.path.join(HERE, "..", "geos-chem_gb300"))
-    import hetstate  # the field list of the batch interface (data only)
+    import hetstate  # the field lists of the batch interface (data only)
 
+    species = _ir(mech)["species"]
     lines = ["/* Generated by oracle/gen_oracle.py from the HetState field list. */", "#pragma once"]
     for name, n in hetstate.FIELDS:
         lines.append("#define OHET_%s %d" % (name, hetstate.OFFSET[name]))
+    for name, n in hetstate.HETIN_FIELDS:
+        lines.append("#define OHIN_%s %d" % (name, hetstate.HETIN_OFFSET[name]))
+    for name in hetstate.SETSTATE_SPECIES:
+        lines.append("#define OSS_%s %d" % (name, species.index(name) if name in species else -1))
     text = "\n".join(lines) + "\n"
     path = os.path.join(outdir, "oracle_het_layout.h")
     old = open(path).read() if os.path.exists(path) else None
@@ -315,7 +322,7 @@ def write_het_layout(outdir):
 
 
 def write_rates(outdir, mech="fullchem"):
-    write_het_layout(outdir)
+    write_het_layout(outdir, mech)
     text, het = generate_rates(_ir(mech))
     path = os.path.join(outdir, "kpp_rates_oracle.c")
     old = open(path).read() if os.path.exists(path) else None

@@ -53,6 +53,9 @@ static inline long long __double_as_longlong(double d) {
 // one emulated thread runs at a time: it is the only active lane of its warp
 static inline unsigned __activemask() { return 1u << (threadIdx.x & 31u); }
 static inline int __ffs(unsigned x) { return __builtin_ffs((int)x); }
+// round-to-nearest products and sums (built -ffp-contract=off: never fused)
+static inline double __dmul_rn(double a, double b) { return a * b; }
+static inline double __dadd_rn(double a, double b) { return a + b; }
 static inline int __popc(unsigned x) { return __builtin_popcount(x); }
 static inline int __shfl_sync(unsigned, int v, int) { return v; }
 static inline int atomicAdd(int* p, int v) {

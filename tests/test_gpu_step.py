@@ -115,19 +115,31 @@ def test_option_errors_give_reference_ierr(solver, step_case, field, value, code
     assert np.array_equal(c, step_case["cells"]["c"])
 
 
-@pytest.mark.parametrize("which", ["rate_updates", "autoreduce"])
+@pytest.mark.parametrize("which", ["rate_updates", "autoreduce_2cells", "autoreduce_target"])
 def test_unsupported_options_are_rejected(solver, step_case, which):
+    """Forms outside the implemented path fail the call with
+    GC_KPP_EUNSUPPORTED: rate updates inside the integrator, auto-reduction
+    with 2 cells per thread (it runs 1 cell per thread only) and a target
+    species outside 1..NVAR."""
     n = step_case["n"]
     ic = step_case["icntrl"].copy()
     if which == "rate_updates":
         ic[14] = 0  # INTEGRATE then defaults ICNTRL(15) to 5: updates inside the integrator
+    elif which == "autoreduce_2cells":
+        ic[11] = 1
+        solver.set(arith="fast2")
     else:
         ic[11] = 1
+        ic[13] = 354  # ICNTRL(14) beyond NVAR
     c = step_case["cells"]["c"].copy()
     r = np.ones((1058, n)) * 1e-12
     ierr = np.zeros(n, np.int32)
-    with pytest.raises(capi.GcKppError) as e:
-        solver.integrate(c, r, step_case["atol"], step_case["rtol"], 0.0, 60.0, ic, step_case["rcntrl"], ierr=ierr)
+    try:
+        with pytest.raises(capi.GcKppError) as e:
+            solver.integrate(c, r, step_case["atol"], step_case["rtol"], 0.0, 60.0, ic, step_case["rcntrl"],
+                             ierr=ierr)
+    finally:
+        solver.set(arith="fast")
     assert e.value.code == capi.GC_KPP_EUNSUPPORTED
 
 
