@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample duration")
     ap.add_argument("--weights", default=WEIGHTS, help="trained proposer weights (.npz)")
     ap.add_argument("--error-cells", type=int, default=2048, help="cells integrated at RTOL 1e-8 for the error")
+    ap.add_argument("--e2e-chunks", type=int, default=4,
+                    help="chunks of the end-to-end step (host copies overlap the solves of other chunks)")
     return ap.parse_args()
 
 
@@ -201,7 +203,7 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times)) * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded standard-atmosphere grid, 24 h CPU spin-up of the sampled cells)",
         "config": {"workload": "fullchem 4x5x72 grid (238,464 cells), one 1200 s step, Rodas3, RTOL 5e-3",
                    "cells": ncell, "dt_s": DT, "sample_cells_per_step": per},
@@ -230,8 +232,11 @@ def run_ours(args):
     from gcchem import build as gbuild
 
     nlon, nlat, nlev = (int(x) for x in args.grid.split("x"))
-    cells = inputs.grid_cells(nlon, nlat, nlev, seed=args.seed + rank)
+    # every rank builds the same grid; with N > 1 ranks each times its own
+    # shard of it (gcchem.shard, balanced by the proposer's stiffness bins)
+    cells = inputs.grid_cells(nlon, nlat, nlev, seed=args.seed)
     ncell = cells["c"].shape[1]
+    ncell_total = ncell
     atol, rtol = inputs.tolerances()
     icntrl, rcntrl = inputs.default_controls()
     stream = torch.cuda.current_stream(dev)
@@ -273,6 +278,25 @@ def run_ours(args):
 
     prop = learned.Proposer(local)
     prop.load_state(dict(np.load(args.weights)))
+
+    shard = (0, ncell)
+    if world > 1:
+        # one grid split N ways with no collective on the data path: every
+        # rank spun up the whole grid (the same bits on every GPU), weighs
+        # each cell by its predicted stiffness bin and keeps its range
+        import gcchem.shard as shard_mod
+
+        x = prop.features(met, ph, c_spun, stream=sp)
+        _, bins = prop.propose(x, stream=sp, hmax=DT)
+        shard = shard_mod.shard_range(ncell, rank, world, shard_mod.work_from_bins(bins.cpu().numpy()))
+        a, b = shard
+        met, ph = met[:, a:b].contiguous(), ph[:, a:b].contiguous()
+        c_spun, hs_spun = c_spun[:, a:b].contiguous(), hs_spun[a:b].contiguous()
+        ncell = b - a
+        ist = torch.zeros((20, ncell), dtype=torch.int32, device=dev)
+        rst = torch.zeros((20, ncell), dtype=torch.float64, device=dev)
+        ierr = torch.zeros(ncell, dtype=torch.int32, device=dev)
+        dev_t.update(met=met, ph=ph, ist=ist, rst=rst, ierr=ierr)
 
     def plain_arm(w, hs):
         solver.set(evict_after=0)
@@ -343,7 +367,7 @@ def run_ours(args):
             t = torch.tensor([ms_step], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             ms_step = float(t.item())
-        return {"ms_per_step": ms_step, "value": world * ncell / (ms_step * 1e-3),
+        return {"ms_per_step": ms_step, "value": ncell_total / (ms_step * 1e-3),
                 "kernel_ms": float(np.mean(kernel_ms)), "gpu_launches": int(launches), "clocks": clocks,
                 "ist": ist.cpu().numpy(), "ierr": ierr.cpu().numpy(), "retried_cells": int(last["nretry"]),
                 "block_per_cell_cells": int(last.get("nblock", 0)) if name.startswith("learned") else 0,
@@ -394,35 +418,62 @@ def run_ours(args):
 
     errors = {name: rel_err(res[name]["c"]) for name in arms}
 
-    # end to end through the public API: pinned host inputs copied in, the
-    # learned plan and the ordered chemistry step, results copied out
+    # end to end through the public API: the grid's inputs in pinned host
+    # memory, the learned chemistry step (gc_kpp_fullchem_step_learned)
+    # streamed in chunks by gcchem.stream.Streamer -- while one chunk solves,
+    # the next chunk's inputs (met, the J-value rows the mechanism reads, C,
+    # KPPHvalue) are copied in and the previous chunk's results (C,
+    # KPPHvalue, ISTATUS(3), IERR) copied out; two solver contexts alternate,
+    # so a chunk's block-per-cell tail overlaps the next chunk's queue kernel
     e2e = None
     if rank == 0 or world > 1:
-        pin = lambda x: x.cpu().pin_memory()
-        h = {"met": pin(met), "ph": pin(ph), "c": pin(c_spun), "hs": pin(cold0)}
-        out = {"c": pin(c_spun), "hs": pin(hs_spun), "ist": pin(ist), "rst": pin(rst), "ierr": pin(ierr)}
-        d = {k: torch.empty_like(v, device=dev) for k, v in h.items()}
-        tt = dict(dev_t, met=d["met"], ph=d["ph"])
+        import gcchem.stream as stream
+
+        nch = max(1, args.e2e_chunks)
+        chunk = -(-ncell // nch)
+        pin = lambda x: x.contiguous().pin_memory()
+        host_in = {"met": met.cpu(), "ph": ph.cpu(), "c": c_spun.cpu(), "hs": cold0.cpu()}
+        chunks = []
+        for i0 in range(0, ncell, chunk):
+            i1 = min(ncell, i0 + chunk)
+            ch = {k: pin(v[..., i0:i1]) for k, v in host_in.items()}
+            ch.update(c_out=torch.empty_like(ch["c"]).pin_memory(), hs_out=torch.empty_like(ch["hs"]).pin_memory(),
+                      steps=torch.zeros(i1 - i0, dtype=torch.int32).pin_memory(),
+                      ierr=torch.zeros(i1 - i0, dtype=torch.int32).pin_memory())
+            chunks.append(ch)
+        cp = learned.CProposer(prop, local)
+        second = capi.Solver(local, arith="fast", schedule=args.schedule)
+        solvers = [solver, second]
+        for sv in solvers:
+            sv.set(evict_after=EVICT_LEARNED)
+        st = stream.Streamer(solver, ncell, chunk, proposer=cp, solvers=solvers, photol_rows=stream.photol_runs())
+        st.step(chunks, DT, at, rt, icntrl, rcntrl)  # synchronous: sizes each context's buffers
+        for sv in solvers:
+            sv.set(async_steps=True)
         tms = []
-        for it in range(1 + min(args.steps, 2)):
+        for it in range(1 + min(args.steps, 3)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            for k in h:
-                d[k].copy_(h[k], non_blocking=True)
-            learned_arm(d["c"], d["hs"], met_=d["met"], ph_=d["ph"], tt=tt)
-            out["c"].copy_(d["c"], non_blocking=True)
-            out["hs"].copy_(d["hs"], non_blocking=True)
-            out["ist"].copy_(ist, non_blocking=True)
-            out["rst"].copy_(rst, non_blocking=True)
-            out["ierr"].copy_(ierr, non_blocking=True)
+            st.step(chunks, DT, at, rt, icntrl, rcntrl)
             torch.cuda.synchronize()
             if it > 0:
                 tms.append(time.perf_counter() - t0)
-        h2d = sum(v.numel() * v.element_size() for v in h.values())
-        d2h = sum(v.numel() * v.element_size() for v in out.values())
-        e2e = {"value": world * ncell / float(np.mean(tms)), "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h),
-               "path": "learned.plan + gc_kpp_fullchem_step_binned, pinned host buffers"}
+        for sv in solvers:
+            sv.set(async_steps=False)
+        steps_e2e = np.concatenate([ch["steps"].numpy() for ch in chunks])
+        h2d, d2h = st.bytes_per_cell()
+        tmax = float(np.mean(tms))
+        if world > 1:
+            t = torch.tensor([tmax], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tmax = float(t.item())
+        e2e = {"value": ncell_total / tmax, "unit": "cells/s", "h2d_bytes_per_step": int(h2d * ncell_total),
+               "d2h_bytes_per_step": int(d2h * ncell_total), "chunks": len(chunks),
+               "steps_match_learned_arm": bool(np.array_equal(steps_e2e, head["ist"][2])),
+               "path": "gcchem.stream.Streamer over gc_kpp_fullchem_step_learned, pinned host buffers, "
+                       "%d chunks on 2 solver contexts" % len(chunks)}
+        second.close()
+        cp.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -431,11 +482,11 @@ def run_ours(args):
         solver.update_rconst(met, ph, c_spun, r_dev)
         threads = os.cpu_count() or 1
         host = {"c": c_spun.cpu().numpy()}
-        m, dt = cpu_baseline_sample(orc, host, r_dev.cpu().numpy(), atol, rtol, icntrl, rcntrl, args.cpu_seconds,
-                                    threads)
-        cpu = {"value": m / dt, "unit": "cells/s", "cores": threads, "kind": "port",
+        m_cpu, dt = cpu_baseline_sample(orc, host, r_dev.cpu().numpy(), atol, rtol, icntrl, rcntrl,
+                                        args.cpu_seconds, threads)
+        cpu = {"value": m_cpu / dt, "unit": "cells/s", "cores": threads, "kind": "port",
                "sample": "%d evenly spaced spun-up cells of the grid, one 1200 s Integrate each from "
-                         "Hstart = 0, oracle -O3 OpenMP DYNAMIC,24 (%.1f s)" % (m, dt)}
+                         "Hstart = 0, oracle -O3 OpenMP DYNAMIC,24 (%.1f s)" % (m_cpu, dt)}
 
     if rank == 0:
         summary = lambda r, name: {"value": r["value"], "ms_per_step": r["ms_per_step"], "kernel_ms": r["kernel_ms"],
@@ -448,12 +499,13 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": head["value"], "unit": "cells/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "scaling": "strong", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded standard-atmosphere 4x5x72 grid, 24 h GPU spin-up)",
             "config": {"workload": "fullchem 4x5x72 grid (238,464 cells), one 1200 s chemistry step, Rodas3, "
                                    "RTOL 5e-3 / ATOL 1e-2, FP64, Hstart = 0 (DeltaMin) unless the network "
                                    "proposes H0",
                        "cells_per_gpu": ncell, "dt_s": DT,
+                       "shard": [int(shard[0]), int(shard[1])] if world > 1 else None,
                        "solver": "%s schedule, fast arithmetic, 1 cell per thread" % args.schedule,
                        "value_is": "learned-binned arm: MLP H0 proposals seed Hstart, stiffness bins order "
                                    "the persistent queue and send the top bin block-per-cell, cells still "

@@ -49,6 +49,7 @@ EXPORTED = [
     "gc_kpp_update_rconst_batch",
     "gc_kpp_update_rconst_het_batch",
     "gc_kpp_set_state_het_batch",
+    "gc_kpp_sulfur_aq_rates_batch",
     "gc_kpp_ctx_set_hetstate",
     "gc_kpp_ctx_set_autoreduce",
     "gc_kpp_fullchem_step",
@@ -93,6 +94,7 @@ def load_library(path=None, mech="fullchem"):
     lib.gc_kpp_ctx_set_hetstate.argtypes = [vp, i32, vp, i64, i32]
     lib.gc_kpp_ctx_set_autoreduce.argtypes = [vp, i32, vp, vp, vp, vp, i32]
     lib.gc_kpp_set_state_het_batch.argtypes = [vp, i32, vp, i64, vp, i64, f64, i32, i32, vp, i64, i32, vp]
+    lib.gc_kpp_sulfur_aq_rates_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, i32, vp]
     if path == _build.lib_path(mech):
         _libs[mech] = lib
     return lib
@@ -329,6 +331,21 @@ class Solver:
                                                  _ld(c, ncell), float(gamma_ho2), int(lpscchem),
                                                  int(turn_off_het_rates), _ptr(het), _ld(het, ncell),
                                                  MEM_DEVICE if dev else MEM_HOST, s)
+        self._check(rc)
+
+    def sulfur_aq_rates(self, hetin, c, met, stream=None):
+        """Batched fullchem_SulfurAqChem (gc_kpp_sulfur_aq_rates_batch): the
+        K_MT rows of met [NMET, ncell] (in/out; TEMP and NUMDEN read) from
+        hetin [NHETIN, ncell] and c [NSPEC, ncell]."""
+        dev = _is_torch(met) and met.is_cuda
+        ncell = met.shape[1]
+        if not dev:
+            hetin = np.ascontiguousarray(hetin, dtype=np.float64)
+            c = np.ascontiguousarray(c, dtype=np.float64)
+        s = ctypes.c_void_p(stream) if stream else None
+        rc = self.lib.gc_kpp_sulfur_aq_rates_batch(self.ctx, ncell, _ptr(hetin), _ld(hetin, ncell), _ptr(c),
+                                                   _ld(c, ncell), _ptr(met), _ld(met, ncell),
+                                                   MEM_DEVICE if dev else MEM_HOST, s)
         self._check(rc)
 
     def update_rconst(self, met, photol, c, rconst, stream=None, het=None):

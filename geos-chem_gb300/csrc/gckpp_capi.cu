@@ -1211,6 +1211,59 @@ int gc_kpp_set_state_het_batch(gc_kpp_ctx* c, int ncell, const double* hetin, lo
   return GC_KPP_OK;
 }
 
+int gc_kpp_sulfur_aq_rates_batch(gc_kpp_ctx* c, int ncell, const double* hetin, long long ldi, const double* conc,
+                                 long long ldc, double* met, long long ldm, int mem, void* stream) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
+  if (ncell == 0) return GC_KPP_OK;
+  if (!hetin || !conc || !met) return fail(GC_KPP_EINVAL, "required array is NULL");
+  if (ldi < ncell || ldc < ncell || ldm < ncell) return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
+  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  GC_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  gchet::SulfurAqArgs a{};
+  a.ncell = ncell;
+  for (int k = 0; k < HSS_N; ++k) {
+    a.ind[k] = RT::hss_ind[k];
+    a.srmw[k] = RT::hss_srmw[k];
+  }
+  a.row_temp = GC_KPP_MET_TEMP;
+  a.row_numden = GC_KPP_MET_NUMDEN;
+  a.row_kmt = GC_KPP_MET_K_MT;
+  const size_t n = (size_t)ncell;
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(c->h_hetin.ensure((size_t)HETIN_NFIELD * n * sizeof(double)));
+    GC_CUDA(c->h_c.ensure(T::NSPEC * n * sizeof(double)));
+    GC_CUDA(c->h_met.ensure(RT::NMET * n * sizeof(double)));
+    GC_CUDA(cudaMemcpy2DAsync(c->h_hetin.p, n * sizeof(double), hetin, ldi * sizeof(double), n * sizeof(double),
+                              HETIN_NFIELD, cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpy2DAsync(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
+                              T::NSPEC, cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpy2DAsync(c->h_met.p, n * sizeof(double), met, ldm * sizeof(double), n * sizeof(double),
+                              RT::NMET, cudaMemcpyHostToDevice, s));
+    a.in = (const double*)c->h_hetin.p;
+    a.c = (const double*)c->h_c.p;
+    a.met = (double*)c->h_met.p;
+    a.ldi = a.ldc = a.ldm = ncell;
+  } else {
+    a.in = hetin;
+    a.ldi = ldi;
+    a.c = conc;
+    a.ldc = ldc;
+    a.met = met;
+    a.ldm = ldm;
+  }
+  cudaError_t e = gchet::sulfur_aq_rates(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "SulfurAqChem kernel launch");
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(cudaMemcpy2DAsync(met + (long long)GC_KPP_MET_K_MT * ldm, ldm * sizeof(double),
+                              a.met + (long long)GC_KPP_MET_K_MT * ncell, n * sizeof(double), n * sizeof(double), 6,
+                              cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+  }
+  return GC_KPP_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -131,7 +131,7 @@
 #define HETIN_KHETI_SLA 87  /* 11 rows */
 #define HETIN_STATE_PSC 98
 #define HETIN_SUNCOS 99
-// KPP species read by fullchem_SetStateHet, in the order of the index table
+// KPP species read by fullchem_SetStateHet and fullchem_SulfurAqChem, in the order of the index table
 #define HSS_SO2 0
 #define HSS_HNO3 1
 #define HSS_HCl 2
@@ -143,4 +143,7 @@
 #define HSS_NIT 8
 #define HSS_NITs 9
 #define HSS_SO4 10
-#define HSS_N 11
+#define HSS_SALAAL 11
+#define HSS_SALCAL 12
+#define HSS_O3 13
+#define HSS_N 14

@@ -9,6 +9,7 @@
 //   Compute_L2G_Local               :325-650
 //   Cld_Params                      KPP/fullchem/rateLawUtilFuncs.F90:281-417
 //   CALC_KH, CALC_HEFF              GeosUtil/henry_mod.F90:74-204
+//   fullchem_SulfurAqChem (K_MT)    KPP/fullchem/fullchem_SulfurChemFuncs.F90:120-305
 //
 // One thread per cell.  Inputs are rows of a cell-interleaved array
 // (HETIN_* of het_layout.h); outputs the HET_NFIELD rows of the HetState
@@ -275,7 +276,51 @@ __global__ void set_state_het_kernel(SetStateArgs a) {
   X.out(HET_SUNCOS, X.in(HETIN_SUNCOS));
 }
 
+// fullchem_SulfurAqChem (KPP/fullchem/fullchem_SulfurChemFuncs.F90:120-305):
+// uptake of SO2 (with O3), HCl and HNO3 on alkaline fine (type 11) and coarse
+// (type 12) sea salt, K_MT(1:6) [1/s or cm3/molec/s], through Ars_L1K and
+// kIIR1Ltd (rateLawUtilFuncs.F90:77-160) at the cell's TEMP and NUMDEN.
+__global__ void sulfur_aq_kernel(SulfurAqArgs a) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= a.ncell) return;
+  auto in = [&](int f) { return a.in[(long long)f * a.ldi + cell]; };
+  auto c = [&](int sp) {
+    const int i = a.ind[sp];
+    return i >= 0 ? a.c[(long long)i * a.ldc + cell] : 0.0;
+  };
+  gcrates::HetCell X{};
+  X.NUMDEN = a.met[(long long)a.row_numden * a.ldm + cell];
+  X.SR_TEMP = sqrt(a.met[(long long)a.row_temp * a.ldm + cell]);
+  double k_mt[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  const bool salaal = c(HSS_SALAAL) > 0.1, salcal = c(HSS_SALCAL) > 0.1, o3 = c(HSS_O3) > 1.0e+10;
+  // fine (t = 0, type 11, eductor SALAAL) then coarse (t = 1, type 12, SALCAL)
+  for (int t = 0; t < 2; ++t) {
+    const bool alk = t == 0 ? salaal : salcal;
+    const double educt = c(t == 0 ? HSS_SALAAL : HSS_SALCAL);
+    const double area = in(HETIN_WetAeroArea + 10 + t), radius = in(HETIN_AeroRadi + 10 + t);
+    double k_ex;
+    if (alk && o3) {
+      k_ex = gcrates::Ars_L1k(X, area, radius, 0.11, a.srmw[HSS_SO2]);
+      k_mt[3 * t] = gcrates::kIIR1Ltd(c(HSS_SO2), educt, k_ex) / c(HSS_O3);
+    }
+    if (alk) {
+      k_ex = gcrates::Ars_L1k(X, area, radius, 0.07, a.srmw[HSS_HCl]);
+      k_mt[3 * t + 1] = gcrates::kIIR1Ltd(c(HSS_HCl), educt, k_ex);
+      k_ex = gcrates::Ars_L1k(X, area, radius, 0.5, a.srmw[HSS_HNO3]);
+      k_mt[3 * t + 2] = gcrates::kIIR1Ltd(c(HSS_HNO3), educt, k_ex);
+    }
+  }
+  for (int k = 0; k < 6; ++k) a.met[(long long)(a.row_kmt + k) * a.ldm + cell] = k_mt[k];
+}
+
 }  // namespace
+
+cudaError_t sulfur_aq_rates(const SulfurAqArgs& a, cudaStream_t s) {
+  if (a.ncell <= 0) return cudaSuccess;
+  const int block = 128;
+  sulfur_aq_kernel<<<(a.ncell + block - 1) / block, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
 
 cudaError_t set_state_het(const SetStateArgs& a, cudaStream_t s) {
   if (a.ncell <= 0) return cudaSuccess;

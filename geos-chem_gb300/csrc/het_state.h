@@ -22,4 +22,22 @@ struct SetStateArgs {
 
 cudaError_t set_state_het(const SetStateArgs& a, cudaStream_t s);
 
+// fullchem_SulfurAqChem: K_MT(1:6) from the fine and coarse alkaline sea
+// salt (types 11 and 12 of the aerosol rows of `in`), written to the K_MT
+// rows of the met array, whose TEMP and NUMDEN rows it reads.
+struct SulfurAqArgs {
+  int ncell;
+  const double* in;  // HETIN_NFIELD rows (WetAeroArea, AeroRadi read)
+  long long ldi;
+  const double* c;   // NSPEC rows
+  long long ldc;
+  int ind[HSS_N];    // KPP index of each HSS_* species
+  double srmw[HSS_N];  // SR_MW of each HSS_* species
+  double* met;       // met rows: TEMP, NUMDEN in; K_MT out
+  long long ldm;
+  int row_temp, row_numden, row_kmt;
+};
+
+cudaError_t sulfur_aq_rates(const SulfurAqArgs& a, cudaStream_t s);
+
 }  // namespace gchet

@@ -81,8 +81,10 @@ for _name, _len in HETIN_FIELDS:
     HETIN_OFFSET[_name] = _o
     _o += _len
 NHETIN = _o
-# KPP species that fullchem_SetStateHet reads through C(ind_X)
-SETSTATE_SPECIES = ["SO2", "HNO3", "HCl", "HBr", "BrSALA", "BrSALC", "SALACL", "SALCCL", "NIT", "NITs", "SO4"]
+# KPP species that fullchem_SetStateHet and fullchem_SulfurAqChem read
+# through C(ind_X)
+SETSTATE_SPECIES = ["SO2", "HNO3", "HCl", "HBr", "BrSALA", "BrSALC", "SALACL", "SALCCL", "NIT", "NITs", "SO4",
+                    "SALAAL", "SALCAL", "O3"]
 
 
 def emit_c():
@@ -95,7 +97,8 @@ def emit_c():
               "#define HETIN_NFIELD %d" % NHETIN]
     for name, n in HETIN_FIELDS:
         lines.append("#define HETIN_%s %d%s" % (name, HETIN_OFFSET[name], "  /* %d rows */" % n if n > 1 else ""))
-    lines.append("// KPP species read by fullchem_SetStateHet, in the order of the index table")
+    lines.append("// KPP species read by fullchem_SetStateHet and fullchem_SulfurAqChem, in the order of the "
+                 "index table")
     for k, name in enumerate(SETSTATE_SPECIES):
         lines.append("#define HSS_%s %d" % (name, k))
     lines.append("#define HSS_N %d" % len(SETSTATE_SPECIES))

@@ -267,7 +267,7 @@ def build_program(ir=None):
     hss = [ir["species"].index(n) if n in ir["species"] else -1 for n in SETSTATE_SPECIES]
     return {"code": code, "start": start, "consts": pool, "nhet": nhet, "hs_ind": ind, "hs_mw": pick(spc["mw"]),
             "hs_srmw": pick(srmw), "hs_hk0": pick(spc["henry_k0"]), "hs_hcr": pick(spc["henry_cr"]),
-            "hss_ind": hss}
+            "hss_ind": hss, "hss_srmw": [srmw[i] if i >= 0 else 0.0 for i in hss]}
 
 
 def emit_c(prog):
@@ -282,7 +282,9 @@ def emit_c(prog):
              "static const int law_nargs[%d] = {%s};" % (len(LAWS), ",".join(str(k) for _, k in LAWS)),
              "static const int het_nargs[%d] = {%s};" % (len(HET_LAWS), ",".join(str(k) for _, k in HET_LAWS)),
              "static const int hs_ind[%d] = {%s};" % (len(HET_SPECIES), ",".join(map(str, prog["hs_ind"]))),
-             "static const int hss_ind[%d] = {%s};" % (len(prog["hss_ind"]), ",".join(map(str, prog["hss_ind"])))]
+             "static const int hss_ind[%d] = {%s};" % (len(prog["hss_ind"]), ",".join(map(str, prog["hss_ind"]))),
+             "static const double hss_srmw[%d] = {%s};" % (len(prog["hss_srmw"]),
+                                                          ",".join(float(v).hex() for v in prog["hss_srmw"]))]
     for key in ("hs_mw", "hs_srmw", "hs_hk0", "hs_hcr"):
         lines.append("static const double %s[%d] = {%s};" % (key, len(HET_SPECIES),
                                                             ",".join(float(v).hex() for v in prog[key])))

@@ -30,14 +30,26 @@ def shard_range(ncell, rank, world, work=None):
     return int(bounds[rank]), int(bounds[rank + 1])
 
 
-def gather_cells(local, ncell, world, group=None):
+# expected Rosenbrock steps per chemistry step of a cell in each stiffness
+# bin of the learned proposer (1 | 2-3 | 4-15 | >= 16 steps): the work
+# estimate that balances the shards when no step counts are known yet
+BIN_WORK = (1.0, 2.5, 8.0, 40.0)
+
+
+def work_from_bins(bins, bin_work=BIN_WORK):
+    """Per-cell work estimate from the proposer's stiffness bins."""
+    return np.asarray(bin_work, dtype=np.float64)[np.asarray(bins, dtype=np.int64)]
+
+
+def gather_cells(local, ncell, world, group=None, work=None):
     """All-gather per-rank [K, n_r] arrays (cell-interleaved) into [K, ncell]
-    with torch.distributed (host tensors, e.g. the gloo backend)."""
+    with torch.distributed (host tensors, e.g. the gloo backend); ``work`` is
+    the estimate the ranges were split by (None: even split)."""
     import torch
     import torch.distributed as dist
 
     local = torch.as_tensor(np.ascontiguousarray(local))
-    sizes = [shard_range(ncell, r, world) for r in range(world)]
+    sizes = [shard_range(ncell, r, world, work) for r in range(world)]
     width = max(b - a for a, b in sizes)
     padded = torch.zeros((local.shape[0], width), dtype=local.dtype)
     padded[:, : local.shape[1]] = local

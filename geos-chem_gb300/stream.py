@@ -38,85 +38,132 @@ def plan_chunks(ncell, free_bytes, reserve_bytes=RESERVE, max_chunk=MAX_CHUNK):
     return [(i, min(ncell, i + per)) for i in range(0, ncell, per)]
 
 
-class Streamer:
-    """Double-buffered chunk streaming of chemistry steps (one CUDA device)."""
+def photol_runs(ir=None):
+    """Contiguous runs [(r0, r1), ...] of the PHOTOL rows that the
+    mechanism's Update_RCONST reads (168 of the 200 for fullchem, in 8 runs):
+    the only J-value rows a step needs on the device."""
+    import re
 
-    def __init__(self, solver, ncell, chunk, proposer=None):
+    from . import mechanism
+
+    ir = ir or mechanism.load_ir()
+    rows = sorted({int(k) for e in ir["rconst"] for k in re.findall(r"PHOTOL\[(\d+)\]", e)})
+    runs = []
+    for r in rows:
+        if runs and runs[-1][1] == r:
+            runs[-1][1] = r + 1
+        else:
+            runs.append([r, r + 1])
+    return [tuple(x) for x in runs]
+
+
+class Streamer:
+    """Double-buffered chunk streaming of chemistry steps (one CUDA device).
+
+    With several solver contexts (``solvers``), consecutive chunks run on
+    different contexts and compute streams, so that one chunk's block-per-cell
+    tail overlaps the next chunk's queue kernel; each context keeps its own
+    scratch, so the chunks stay independent.  Host-to-device copies run on one
+    copy stream, device-to-host copies on another.  With ``photol_rows`` (the
+    runs of ``photol_runs``) only the J-value rows the mechanism reads are
+    copied; the device buffer's other rows stay zero."""
+
+    def __init__(self, solver, ncell, chunk, proposer=None, solvers=None, photol_rows=None):
         import torch
 
         self.torch = torch
-        self.solver = solver
+        self.solvers = list(solvers) if solvers else [solver]
+        self.solver = self.solvers[0]
         self.dev = torch.device("cuda", 0)
         self.chunk = chunk
         self.proposer = proposer  # learned.CProposer or None (plain step)
-        self.copy = torch.cuda.Stream(self.dev)
-        self.comp = torch.cuda.Stream(self.dev)
+        self.photol_rows = photol_rows
+        self.h2d = torch.cuda.Stream(self.dev)
+        self.d2h = torch.cuda.Stream(self.dev)
+        self.comp = [torch.cuda.Stream(self.dev) for _ in self.solvers]
+        nbuf = max(2, len(self.solvers))
+        self.nbuf = nbuf
         # flat buffers: a chunk of m cells uses the first rows*m entries as a
         # contiguous [rows, m] array, so host<->device copies are plain copies
         self.rows = {"met": NMET, "ph": NPHOTOL, "c": 356, "hs": 1, "ist": 20, "rst": 20, "ierr": 1}
         dts = {"ist": torch.int32, "ierr": torch.int32}
-        self.buf = [{k: torch.empty(r * chunk, dtype=dts.get(k, torch.float64), device=self.dev)
-                     for k, r in self.rows.items()} for _ in range(2)]
-        self.staged = [torch.cuda.Event() for _ in range(2)]
-        self.solved = [torch.cuda.Event() for _ in range(2)]
-        self.freed = [torch.cuda.Event() for _ in range(2)]
+        self.buf = [{k: torch.zeros(r * chunk, dtype=dts.get(k, torch.float64), device=self.dev)
+                     for k, r in self.rows.items()} for _ in range(nbuf)]
+        self.staged = [torch.cuda.Event() for _ in range(nbuf)]
+        self.solved = [torch.cuda.Event() for _ in range(nbuf)]
+        self.freed = [torch.cuda.Event() for _ in range(nbuf)]
 
     def _view(self, b, key, m):
         r = self.rows[key]
         flat = b[key][: r * m]
         return flat if key in ("hs", "ierr") else flat.view(r, m)
 
+    def bytes_per_cell(self):
+        """(host-to-device, device-to-host) bytes per cell of one step."""
+        nph = NPHOTOL if self.photol_rows is None else sum(b - a for a, b in self.photol_rows)
+        return 8 * (NMET + nph + 356 + 1), 8 * (356 + 1) + 4 + 4
+
     def step(self, chunks, dt, atol, rtol, icntrl, rcntrl):
         """One chemistry step over host chunks: a list of dicts of pinned,
-        contiguous torch CPU tensors met [18, m], ph [200, m], c [356, m]
-        (in/out), hs [m] (in/out, the KPPHvalue chain), steps [m] and ierr
-        [m] (out: ISTATUS(3), IERR), m <= the chunk size.  Returns the number
-        of cells retried (the reference's second Integrate)."""
+        contiguous torch CPU tensors met [18, m], ph [200, m], c [356, m],
+        hs [m] (the KPPHvalue chain), steps [m] and ierr [m] (out: ISTATUS(3),
+        IERR), m <= the chunk size.  Results go to c_out / hs_out when a chunk
+        has them, else back into c / hs.  Returns the number of cells retried
+        (the reference's second Integrate)."""
         torch = self.torch
         retried = [0]
+        nb = self.nbuf
 
         def stage(k):
-            h, b = chunks[k], self.buf[k % 2]
+            h, b = chunks[k], self.buf[k % nb]
             m = h["c"].shape[1]
-            with torch.cuda.stream(self.copy):
-                self.copy.wait_event(self.freed[k % 2])
-                for key in ("met", "ph", "c", "hs"):
+            with torch.cuda.stream(self.h2d):
+                self.h2d.wait_event(self.freed[k % nb])
+                for key in ("met", "c", "hs"):
                     self._view(b, key, m).copy_(h[key], non_blocking=True)
-                self.staged[k % 2].record(self.copy)
+                ph = self._view(b, "ph", m)
+                if self.photol_rows is None:
+                    ph.copy_(h["ph"], non_blocking=True)
+                else:
+                    for r0, r1 in self.photol_rows:
+                        ph[r0:r1].copy_(h["ph"][r0:r1], non_blocking=True)
+                self.staged[k % nb].record(self.h2d)
 
         def retrieve(k):
-            h, b = chunks[k], self.buf[k % 2]
+            h, b = chunks[k], self.buf[k % nb]
             m = h["c"].shape[1]
-            with torch.cuda.stream(self.copy):
-                self.copy.wait_event(self.solved[k % 2])
-                h["c"].copy_(self._view(b, "c", m), non_blocking=True)
-                h["hs"].copy_(self._view(b, "hs", m), non_blocking=True)
+            with torch.cuda.stream(self.d2h):
+                self.d2h.wait_event(self.solved[k % nb])
+                h.get("c_out", h["c"]).copy_(self._view(b, "c", m), non_blocking=True)
+                h.get("hs_out", h["hs"]).copy_(self._view(b, "hs", m), non_blocking=True)
                 h["steps"].copy_(self._view(b, "ist", m)[2], non_blocking=True)
                 h["ierr"].copy_(self._view(b, "ierr", m), non_blocking=True)
-                self.freed[k % 2].record(self.copy)
+                self.freed[k % nb].record(self.d2h)
 
         for e in self.freed:
-            e.record(self.copy)
+            e.record(self.d2h)
         stage(0)
         for k in range(len(chunks)):
             if k + 1 < len(chunks):
                 stage(k + 1)  # overlaps the solve of chunk k
             m = chunks[k]["c"].shape[1]
-            b = self.buf[k % 2]
-            self.comp.wait_event(self.staged[k % 2])
+            b = self.buf[k % nb]
+            solver = self.solvers[k % len(self.solvers)]
+            comp = self.comp[k % len(self.solvers)]
+            comp.wait_event(self.staged[k % nb])
             v = {key: self._view(b, key, m) for key in self.rows}
-            sp = self.comp.cuda_stream
+            sp = comp.cuda_stream
             if self.proposer is not None:
-                nr, _ = self.solver.fullchem_step_learned(self.proposer.handle, dt, v["met"], v["ph"], v["c"], atol,
-                                                          rtol, icntrl, rcntrl, v["hs"], v["ist"], v["rst"],
-                                                          v["ierr"], stream=sp)
+                nr, _ = solver.fullchem_step_learned(self.proposer.handle, dt, v["met"], v["ph"], v["c"], atol,
+                                                     rtol, icntrl, rcntrl, v["hs"], v["ist"], v["rst"], v["ierr"],
+                                                     stream=sp)
             else:
-                nr = self.solver.fullchem_step(dt, v["met"], v["ph"], v["c"], atol, rtol, icntrl, rcntrl, v["hs"],
-                                               v["ist"], v["rst"], v["ierr"], stream=sp)
+                nr = solver.fullchem_step(dt, v["met"], v["ph"], v["c"], atol, rtol, icntrl, rcntrl, v["hs"],
+                                          v["ist"], v["rst"], v["ierr"], stream=sp)
             retried[0] += max(nr, 0)
-            self.solved[k % 2].record(self.comp)
+            self.solved[k % nb].record(comp)
             retrieve(k)  # overlaps the solve of chunk k + 1
-        self.copy.synchronize()
+        self.d2h.synchronize()
         return retried[0]
 
 

@@ -229,6 +229,20 @@ int gc_kpp_set_state_het_batch(gc_kpp_ctx* ctx, int ncell, const double* hetin, 
                                const double* c, long long ldc, double gamma_ho2, int lpscchem,
                                int turn_off_het_rates, double* het, long long ldh, int mem, void* stream);
 
+/* Batched fullchem_SulfurAqChem (KPP/fullchem/fullchem_SulfurChemFuncs.F90:
+ * 120-305, called from Set_Sulfur_Chem_Rates at GeosCore/fullchem_mod.F90:
+ * 861): K_MT(1:6), the uptake of SO2 (by O3), HCl and HNO3 on alkaline fine
+ * and coarse sea salt, from the wet area and radius of aerosol types 11 and
+ * 12 (AeroArea/WetAeroArea/AeroRadi rows of hetin) and C(SALAAL), C(SALCAL),
+ * C(O3), C(SO2), C(HCl), C(HNO3).
+ *
+ *   met  [GC_KPP_NMET][ldm]  in/out  TEMP and NUMDEN read; the six K_MT rows
+ *                                     (GC_KPP_MET_K_MT..+5) written, the
+ *                                     other rows untouched */
+int gc_kpp_sulfur_aq_rates_batch(gc_kpp_ctx* ctx, int ncell, const double* hetin, long long ldi,
+                                 const double* c, long long ldc, double* met, long long ldm, int mem,
+                                 void* stream);
+
 /* HetState of the cells of the following chemistry steps on this context
  * (gc_kpp_fullchem_step and its ordered/binned/learned forms evaluate the
  * heterogeneous rates from it): het [GC_KPP_NHET][ldh] for `ncell` cells, in

@@ -15,6 +15,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+NHET = 168  # rows of the HetState array (the batch interface's field list)
 _libs = {}
 
 
@@ -56,6 +57,7 @@ def load(variant="strict", mech="fullchem"):
     lib.oracle_kpp_decomp.restype = i32
     lib.oracle_max_threads.restype = i32
     lib.oracle_set_state_het_batch.argtypes = [i32, vp, i64, vp, i64, f64, i32, i32, vp, i64]
+    lib.oracle_sulfur_aq_rates_batch.argtypes = [i32, vp, i64, vp, i64, vp, vp, vp, i64]
     _libs[key] = lib
     return lib
 
@@ -132,15 +134,21 @@ def set_state_het(hetin, c, gamma_ho2=0.2, lpscchem=1, turn_off_het_rates=0, mec
     hetin = _c(hetin, np.float64)
     c = _c(c, np.float64)
     n = hetin.shape[1]
-    sys_path = os.path.join(HERE, "..", "geos-chem_gb300")
-    import importlib.util
-
-    spec = importlib.util.spec_from_file_location("_oracle_hetstate", os.path.join(sys_path, "hetstate.py"))
-    hs = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(hs)
-    out = np.zeros((hs.NFIELD, n), np.float64)
+    out = np.zeros((NHET, n), np.float64)
     lib.oracle_set_state_het_batch(n, _p(hetin), n, _p(c), n, float(gamma_ho2), int(lpscchem),
                                    int(turn_off_het_rates), _p(out), n)
+    return out
+
+
+def sulfur_aq_rates(hetin, c, temp, numden, mech="fullchem"):
+    """Batched fullchem_SulfurAqChem: K_MT(1:6) [6, n] from the grid-box
+    fields hetin [NHETIN, n], c [NSPEC, n], TEMP [n] and NUMDEN [n]."""
+    lib = load("strict", mech)
+    hetin, c = _c(hetin, np.float64), _c(c, np.float64)
+    temp, numden = _c(temp, np.float64), _c(numden, np.float64)
+    n = hetin.shape[1]
+    out = np.zeros((6, n), np.float64)
+    lib.oracle_sulfur_aq_rates_batch(n, _p(hetin), n, _p(c), n, _p(temp), _p(numden), _p(out), n)
     return out
 
 

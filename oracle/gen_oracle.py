@@ -304,14 +304,20 @@ def write_het_layout(outdir, mech="fullchem"):
     sys.path.insert(0, os.path.join(HERE, "..", "geos-chem_gb300"))
     import hetstate  # the field lists of the batch interface (data only)
 
+    import math
+
     species = _ir(mech)["species"]
+    with open(os.path.join(HERE, "..", "geos-chem_gb300", "mechanism", mech + "_species.json")) as fh:
+        mw = json.load(fh)["mw"]
     lines = ["/* Generated by oracle/gen_oracle.py from the HetState field list. */", "#pragma once"]
     for name, n in hetstate.FIELDS:
         lines.append("#define OHET_%s %d" % (name, hetstate.OFFSET[name]))
     for name, n in hetstate.HETIN_FIELDS:
         lines.append("#define OHIN_%s %d" % (name, hetstate.HETIN_OFFSET[name]))
     for name in hetstate.SETSTATE_SPECIES:
-        lines.append("#define OSS_%s %d" % (name, species.index(name) if name in species else -1))
+        k = species.index(name) if name in species else -1
+        lines.append("#define OSS_%s %d" % (name, k))
+        lines.append("#define OSS_SRMW_%s %s" % (name, repr(math.sqrt(mw[k])) if k >= 0 else "0.0"))
     text = "\n".join(lines) + "\n"
     path = os.path.join(outdir, "oracle_het_layout.h")
     old = open(path).read() if os.path.exists(path) else None

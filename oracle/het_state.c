@@ -10,6 +10,8 @@
  *   Compute_L2G_Local        :615-650
  *   Cld_Params               KPP/fullchem/rateLawUtilFuncs.F90:281-417
  *   CALC_KH, CALC_HEFF       GeosUtil/henry_mod.F90:74-204
+ *   fullchem_SulfurAqChem    KPP/fullchem/fullchem_SulfurChemFuncs.F90:120-305
+ *   Ars_L1K, kIIR1Ltd        KPP/fullchem/rateLawUtilFuncs.F90:77-160
  *   AVO, PI                  Headers/physconstants.F90:32, 40
  *
  * Input rows OHIN_* and output rows OHET_* come from oracle_het_layout.h
@@ -398,4 +400,85 @@ void oracle_set_state_het_batch(int ncell, const double* in, long long ldi, cons
                                 double gamma_HO2, int LPSCCHEM, int TurnOffHetRates, double* het, long long ldh) {
   for (int cell = 0; cell < ncell; ++cell)
     set_state_het_cell(in + cell, ldi, C + cell, ldc, gamma_HO2, LPSCCHEM, TurnOffHetRates, het + cell, ldh);
+}
+
+/* Ars_L1K at NUMDEN and SR_TEMP */
+static double ss_ars_l1k(double NUMDEN, double SR_TEMP, double area, double radius, double gamma, double srMw) {
+  double dfkg;
+  if (gamma < 1.0e-30 || radius < 1.0e-30) return 0.0;
+  dfkg = (9.45E+17 / NUMDEN) * SR_TEMP * sqrt(3.472E-2 + 1.0 / (srMw * srMw));
+  return area / ((radius / dfkg) + 2.749064E-4 * srMw / (gamma * SR_TEMP));
+}
+
+static int ss_is_safediv(double num, double denom) {
+  int ediff = ss_exponent(num) - ss_exponent(denom);
+  return !(ediff < -1020 || ediff > 1023 || denom == 0.0);
+}
+
+/* kIIR1Ltd */
+static double ss_kiir1ltd(double concGas, double concEduct, double kISource) {
+  const double HET_MIN_LIFE = 1.e-3, HET_MIN_RATE = 1.0 / 1.e-3;
+  double kIGas, kIEduct, kII = 0.0, lifeA, lifeB;
+  if (concEduct < 1.0) return kII;
+  if (!ss_is_safediv(concGas * kISource, concEduct)) return kII;
+  kIGas = kISource;
+  kIEduct = kIGas * concGas / concEduct;
+  kII = kIGas / concEduct;
+  if (kIGas > 0.0) {
+    lifeA = ss_SafeDiv(1.0, kIGas, 0.0);
+    lifeB = ss_SafeDiv(1.0, kIEduct, 0.0);
+    if ((lifeA < lifeB) && (lifeA < HET_MIN_LIFE))
+      kII = ss_SafeDiv(HET_MIN_RATE, concEduct, 0.0);
+    else if (lifeB < HET_MIN_LIFE)
+      kII = ss_SafeDiv(HET_MIN_RATE, concGas, 0.0);
+  }
+  return kII;
+}
+
+/* fullchem_SulfurAqChem for one cell: K_MT(1:6) into kmt[0..5] */
+static void sulfur_aq_cell(const double* in, long long ldi, const double* C, long long ldc, double TEMP,
+                           double NUMDEN, double* kmt) {
+#define IN(f) in[(long long)(f) * ldi]
+  const double SR_TEMP = sqrt(TEMP);
+  double k_ex = 0.0;
+  int SALAAL_gt_0_1, SALCAL_gt_0_1, O3_gt_1e10;
+  for (int k = 0; k < 6; ++k) kmt[k] = 0.0;
+  SALAAL_gt_0_1 = ss_C(C, ldc, OSS_SALAAL) > 0.1;
+  SALCAL_gt_0_1 = ss_C(C, ldc, OSS_SALCAL) > 0.1;
+  O3_gt_1e10 = ss_C(C, ldc, OSS_O3) > 1.0e+10;
+  if (SALAAL_gt_0_1 && O3_gt_1e10) {
+    k_ex = ss_ars_l1k(NUMDEN, SR_TEMP, IN(OHIN_WetAeroArea + 10), IN(OHIN_AeroRadi + 10), 0.11, OSS_SRMW_SO2);
+    kmt[0] = ss_kiir1ltd(ss_C(C, ldc, OSS_SO2), ss_C(C, ldc, OSS_SALAAL), k_ex) / ss_C(C, ldc, OSS_O3);
+  }
+  if (SALAAL_gt_0_1) {
+    k_ex = ss_ars_l1k(NUMDEN, SR_TEMP, IN(OHIN_WetAeroArea + 10), IN(OHIN_AeroRadi + 10), 0.07, OSS_SRMW_HCl);
+    kmt[1] = ss_kiir1ltd(ss_C(C, ldc, OSS_HCl), ss_C(C, ldc, OSS_SALAAL), k_ex);
+  }
+  if (SALAAL_gt_0_1) {
+    k_ex = ss_ars_l1k(NUMDEN, SR_TEMP, IN(OHIN_WetAeroArea + 10), IN(OHIN_AeroRadi + 10), 0.5, OSS_SRMW_HNO3);
+    kmt[2] = ss_kiir1ltd(ss_C(C, ldc, OSS_HNO3), ss_C(C, ldc, OSS_SALAAL), k_ex);
+  }
+  if (SALCAL_gt_0_1 && O3_gt_1e10) {
+    k_ex = ss_ars_l1k(NUMDEN, SR_TEMP, IN(OHIN_WetAeroArea + 11), IN(OHIN_AeroRadi + 11), 0.11, OSS_SRMW_SO2);
+    kmt[3] = ss_kiir1ltd(ss_C(C, ldc, OSS_SO2), ss_C(C, ldc, OSS_SALCAL), k_ex) / ss_C(C, ldc, OSS_O3);
+  }
+  if (SALCAL_gt_0_1) {
+    k_ex = ss_ars_l1k(NUMDEN, SR_TEMP, IN(OHIN_WetAeroArea + 11), IN(OHIN_AeroRadi + 11), 0.07, OSS_SRMW_HCl);
+    kmt[4] = ss_kiir1ltd(ss_C(C, ldc, OSS_HCl), ss_C(C, ldc, OSS_SALCAL), k_ex);
+  }
+  if (SALCAL_gt_0_1) {
+    k_ex = ss_ars_l1k(NUMDEN, SR_TEMP, IN(OHIN_WetAeroArea + 11), IN(OHIN_AeroRadi + 11), 0.5, OSS_SRMW_HNO3);
+    kmt[5] = ss_kiir1ltd(ss_C(C, ldc, OSS_HNO3), ss_C(C, ldc, OSS_SALCAL), k_ex);
+  }
+#undef IN
+}
+
+/* K_MT of every cell: temp/numden [n], kmt out [6][ldk] */
+void oracle_sulfur_aq_rates_batch(int ncell, const double* in, long long ldi, const double* C, long long ldc,
+                                  const double* temp, const double* numden, double* kmt, long long ldk) {
+  for (int cell = 0; cell < ncell; ++cell) {
+    double k[6];
+    sulfur_aq_cell(in + cell, ldi, C + cell, ldc, temp[cell], numden[cell], k);
+    for (int r = 0; r < 6; ++r) kmt[(long long)r * ldk + cell] = k[r];
+  }
 }

@@ -56,7 +56,9 @@ def _same(got, ref, bar=1e-9, strict_seq=True):
     assert np.array_equal(ierr, ierr_ref)
     if strict_seq:
         assert np.array_equal(ist[:8], ist_ref[:8])
-        assert np.array_equal(rst[:3], rst_ref[:3]) or np.allclose(rst[:3], rst_ref[:3], rtol=1e-12, atol=0)
+        # Texit, Hexit, Hnew: the step-size factors come from pow (CUDA's and
+        # glibc's differ in the last bit), so to the concentrations' bar
+        assert np.allclose(rst[:3], rst_ref[:3], rtol=bar, atol=0)
     a, b = c[:NVAR], c_ref[:NVAR]
     assert np.array_equal(np.isnan(a), np.isnan(b))
     fin = np.isfinite(b) & (np.abs(b) > 1e4)

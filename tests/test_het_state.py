@@ -257,3 +257,95 @@ def test_gpu_chemistry_step_from_produced_hetstate(orc):
     big = np.abs(c_ref) > 1e4
     rel = np.abs(cg - c_ref) / np.maximum(np.abs(c_ref), 1e-300)
     assert np.max(np.where(big, rel, 0.0)[:, same]) < 1e-9
+
+
+def _numpy_kmt(ir, hin, c, temp, numden):
+    """fullchem_SulfurAqChem restated in numpy (Ars_L1K, kIIR1Ltd)."""
+    import json
+
+    import gcchem.hetstate as hs
+
+    sp = ir["species"]
+    with open(os.path.join(ROOT, "geos-chem_gb300", "mechanism", "fullchem_species.json")) as fh:
+        mw = json.load(fh)["mw"]
+    srmw = lambda name: np.sqrt(mw[sp.index(name)])
+    C = lambda name: c[sp.index(name)]
+    o = hs.HETIN_OFFSET
+    sr_t = np.sqrt(temp)
+
+    def ars(area, radius, gamma, s):
+        dfkg = (9.45e17 / numden) * sr_t * np.sqrt(3.472e-2 + 1.0 / (s * s))
+        return np.where((gamma < 1e-30) | (radius < 1e-30), 0.0,
+                        area / ((radius / dfkg) + 2.749064e-4 * s / (gamma * sr_t)))
+
+    def kiir(gas, educt, k):
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            kii = np.where(educt < 1.0, 0.0, k / educt)
+            life_a = np.where(k > 0, 1.0 / k, 0.0)
+            k_educt = k * gas / educt
+            life_b = np.where(k_educt != 0, 1.0 / k_educt, 0.0)
+            lim_a = (k > 0) & (life_a < life_b) & (life_a < 1e-3)
+            lim_b = (k > 0) & ~lim_a & (life_b < 1e-3)
+            kii = np.where(lim_a, 1e3 / educt, np.where(lim_b, 1e3 / gas, kii))
+            return np.where(educt < 1.0, 0.0, kii)
+
+    out = np.zeros((6, c.shape[1]))
+    o3 = C("O3") > 1e10
+    for t, (educt, typ) in enumerate((("SALAAL", 11), ("SALCAL", 12))):
+        alk = C(educt) > 0.1
+        area = hin[o["WetAeroArea"] + typ - 1]
+        radius = hin[o["AeroRadi"] + typ - 1]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            k = kiir(C("SO2"), C(educt), ars(area, radius, 0.11, srmw("SO2"))) / C("O3")
+        out[3 * t] = np.where(alk & o3, k, 0.0)
+        out[3 * t + 1] = np.where(alk, kiir(C("HCl"), C(educt), ars(area, radius, 0.07, srmw("HCl"))), 0.0)
+        out[3 * t + 2] = np.where(alk, kiir(C("HNO3"), C(educt), ars(area, radius, 0.5, srmw("HNO3"))), 0.0)
+    return out
+
+
+def _kmt_case(n, seed):
+    ir, cells, hin = _case(n, seed)
+    rng = np.random.default_rng(seed + 7)
+    sp = ir["species"]
+    # alkaline sea salt above and below the 0.1 molec/cm3 switch, O3 around 1e10
+    for name in ("SALAAL", "SALCAL"):
+        cells["c"][sp.index(name)] = np.where(rng.uniform(size=n) < 0.2, 0.05,
+                                              np.exp(rng.uniform(np.log(1.0), np.log(1e9), n)))
+    cells["c"][sp.index("O3")] = np.exp(rng.uniform(np.log(1e9), np.log(1e13), n))
+    return ir, cells, hin
+
+
+def test_oracle_sulfur_aq_matches_numpy_restatement(orc):
+    from gcchem.rates_program import MET_FIELDS
+
+    n = 2048
+    ir, cells, hin = _kmt_case(n, 17)
+    temp = cells["met"][MET_FIELDS.index("TEMP")]
+    numden = cells["met"][MET_FIELDS.index("NUMDEN")]
+    k = orc.sulfur_aq_rates(hin, cells["c"], temp, numden)
+    ref = _numpy_kmt(ir, hin, cells["c"], temp, numden)
+    np.testing.assert_allclose(k, ref, rtol=1e-12, atol=0)
+    for r in range(6):
+        assert (k[r] == 0).any() and (k[r] > 0).any(), r
+
+
+@pytest.mark.gpu
+def test_gpu_sulfur_aq_matches_oracle(orc):
+    import gcchem.capi as capi
+    from gcchem.rates_program import MET_FIELDS
+
+    n = 4096
+    ir, cells, hin = _kmt_case(n, 18)
+    met = cells["met"].copy()
+    met[MET_FIELDS.index("K_MT0"):MET_FIELDS.index("K_MT0") + 6] = -1.0
+    s = capi.Solver(0)
+    s.sulfur_aq_rates(hin, cells["c"], met)
+    s.close()
+    ref = orc.sulfur_aq_rates(hin, cells["c"], met[MET_FIELDS.index("TEMP")], met[MET_FIELDS.index("NUMDEN")])
+    k = met[MET_FIELDS.index("K_MT0"):MET_FIELDS.index("K_MT0") + 6]
+    assert np.array_equal(k == 0, ref == 0)
+    rel = np.abs(k - ref) / np.maximum(np.abs(ref), 1e-300)
+    assert rel.max() < 1e-14, rel.max()
+    # the other met rows are untouched
+    others = [i for i, f in enumerate(MET_FIELDS) if not f.startswith("K_MT")]
+    assert np.array_equal(met[others], cells["met"][others])

@@ -1,5 +1,7 @@
 """Multi-rank path on the CPU: two gloo ranks integrate disjoint cell ranges
-(oracle), gather, and reproduce the single-process result exactly."""
+of one grid (the oracle stands in for the GPU solver), gather, and reproduce
+the single-process result exactly -- with an even split and with the split
+bench.py uses on N GPUs, balanced by per-cell work from stiffness bins."""
 import os
 import socket
 import sys
@@ -36,7 +38,12 @@ def _free_port():
     return p
 
 
-def _worker(rank, world, port, out_path):
+def _bins(n):
+    # stiffness bins as the proposer would give them (seeded stand-in)
+    return np.random.default_rng(3).integers(0, 4, n)
+
+
+def _worker(rank, world, port, out_path, weighted=False):
     sys.path.insert(0, ROOT)
     import torch.distributed as dist
 
@@ -44,7 +51,7 @@ def _worker(rank, world, port, out_path):
 
     __graft_entry__.load_package()
     import gcchem.inputs as inputs
-    from gcchem.shard import gather_cells, shard_range
+    from gcchem.shard import gather_cells, shard_range, work_from_bins
 
     orc = __graft_entry__.load_oracle()
     dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
@@ -52,24 +59,26 @@ def _worker(rank, world, port, out_path):
     cells = inputs.box_cells(n, seed=9)
     atol, rtol = inputs.tolerances()
     icntrl, rcntrl = inputs.default_controls()
-    a, b = shard_range(n, rank, world)
+    work = work_from_bins(_bins(n)) if weighted else None
+    a, b = shard_range(n, rank, world, work)
     r = orc.update_rconst(cells["met"][:, a:b], cells["photol"][:, a:b], cells["c"][:, a:b])
     c, ist, _, ierr = orc.integrate(cells["c"][:, a:b], r, atol, rtol, 0.0, 120.0, icntrl, rcntrl, nthreads=1)
-    full = gather_cells(c, n, world)
-    steps = gather_cells(ist[2:3].astype(np.float64), n, world)
+    full = gather_cells(c, n, world, work=work)
+    steps = gather_cells(ist[2:3].astype(np.float64), n, world, work=work)
     if rank == 0:
         np.savez(out_path, c=full, steps=steps)
     dist.destroy_process_group()
 
 
-def test_two_gloo_ranks_match_single_process(tmp_path, orc):
+@pytest.mark.parametrize("weighted", [False, True])
+def test_two_gloo_ranks_match_single_process(tmp_path, orc, weighted):
     sys.path.insert(0, ROOT)
     import gcchem.inputs as inputs
 
     out = str(tmp_path / "gathered.npz")
     ctx = mp.get_context("spawn")
     port = _free_port()
-    procs = [ctx.Process(target=_worker, args=(r, 2, port, out)) for r in range(2)]
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, out, weighted)) for r in range(2)]
     for p in procs:
         p.start()
     for p in procs:
