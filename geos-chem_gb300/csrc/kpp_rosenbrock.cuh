@@ -280,7 +280,10 @@ struct Rosenbrock {
           const double yi = yw[i * TSN];
           if (k <= 1.0e-30 || yi <= 1.0e-30) continue;
           const double term = pr[i * TSN] / k;
-          yw[i * TSN] = term + (yi - term) * exp(-k * dt);
+          // each operation rounded on its own, as the reference: when
+          // P/k >> y the sum cancels, and a fused multiply-add would round
+          // the cancelling terms differently from the reference
+          yw[i * TSN] = __dadd_rn(term, __dmul_rn(__dadd_rn(yi, -term), exp(__dmul_rn(-k, dt))));
         }
       }
     }

@@ -43,9 +43,10 @@ def test_ir_dimensions(ir):
 
 
 def test_ir_matches_reference_sources():
-    ref = "/root/reference"
-    if not os.path.isdir(os.path.join(ref, "KPP", "fullchem")):
-        pytest.skip("GEOS-Chem source tree not present")
+    # the GEOS-Chem source tree, where one is checked out (GEOSCHEM_SRC)
+    ref = os.environ.get("GEOSCHEM_SRC", "")
+    if not ref or not os.path.isdir(os.path.join(ref, "KPP", "fullchem")):
+        pytest.skip("GEOS-Chem source tree not present (set GEOSCHEM_SRC)")
     import importlib.util
 
     path = os.path.join(ROOT, "geos-chem_gb300", "mechanism", "extract_kpp.py")
