@@ -36,10 +36,12 @@ METRIC = "fullchem cells/s per 1200 s step, learned-binned vs plain GPU, at RTOL
 GRID = (72, 46, 72)
 DT = 1200.0
 SPINUP_S = 86400.0
-# hand-over point of the learned arms, best of a sweep over k = 1-4 on this
-# grid: from a cold start k = 2 (762k cells/s; k = 1 468k, k = 3 747k), on the
-# KPPHvalue chain k = 1 (1.15M cells/s; k = 2 964k, k = 3 855k)
-EVICT_LEARNED = 2
+# hand-over point of the learned arms.  From a cold start the proposals are
+# capped at learned.H0_CAP (16.8 s, a step of the plain method's ramp from
+# DeltaMin), so a cell needs about 4 Rosenbrock steps; the best k of a sweep
+# with that cap on this grid was 4 (k = 5, 6 slower).  On the KPPHvalue chain
+# k = 1 (1.15M cells/s; k = 2 964k, k = 3 855k).
+EVICT_LEARNED = 4
 EVICT_LEARNED_CHAINED = 1
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "geos-chem_gb300", "weights", "proposer_fullchem.npz")
 
@@ -58,7 +60,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample duration")
     ap.add_argument("--weights", default=WEIGHTS, help="trained proposer weights (.npz)")
     ap.add_argument("--error-cells", type=int, default=2048, help="cells integrated at RTOL 1e-8 for the error")
-    ap.add_argument("--e2e-chunks", type=int, default=4,
+    ap.add_argument("--e2e-chunks", type=int, default=1,
                     help="chunks of the end-to-end step (host copies overlap the solves of other chunks)")
     return ap.parse_args()
 
@@ -414,17 +416,19 @@ def run_ours(args):
         ref = c_ref[:nvar]
         mask = ref > 1e4
         e = ((got - ref).abs() / ref.clamp_min(1e-300))[mask]
-        return {"max": float(e.max().item()), "median": float(e.median().item())}
+        q = torch.quantile(e.float(), torch.tensor([0.5, 0.99, 0.999], device=e.device)).tolist()
+        return {"max": float(e.max().item()), "p99.9": q[2], "p99": q[1], "median": float(e.median().item())}
 
     errors = {name: rel_err(res[name]["c"]) for name in arms}
 
     # end to end through the public API: the grid's inputs in pinned host
     # memory, the learned chemistry step (gc_kpp_fullchem_step_learned)
-    # streamed in chunks by gcchem.stream.Streamer -- while one chunk solves,
-    # the next chunk's inputs (met, the J-value rows the mechanism reads, C,
-    # KPPHvalue) are copied in and the previous chunk's results (C,
-    # KPPHvalue, ISTATUS(3), IERR) copied out; two solver contexts alternate,
-    # so a chunk's block-per-cell tail overlaps the next chunk's queue kernel
+    # through gcchem.stream.Streamer: met, the J-value rows the mechanism
+    # reads, C and KPPHvalue copied in, C, KPPHvalue, ISTATUS(3) and IERR
+    # copied out.  One chunk by default: the copies take ~10 ms at the
+    # measured ~200 GB/s, while cutting the learned step into chunks repeats
+    # its stiff-cell tail per chunk (2 and 4 chunks on two alternating solver
+    # contexts measured 8 % and 35 % slower than one).
     e2e = None
     if rank == 0 or world > 1:
         import gcchem.stream as stream
@@ -442,8 +446,9 @@ def run_ours(args):
                       ierr=torch.zeros(i1 - i0, dtype=torch.int32).pin_memory())
             chunks.append(ch)
         cp = learned.CProposer(prop, local)
-        second = capi.Solver(local, arith="fast", schedule=args.schedule)
-        solvers = [solver, second]
+        solvers = [solver]
+        if len(chunks) > 1:
+            solvers.append(capi.Solver(local, arith="fast", schedule=args.schedule))
         for sv in solvers:
             sv.set(evict_after=EVICT_LEARNED)
         st = stream.Streamer(solver, ncell, chunk, proposer=cp, solvers=solvers, photol_rows=stream.photol_runs())
@@ -471,8 +476,9 @@ def run_ours(args):
                "d2h_bytes_per_step": int(d2h * ncell_total), "chunks": len(chunks),
                "steps_match_learned_arm": bool(np.array_equal(steps_e2e, head["ist"][2])),
                "path": "gcchem.stream.Streamer over gc_kpp_fullchem_step_learned, pinned host buffers, "
-                       "%d chunks on 2 solver contexts" % len(chunks)}
-        second.close()
+                       "%d chunk(s) on %d solver context(s)" % (len(chunks), len(solvers))}
+        for sv in solvers[1:]:
+            sv.close()
         cp.close()
 
     cpu = None
@@ -507,9 +513,10 @@ def run_ours(args):
                        "cells_per_gpu": ncell, "dt_s": DT,
                        "shard": [int(shard[0]), int(shard[1])] if world > 1 else None,
                        "solver": "%s schedule, fast arithmetic, 1 cell per thread" % args.schedule,
-                       "value_is": "learned-binned arm: MLP H0 proposals seed Hstart, stiffness bins order "
-                                   "the persistent queue and send the top bin block-per-cell, cells still "
-                                   "running after 2 steps finish block-per-cell",
+                       "value_is": "learned-binned arm: MLP H0 proposals (at most %.3g s) seed Hstart, "
+                                   "stiffness bins order the persistent queue and send the top bin "
+                                   "block-per-cell, cells still running after %d steps finish block-per-cell"
+                                   % (prop.h0_cap, EVICT_LEARNED),
                        "l2": "inputs larger than L2 (C 0.68 GB, RCONST 2.0 GB per step)",
                        "weights": os.path.basename(args.weights),
                        "spinup_s": args.spinup, "spinup_wall_s": spin_s, "spinup_steps_per_cell": spin_steps,

@@ -58,6 +58,7 @@ EXPORTED = [
     "gc_kpp_fullchem_step_learned",
     "gc_kpp_proposer_create",
     "gc_kpp_proposer_destroy",
+    "gc_kpp_proposer_set_h0_cap",
     "gc_kpp_integrate_batch_noalloc",
     "gc_kpp_last_launch_count",
     "gc_kpp_last_kernel_ms",

@@ -214,6 +214,11 @@ int gc_kpp_ctx_create(gc_kpp_ctx** out, int device) {
              &m.prod_packed, c->owned);
   if (e != cudaSuccess) { gc_kpp_ctx_destroy(c); return cuda_fail(e, "upload prod_packed"); }
   m.naux = T::NAUX;
+  UP(prod_ids_a, prod_ids_a) UP(prod_ids_b, prod_ids_b)
+  for (int i = 0; i < 9; ++i) {
+    m.a_cls[i] = T::a_cls_start[i];
+    m.b_cls[i] = T::b_cls_start[i];
+  }
   UP(pre_lit, pre_literals) UP(p_start, p_start) UP(p_sterm, p_sterm) UP(slit, slit)
   UP(d_start, d_start) UP(d_sterm, d_sterm) UP(j_start, j_start) UP(j_sterm, j_sterm)
   UP(lu_crow, lu_crow) UP(lu_diag, lu_diag) UP(lu_icol, lu_icol) UP(lrow_start, lrow_start)
@@ -1285,6 +1290,8 @@ static __device__ __align__(256) double g_noalloc_ws[(size_t)NOALLOC_MAX_CELLS *
 
 #define GC_NA_TABLE(type, name) static __device__ type g_na_##name[sizeof(T::name) / sizeof(T::name[0])];
 GC_NA_TABLE(unsigned, prod_packed)
+GC_NA_TABLE(int, prod_ids_a)
+GC_NA_TABLE(int, prod_ids_b)
 GC_NA_TABLE(double, pre_literals)
 GC_NA_TABLE(int, p_start)
 GC_NA_TABLE(unsigned, p_sterm)
@@ -1331,6 +1338,12 @@ int noalloc_setup(int dev, NoAllocDevice** out) {
     GC_CUDA(cudaGetSymbolAddress(&p, g_na_##name));                                          \
     m.field = reinterpret_cast<type>(p);
     GC_NA_FILL(prod_packed, prod_packed, const uint2*)
+    GC_NA_FILL(prod_ids_a, prod_ids_a, const int*)
+    GC_NA_FILL(prod_ids_b, prod_ids_b, const int*)
+    for (int i = 0; i < 9; ++i) {
+      m.a_cls[i] = T::a_cls_start[i];
+      m.b_cls[i] = T::b_cls_start[i];
+    }
     GC_NA_FILL(pre_lit, pre_literals, const double*)
     GC_NA_FILL(p_start, p_start, const int*)
     GC_NA_FILL(p_sterm, p_sterm, const unsigned*)

@@ -18,6 +18,7 @@ using namespace gcmlp;
 struct gc_kpp_proposer {
   int device = 0;
   double scale = 1.0;
+  double h0_cap = 0.0;  // largest proposed H0 [s]; 0 = the step length
   __nv_bfloat16 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr;
   float *b1 = nullptr, *b2 = nullptr, *b3 = nullptr;
   double *mean = nullptr, *inv_std = nullptr;
@@ -140,6 +141,13 @@ int gc_kpp_proposer_create(int device, const float* w1, const float* b1, const f
   return GC_KPP_OK;
 }
 
+int gc_kpp_proposer_set_h0_cap(gc_kpp_proposer* q, double cap) {
+  if (!q) return gckpp_set_error(GC_KPP_EINVAL, "proposer is NULL");
+  if (!(cap >= 0.0)) return gckpp_set_error(GC_KPP_EINVAL, "H0 cap must be >= 0");
+  q->h0_cap = cap;
+  return GC_KPP_OK;
+}
+
 int gc_kpp_proposer_destroy(gc_kpp_proposer* q) {
   if (!q) return GC_KPP_OK;
   cudaSetDevice(q->device);
@@ -198,7 +206,8 @@ int gc_kpp_fullchem_step_learned(gc_kpp_ctx* ctx, gc_kpp_proposer* q, int ncell,
   GC_L_CUDA(gemm_fwd(q->x, q->w1, q->b1, nullptr, q->h1, ncell, NFEAT, HID, 1, s));
   GC_L_CUDA(gemm_fwd(q->h1, q->w2, q->b2, nullptr, q->h2, ncell, HID, HID, 1, s));
   GC_L_CUDA(gemm_fwd(q->h2, q->w3, q->b3, nullptr, q->out, ncell, HID, NOUT, 0, s));
-  GC_L_CUDA(propose(q->out, ncell, q->scale, 1.0e-5, dt, dhs, q->bins, 1, s));
+  const double hmax = (q->h0_cap > 0.0 && q->h0_cap < dt) ? q->h0_cap : dt;
+  GC_L_CUDA(propose(q->out, ncell, q->scale, 1.0e-5, hmax, dhs, q->bins, 1, s));
   GC_L_CUDA(bin_order(q->bins, ncell, q->counts, q->scratch, q->order, s));
   if (gckpp_ctx_async(ctx)) {
     // the top bin's size stays on the device (no host synchronisation)

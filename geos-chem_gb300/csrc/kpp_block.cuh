@@ -55,19 +55,6 @@ __host__ __device__ inline BlockLayout block_layout(int naux, int nspec, int nva
   return l;
 }
 
-// pre [* 2] * s1 * s2 * s3 in the Fortran's left-to-right order (the
-// operations of product<1> in kpp_mech.cuh).
-__device__ __forceinline__ double bk_product(const MechDev& m, int p, const double* Y, const double* aux) {
-  const uint2 t = __ldg(m.prod_packed + p);
-  const unsigned ns = (t.x >> 13) & 3u;
-  double r = aux[t.x & 0xfffu];
-  if (t.x & 0x1000u) r = r * 2.0;
-  if (ns >= 1u) r = r * Y[t.x >> 16];
-  if (ns >= 2u) r = r * Y[t.y & 0xffffu];
-  if (ns >= 3u) r = r * Y[t.y >> 16];
-  return r;
-}
-
 // Sum of signed terms slit[c] * X[idx] (the operations of term_sum<.,.,1>).
 template <bool STRICT, bool FLIP>
 __device__ __forceinline__ double bk_term_sum(const MechDev& m, const unsigned* __restrict__ terms, int s, int e,
@@ -88,9 +75,40 @@ __device__ __forceinline__ double bk_term_sum(const MechDev& m, const unsigned* 
   return acc;
 }
 
+// The products of one class (NS species factors, TIMES2) at list positions
+// [s, e), spread over the block's threads: out[id] = pre [* 2] * s1 * s2 *
+// s3 in the Fortran's left-to-right order (the operations of product_class
+// in kpp_mech.cuh) for id = ids[i], product index base + id.
+template <int NS, bool TIMES2>
+__device__ __forceinline__ void bk_product_class(const MechDev& m, const int* ids, int s, int e, int base,
+                                                 const double* Y, const double* aux, double* out) {
+  for (int i = s + threadIdx.x; i < e; i += blockDim.x) {
+    const int id = __ldg(ids + i);
+    const uint2 t = __ldg(m.prod_packed + base + id);
+    double r = aux[t.x & 0xfffu];
+    if (TIMES2) r = r * 2.0;
+    if (NS >= 1) r = r * Y[t.x >> 16];
+    if (NS >= 2) r = r * Y[t.y & 0xffffu];
+    if (NS >= 3) r = r * Y[t.y >> 16];
+    out[id] = r;
+  }
+}
+
+__device__ __forceinline__ void bk_products_by_class(const MechDev& m, const int* ids, const int* cls, int base,
+                                                     const double* Y, const double* aux, double* out) {
+  bk_product_class<0, false>(m, ids, cls[0], cls[1], base, Y, aux, out);
+  bk_product_class<0, true>(m, ids, cls[1], cls[2], base, Y, aux, out);
+  bk_product_class<1, false>(m, ids, cls[2], cls[3], base, Y, aux, out);
+  bk_product_class<1, true>(m, ids, cls[3], cls[4], base, Y, aux, out);
+  bk_product_class<2, false>(m, ids, cls[4], cls[5], base, Y, aux, out);
+  bk_product_class<2, true>(m, ids, cls[5], cls[6], base, Y, aux, out);
+  bk_product_class<3, false>(m, ids, cls[6], cls[7], base, Y, aux, out);
+  bk_product_class<3, true>(m, ids, cls[7], cls[8], base, Y, aux, out);
+}
+
 // B products at Y (Jac_SP partials, also Fun's D_VAR products).
 __device__ __forceinline__ void bk_b_products(const MechDev& m, const double* Y, const double* aux, double* B) {
-  for (int b = threadIdx.x; b < m.nb; b += blockDim.x) B[b] = bk_product(m, m.nreact + b, Y, aux);
+  bk_products_by_class(m, m.prod_ids_b, m.b_cls, m.nreact, Y, aux, B);
 }
 
 // Fun_SPLIT at V; B must hold the B products at V and be visible to the
@@ -98,7 +116,7 @@ __device__ __forceinline__ void bk_b_products(const MechDev& m, const double* Y,
 template <bool STRICT>
 __device__ void bk_fun(const MechDev& m, const double* V, const double* aux, double* A, const double* B,
                        double* Vdot) {
-  for (int r = threadIdx.x; r < m.nreact; r += blockDim.x) A[r] = bk_product(m, r, V, aux);
+  bk_products_by_class(m, m.prod_ids_a, m.a_cls, 0, V, aux, A);
   __syncthreads();
   for (int n = threadIdx.x; n < m.nvar; n += blockDim.x) {
     const int i = __ldg(m.fun_rows_by_len + n);
@@ -370,7 +388,7 @@ __device__ __forceinline__ void split_run(const MechDev& m, int ph, const PH& f)
 // scratch vector of NVAR.  Ends with a barrier.
 __device__ inline void bk_fun_split(const MechDev& m, const double* V, const double* aux, double* A, const double* B,
                              double* Vdot, double* D) {
-  for (int r = threadIdx.x; r < m.nreact; r += blockDim.x) A[r] = bk_product(m, r, V, aux);
+  bk_products_by_class(m, m.prod_ids_a, m.a_cls, 0, V, aux, A);
   __syncthreads();
   split_run(m, SP_FUN, SplitFun{m, A, B, Vdot, D});
   if (m.sp_nt[SP_FUN] < (int)blockDim.x) __syncthreads();
@@ -521,9 +539,10 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
             for (int i = tid; i < nvar; i += nt) {
               double y = Y[i];
               for (int j = 0; j < s; ++j) {
-                const double a = r.A[(s * (s - 1)) / 2 + j];
+                const int ia = (s * (s - 1)) / 2 + j;
+                if (!((r.nzA >> ia) & 1u)) continue;  // WAXPY's alpha = 0 skip
                 const double kj = K[j * nvar + i];
-                if (a != 0.0) y = STRICT ? y + a * kj : fma(a, kj, y);
+                y = STRICT ? y + r.A[ia] * kj : fma(r.A[ia], kj, y);
               }
               Ynew[i] = y;
             }
@@ -538,15 +557,20 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
             fcn = F;
           }
           double hc[SMAX];
-          for (int j = 0; j < s; ++j) hc[j] = r.C[(s * (s - 1)) / 2 + j] / (dir * sh.L.H);
+          unsigned hbits = 0u;  // bit j: hc(j) != 0 (WAXPY's alpha = 0 skip)
+          for (int j = 0; j < s; ++j) {
+            hc[j] = r.C[(s * (s - 1)) / 2 + j] / (dir * sh.L.H);
+            if (hc[j] != 0.0) hbits |= 1u << j;
+          }
           const double hg = dir * sh.L.H * r.Gamma[s];
           const bool use_dfdt = (!p.autonomous) && (r.Gamma[s] != 0.0);
           double* Ks = K + s * nvar;
           for (int i = tid; i < nvar; i += nt) {
             double k = fcn[i];
             for (int j = 0; j < s; ++j) {
+              if (!((hbits >> j) & 1u)) continue;
               const double kj = K[j * nvar + i];
-              if (hc[j] != 0.0) k = STRICT ? k + hc[j] * kj : fma(hc[j], kj, k);
+              k = STRICT ? k + hc[j] * kj : fma(hc[j], kj, k);
             }
             if (use_dfdt && hg != 0.0) {
               const double dd = dfdt[i];
@@ -570,8 +594,8 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
           double yerr = 0.0;
           for (int j = 0; j < r.S; ++j) {
             const double kj = K[j * nvar + i];
-            if (r.M[j] != 0.0) y = STRICT ? y + r.M[j] * kj : fma(r.M[j], kj, y);
-            if (r.E[j] != 0.0) yerr = STRICT ? yerr + r.E[j] * kj : fma(r.E[j], kj, yerr);
+            if ((r.nzM >> j) & 1u) y = STRICT ? y + r.M[j] * kj : fma(r.M[j], kj, y);
+            if ((r.nzE >> j) & 1u) yerr = STRICT ? yerr + r.E[j] * kj : fma(r.E[j], kj, yerr);
           }
           Ynew[i] = y;
           const double ymax = fmax(fabs(y0), fabs(y));

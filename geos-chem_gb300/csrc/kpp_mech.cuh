@@ -31,6 +31,11 @@ struct MechDev {
   const uint2* prod_packed;  // pre | times2<<12 | nspecies<<13 | s1<<16, s2 | s3<<16
   const double* pre_lit;     // constant-rate literals, appended to RCT in aux
   int naux;
+  // the A products (reaction r) and B products (b) listed by class
+  // c = 2 * nspecies + times2; class c is [x_cls[c], x_cls[c + 1]) of the list
+  const int* prod_ids_a;
+  const int* prod_ids_b;
+  int a_cls[9], b_cls[9];
   const int* p_start;
   const unsigned* p_sterm;
   const int* d_start;
@@ -89,33 +94,55 @@ __device__ __forceinline__ bool tiny_abs(double x) {
          0x0010000000000000ULL;
 }
 
-// One product of the mechanism, pre [* 2] * s1 * s2 * s3, in the Fortran's
-// left-to-right order, for the thread's NC cells.  aux holds RCT (and the
-// constant-rate literals), Y the species [V | F].  All loads are issued
-// before the multiplications.
-template <int NC>
-__device__ __forceinline__ void product(const MechDev& m, int p, const double* Y, const double* aux, double* out) {
+// The products of one class (NS species factors, TIMES2) at list positions
+// [s, e): out[id] = pre [* 2] * s1 * s2 * s3, in the Fortran's left-to-right
+// order, for id = ids[i], product index base + id.  aux holds RCT (and the
+// constant-rate literals), Y the species [V | F].  The factor count is fixed
+// at compile time, so a warp executes only the multiplications the products
+// have, and all loads are issued before the multiplications.
+template <int NS, bool TIMES2, int NC>
+__device__ __forceinline__ void product_class(const MechDev& m, const int* __restrict__ ids, int s, int e, int base,
+                                              const double* Y, const double* aux, double* out) {
   constexpr int TSN = TS * NC;
-  const uint2 t = __ldg(m.prod_packed + p);
-  const unsigned ns = (t.x >> 13) & 3u;
-  const int ia = (t.x & 0xfffu) * TSN, i1 = (t.x >> 16) * TSN, i2 = (t.y & 0xffffu) * TSN, i3 = (t.y >> 16) * TSN;
-  double a[NC], v1[NC], v2[NC], v3[NC];
+#pragma unroll 2
+  for (int i = s; i < e; ++i) {
+    const int id = ldi(ids + i);
+    const uint2 t = __ldg(m.prod_packed + base + id);
+    const int ia = (t.x & 0xfffu) * TSN, i1 = (t.x >> 16) * TSN, i2 = (t.y & 0xffffu) * TSN,
+              i3 = (t.y >> 16) * TSN;
+    double a[NC], v1[NC], v2[NC], v3[NC];
 #pragma unroll
-  for (int q = 0; q < NC; ++q) {
-    a[q] = ldw(aux + ia + q * TS);
-    v1[q] = ldw(Y + i1 + q * TS);
-    v2[q] = ldw(Y + i2 + q * TS);
-    v3[q] = ldw(Y + i3 + q * TS);
-  }
+    for (int q = 0; q < NC; ++q) {
+      a[q] = ldw(aux + ia + q * TS);
+      if (NS >= 1) v1[q] = ldw(Y + i1 + q * TS);
+      if (NS >= 2) v2[q] = ldw(Y + i2 + q * TS);
+      if (NS >= 3) v3[q] = ldw(Y + i3 + q * TS);
+    }
 #pragma unroll
-  for (int q = 0; q < NC; ++q) {
-    double r = a[q];
-    if (t.x & 0x1000u) r = r * 2.0;
-    if (ns >= 1u) r = r * v1[q];
-    if (ns >= 2u) r = r * v2[q];
-    if (ns >= 3u) r = r * v3[q];
-    out[q] = r;
+    for (int q = 0; q < NC; ++q) {
+      double r = a[q];
+      if (TIMES2) r = r * 2.0;
+      if (NS >= 1) r = r * v1[q];
+      if (NS >= 2) r = r * v2[q];
+      if (NS >= 3) r = r * v3[q];
+      out[id * TSN + q * TS] = r;
+    }
   }
+}
+
+// Every product of a list (A: base 0, ids prod_ids_a, cls a_cls; B: base
+// nreact, ids prod_ids_b, cls b_cls), class by class.
+template <int NC>
+__device__ __forceinline__ void products_by_class(const MechDev& m, const int* ids, const int* cls, int base,
+                                                  const double* Y, const double* aux, double* out) {
+  product_class<0, false, NC>(m, ids, cls[0], cls[1], base, Y, aux, out);
+  product_class<0, true, NC>(m, ids, cls[1], cls[2], base, Y, aux, out);
+  product_class<1, false, NC>(m, ids, cls[2], cls[3], base, Y, aux, out);
+  product_class<1, true, NC>(m, ids, cls[3], cls[4], base, Y, aux, out);
+  product_class<2, false, NC>(m, ids, cls[4], cls[5], base, Y, aux, out);
+  product_class<2, true, NC>(m, ids, cls[5], cls[6], base, Y, aux, out);
+  product_class<3, false, NC>(m, ids, cls[6], cls[7], base, Y, aux, out);
+  product_class<3, true, NC>(m, ids, cls[7], cls[8], base, Y, aux, out);
 }
 
 // Sum of signed terms  slit[c] * X[idx]  (sterm = c << 20 | idx) in the
@@ -176,14 +203,7 @@ __device__ __forceinline__ void term_sum_exact(const MechDev& m, const unsigned*
 template <int NC>
 __device__ __forceinline__ void b_products(const MechDev& m, const double* __restrict__ Y,
                                            const double* __restrict__ aux, double* __restrict__ B) {
-  constexpr int TSN = TS * NC;
-#pragma unroll 2
-  for (int b = 0; b < m.nb; ++b) {
-    double v[NC];
-    product<NC>(m, m.nreact + b, Y, aux, v);
-#pragma unroll
-    for (int q = 0; q < NC; ++q) B[b * TSN + q * TS] = v[q];
-  }
+  products_by_class<NC>(m, m.prod_ids_b, m.b_cls, m.nreact, Y, aux, B);
 }
 
 // Fun_SPLIT: Vdot = P_VAR - D_VAR*V at point Y = [V | F] (aux = RCT).
@@ -197,13 +217,7 @@ __device__ void fun_split(const MechDev& m, const double* __restrict__ V, const 
                           double* __restrict__ A, const double* __restrict__ B, double* __restrict__ Vdot,
                           double* __restrict__ P = nullptr, double* __restrict__ D = nullptr) {
   constexpr int TSN = TS * NC;
-#pragma unroll 2
-  for (int r = 0; r < m.nreact; ++r) {
-    double v[NC];
-    product<NC>(m, r, V, aux, v);
-#pragma unroll
-    for (int q = 0; q < NC; ++q) A[r * TSN + q * TS] = v[q];
-  }
+  products_by_class<NC>(m, m.prod_ids_a, m.a_cls, 0, V, aux, A);
   for (int i = 0; i < m.nvar; ++i) {
     double p[NC], d[NC];
     term_sum<STRICT, false, NC>(m, m.p_sterm, ldi(m.p_start + i), ldi(m.p_start + i + 1), A, p);
@@ -313,11 +327,37 @@ __device__ void decomp(const MechDev& m, const double* __restrict__ J0, const do
   }
 }
 
+// acc -= sum of L(k,j)*U(j,c) over the dot-product terms of LU entry e, in
+// the table's order.
+template <bool STRICT, int NC>
+__device__ __forceinline__ void dot_terms(const MechDev& m, const double* __restrict__ G, int e, double* acc) {
+  constexpr int TSN = TS * NC;
+  const int t0 = ldi(m.dot_start + e), t1 = ldi(m.dot_start + e + 1);
+#pragma unroll 4
+  for (int t = t0; t < t1; ++t) {
+    const unsigned op = ldu(m.dot_term + t);
+    const double* lp = G + (op >> 16) * TSN;
+    const double* up = G + (op & 0xffffu) * TSN;
+    double l[NC], u[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      l[q] = ldw(lp + q * TS);
+      u[q] = ldw(up + q * TS);
+    }
+#pragma unroll
+    for (int q = 0; q < NC; ++q) acc[q] = STRICT ? acc[q] - l[q] * u[q] : fma(-l[q], u[q], acc[q]);
+  }
+}
+
 // The same factorization, with every entry (k,c) of row k computed as one
 // accumulation in a register:  W(c) = Ghimj(k,c) - sum_j L(k,j)*U(j,c) over
 // the L entries j < c of row k in ascending order -- the updates KppDecomp
 // applies to W(c), in the same order, so STRICT stays bit-for-bit.  Each
-// entry is loaded from Jac0 and stored once, and Ghimj is never stored.
+// entry is loaded from Jac0 and stored once, and Ghimj is never stored.  A
+// row runs as three loops -- its L entries (divided by, or in the fast form
+// multiplied by the reciprocal of, their pivot), its diagonal (+ 1/(H gamma);
+// the fast form stores the reciprocal) and its U entries -- so that no entry
+// executes another part's arithmetic under a predicate.
 template <bool STRICT, int NC>
 __device__ void decomp_rows(const MechDev& m, const double* __restrict__ J0, const double* ghinv,
                             double* __restrict__ G, int* ier) {
@@ -325,40 +365,40 @@ __device__ void decomp_rows(const MechDev& m, const double* __restrict__ J0, con
   singular_rows<STRICT, NC>(m, J0, ghinv, ier);
   for (int k = 0; k < m.nvar; ++k) {
     const int e0 = ldi(m.lu_crow + k), e1 = ldi(m.lu_crow + k + 1), dk = ldi(m.lu_diag + k);
-    for (int e = e0; e < e1; ++e) {
+    for (int e = e0; e < dk; ++e) {
       double acc[NC];
 #pragma unroll
       for (int q = 0; q < NC; ++q) {
         const double j = ldw(J0 + e * TSN + q * TS);
         acc[q] = STRICT ? -j : j;
-        if (e == dk) acc[q] = acc[q] + ghinv[q];
       }
-      const int t0 = ldi(m.dot_start + e), t1 = ldi(m.dot_start + e + 1);
-#pragma unroll 4
-      for (int t = t0; t < t1; ++t) {
-        const unsigned op = ldu(m.dot_term + t);
-        const double* lp = G + (op >> 16) * TSN;
-        const double* up = G + (op & 0xffffu) * TSN;
-        double l[NC], u[NC];
+      dot_terms<STRICT, NC>(m, G, e, acc);
+      const double* pv = G + ldi(m.lu_diag + ldi(m.lu_icol + e)) * TSN;
 #pragma unroll
-        for (int q = 0; q < NC; ++q) {
-          l[q] = ldw(lp + q * TS);
-          u[q] = ldw(up + q * TS);
-        }
-#pragma unroll
-        for (int q = 0; q < NC; ++q) acc[q] = STRICT ? acc[q] - l[q] * u[q] : fma(-l[q], u[q], acc[q]);
+      for (int q = 0; q < NC; ++q) {
+        const double piv = ldw(pv + q * TS);
+        G[e * TSN + q * TS] = STRICT ? acc[q] / piv : acc[q] * piv;  // fast: diag holds 1/pivot
       }
-      if (e < dk) {
-        const double* pv = G + ldi(m.lu_diag + ldi(m.lu_icol + e)) * TSN;
+    }
+    {
+      double acc[NC];
 #pragma unroll
-        for (int q = 0; q < NC; ++q) {
-          const double piv = ldw(pv + q * TS);
-          acc[q] = STRICT ? acc[q] / piv : acc[q] * piv;  // fast: diag holds 1/pivot
-        }
-      } else if (e == dk && !STRICT) {
-#pragma unroll
-        for (int q = 0; q < NC; ++q) acc[q] = 1.0 / acc[q];
+      for (int q = 0; q < NC; ++q) {
+        const double j = ldw(J0 + dk * TSN + q * TS);
+        acc[q] = (STRICT ? -j : j) + ghinv[q];
       }
+      dot_terms<STRICT, NC>(m, G, dk, acc);
+#pragma unroll
+      for (int q = 0; q < NC; ++q) G[dk * TSN + q * TS] = STRICT ? acc[q] : 1.0 / acc[q];
+    }
+    for (int e = dk + 1; e < e1; ++e) {
+      double acc[NC];
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        const double j = ldw(J0 + e * TSN + q * TS);
+        acc[q] = STRICT ? -j : j;
+      }
+      dot_terms<STRICT, NC>(m, G, e, acc);
 #pragma unroll
       for (int q = 0; q < NC; ++q) G[e * TSN + q * TS] = acc[q];
     }

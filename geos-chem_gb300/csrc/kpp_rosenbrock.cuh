@@ -30,6 +30,12 @@ struct RosMethod {
   int S;
   double A[15], C[15], M[SMAX], E[SMAX], Alpha[SMAX], Gamma[SMAX], ELO;
   int NewF[SMAX];
+  unsigned nzA, nzC, nzM, nzE;  // nonzero-coefficient bits (method_masks)
+  // the nonzero A(s, j), M(j), E(j) as lists (method_masks): stage s adds
+  // a_n[s] terms j = a_j[s][t]; the new solution m_n terms m_j[t], the
+  // error estimate e_n terms e_j[t] -- loops that run only the terms the
+  // method has (WAXPY's alpha = 0 skip without a test per species)
+  int a_n[SMAX], a_j[SMAX][SMAX], m_n, m_j[SMAX], e_n, e_j[SMAX];
 };
 
 struct WsLayout {
@@ -478,10 +484,11 @@ struct Rosenbrock {
 #pragma unroll
           for (int q = 0; q < NC; ++q) {
             double y = Y[i * TSN + q * TS];
-            for (int j = 0; j < s; ++j) {
+            for (int t = 0; t < r.a_n[s]; ++t) {
+              const int j = r.a_j[s][t];
               const double a = r.A[(s * (s - 1)) / 2 + j];
               const double kj = K[j * kst + i * TSN + q * TS];
-              if (a != 0.0) y = STRICT ? y + a * kj : fma(a, kj, y);
+              y = STRICT ? y + a * kj : fma(a, kj, y);
             }
             Ynew[i * TSN + q * TS] = y;
           }
@@ -494,9 +501,14 @@ struct Rosenbrock {
         fcn = arr(w, p.lay.fcn, 0);
       }
       double hc[NC][SMAX], hg[NC];
+      unsigned hbits[NC];  // WAXPY's alpha = 0 skip, tested once per stage: bit j set if hc(j) != 0
 #pragma unroll
       for (int q = 0; q < NC; ++q) {
-        for (int j = 0; j < s; ++j) hc[q][j] = r.C[(s * (s - 1)) / 2 + j] / (dir * L[q].H);
+        hbits[q] = 0u;
+        for (int j = 0; j < s; ++j) {
+          hc[q][j] = r.C[(s * (s - 1)) / 2 + j] / (dir * L[q].H);
+          if (hc[q][j] != 0.0) hbits[q] |= 1u << j;
+        }
         hg[q] = dir * L[q].H * r.Gamma[s];
       }
       const bool use_dfdt = (!p.autonomous) && (r.Gamma[s] != 0.0);
@@ -507,8 +519,9 @@ struct Rosenbrock {
         for (int q = 0; q < NC; ++q) {
           double k = fcn[i * TSN + q * TS];
           for (int j = 0; j < s; ++j) {
+            if (!((hbits[q] >> j) & 1u)) continue;
             const double kj = K[j * kst + i * TSN + q * TS];
-            if (hc[q][j] != 0.0) k = STRICT ? k + hc[q][j] * kj : fma(hc[q][j], kj, k);
+            k = STRICT ? k + hc[q][j] * kj : fma(hc[q][j], kj, k);
           }
           if (use_dfdt && hg[q] != 0.0) {
             const double dd = dfdt[i * TSN + q * TS];
@@ -538,10 +551,16 @@ struct Rosenbrock {
         const double y0 = Y[i * TSN + q * TS];
         double y = y0;
         double yerr = 0.0;
-        for (int j = 0; j < r.S; ++j) {
+        // the M and E terms in ascending j, each sum in its own order
+        for (int t = 0; t < r.m_n; ++t) {
+          const int j = r.m_j[t];
           const double kj = K[j * kst + i * TSN + q * TS];
-          if (r.M[j] != 0.0) y = STRICT ? y + r.M[j] * kj : fma(r.M[j], kj, y);
-          if (r.E[j] != 0.0) yerr = STRICT ? yerr + r.E[j] * kj : fma(r.E[j], kj, yerr);
+          y = STRICT ? y + r.M[j] * kj : fma(r.M[j], kj, y);
+        }
+        for (int t = 0; t < r.e_n; ++t) {
+          const int j = r.e_j[t];
+          const double kj = K[j * kst + i * TSN + q * TS];
+          yerr = STRICT ? yerr + r.E[j] * kj : fma(r.E[j], kj, yerr);
         }
         Ynew[i * TSN + q * TS] = y;
         const double ymax = fmax(fabs(y0), fabs(y));

@@ -26,6 +26,14 @@ import numpy as np
 from . import capi, inputs, mechanism
 
 NFEAT, HID, NOUT, NJ, NSPC, NBIN = 56, 128, 5, 20, 32, 4
+# largest proposed H0 [s] of a cold-started cell: DeltaMin * FacMax**8 =
+# 1e-5 * 6**8 = 16.8 s, the step the plain method's cold start reaches at its
+# ninth step when no step is limited by the error.  A first step far beyond
+# the sizes of that ramp leaves the integration's last steps larger than the
+# plain method's and its error against an RTOL 1e-8 integration larger; from
+# this cap on the remaining steps follow the ramp, so the error stays at the
+# plain method's level while the ramp's first eight steps are skipped.
+H0_CAP = 1.0e-5 * 6.0 ** 8
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "proposer_fullchem.npz")
 BIN_EDGES = (2, 4, 16)  # Rosenbrock steps per chemistry step: 1 | 2-3 | 4-15 | >= 16
 
@@ -105,6 +113,7 @@ class Proposer:
         self.mean = torch.zeros(NFEAT, dtype=torch.float64, device=self.dev)
         self.inv_std = torch.ones(NFEAT, dtype=torch.float64, device=self.dev)
         self.h0_scale = h0_scale
+        self.h0_cap = H0_CAP
         self.bin_edges = [0.0, 0.0, 0.0]
         self.y_mean = 0.0
 
@@ -373,6 +382,10 @@ class CProposer:
                                         ctypes.byref(self.handle))
         if rc != 0:
             raise capi.GcKppError(rc, lib.gc_kpp_last_error().decode())
+        lib.gc_kpp_proposer_set_h0_cap.argtypes = [vp, f64]
+        rc = lib.gc_kpp_proposer_set_h0_cap(self.handle, float(prop.h0_cap or 0.0))
+        if rc != 0:
+            raise capi.GcKppError(rc, lib.gc_kpp_last_error().decode())
 
     def close(self):
         if self.handle:
@@ -391,12 +404,15 @@ PLAN_LAUNCHES = 8  # features 1, forward 3, propose 1, bin order 3
 
 def plan(prop, met, photol, c, stream=None, hstart=None, hmax=1.0e9):
     """The learned part of a chemistry step, on the GPU: features of every
-    cell, the MLP, H0 proposals and stiffness bins, and the queue order
-    (heaviest predicted bin first).  Launches PLAN_LAUNCHES kernels.  The
-    per-bin cell counts are left in ``prop.last_counts`` (device).  With
-    `hstart` (the KPPHvalue array), proposals fill it in place where it is not
-    positive and it is returned as H0."""
+    cell, the MLP, H0 proposals (at most min(hmax, prop.h0_cap)) and
+    stiffness bins, and the queue order (heaviest predicted bin first).
+    Launches PLAN_LAUNCHES kernels.  The per-bin cell counts are left in
+    ``prop.last_counts`` (device).  With `hstart` (the KPPHvalue array),
+    proposals fill it in place where it is not positive and it is returned
+    as H0."""
     x = prop.features(met, photol, c, stream=stream)
+    if prop.h0_cap:
+        hmax = min(hmax, prop.h0_cap)
     h0, bins = prop.propose(x, stream=stream, h0=hstart, hmax=hmax)
     order = prop.bin_order(bins, stream=stream)
     return h0, bins, order

@@ -124,6 +124,13 @@ class Tables:
             packed.append((pre | (two << 12) | (len(sp) << 13) | (s[0] << 16), s[1] | (s[2] << 16)))
         self.prod_packed = np.array(packed, np.uint32)
         self.naux = self.nreact + len(self.pre_literals)
+        # the A products (reactions) and the B products, each listed by class
+        # c = 2 * nspecies + times2 (stable within a class): a loop over one
+        # class multiplies a fixed number of times, with no per-product test
+        x = self.prod_packed[:, 0].astype(np.int64)
+        cls = ((x >> 13) & 3) * 2 + ((x >> 12) & 1)
+        self.prod_ids_a, self.a_cls_start = _by_class(cls[: self.nreact])
+        self.prod_ids_b, self.b_cls_start = _by_class(cls[self.nreact:])
 
         def coef_terms(lists):
             start = np.zeros(len(lists) + 1, np.int32)
@@ -395,6 +402,10 @@ class Tables:
         arr("prod_start", self.prod_start)
         arr("prod_fac", self.prod_fac)
         arr("prod_packed", self.prod_packed.reshape(-1), "unsigned")
+        arr("prod_ids_a", self.prod_ids_a)
+        arr("prod_ids_b", self.prod_ids_b)
+        arr("a_cls_start", self.a_cls_start)
+        arr("b_cls_start", self.b_cls_start)
         arr("p_sterm", self.p_sterm, "unsigned")
         arr("d_sterm", self.d_sterm, "unsigned")
         arr("j_sterm", self.j_sterm, "unsigned")
@@ -441,6 +452,13 @@ class Tables:
             len(self.literals), ",".join(_hexfloat(v) for v in self.literals)))
         out.append("}  // namespace gcmech_tables")
         return "\n".join(out) + "\n"
+
+
+def _by_class(cls, nclass=8):
+    """Indices sorted by class (stable) and the start of each class, [nclass + 1]."""
+    order = np.argsort(cls, kind="stable").astype(np.int32)
+    start = np.searchsorted(cls[order], np.arange(nclass + 1)).astype(np.int32)
+    return order, start
 
 
 def build_tables(ir=None):

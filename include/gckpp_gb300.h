@@ -345,10 +345,16 @@ int gc_kpp_proposer_create(int device, const float* w1, const float* b1, const f
                            const float* w3, const float* b3, const double* mean, const double* inv_std,
                            const int* jrows, const int* srows, double scale, gc_kpp_proposer** proposer);
 int gc_kpp_proposer_destroy(gc_kpp_proposer* proposer);
+/* Largest H0 the proposer proposes [s] (cap > 0; 0 restores the default, the
+ * chemistry step's length).  A cap keeps the first step of a cold-started
+ * cell near the sizes the plain integration reaches on its own, which holds
+ * the learned step's error to the plain step's.  No counterpart in the
+ * reference. */
+int gc_kpp_proposer_set_h0_cap(gc_kpp_proposer* proposer, double cap);
 
 /* gc_kpp_fullchem_step with the learned plan in front: features of every
  * cell, the MLP, H0 proposals written into hstart where it is not positive
- * (cells without a KPPHvalue; clamped to [1e-5, dt]), stiffness bins, the
+ * (cells without a KPPHvalue; clamped to [1e-5, min(dt, H0 cap)]), stiffness bins, the
  * stable heaviest-bin-first queue order, and gc_kpp_fullchem_step_binned
  * with the top bin block-per-cell (*nblock receives its size).  Same
  * arguments and results as gc_kpp_fullchem_step; with device memory, hstart

@@ -117,6 +117,12 @@ int main(int argc, char** argv) {
   m.nb = T::NB;
   m.lit0 = T::LIT0;
   m.prod_packed = reinterpret_cast<const uint2*>(T::prod_packed);
+  m.prod_ids_a = T::prod_ids_a;
+  m.prod_ids_b = T::prod_ids_b;
+  for (int i = 0; i < 9; ++i) {
+    m.a_cls[i] = T::a_cls_start[i];
+    m.b_cls[i] = T::b_cls_start[i];
+  }
   m.naux = T::NAUX;
   m.pre_lit = T::pre_literals;
   m.p_start = T::p_start;

@@ -3,8 +3,10 @@ it was not trained on (counts, not timings: the timed comparison is
 bench.py's learned vs plain arms).
 
 * Cold start (no KPPHvalue, RCNTRL(3) = 0): seeding Hstart with the
-  network's H0 cuts the Rosenbrock steps, at an error against an RTOL = 1e-8
-  integration no worse than the plain step's.
+  network's H0 (capped at learned.H0_CAP) cuts the Rosenbrock steps, at an
+  error against an RTOL = 1e-8 integration no worse than the plain step's:
+  the largest, the 99.9th-percentile and the median relative error over
+  species above 1e4 molec/cm3 each within 5 % of the plain step's.
 * The top stiffness bin finds the cells that need tens of steps, which the
   binned step then runs block-per-cell.
 """
@@ -77,12 +79,15 @@ def test_h0_proposals_cut_steps_at_equal_error(held_out):
         got = c.index_select(1, idx)[:353]
         ref = c_ref[:353]
         m = ref > 1e4
-        return float(((got - ref).abs() / ref)[m].median().item())
+        e = ((got - ref).abs() / ref)[m]
+        q = torch.quantile(e.float(), torch.tensor([0.5, 0.999], device=e.device)).tolist()
+        return {"max": float(e.max().item()), "p99.9": q[1], "median": q[0]}
 
     e_plain, e_learned = err(c_plain), err(c_learned)
-    print("median error vs RTOL 1e-8: plain %.3e learned %.3e; steps plain %d learned %d"
+    print("error vs RTOL 1e-8: plain %s learned %s; steps plain %d learned %d"
           % (e_plain, e_learned, steps_plain, steps_learned))
-    assert e_learned <= max(2.0 * e_plain, 1e-3), (e_learned, e_plain)
+    for key in ("max", "p99.9", "median"):
+        assert e_learned[key] <= 1.05 * e_plain[key], (key, e_learned[key], e_plain[key])
 
 
 def test_top_bin_finds_the_stiff_cells(held_out):
