@@ -118,6 +118,16 @@ def build(verbose=False, force=False):
         out, _ = p.communicate()
         if p.returncode != 0:
             raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), out.decode()))
+    # profiling aid: the mechanism routines one launch each (not the C ABI)
+    rb = routines_path()
+    rb_src = os.path.join(CSRC, "routine_bench.cu")
+    rb_deps = deps + [os.path.join(GEN, "fullchem", f) for f in os.listdir(os.path.join(GEN, "fullchem"))]
+    if force or _stale(rb, rb_deps):
+        cmd = [exe] + NVCC_FLAGS + ["-I", os.path.join(GEN, "fullchem"), "-shared", "-cudart", "shared", rb_src,
+                                    "-o", rb]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        if r.returncode != 0:
+            raise RuntimeError("routine bench build failed: %s\n%s" % (" ".join(cmd), r.stdout.decode()))
     lib = lib_path()
     probe = probe_path()
     src = os.path.join(CSRC, "fp64_probe.cu")
@@ -127,6 +137,11 @@ def build(verbose=False, force=False):
         if r.returncode != 0:
             raise RuntimeError("probe build failed: %s\n%s" % (" ".join(cmd), r.stdout.decode()))
     return lib
+
+
+def routines_path():
+    """Per-routine launches of the fullchem tables for profiling, not part of the C ABI."""
+    return os.path.join(LIBDIR, "libgckpp_routines.so")
 
 
 def probe_path():

@@ -4,6 +4,7 @@
     python geos-chem_gb300/profile_case.py --grid 72x46x8 --binned 64
     python geos-chem_gb300/profile_case.py --grid 72x46x24 --learned
     python geos-chem_gb300/profile_case.py --grid 72x46x24 --autoreduce 100 [--append]
+    python geos-chem_gb300/profile_case.py --routines 4096
 
 Box cells (``inputs.box_cells``) are integrated once from 0 to TOUT with
 ``Solver.integrate``; ``--grid`` instead spins up a grid and runs one 1200 s
@@ -32,10 +33,14 @@ def main(argv=None):
     ap.add_argument("--grid", default=None, help="NLONxNLATxNLEV: grid step instead of box cells")
     ap.add_argument("--binned", type=int, default=0, help="grid step: cells sent block-per-cell")
     ap.add_argument("--learned", action="store_true",
-                    help="grid step: the learned form (cold start, H0 proposals, bins, hand-over after 2 steps)")
+                    help="grid step: the learned form (cold start, capped H0 proposals, bins, hand-over)")
+    ap.add_argument("--evict", type=int, default=4, help="with --learned: hand-over after this many steps")
     ap.add_argument("--block-form", default="split", choices=["split", "level"],
                     help="block-per-cell kernel form (GC_KPP_OPT_BLOCK_SPLIT 1 or 0)")
     ap.add_argument("--probe", action="store_true")
+    ap.add_argument("--routines", type=int, default=0,
+                    help="> 0: only launch each mechanism routine once over this many cells (decomp, solve, "
+                         "fun, bprod, jac; libgckpp_routines.so), to count instructions per routine")
     ap.add_argument("--autoreduce", type=float, default=0.0,
                     help="> 0: the timed step or integration with auto-reduction (ICNTRL(12)=1) at this "
                          "RCNTRL(12) threshold (thread-per-cell kernel; not with --learned/--binned)")
@@ -51,6 +56,15 @@ def main(argv=None):
     import torch
 
     import gcchem.build as build
+
+    if args.routines:
+        rb = ctypes.CDLL(build.routines_path())
+        rb.gc_routine_bench.argtypes = [ctypes.c_int, ctypes.c_int]
+        rcode = rb.gc_routine_bench(0, args.routines)
+        print("routines over %d cells: rc %d" % (args.routines, rcode))
+        if rcode != 0:
+            raise SystemExit(1)
+        return
     import gcchem.capi as capi
     import gcchem.inputs as inputs
     from gcchem.mechanism import load_ir
@@ -91,7 +105,7 @@ def main(argv=None):
             hs.zero_()
             _, _, order = learned.plan(prop, met, ph, c, hstart=hs, hmax=1200.0)
             nb = int(prop.last_counts[learned.NBIN - 1].item())
-            s.set(evict_after=2)
+            s.set(evict_after=args.evict)
         elif args.binned:
             s.fullchem_step(1200.0, met, ph, c.clone(), at, rt, ic, rc, hs.clone(), ist, rst, ierr)
             order = torch.argsort(ist[2], descending=True, stable=True).int()
