@@ -43,6 +43,12 @@ SPINUP_S = 86400.0
 # k = 1 (1.15M cells/s; k = 2 964k, k = 3 855k).
 EVICT_LEARNED = 4
 EVICT_LEARNED_CHAINED = 1
+# DRAM bytes (read + write) per Rosenbrock step attempt of the learned
+# step's three Rosenbrock launches, measured with ncu (dram__bytes_read.sum
+# + dram__bytes_write.sum) on this workload: 1,090.3 GB for 998,044 attempts
+# (profiles/learned_step_grid72x46x72_launch_list.md).  roofline.traffic is
+# this figure times the attempts (ISTATUS(6), decompositions) of the timed step.
+DRAM_BYTES_PER_ATTEMPT = 1.0924e6
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "geos-chem_gb300", "weights", "proposer_fullchem.npz")
 
 
@@ -536,7 +542,11 @@ def run_ours(args):
             "gpu_launches": head["gpu_launches"],
             "roofline": {"bound": "fp64", "achieved": achieved_tf,
                          "peak": (peak_gf / 1e3) if peak_gf else None, "unit": "TFLOP/s",
-                         "frac": (achieved_tf / (peak_gf / 1e3)) if peak_gf else None, "traffic": None,
+                         "frac": (achieved_tf / (peak_gf / 1e3)) if peak_gf else None,
+                         "traffic": float(DRAM_BYTES_PER_ATTEMPT * head["ist"][5].sum(dtype=np.int64)),
+                         "traffic_note": "bytes per launch: ncu DRAM read + write per step attempt of this "
+                                         "workload (1.09 MB) x the step attempts of the timed step; the "
+                                         "algorithmic minimum is the cells' inputs and outputs (~3 KB a cell)",
                          "kernel": "gckpp::ros_kernel (thread per cell) + gckpp::ros_block_kernel (block per "
                                    "cell), learned arm, one step's Rosenbrock launches",
                          "kernel_ms": head["kernel_ms"], "flops_per_launch": flops,

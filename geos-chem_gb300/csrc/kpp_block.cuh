@@ -362,18 +362,30 @@ __device__ __forceinline__ void split_run(const MechDev& m, int ph, const PH& f)
     split_terms(f, nxt);
     nxt.info = p + 1 < np ? __ldg(pw + p + 1) : 0u;
     const int item = cur.t.x & 0xffff;
-    const int seg = 1 << ((cur.t.x >> 16) & 7);
+    const bool busy = item != 0xffff;
+    const int seglog = busy ? (cur.t.x >> 16) & 7 : 0;
+    const int seg = 1 << seglog;
     const int n = (cur.t.x >> 19) & 31;
-    const bool lead = item != 0xffff && (tid & (seg - 1)) == 0;
-    double acc = lead ? f.base(item, cur.t.z, cur.pre) : 0.0;
+    // A warp runs as many multiply-adds as its longest chunk and as many
+    // butterfly levels as its widest segment; a warp with no item in this
+    // pass issues no arithmetic (predicated-off FP64 instructions still
+    // take the SM's FP64 pipe).
+    if (__any_sync(0xffffffffu, busy)) {
+      const int nmax = __reduce_max_sync(0xffffffffu, (unsigned)n);
+      const int lmax = __reduce_max_sync(0xffffffffu, (unsigned)seglog);
+      const bool lead = busy && (tid & (seg - 1)) == 0;
+      double acc = lead ? f.base(item, cur.t.z, cur.pre) : 0.0;
 #pragma unroll
-    for (int k = 0; k < SPLIT_MAXCH; ++k)
-      if (k < n) acc = f.term(item, (int)cur.t.y + k, cur.w[k], acc);
-    for (int o = (1 << (cur.info & 7)) >> 1; o > 0; o >>= 1) {
-      const double v = __shfl_xor_sync(0xffffffffu, acc, o);
-      if (o < seg) acc += v;
+      for (int k = 0; k < SPLIT_MAXCH; ++k) {
+        if (k >= nmax) break;
+        if (k < n) acc = f.term(item, (int)cur.t.y + k, cur.w[k], acc);
+      }
+      for (int o = (1 << lmax) >> 1; o > 0; o >>= 1) {
+        const double v = __shfl_xor_sync(0xffffffffu, acc, o);
+        if (o < seg) acc += v;
+      }
+      if (lead) f.finish(item, cur.t.z, acc);
     }
-    if (lead) f.finish(item, cur.t.z, acc);
     if (cur.info & 8u) {
       if (nt == 32)
         __syncwarp();

@@ -32,11 +32,15 @@ def main(argv=None):
     ap.add_argument("--max-slots", type=int, default=0, help="cap on cells in flight (0: all resident threads)")
     ap.add_argument("--grid", default=None, help="NLONxNLATxNLEV: grid step instead of box cells")
     ap.add_argument("--binned", type=int, default=0, help="grid step: cells sent block-per-cell")
+    ap.add_argument("--cold", action="store_true",
+                    help="grid step without --learned: Hstart = 0 (DeltaMin) instead of the spin-up's KPPHvalue")
     ap.add_argument("--learned", action="store_true",
                     help="grid step: the learned form (cold start, capped H0 proposals, bins, hand-over)")
     ap.add_argument("--evict", type=int, default=4, help="with --learned: hand-over after this many steps")
     ap.add_argument("--block-form", default="split", choices=["split", "level"],
                     help="block-per-cell kernel form (GC_KPP_OPT_BLOCK_SPLIT 1 or 0)")
+    ap.add_argument("--repeat", type=int, default=1,
+                    help="grid step: run the timed step this many times from the same state (the last is reported)")
     ap.add_argument("--probe", action="store_true")
     ap.add_argument("--routines", type=int, default=0,
                     help="> 0: only launch each mechanism routine once over this many cells (decomp, solve, "
@@ -96,6 +100,8 @@ def main(argv=None):
     if args.grid:
         hs = torch.zeros(n, dtype=torch.float64, device=dev)
         s.fullchem_step(86400.0, met, ph, c, at, rt, ic, rc, hs, ist, rst, ierr)
+        if args.cold:
+            hs.zero_()
         order, nb = None, 0
         if args.learned:
             import gcchem.learned as learned
@@ -110,6 +116,16 @@ def main(argv=None):
             s.fullchem_step(1200.0, met, ph, c.clone(), at, rt, ic, rc, hs.clone(), ist, rst, ierr)
             order = torch.argsort(ist[2], descending=True, stable=True).int()
             nb = args.binned
+        c0, hs0 = c.clone(), hs.clone()
+        for rep in range(args.repeat - 1):  # earlier runs of the same step, each from the same state
+            torch.cuda.synchronize()
+            t0.record()
+            s.fullchem_step(1200.0, met, ph, c, at, rt, ic_t, rc_t, hs, ist, rst, ierr, order=order, nblock=nb)
+            t1.record()
+            torch.cuda.synchronize()
+            print("run %d: %.3f ms" % (rep, t0.elapsed_time(t1)))
+            c.copy_(c0)
+            hs.copy_(hs0)
         torch.cuda.synchronize()
         t0.record()
         s.fullchem_step(1200.0, met, ph, c, at, rt, ic_t, rc_t, hs, ist, rst, ierr, order=order, nblock=nb)
@@ -122,7 +138,8 @@ def main(argv=None):
         s.integrate(c, r, at, rt, 0.0, args.tout, ic_t, rc_t, istatus=ist, ierr=ierr)
         t1.record()
     torch.cuda.synchronize()
-    print("timed call %.3f ms (one cold run, default stream)" % t0.elapsed_time(t1))
+    print("timed call %.3f ms (%s, default stream)" % (t0.elapsed_time(t1), "one cold run" if args.repeat <= 1 else
+                                                         "after %d runs of the same step" % (args.repeat - 1)))
     ih = ist.cpu().numpy().astype(np.int64)
     t = Tables(load_ir())
     f = t.flops()
@@ -131,6 +148,9 @@ def main(argv=None):
              + ih[6].sum() * f["solve"] + ih[2].sum() * vec)
     print("cells %d steps/cell %.3f max %d" % (n, ih[2].mean(), ih[2].max()))
     print("ISTATUS sums fun jac stp acc rej dec sol sng", ih[:8].sum(axis=1).tolist())
+    if args.grid and nb > 0:
+        sel = order[:nb].long().cpu().numpy()
+        print("block-per-cell cells %d: ISTATUS sums %s" % (nb, ih[:8, sel].sum(axis=1).tolist()))
     print("algorithmic FP64 flops %.4e" % flops)
     if args.probe:
         probe = ctypes.CDLL(build.probe_path())
