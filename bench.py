@@ -66,8 +66,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample duration")
     ap.add_argument("--weights", default=WEIGHTS, help="trained proposer weights (.npz)")
     ap.add_argument("--error-cells", type=int, default=2048, help="cells integrated at RTOL 1e-8 for the error")
-    ap.add_argument("--e2e-chunks", type=int, default=1,
-                    help="chunks of the end-to-end step (host copies overlap the solves of other chunks)")
+    ap.add_argument("--e2e-chunks", type=int, default=0,
+                    help="> 0: the end-to-end step streams this many chunks through gcchem.stream.Streamer "
+                         "(0: one host-memory call of the C ABI)")
     return ap.parse_args()
 
 
@@ -427,64 +428,89 @@ def run_ours(args):
 
     errors = {name: rel_err(res[name]["c"]) for name in arms}
 
-    # end to end through the public API: the grid's inputs in pinned host
-    # memory, the learned chemistry step (gc_kpp_fullchem_step_learned)
-    # through gcchem.stream.Streamer: met, the J-value rows the mechanism
-    # reads, C and KPPHvalue copied in, C, KPPHvalue, ISTATUS(3) and IERR
-    # copied out.  One chunk by default: the copies take ~10 ms at the
-    # measured ~200 GB/s, while cutting the learned step into chunks repeats
-    # its stiff-cell tail per chunk (2 and 4 chunks on two alternating solver
-    # contexts measured 8 % and 35 % slower than one).
+    # end to end through the reference-facing call: the grid's arrays in
+    # page-locked host memory and one gc_kpp_fullchem_step_learned with
+    # GC_KPP_MEM_HOST, which stages met, the J-value rows that the rates and
+    # the features read, C and KPPHvalue in, and C, KPPHvalue, ISTATUS and
+    # IERR out (SM copies through the host memory's device alias), all inside
+    # the timed region.  --e2e-chunks N > 0 streams N chunks through
+    # gcchem.stream.Streamer instead.
     e2e = None
     if rank == 0 or world > 1:
-        import gcchem.stream as stream
-
-        nch = max(1, args.e2e_chunks)
-        chunk = -(-ncell // nch)
-        pin = lambda x: x.contiguous().pin_memory()
-        host_in = {"met": met.cpu(), "ph": ph.cpu(), "c": c_spun.cpu(), "hs": cold0.cpu()}
-        chunks = []
-        for i0 in range(0, ncell, chunk):
-            i1 = min(ncell, i0 + chunk)
-            ch = {k: pin(v[..., i0:i1]) for k, v in host_in.items()}
-            ch.update(c_out=torch.empty_like(ch["c"]).pin_memory(), hs_out=torch.empty_like(ch["hs"]).pin_memory(),
-                      steps=torch.zeros(i1 - i0, dtype=torch.int32).pin_memory(),
-                      ierr=torch.zeros(i1 - i0, dtype=torch.int32).pin_memory())
-            chunks.append(ch)
         cp = learned.CProposer(prop, local)
-        solvers = [solver]
-        if len(chunks) > 1:
-            solvers.append(capi.Solver(local, arith="fast", schedule=args.schedule))
-        for sv in solvers:
-            sv.set(evict_after=EVICT_LEARNED)
-        st = stream.Streamer(solver, ncell, chunk, proposer=cp, solvers=solvers, photol_rows=stream.photol_runs())
-        st.step(chunks, DT, at, rt, icntrl, rcntrl)  # synchronous: sizes each context's buffers
-        for sv in solvers:
-            sv.set(async_steps=True)
-        tms = []
-        for it in range(1 + min(args.steps, 3)):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            st.step(chunks, DT, at, rt, icntrl, rcntrl)
-            torch.cuda.synchronize()
-            if it > 0:
-                tms.append(time.perf_counter() - t0)
-        for sv in solvers:
-            sv.set(async_steps=False)
-        steps_e2e = np.concatenate([ch["steps"].numpy() for ch in chunks])
-        h2d, d2h = st.bytes_per_cell()
+        solver.set(evict_after=EVICT_LEARNED, async_steps=False)
+        pin = lambda x: x.contiguous().cpu().pin_memory()
+        if args.e2e_chunks <= 0:
+            h = {"met": pin(met), "ph": pin(ph), "c0": pin(c_spun), "at": at.cpu().numpy(), "rt": rt.cpu().numpy()}
+            h["c"] = torch.empty_like(h["c0"]).pin_memory()
+            h["hs"] = torch.zeros(ncell, dtype=torch.float64).pin_memory()
+            h["ist"] = torch.zeros((20, ncell), dtype=torch.int32).pin_memory()
+            h["ierr"] = torch.zeros(ncell, dtype=torch.int32).pin_memory()
+            tms = []
+            for it in range(1 + min(args.steps, 3)):
+                h["c"].copy_(h["c0"])  # the step's input state (host memcpy, outside the timed region)
+                h["hs"].zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                solver.fullchem_step_learned(cp.handle, DT, h["met"], h["ph"], h["c"], h["at"], h["rt"], icntrl,
+                                             rcntrl, h["hs"], h["ist"], None, h["ierr"])
+                torch.cuda.synchronize()
+                if it > 0:
+                    tms.append(time.perf_counter() - t0)
+            steps_e2e = h["ist"][2].numpy()
+            nph = int((capi.photol_rows(solver.lib) | np.isin(np.arange(200), learned.feature_rows()[0])).sum())
+            h2d = 8 * (18 + nph + c_spun.shape[0] + 1)
+            d2h = 8 * (c_spun.shape[0] + 1) + 4 * (20 + 1)
+            path = ("gc_kpp_fullchem_step_learned with GC_KPP_MEM_HOST on page-locked host arrays (SM staging "
+                    "copies, %d of 200 PHOTOL rows)" % nph)
+            nch = 1
+        else:
+            import gcchem.stream as stream
+
+            nch = args.e2e_chunks
+            chunk = -(-ncell // nch)
+            host_in = {"met": met.cpu(), "ph": ph.cpu(), "c": c_spun.cpu(), "hs": cold0.cpu()}
+            chunks = []
+            for i0 in range(0, ncell, chunk):
+                i1 = min(ncell, i0 + chunk)
+                ch = {k: v[..., i0:i1].contiguous().pin_memory() for k, v in host_in.items()}
+                ch.update(c_out=torch.empty_like(ch["c"]).pin_memory(), hs_out=torch.empty_like(ch["hs"]).pin_memory(),
+                          steps=torch.zeros(i1 - i0, dtype=torch.int32).pin_memory(),
+                          ierr=torch.zeros(i1 - i0, dtype=torch.int32).pin_memory())
+                chunks.append(ch)
+            solvers = [solver]
+            if len(chunks) > 1:
+                solvers.append(capi.Solver(local, arith="fast", schedule=args.schedule))
+            for sv in solvers:
+                sv.set(evict_after=EVICT_LEARNED)
+            st = stream.Streamer(solver, ncell, chunk, proposer=cp, solvers=solvers, photol_rows=stream.photol_runs())
+            st.step(chunks, DT, at, rt, icntrl, rcntrl)  # synchronous: sizes each context's buffers
+            for sv in solvers:
+                sv.set(async_steps=True)
+            tms = []
+            for it in range(1 + min(args.steps, 3)):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                st.step(chunks, DT, at, rt, icntrl, rcntrl)
+                torch.cuda.synchronize()
+                if it > 0:
+                    tms.append(time.perf_counter() - t0)
+            for sv in solvers:
+                sv.set(async_steps=False)
+            steps_e2e = np.concatenate([ch["steps"].numpy() for ch in chunks])
+            h2d, d2h = st.bytes_per_cell()
+            path = ("gcchem.stream.Streamer over gc_kpp_fullchem_step_learned, pinned host chunks, %d chunk(s) on "
+                    "%d solver context(s)" % (len(chunks), len(solvers)))
+            for sv in solvers[1:]:
+                sv.close()
         tmax = float(np.mean(tms))
         if world > 1:
             t = torch.tensor([tmax], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             tmax = float(t.item())
         e2e = {"value": ncell_total / tmax, "unit": "cells/s", "h2d_bytes_per_step": int(h2d * ncell_total),
-               "d2h_bytes_per_step": int(d2h * ncell_total), "chunks": len(chunks),
-               "steps_match_learned_arm": bool(np.array_equal(steps_e2e, head["ist"][2])),
-               "path": "gcchem.stream.Streamer over gc_kpp_fullchem_step_learned, pinned host buffers, "
-                       "%d chunk(s) on %d solver context(s)" % (len(chunks), len(solvers))}
-        for sv in solvers[1:]:
-            sv.close()
+               "d2h_bytes_per_step": int(d2h * ncell_total), "chunks": nch,
+               "steps_match_learned_arm": bool(np.array_equal(steps_e2e, head["ist"][2])), "path": path}
         cp.close()
 
     cpu = None

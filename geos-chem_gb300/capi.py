@@ -62,6 +62,8 @@ EXPORTED = [
     "gc_kpp_integrate_batch_noalloc",
     "gc_kpp_last_launch_count",
     "gc_kpp_last_kernel_ms",
+    "gc_kpp_copy_rows",
+    "gc_kpp_photol_rows",
 ]
 
 _libs = {}
@@ -96,6 +98,8 @@ def load_library(path=None, mech="fullchem"):
     lib.gc_kpp_ctx_set_autoreduce.argtypes = [vp, i32, vp, vp, vp, vp, i32]
     lib.gc_kpp_set_state_het_batch.argtypes = [vp, i32, vp, i64, vp, i64, f64, i32, i32, vp, i64, i32, vp]
     lib.gc_kpp_sulfur_aq_rates_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, i32, vp]
+    lib.gc_kpp_copy_rows.argtypes = [vp, i64, vp, i64, i64, i64, vp]
+    lib.gc_kpp_photol_rows.argtypes = [vp]
     if path == _build.lib_path(mech):
         _libs[mech] = lib
     return lib
@@ -369,3 +373,38 @@ class Solver:
                 self.ctx, ncell, _ptr(met), _ld(met, ncell), _ptr(photol), _ld(photol, ncell), _ptr(c),
                 _ld(c, ncell), _ptr(het), _ld(het, ncell), _ptr(rconst), _ld(rconst, ncell), mem, s)
         self._check(rc)
+
+
+def copy_rows(dst, src, stream=None, lib=None):
+    """dst.copy_(src) for two 2-D arrays of the same shape and dtype (rows of
+    contiguous elements, any row stride; torch tensors, host or CUDA) through
+    gc_kpp_copy_rows: page-locked host memory is read and written by the
+    SMs, which after a chemistry step is an order of magnitude faster than a
+    copy engine.  Stream-ordered on `stream` (a CUDA stream handle, default
+    the current torch stream)."""
+    import torch
+
+    lib = lib or load_library()
+    if dst.shape != src.shape or dst.dtype != src.dtype:
+        raise ValueError("copy_rows: shapes or dtypes differ")
+    d2 = dst if dst.dim() == 2 else dst.reshape(1, -1)
+    s2 = src if src.dim() == 2 else src.reshape(1, -1)
+    if d2.stride(1) != 1 or s2.stride(1) != 1:
+        raise ValueError("copy_rows: rows must be contiguous")
+    es = dst.element_size()
+    if stream is None:
+        stream = torch.cuda.current_stream().cuda_stream
+    rc = lib.gc_kpp_copy_rows(ctypes.c_void_p(d2.data_ptr()), d2.stride(0) * es, ctypes.c_void_p(s2.data_ptr()),
+                              s2.stride(0) * es, d2.shape[1] * es, d2.shape[0], ctypes.c_void_p(stream))
+    if rc != GC_KPP_OK:
+        raise GcKppError(rc, lib.gc_kpp_last_error().decode())
+
+
+def photol_rows(lib=None):
+    """Boolean mask of the PHOTOL rows the mechanism's rates read."""
+    lib = lib or load_library()
+    mask = np.zeros(200, dtype=np.uint8)
+    rc = lib.gc_kpp_photol_rows(mask.ctypes.data_as(ctypes.c_void_p))
+    if rc != GC_KPP_OK:
+        raise GcKppError(rc, lib.gc_kpp_last_error().decode())
+    return mask.astype(bool)

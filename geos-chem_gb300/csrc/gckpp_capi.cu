@@ -728,15 +728,25 @@ int stage_in(DevBuf& buf, const X* host, long long ld, size_t ncell, size_t rows
   GC_CUDA(buf.ensure(rows * ncell * sizeof(X)));
   *dev = (X*)buf.p;
   if (host)
-    GC_CUDA(cudaMemcpy2DAsync(buf.p, ncell * sizeof(X), host, ld * sizeof(X), ncell * sizeof(X), rows,
-                              cudaMemcpyHostToDevice, s));
+    GC_CUDA(gcutil::copy_rows(buf.p, ncell * sizeof(X), host, ld * sizeof(X), ncell * sizeof(X), rows, s));
+  return GC_KPP_OK;
+}
+
+// The PHOTOL rows that the rate program reads, staged into a device buffer
+// of all GC_KPP_NPHOTOL rows (the others are never read).
+int stage_photol(DevBuf& buf, const double* host, long long ld, size_t ncell, cudaStream_t s, double** dev) {
+  GC_TRY(stage_in<double>(buf, nullptr, ld, ncell, GC_KPP_NPHOTOL, s, dev));
+  for (int r = 0; r < RT::NPHOTOL_RUNS; ++r) {
+    const int a = RT::photol_runs[2 * r], b = RT::photol_runs[2 * r + 1];
+    GC_CUDA(gcutil::copy_rows(*dev + (size_t)a * ncell, ncell * sizeof(double), host + (long long)a * ld,
+                              ld * sizeof(double), ncell * sizeof(double), b - a, s));
+  }
   return GC_KPP_OK;
 }
 
 template <typename X>
 int stage_out(X* host, long long ld, const X* dev, size_t ncell, size_t rows, cudaStream_t s) {
-  GC_CUDA(cudaMemcpy2DAsync(host, ld * sizeof(X), dev, ncell * sizeof(X), ncell * sizeof(X), rows,
-                            cudaMemcpyDeviceToHost, s));
+  GC_CUDA(gcutil::copy_rows(host, ld * sizeof(X), dev, ncell * sizeof(X), ncell * sizeof(X), rows, s));
   return GC_KPP_OK;
 }
 
@@ -864,7 +874,7 @@ static int fullchem_step_impl(gc_kpp_ctx* c, int ncell, double dt, const double*
       dorder = t;
     }
     GC_TRY(stage_in(c->h_met, met, ldm, n, RT::NMET, s, &tmp)); dmet = tmp;
-    GC_TRY(stage_in(c->h_ph, photol, ldp, n, GC_KPP_NPHOTOL, s, &tmp)); dph = tmp;
+    GC_TRY(stage_photol(c->h_ph, photol, ldp, n, s, &tmp)); dph = tmp;
     GC_TRY(stage_in(c->h_c, (const double*)cc, ldc, n, T::NSPEC, s, &dc));
     GC_TRY(stage_in(c->h_at, atol, (long long)ntol, ntol, 1, s, &tmp)); dat = tmp;
     GC_TRY(stage_in(c->h_rt, rtol, (long long)ntol, ntol, 1, s, &tmp)); drt = tmp;
@@ -1128,12 +1138,12 @@ int gc_kpp_update_rconst_het_batch(gc_kpp_ctx* c, int ncell, const double* met, 
     GC_CUDA(c->h_ph.ensure(GC_KPP_NPHOTOL * n * sizeof(double)));
     GC_CUDA(c->h_c.ensure(T::NSPEC * n * sizeof(double)));
     GC_CUDA(c->h_r.ensure(T::NREACT * n * sizeof(double)));
-    GC_CUDA(cudaMemcpy2DAsync(c->h_met.p, n * sizeof(double), met, ldm * sizeof(double), n * sizeof(double),
-                              RT::NMET, cudaMemcpyHostToDevice, s));
-    GC_CUDA(cudaMemcpy2DAsync(c->h_ph.p, n * sizeof(double), photol, ldp * sizeof(double), n * sizeof(double),
-                              GC_KPP_NPHOTOL, cudaMemcpyHostToDevice, s));
-    GC_CUDA(cudaMemcpy2DAsync(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
-                              T::NSPEC, cudaMemcpyHostToDevice, s));
+    GC_CUDA(gcutil::copy_rows(c->h_met.p, n * sizeof(double), met, ldm * sizeof(double), n * sizeof(double),
+                              RT::NMET, s));
+    GC_CUDA(gcutil::copy_rows(c->h_ph.p, n * sizeof(double), photol, ldp * sizeof(double), n * sizeof(double),
+                              GC_KPP_NPHOTOL, s));
+    GC_CUDA(gcutil::copy_rows(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
+                              T::NSPEC, s));
     a.met = (const double*)c->h_met.p;
     a.photol = (const double*)c->h_ph.p;
     a.c = (const double*)c->h_c.p;
@@ -1141,8 +1151,8 @@ int gc_kpp_update_rconst_het_batch(gc_kpp_ctx* c, int ncell, const double* met, 
     a.ldm = a.ldp = a.ldc = a.ldr = ncell;
     if (het) {
       GC_CUDA(c->h_het.ensure((size_t)HET_NFIELD * n * sizeof(double)));
-      GC_CUDA(cudaMemcpy2DAsync(c->h_het.p, n * sizeof(double), het, ldh * sizeof(double), n * sizeof(double),
-                                HET_NFIELD, cudaMemcpyHostToDevice, s));
+      GC_CUDA(gcutil::copy_rows(c->h_het.p, n * sizeof(double), het, ldh * sizeof(double), n * sizeof(double),
+                                HET_NFIELD, s));
       a.het = (const double*)c->h_het.p;
       a.ldh = ncell;
     }
@@ -1161,8 +1171,8 @@ int gc_kpp_update_rconst_het_batch(gc_kpp_ctx* c, int ncell, const double* met, 
   cudaError_t e = c->rates_direct ? gcrates::launch_rates_direct(c->rates, a, s) : gcrates::launch_rates(c->rates, a, s);
   if (e != cudaSuccess) return cuda_fail(e, "rates kernel launch");
   if (mem == GC_KPP_MEM_HOST) {
-    GC_CUDA(cudaMemcpy2DAsync(rconst, ldr * sizeof(double), a.rconst, n * sizeof(double), n * sizeof(double),
-                              T::NREACT, cudaMemcpyDeviceToHost, s));
+    GC_CUDA(gcutil::copy_rows(rconst, ldr * sizeof(double), a.rconst, n * sizeof(double), n * sizeof(double),
+                              T::NREACT, s));
     GC_CUDA(cudaStreamSynchronize(s));
   }
   return GC_KPP_OK;
@@ -1190,10 +1200,10 @@ int gc_kpp_set_state_het_batch(gc_kpp_ctx* c, int ncell, const double* hetin, lo
     GC_CUDA(c->h_hetin.ensure((size_t)HETIN_NFIELD * n * sizeof(double)));
     GC_CUDA(c->h_c.ensure(T::NSPEC * n * sizeof(double)));
     GC_CUDA(c->h_het.ensure((size_t)HET_NFIELD * n * sizeof(double)));
-    GC_CUDA(cudaMemcpy2DAsync(c->h_hetin.p, n * sizeof(double), hetin, ldi * sizeof(double), n * sizeof(double),
-                              HETIN_NFIELD, cudaMemcpyHostToDevice, s));
-    GC_CUDA(cudaMemcpy2DAsync(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
-                              T::NSPEC, cudaMemcpyHostToDevice, s));
+    GC_CUDA(gcutil::copy_rows(c->h_hetin.p, n * sizeof(double), hetin, ldi * sizeof(double), n * sizeof(double),
+                              HETIN_NFIELD, s));
+    GC_CUDA(gcutil::copy_rows(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
+                              T::NSPEC, s));
     a.in = (const double*)c->h_hetin.p;
     a.c = (const double*)c->h_c.p;
     a.het = (double*)c->h_het.p;
@@ -1209,8 +1219,7 @@ int gc_kpp_set_state_het_batch(gc_kpp_ctx* c, int ncell, const double* hetin, lo
   cudaError_t e = gchet::set_state_het(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "SetStateHet kernel launch");
   if (mem == GC_KPP_MEM_HOST) {
-    GC_CUDA(cudaMemcpy2DAsync(het, ldh * sizeof(double), a.het, n * sizeof(double), n * sizeof(double), HET_NFIELD,
-                              cudaMemcpyDeviceToHost, s));
+    GC_CUDA(gcutil::copy_rows(het, ldh * sizeof(double), a.het, n * sizeof(double), n * sizeof(double), HET_NFIELD, s));
     GC_CUDA(cudaStreamSynchronize(s));
   }
   return GC_KPP_OK;
@@ -1240,12 +1249,12 @@ int gc_kpp_sulfur_aq_rates_batch(gc_kpp_ctx* c, int ncell, const double* hetin, 
     GC_CUDA(c->h_hetin.ensure((size_t)HETIN_NFIELD * n * sizeof(double)));
     GC_CUDA(c->h_c.ensure(T::NSPEC * n * sizeof(double)));
     GC_CUDA(c->h_met.ensure(RT::NMET * n * sizeof(double)));
-    GC_CUDA(cudaMemcpy2DAsync(c->h_hetin.p, n * sizeof(double), hetin, ldi * sizeof(double), n * sizeof(double),
-                              HETIN_NFIELD, cudaMemcpyHostToDevice, s));
-    GC_CUDA(cudaMemcpy2DAsync(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
-                              T::NSPEC, cudaMemcpyHostToDevice, s));
-    GC_CUDA(cudaMemcpy2DAsync(c->h_met.p, n * sizeof(double), met, ldm * sizeof(double), n * sizeof(double),
-                              RT::NMET, cudaMemcpyHostToDevice, s));
+    GC_CUDA(gcutil::copy_rows(c->h_hetin.p, n * sizeof(double), hetin, ldi * sizeof(double), n * sizeof(double),
+                              HETIN_NFIELD, s));
+    GC_CUDA(gcutil::copy_rows(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
+                              T::NSPEC, s));
+    GC_CUDA(gcutil::copy_rows(c->h_met.p, n * sizeof(double), met, ldm * sizeof(double), n * sizeof(double),
+                              RT::NMET, s));
     a.in = (const double*)c->h_hetin.p;
     a.c = (const double*)c->h_c.p;
     a.met = (double*)c->h_met.p;
@@ -1261,9 +1270,8 @@ int gc_kpp_sulfur_aq_rates_batch(gc_kpp_ctx* c, int ncell, const double* hetin, 
   cudaError_t e = gchet::sulfur_aq_rates(a, s);
   if (e != cudaSuccess) return cuda_fail(e, "SulfurAqChem kernel launch");
   if (mem == GC_KPP_MEM_HOST) {
-    GC_CUDA(cudaMemcpy2DAsync(met + (long long)GC_KPP_MET_K_MT * ldm, ldm * sizeof(double),
-                              a.met + (long long)GC_KPP_MET_K_MT * ncell, n * sizeof(double), n * sizeof(double), 6,
-                              cudaMemcpyDeviceToHost, s));
+    GC_CUDA(gcutil::copy_rows(met + (long long)GC_KPP_MET_K_MT * ldm, ldm * sizeof(double),
+                              a.met + (long long)GC_KPP_MET_K_MT * ncell, n * sizeof(double), n * sizeof(double), 6, s));
     GC_CUDA(cudaStreamSynchronize(s));
   }
   return GC_KPP_OK;
@@ -1375,6 +1383,8 @@ int noalloc_setup(int dev, NoAllocDevice** out) {
 
 }  // namespace
 
+void gckpp_photol_rows(unsigned char* mask);
+
 extern "C" {
 
 int gc_kpp_integrate_batch_noalloc(int ncell, double tin, double tout, double* c, long long ldc, const double* rconst,
@@ -1458,6 +1468,22 @@ int gc_kpp_integrate_batch_noalloc(int ncell, double tin, double tout, double* c
   return GC_KPP_OK;
 }
 
+int gc_kpp_copy_rows(void* dst, long long dpitch, const void* src, long long spitch, long long width, long long rows,
+                     void* stream) {
+  if (rows < 0 || width < 0 || dpitch < width || spitch < width) return fail(GC_KPP_EINVAL, "bad copy shape");
+  if (rows > 0 && width > 0 && (!dst || !src)) return fail(GC_KPP_EINVAL, "NULL array");
+  cudaError_t e = gcutil::copy_rows(dst, (size_t)dpitch, src, (size_t)spitch, (size_t)width, (size_t)rows,
+                                    (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "row copy");
+  return GC_KPP_OK;
+}
+
+int gc_kpp_photol_rows(unsigned char* mask) {
+  if (!mask) return fail(GC_KPP_EINVAL, "NULL mask");
+  gckpp_photol_rows(mask);
+  return GC_KPP_OK;
+}
+
 }  // extern "C"
 
 // Error text for the library's other translation units (gckpp_learned_capi.cu).
@@ -1477,3 +1503,10 @@ int gckpp_step_binned_dev(gc_kpp_ctx* c, int ncell, double dt, const double* met
 }
 
 int gckpp_ctx_async(const gc_kpp_ctx* c) { return c ? c->async : 0; }
+
+// mask[r] = 1 for the PHOTOL rows r that the rate program reads (GC_KPP_NPHOTOL entries).
+void gckpp_photol_rows(unsigned char* mask) {
+  for (int r = 0; r < GC_KPP_NPHOTOL; ++r) mask[r] = 0;
+  for (int k = 0; k < RT::NPHOTOL_RUNS; ++k)
+    for (int r = RT::photol_runs[2 * k]; r < RT::photol_runs[2 * k + 1]; ++r) mask[r] = 1;
+}

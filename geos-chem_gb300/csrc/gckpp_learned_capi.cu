@@ -12,6 +12,7 @@
 
 #include "../../include/gckpp_gb300.h"
 #include "kpp_mlp.h"
+#include "kpp_util.h"
 
 using namespace gcmlp;
 
@@ -23,6 +24,8 @@ struct gc_kpp_proposer {
   float *b1 = nullptr, *b2 = nullptr, *b3 = nullptr;
   double *mean = nullptr, *inv_std = nullptr;
   int *jrows = nullptr, *srows = nullptr;
+  // PHOTOL rows a host-memory call stages: the rate program's and the features'
+  unsigned char photol_rows[GC_KPP_NPHOTOL] = {};
   // per-call buffers, grown to the largest batch seen
   size_t cap = 0;
   float *x = nullptr, *h1 = nullptr, *h2 = nullptr, *out = nullptr;
@@ -104,6 +107,7 @@ cudaError_t ensure_host_staging(gc_kpp_proposer* q, size_t n, int nspec, int nva
 
 int gckpp_set_error(int code, const char* msg);
 int gckpp_ctx_async(const gc_kpp_ctx* c);
+void gckpp_photol_rows(unsigned char* mask);
 int gckpp_step_binned_dev(gc_kpp_ctx* c, int ncell, double dt, const double* met, long long ldm, const double* photol,
                           long long ldp, double* cc, long long ldc, const double* atol, const double* rtol,
                           const int* icntrl_u, const double* rcntrl_u, double* hstart, int* istatus, double* rstatus,
@@ -117,11 +121,19 @@ int gc_kpp_proposer_create(int device, const float* w1, const float* b1, const f
   if (!out || !w1 || !b1 || !w2 || !b2 || !w3 || !b3 || !mean || !inv_std || !jrows || !srows)
     return gckpp_set_error(GC_KPP_EINVAL, "NULL argument");
   if (!(scale > 0.0)) return gckpp_set_error(GC_KPP_EINVAL, "scale must be positive");
+  int nspec = 0;
+  gc_kpp_mechanism_dims(&nspec, nullptr, nullptr, nullptr, nullptr);
+  for (int k = 0; k < NJ; ++k)
+    if (jrows[k] < 0 || jrows[k] >= GC_KPP_NPHOTOL) return gckpp_set_error(GC_KPP_EINVAL, "jrows outside PHOTOL");
+  for (int k = 0; k < NSPC; ++k)
+    if (srows[k] < 0 || srows[k] >= nspec) return gckpp_set_error(GC_KPP_EINVAL, "srows outside the species");
   *out = nullptr;
   if (cudaSetDevice(device) != cudaSuccess) return gckpp_set_error(GC_KPP_ECUDA, "cudaSetDevice");
   gc_kpp_proposer* q = new gc_kpp_proposer();
   q->device = device;
   q->scale = scale;
+  gckpp_photol_rows(q->photol_rows);
+  for (int k = 0; k < NJ; ++k) q->photol_rows[jrows[k]] = 1;
   cudaError_t e = upload_bf16(&q->w1, w1, (size_t)HID * NFEAT);
   if (e == cudaSuccess) e = upload_bf16(&q->w2, w2, (size_t)HID * HID);
   if (e == cudaSuccess) e = upload_bf16(&q->w3, w3, (size_t)NOUT * HID);
@@ -187,12 +199,23 @@ int gc_kpp_fullchem_step_learned(gc_kpp_ctx* ctx, gc_kpp_proposer* q, int ncell,
   if (host) {
     if (ensure_host_staging(q, n, nspec, nvar) != cudaSuccess)
       return gckpp_set_error(GC_KPP_ENOMEM, "proposer staging buffers");
-    GC_L_CUDA(cudaMemcpy2DAsync(q->met, n * 8, met, ldm * 8, n * 8, GC_KPP_NMET, cudaMemcpyHostToDevice, s));
-    GC_L_CUDA(cudaMemcpy2DAsync(q->ph, n * 8, photol, ldp * 8, n * 8, GC_KPP_NPHOTOL, cudaMemcpyHostToDevice, s));
-    GC_L_CUDA(cudaMemcpy2DAsync(q->c, n * 8, c, ldc * 8, n * 8, nspec, cudaMemcpyHostToDevice, s));
+    GC_L_CUDA(gcutil::copy_rows(q->met, n * 8, met, ldm * 8, n * 8, GC_KPP_NMET, s));
+    // only the PHOTOL rows that the rates and the features read
+    for (int r0 = 0; r0 < GC_KPP_NPHOTOL;) {
+      if (!q->photol_rows[r0]) {
+        ++r0;
+        continue;
+      }
+      int r1 = r0 + 1;
+      while (r1 < GC_KPP_NPHOTOL && q->photol_rows[r1]) ++r1;
+      GC_L_CUDA(gcutil::copy_rows(q->ph + (size_t)r0 * n, n * 8, photol + (long long)r0 * ldp, ldp * 8, n * 8,
+                                  r1 - r0, s));
+      r0 = r1;
+    }
+    GC_L_CUDA(gcutil::copy_rows(q->c, n * 8, c, ldc * 8, n * 8, nspec, s));
     GC_L_CUDA(cudaMemcpyAsync(q->tol, atol, ntol * 8, cudaMemcpyHostToDevice, s));
     GC_L_CUDA(cudaMemcpyAsync(q->tol + nvar, rtol, ntol * 8, cudaMemcpyHostToDevice, s));
-    if (hstart) GC_L_CUDA(cudaMemcpyAsync(q->hs, hstart, n * 8, cudaMemcpyHostToDevice, s));
+    if (hstart) GC_L_CUDA(gcutil::copy_rows(q->hs, n * 8, hstart, n * 8, n * 8, 1, s));
     dmet = q->met; dph = q->ph; dc = q->c; dat = q->tol; drt = q->tol + nvar;
     dhs = q->hs; dis = q->is; drs = q->rs; die = q->ie;
     lm = lp = lc = lo = ncell;
@@ -225,11 +248,11 @@ int gc_kpp_fullchem_step_learned(gc_kpp_ctx* ctx, gc_kpp_proposer* q, int ncell,
                                        dis, drs, lo, die, nretry, q->order, nb, GC_KPP_MEM_DEVICE, stream);
   if (rc != GC_KPP_OK) return rc;
   if (host) {
-    GC_L_CUDA(cudaMemcpy2DAsync(c, ldc * 8, q->c, n * 8, n * 8, nspec, cudaMemcpyDeviceToHost, s));
-    GC_L_CUDA(cudaMemcpyAsync(ierr, q->ie, n * 4, cudaMemcpyDeviceToHost, s));
-    if (istatus) GC_L_CUDA(cudaMemcpy2DAsync(istatus, ldo * 4, q->is, n * 4, n * 4, 20, cudaMemcpyDeviceToHost, s));
-    if (rstatus) GC_L_CUDA(cudaMemcpy2DAsync(rstatus, ldo * 8, q->rs, n * 8, n * 8, 20, cudaMemcpyDeviceToHost, s));
-    if (hstart) GC_L_CUDA(cudaMemcpyAsync(hstart, q->hs, n * 8, cudaMemcpyDeviceToHost, s));
+    GC_L_CUDA(gcutil::copy_rows(c, ldc * 8, q->c, n * 8, n * 8, nspec, s));
+    GC_L_CUDA(gcutil::copy_rows(ierr, n * 4, q->ie, n * 4, n * 4, 1, s));
+    if (istatus) GC_L_CUDA(gcutil::copy_rows(istatus, ldo * 4, q->is, n * 4, n * 4, 20, s));
+    if (rstatus) GC_L_CUDA(gcutil::copy_rows(rstatus, ldo * 8, q->rs, n * 8, n * 8, 20, s));
+    if (hstart) GC_L_CUDA(gcutil::copy_rows(hstart, n * 8, q->hs, n * 8, n * 8, 1, s));
     GC_L_CUDA(cudaStreamSynchronize(s));
   }
   return GC_KPP_OK;

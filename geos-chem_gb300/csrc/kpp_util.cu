@@ -1,6 +1,9 @@
 // Small element-wise kernels of the chemistry-step boundary.
 #include "kpp_util.h"
 
+#include <algorithm>
+#include <cstdint>
+
 namespace gcutil {
 
 // C(k, cell) = MAX(C(k, cell), 0) for all species (fullchem_mod.F90:1329-1350)
@@ -19,6 +22,66 @@ cudaError_t clamp_nonneg(double* c, long long ldc, int nrows, int ncell, cudaStr
   const int block = 256;
   const long long grid = (total + block - 1) / block;
   clamp_nonneg_kernel<<<(unsigned)grid, block, 0, s>>>(c, ldc, nrows, ncell);
+  return cudaGetLastError();
+}
+
+// Rows of m elements of type V; each thread keeps four loads in flight.
+template <typename V>
+__global__ void copy_rows_kernel(char* dst, size_t dpitch, const char* src, size_t spitch, long long m,
+                                 long long rows) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long r = blockIdx.y; r < rows; r += gridDim.y) {
+    V* d = reinterpret_cast<V*>(dst + r * (long long)dpitch);
+    const V* s = reinterpret_cast<const V*>(src + r * (long long)spitch);
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < m; i += 4 * stride) {
+      const V a = s[i], b = s[i + stride], c = s[i + 2 * stride], e = s[i + 3 * stride];
+      d[i] = a;
+      d[i + stride] = b;
+      d[i + 2 * stride] = c;
+      d[i + 3 * stride] = e;
+    }
+    for (; i < m; i += stride) d[i] = s[i];
+  }
+}
+
+// The address at which the current device reaches p, or nullptr when it
+// cannot (pageable host memory).
+static void* device_alias(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return const_cast<void*>(p);
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+    // offset of p within what the attributes describe (0 when they describe p itself)
+    const char* hp = a.hostPointer ? static_cast<const char*>(a.hostPointer) : static_cast<const char*>(p);
+    return static_cast<char*>(a.devicePointer) + (static_cast<const char*>(p) - hp);
+  }
+  return nullptr;
+}
+
+cudaError_t copy_rows(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t rows,
+                      cudaStream_t s) {
+  if (rows == 0 || width == 0) return cudaSuccess;
+  void* d = device_alias(dst);
+  const void* sp = device_alias(src);
+  const size_t bits = (size_t)(uintptr_t)d | (size_t)(uintptr_t)sp | dpitch | spitch | width;
+  if (!d || !sp || (bits & 3)) return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, cudaMemcpyDefault, s);
+  const int g = (bits & 15) == 0 ? 16 : (bits & 7) == 0 ? 8 : 4;
+  const long long m = (long long)(width / g);
+  const int threads = 256;
+  const long long gx = std::min<long long>((m + 4LL * threads - 1) / (4LL * threads), 65535LL);
+  const dim3 grid((unsigned)gx, (unsigned)std::min<size_t>(rows, 65535));
+  char* dc = static_cast<char*>(d);
+  const char* sc = static_cast<const char*>(sp);
+  if (g == 16)
+    copy_rows_kernel<uint4><<<grid, threads, 0, s>>>(dc, dpitch, sc, spitch, m, (long long)rows);
+  else if (g == 8)
+    copy_rows_kernel<uint2><<<grid, threads, 0, s>>>(dc, dpitch, sc, spitch, m, (long long)rows);
+  else
+    copy_rows_kernel<unsigned><<<grid, threads, 0, s>>>(dc, dpitch, sc, spitch, m, (long long)rows);
   return cudaGetLastError();
 }
 

@@ -265,9 +265,22 @@ def build_program(ir=None):
     from .hetstate import SETSTATE_SPECIES
 
     hss = [ir["species"].index(n) if n in ir["species"] else -1 for n in SETSTATE_SPECIES]
-    return {"code": code, "start": start, "consts": pool, "nhet": nhet, "hs_ind": ind, "hs_mw": pick(spc["mw"]),
+    photol_rows = sorted({int(k) for e in ir["rconst"] for k in re.findall(r"PHOTOL\[(\d+)\]", e)})
+    return {"code": code, "start": start, "consts": pool, "nhet": nhet, "photol_rows": photol_rows,
+            "hs_ind": ind, "hs_mw": pick(spc["mw"]),
             "hs_srmw": pick(srmw), "hs_hk0": pick(spc["henry_k0"]), "hs_hcr": pick(spc["henry_cr"]),
             "hss_ind": hss, "hss_srmw": [srmw[i] if i >= 0 else 0.0 for i in hss]}
+
+
+def _runs(rows):
+    """Sorted row indices as contiguous runs [(first, last + 1), ...]."""
+    runs = []
+    for r in rows:
+        if runs and runs[-1][1] == r:
+            runs[-1][1] = r + 1
+        else:
+            runs.append([r, r + 1])
+    return [tuple(x) for x in runs]
 
 
 def emit_c(prog):
@@ -284,7 +297,12 @@ def emit_c(prog):
              "static const int hs_ind[%d] = {%s};" % (len(HET_SPECIES), ",".join(map(str, prog["hs_ind"]))),
              "static const int hss_ind[%d] = {%s};" % (len(prog["hss_ind"]), ",".join(map(str, prog["hss_ind"]))),
              "static const double hss_srmw[%d] = {%s};" % (len(prog["hss_srmw"]),
-                                                          ",".join(float(v).hex() for v in prog["hss_srmw"]))]
+                                                          ",".join(float(v).hex() for v in prog["hss_srmw"])),
+             "// PHOTOL rows that the rate program reads, as runs [first, last + 1)",
+             "constexpr int NPHOTOL_RUNS = %d;" % len(_runs(prog["photol_rows"])),
+             "static const int photol_runs[%d] = {%s};" % (
+                 max(1, 2 * len(_runs(prog["photol_rows"]))),
+                 ",".join("%d,%d" % r for r in _runs(prog["photol_rows"])) or "0")]
     for key in ("hs_mw", "hs_srmw", "hs_hk0", "hs_hcr"):
         lines.append("static const double %s[%d] = {%s};" % (key, len(HET_SPECIES),
                                                             ",".join(float(v).hex() for v in prog[key])))

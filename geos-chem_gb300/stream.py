@@ -13,6 +13,8 @@ cells), whose per-cell inputs and workspace do not fit at once.
 """
 import numpy as np
 
+from . import capi
+
 
 NMET, NPHOTOL = 18, 200
 # device bytes per cell of a chunk: inputs and outputs (two buffers each),
@@ -114,19 +116,23 @@ class Streamer:
         retried = [0]
         nb = self.nbuf
 
+        # the copies run on the SMs (gc_kpp_copy_rows reads and writes the
+        # page-locked host chunks directly), stream-ordered on the copy streams
+        cp = lambda dst, src, st: capi.copy_rows(dst, src, stream=st.cuda_stream, lib=self.solver.lib)
+
         def stage(k):
             h, b = chunks[k], self.buf[k % nb]
             m = h["c"].shape[1]
             with torch.cuda.stream(self.h2d):
                 self.h2d.wait_event(self.freed[k % nb])
                 for key in ("met", "c", "hs"):
-                    self._view(b, key, m).copy_(h[key], non_blocking=True)
+                    cp(self._view(b, key, m), h[key], self.h2d)
                 ph = self._view(b, "ph", m)
                 if self.photol_rows is None:
-                    ph.copy_(h["ph"], non_blocking=True)
+                    cp(ph, h["ph"], self.h2d)
                 else:
                     for r0, r1 in self.photol_rows:
-                        ph[r0:r1].copy_(h["ph"][r0:r1], non_blocking=True)
+                        cp(ph[r0:r1], h["ph"][r0:r1], self.h2d)
                 self.staged[k % nb].record(self.h2d)
 
         def retrieve(k):
@@ -134,10 +140,10 @@ class Streamer:
             m = h["c"].shape[1]
             with torch.cuda.stream(self.d2h):
                 self.d2h.wait_event(self.solved[k % nb])
-                h.get("c_out", h["c"]).copy_(self._view(b, "c", m), non_blocking=True)
-                h.get("hs_out", h["hs"]).copy_(self._view(b, "hs", m), non_blocking=True)
-                h["steps"].copy_(self._view(b, "ist", m)[2], non_blocking=True)
-                h["ierr"].copy_(self._view(b, "ierr", m), non_blocking=True)
+                cp(h.get("c_out", h["c"]), self._view(b, "c", m), self.d2h)
+                cp(h.get("hs_out", h["hs"]), self._view(b, "hs", m), self.d2h)
+                cp(h["steps"], self._view(b, "ist", m)[2], self.d2h)
+                cp(h["ierr"], self._view(b, "ierr", m), self.d2h)
                 self.freed[k % nb].record(self.d2h)
 
         for e in self.freed:

@@ -401,6 +401,24 @@ int gc_kpp_last_launch_count(gc_kpp_ctx* ctx);
  * launches of the last integrate/step call (waits for them to finish). */
 int gc_kpp_last_kernel_ms(gc_kpp_ctx* ctx, double* ms, int* nlaunch);
 
+/* Stream-ordered copy of `rows` rows of `width` bytes from src (row pitch
+ * spitch bytes) to dst (row pitch dpitch), each side in host or device
+ * memory of the current device.  Page-locked host memory (cudaHostAlloc,
+ * cudaHostRegister) is read and written by the GPU's SMs through its device
+ * alias; pageable host memory goes through cudaMemcpy2DAsync.  The
+ * library's own host-memory calls stage their arrays this way: on GB300,
+ * after a chemistry step a copy engine needs ~60-90 ms for the first 1 GB of
+ * a page-locked buffer and the SMs ~5-10 ms.  No counterpart in the
+ * reference (its arrays never leave the host). */
+int gc_kpp_copy_rows(void* dst, long long dpitch, const void* src, long long spitch, long long width, long long rows,
+                     void* stream);
+
+/* mask[r] = 1 for the GC_KPP_NPHOTOL rows r of PHOTOL that the mechanism's
+ * Update_RCONST reads (168 of 200 for fullchem), 0 for the others, which a
+ * caller need not send; host-memory steps copy only these rows.  No
+ * counterpart in the reference. */
+int gc_kpp_photol_rows(unsigned char* mask);
+
 #ifdef __cplusplus
 }
 #endif

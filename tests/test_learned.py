@@ -183,10 +183,24 @@ def test_learned_step_c_abi_matches_python_plan():
     ierrh = np.zeros(n, np.int32)
     _, nb_h = solver.fullchem_step_learned(cp.handle, 600.0, cells["met"], cells["photol"], ch, atol, rtol, ic, rc,
                                            hsh, isth, rsth, ierrh)
-    assert nb_d == nb_h == nb
-    for got in (got_d, [ch, hsh, isth, rsth, ierrh]):
+    # C ABI, page-locked host memory with padded rows (SM staging copies, the
+    # PHOTOL rows that the rates and features read)
+    ld = n + 5
+    pinned = lambda a, dt=torch.float64: torch.zeros(a, dtype=dt).pin_memory()
+    metp, php, cpn = pinned((18, ld)), pinned((200, ld)), pinned((cells["c"].shape[0], ld))
+    metp[:, :n] = torch.from_numpy(cells["met"])
+    php[:, :n] = torch.from_numpy(cells["photol"])
+    cpn[:, :n] = torch.from_numpy(cells["c"])
+    hsp, istp, rstp = pinned(n), pinned((20, ld), torch.int32), pinned((20, ld))
+    ierrp = pinned(n, torch.int32)
+    _, nb_p = solver.fullchem_step_learned(cp.handle, 600.0, metp[:, :n], php[:, :n], cpn[:, :n], atol, rtol, ic, rc,
+                                           hsp, istp[:, :n], rstp[:, :n], ierrp)
+    got_p = [x.numpy() for x in (cpn[:, :n], hsp, istp[:, :n], rstp[:, :n], ierrp)]
+    assert nb_d == nb_h == nb_p == nb
+    for got in (got_d, [ch, hsh, isth, rsth, ierrh], got_p):
         for a, b in zip(got, ref):
             assert np.array_equal(a, b)
+    assert np.all(cpn[:, n:].numpy() == 0) and np.all(istp[:, n:].numpy() == 0)  # padding untouched
     cp.close()
 
 
