@@ -50,6 +50,7 @@ EXPORTED = [
     "gc_kpp_update_rconst_het_batch",
     "gc_kpp_set_state_het_batch",
     "gc_kpp_sulfur_aq_rates_batch",
+    "gc_kpp_sulfur_cld_rates_batch",
     "gc_kpp_ctx_set_hetstate",
     "gc_kpp_ctx_set_autoreduce",
     "gc_kpp_fullchem_step",
@@ -98,6 +99,7 @@ def load_library(path=None, mech="fullchem"):
     lib.gc_kpp_ctx_set_autoreduce.argtypes = [vp, i32, vp, vp, vp, vp, i32]
     lib.gc_kpp_set_state_het_batch.argtypes = [vp, i32, vp, i64, vp, i64, f64, i32, i32, vp, i64, i32, vp]
     lib.gc_kpp_sulfur_aq_rates_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, i32, vp]
+    lib.gc_kpp_sulfur_cld_rates_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, i32, vp, i32, vp]
     lib.gc_kpp_copy_rows.argtypes = [vp, i64, vp, i64, i64, i64, vp]
     lib.gc_kpp_photol_rows.argtypes = [vp]
     if path == _build.lib_path(mech):
@@ -336,6 +338,25 @@ class Solver:
                                                  _ld(c, ncell), float(gamma_ho2), int(lpscchem),
                                                  int(turn_off_het_rates), _ptr(het), _ld(het, ncell),
                                                  MEM_DEVICE if dev else MEM_HOST, s)
+        self._check(rc)
+
+    def sulfur_cld_rates(self, hetin, c, met, lmetalcatso2=1, size_res=None, stream=None):
+        """Batched SET_SO2 (gc_kpp_sulfur_cld_rates_batch): K_CLD rows of met
+        [NMET, ncell] (the other rows untouched), the HSO3_aq, SO3_aq, pHCloud
+        (and fupdateHOBr/HOCl = 1) rows of hetin [NHETIN, ncell] rewritten in
+        place, size_res [ncell] int32 (optional) out.  All numpy (host) or all
+        CUDA torch tensors (device)."""
+        dev = _is_torch(met) and met.is_cuda
+        ncell = met.shape[1]
+        if not dev:
+            for a in (hetin, met):
+                if not (isinstance(a, np.ndarray) and a.flags.c_contiguous and a.dtype == np.float64):
+                    raise ValueError("host arrays written in place must be C-contiguous float64 numpy arrays")
+            c = np.ascontiguousarray(c, dtype=np.float64)
+        s = ctypes.c_void_p(stream) if stream else None
+        rc = self.lib.gc_kpp_sulfur_cld_rates_batch(self.ctx, ncell, _ptr(hetin), _ld(hetin, ncell), _ptr(c),
+                                                    _ld(c, ncell), _ptr(met), _ld(met, ncell), int(lmetalcatso2),
+                                                    _ptr(size_res), MEM_DEVICE if dev else MEM_HOST, s)
         self._check(rc)
 
     def sulfur_aq_rates(self, hetin, c, met, stream=None):

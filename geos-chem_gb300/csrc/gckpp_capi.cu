@@ -1277,6 +1277,64 @@ int gc_kpp_sulfur_aq_rates_batch(gc_kpp_ctx* c, int ncell, const double* hetin, 
   return GC_KPP_OK;
 }
 
+int gc_kpp_sulfur_cld_rates_batch(gc_kpp_ctx* c, int ncell, double* hetin, long long ldi, const double* conc,
+                                  long long ldc, double* met, long long ldm, int lmetalcatso2, int* size_res, int mem,
+                                  void* stream) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
+  if (ncell == 0) return GC_KPP_OK;
+  if (!hetin || !conc || !met) return fail(GC_KPP_EINVAL, "required array is NULL");
+  if (ldi < ncell || ldc < ncell || ldm < ncell) return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
+  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  if (lmetalcatso2 != 0 && lmetalcatso2 != 1) return fail(GC_KPP_EINVAL, "lmetalcatso2 must be 0 or 1");
+  GC_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  gchet::SulfurCldArgs a{};
+  a.ncell = ncell;
+  for (int k = 0; k < HSS_N; ++k) a.ind[k] = RT::hss_ind[k];
+  a.row_kcld = GC_KPP_MET_K_CLD;
+  a.lmetalcatso2 = lmetalcatso2;
+  const size_t n = (size_t)ncell;
+  // the rows SET_SO2 (and Set_Sulfur_Chem_Rates) write back into hetin
+  const int out_rows[] = {HETIN_HSO3_aq, HETIN_SO3_aq, HETIN_pHCloud, HETIN_fupdateHOBr, HETIN_fupdateHOCl};
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(c->h_hetin.ensure((size_t)HETIN_NFIELD * n * sizeof(double)));
+    GC_CUDA(c->h_c.ensure(T::NSPEC * n * sizeof(double)));
+    GC_CUDA(c->h_met.ensure(RT::NMET * n * sizeof(double)));
+    GC_CUDA(c->h_ie.ensure(n * sizeof(int)));
+    GC_CUDA(gcutil::copy_rows(c->h_hetin.p, n * sizeof(double), hetin, ldi * sizeof(double), n * sizeof(double),
+                              HETIN_NFIELD, s));
+    GC_CUDA(gcutil::copy_rows(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
+                              T::NSPEC, s));
+    a.in = (double*)c->h_hetin.p;
+    a.c = (const double*)c->h_c.p;
+    a.met = (double*)c->h_met.p;
+    a.ldi = a.ldc = a.ldm = ncell;
+    a.size_res = size_res ? (int*)c->h_ie.p : nullptr;
+  } else {
+    a.in = hetin;
+    a.ldi = ldi;
+    a.c = conc;
+    a.ldc = ldc;
+    a.met = met;
+    a.ldm = ldm;
+    a.size_res = size_res;
+  }
+  cudaError_t e = gchet::sulfur_cld_rates(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "SulfurCldChem kernel launch");
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(gcutil::copy_rows(met + (long long)GC_KPP_MET_K_CLD * ldm, ldm * sizeof(double),
+                              a.met + (long long)GC_KPP_MET_K_CLD * ncell, n * sizeof(double), n * sizeof(double), 6,
+                              s));
+    for (int r : out_rows)
+      GC_CUDA(gcutil::copy_rows(hetin + (long long)r * ldi, ldi * sizeof(double), a.in + (long long)r * ncell,
+                                n * sizeof(double), n * sizeof(double), 1, s));
+    if (size_res) GC_CUDA(gcutil::copy_rows(size_res, n * sizeof(int), a.size_res, n * sizeof(int), n * sizeof(int), 1, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+  }
+  return GC_KPP_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

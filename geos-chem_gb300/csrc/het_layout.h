@@ -94,7 +94,7 @@
 #define HET_TurnOffHetRates 166
 #define HET_SUNCOS 167
 // rows of the cell-interleaved fullchem_SetStateHet input array
-#define HETIN_NFIELD 100
+#define HETIN_NFIELD 111
 #define HETIN_T 0
 #define HETIN_CLDF 1
 #define HETIN_QI 2
@@ -131,6 +131,11 @@
 #define HETIN_KHETI_SLA 87  /* 11 rows */
 #define HETIN_STATE_PSC 98
 #define HETIN_SUNCOS 99
+#define HETIN_PMID_DRY 100
+#define HETIN_NH4 101
+#define HETIN_NH3 102
+#define HETIN_DSTbin 103  /* 7 rows */
+#define HETIN_pFe 110
 // KPP species read by fullchem_SetStateHet and fullchem_SulfurAqChem, in the order of the index table
 #define HSS_SO2 0
 #define HSS_HNO3 1
@@ -146,4 +151,14 @@
 #define HSS_SALAAL 11
 #define HSS_SALCAL 12
 #define HSS_O3 13
-#define HSS_N 14
+#define HSS_H2O2 14
+#define HSS_CH2O 15
+#define HSS_SO4s 16
+#define HSS_HMS 17
+#define HSS_HCOOH 18
+#define HSS_ACTA 19
+#define HSS_N 20
+// MW_g of the non-KPP species SET_SO2 reads (species database)
+#define HSS_MW_DSTbin1 29.0
+#define HSS_MW_pFe 55.85
+#define HSS_MW_SALA 31.4

@@ -10,6 +10,8 @@
 //   Cld_Params                      KPP/fullchem/rateLawUtilFuncs.F90:281-417
 //   CALC_KH, CALC_HEFF              GeosUtil/henry_mod.F90:74-204
 //   fullchem_SulfurAqChem (K_MT)    KPP/fullchem/fullchem_SulfurChemFuncs.F90:120-305
+//   fullchem_SulfurCldChem / SET_SO2 (K_CLD, cloud pH, HSO3_aq, SO3_aq)
+//                                   :320-398, 865-1620, 1635-3549
 //
 // One thread per cell.  Inputs are rows of a cell-interleaved array
 // (HETIN_* of het_layout.h); outputs the HET_NFIELD rows of the HetState
@@ -313,7 +315,299 @@ __global__ void sulfur_aq_kernel(SulfurAqArgs a) {
   for (int k = 0; k < 6; ++k) a.met[(long long)(a.row_kmt + k) * a.ldm + cell] = k_mt[k];
 }
 
+// ---------------------------------------------------------------------------
+// SET_SO2, the in-cloud branch of fullchem_SulfurCldChem
+// (KPP/fullchem/fullchem_SulfurChemFuncs.F90:865-1620): cloud pH from
+// GET_HPLUS (:1635-1853, Newton's method on the cloud water's
+// electroneutrality with the Henry/dissociation functions kCO21..dkAA and
+// CaCO3_PRECIP, :1867-3156), the aqueous S(IV) oxidation rates of
+// AQCHEM_SO2 (:3171-3549) and the Fahey and Seinfeld size_res decision.
+//
+// The Fortran functions re-evaluate their temperature-dependent constants
+// (about 40 exp() calls) at every Newton iteration; here they, and every
+// [H+]-independent leading product of the functions' expressions, are
+// evaluated once per cell (SO2Equil), and each iteration only does the
+// [H+]-dependent rest in the Fortran's order, so the values are the ones the
+// per-call evaluation gives.  Literals the Fortran writes without a kind
+// (Kc1 = 4.3e-7 ...) are default REAL there: their single-precision value.
+namespace so2 {
+
+constexpr double AIRMW = 28.9644;  // Headers/physconstants.F90:26
+constexpr double ATM = 1.01325e+5;  // :70
+constexpr double RL = 0.08205;      // the functions' gas constant [L atm/mol/K]
+
+__device__ __forceinline__ double tf(double D, double T) { return exp(D * ((1.0 / T) - (1.0 / 298.0))); }
+__device__ __forceinline__ double sq(double x) { return x * x; }
+
+// one acid (or base) with a single dissociation: kHNO3/dkHNO3, kHCl/dkHCl,
+// kFA/dkFA, kAA/dkAA share this form
+struct Mono {
+  double H_T, K_T, HK;         // Henry and dissociation constants at T; H_T * K_T
+  double XP, num_d, a1, a2;    // X*P; dk numerator; K_T*H_T*RL*T*LWC; H_T*RL*T*LWC
+  __device__ void init(double H_T_, double K_T_, double X, double P, double T, double LWC) {
+    H_T = H_T_;
+    K_T = K_T_;
+    HK = H_T * K_T;
+    XP = X * P;
+    num_d = -1.0 * K_T * H_T * X * P * (1.0 + H_T * RL * T * LWC);
+    a1 = K_T * H_T * RL * T * LWC;
+    a2 = H_T * RL * T * LWC;
+  }
+  __device__ double f(double H, double T, double LWC) const {
+    const double Heff = H_T * (1.0 + (K_T / H));
+    const double x = 1.0 / (1.0 + (Heff * RL * T * LWC));
+    return HK * (XP * x) / H;
+  }
+  __device__ double df(double H) const { return num_d / sq(a1 + a2 * H + H); }
+};
+
+// H2CO3 (CO2) or H2SO3 (SO2) with two dissociations: kCO21/kCO22/dkCO21/
+// dkCO22, kSO21/kSO22/dkSO21/dkSO22
+struct Di {
+  double H_T, K1_T, K2_T, K12, HK1, HK12;  // Henry, K1, K2 at T; K1*K2; H*K1 or K1*H; K1*K2*H
+  double XP, pre1, pre2;                   // X*P; K1*H*X*P; -1*K1*K2*H*X*P
+  double a1, a2, a3, b2;                   // K1*K2*H*RL*T*LWC; H*RL*T*LWC; K1*H*RL*T*LWC; 2*H*RL*T*LWC
+  __device__ void init(double H_T_, double K1_T_, double K2_T_, double X, double P, double T, double LWC, bool so2) {
+    H_T = H_T_;
+    K1_T = K1_T_;
+    K2_T = K2_T_;
+    K12 = K1_T * K2_T;
+    HK1 = so2 ? H_T * K1_T : 0.0;  // kSO21 multiplies Hso2_T * Ks1_T first
+    HK12 = K1_T * K2_T * H_T;
+    XP = X * P;
+    pre1 = K1_T * H_T * X * P;
+    pre2 = -1.0 * K1_T * K2_T * H_T * X * P;
+    a1 = K1_T * K2_T * H_T * RL * T * LWC;
+    a2 = H_T * RL * T * LWC;
+    a3 = K1_T * H_T * RL * T * LWC;
+    b2 = 2.0 * H_T * RL * T * LWC;
+  }
+  // partial pressure X * P * x of the gas at [H+] = H
+  __device__ double pgas(double H, double T, double LWC) const {
+    const double Heff = H_T * (1.0 + (K1_T / H) + (K12 / (H * H)));
+    const double x = 1.0 / (1.0 + (Heff * RL * T * LWC));
+    return XP * x;
+  }
+  __device__ double den(double H) const { return sq(a1 + a3 * H + a2 * H * H + H * H); }
+  __device__ double d1(double H, double dn) const { return pre1 * (a1 - a2 * H * H - H * H) / dn; }
+  __device__ double d2(double H, double dn) const { return pre2 * (a3 + b2 * H + 2.0 * H) / dn; }
+};
+
+// The [H+]-independent part of GET_HPLUS's functions for one cell.
+struct SO2Equil {
+  Di co2, so2;
+  Mono hno3, hcl, fa, aa;
+  double Hnh3_T, Ka1_T, NH3P, nh3_num, nh3_a2;  // kNH3 / dkNH3
+  double Ksp_T, ca_den, Ksp2;                    // CaCO3_PRECIP
+  double Kw_T;
+};
+
+__device__ void equil_init(SO2Equil& E, double T, double P, double LWC, double SO2, double TNO3, double TNH3,
+                           double CL, double TFA, double TAA) {
+  const double CO2 = 390.0e-6;
+  // kCO2x: Kc1 = 4.3e-7, Kc2 = 4.68e-11, Hco2 = 3.4e-2 (single precision)
+  E.co2.init((double)3.4e-2f * tf(2.44e+3, T), (double)4.3e-7f * tf(-1000.0, T), (double)4.68e-11f * tf(-1760.0, T),
+             CO2, P, T, LWC, false);
+  // kSO2x: Ks1 = 1.3e-2, Ks2 = 6.6e-8, Hso2 = 1.23 (single precision)
+  E.so2.init((double)1.23f * tf(3.14e+3, T), (double)1.3e-2f * tf(1960.0, T), (double)6.6e-8f * tf(1500.0, T), SO2,
+             P, T, LWC, true);
+  // kHNO3: Kn1 = 15.4, Hhno3 = 2.1e5 (single precision), Dhhno3 = 0
+  E.hno3.init((double)2.1e5f * tf(0.0, T), (double)15.4f * tf(8700.0, T), TNO3, P, T, LWC);
+  E.hcl.init(1.5e+3 * tf(2.3e+3, T), 1.74e+6 * tf(6900.0, T), CL, P, T, LWC);
+  E.fa.init(8800.0 * tf(6100.0, T), 1.8e-4 * tf(151.0, T), TFA, P, T, LWC);
+  E.aa.init(4100.0 * tf(6200.0, T), 1.75e-5 * tf(50.0, T), TAA, P, T, LWC);
+  // kNH3: Ka1 = 1.7e-5 (single precision), Hnh3 = 60
+  E.Kw_T = 1.0e-14 * exp(-6710.0 * ((1.0 / T) - (1.0 / 298.0)));
+  E.Hnh3_T = 60.0 * tf(4200.0, T);
+  E.Ka1_T = (double)1.7e-5f * tf(-450.0, T);
+  E.NH3P = TNH3 * P;
+  E.nh3_num = E.Ka1_T * E.Hnh3_T * TNH3 * E.Kw_T * P * (1.0 + E.Hnh3_T * RL * T * LWC);
+  E.nh3_a2 = E.Hnh3_T * RL * T * LWC;
+  // CaCO3_PRECIP (double-precision constants)
+  const double Hco2_T = 3.4e-2 * tf(2.44e+3, T), Kc1_T = 4.3e-7 * tf(-1000.0, T), Kc2_T = 4.68e-11 * tf(-1760.0, T);
+  E.Ksp_T = 3.3e-9 * tf(-1200.0, T);
+  E.ca_den = Kc1_T * Kc2_T * Hco2_T * CO2 * P;
+  E.Ksp2 = 2.0 * E.Ksp_T;
+}
+
+// GET_HPLUS: [H+] of the cloud water; *niter = Newton iterations
+__device__ double get_hplus(const SO2Equil& E, double SO4nss, double TNA, double TDCA, double T, double LWC,
+                            double iHPLUS, int* niter) {
+  const double Kw = 1.0e-14, MINVAL_ = (double)0.01f;
+  double ipH = -log10(iHPLUS), newpH = 0.0;
+  int count = 0;
+  while (fabs(ipH - newpH) > MINVAL_) {
+    count = count + 1;
+    if (count != 1) ipH = newpH;
+    const double H = pow(10.0, -ipH);
+    // f(x) terms
+    const double pco2 = E.co2.pgas(H, T, LWC);
+    const double fHCO3 = E.co2.H_T / H * E.co2.K1_T * pco2;
+    const double fCO3 = E.co2.HK12 / H / H * pco2;
+    const double pso2 = E.so2.pgas(H, T, LWC);
+    const double fHSO3 = E.so2.HK1 * pso2 / H;
+    const double fSO3 = E.so2.HK12 / H / H * pso2;
+    const double fHNO3 = E.hno3.f(H, T, LWC);
+    const double Hnh3eff = E.Hnh3_T * (1.0 + ((E.Ka1_T * H) / E.Kw_T));
+    const double xNH3 = 1.0 / (1.0 + (Hnh3eff * RL * T * LWC));
+    const double fNH4 = H * E.Hnh3_T * E.Ka1_T * (E.NH3P * xNH3) / E.Kw_T;
+    const double fHCl = E.hcl.f(H, T, LWC);
+    const double fFA = E.fa.f(H, T, LWC);
+    const double fAA = E.aa.f(H, T, LWC);
+    // f'(x) terms
+    const double dnc = E.co2.den(H), dns = E.so2.den(H);
+    const double dHCO3 = E.co2.d1(H, dnc), dCO3 = E.co2.d2(H, dnc);
+    const double dHSO3 = E.so2.d1(H, dns), dSO3 = E.so2.d2(H, dns);
+    const double dHNO3 = E.hno3.df(H);
+    const double dNH4 = E.nh3_num / sq(E.nh3_a2 * (E.Kw_T + E.Ka1_T * H) + E.Kw_T);
+    const double dHCl = E.hcl.df(H), dFA = E.fa.df(H), dAA = E.aa.df(H);
+    // CaCO3_PRECIP
+    const double fCa = E.Ksp_T * H * H / E.ca_den;
+    const double dCa = E.Ksp2 * H / E.ca_den;
+    double f, df;
+    if (fCa >= TDCA) {
+      const double D = (2.0 * SO4nss) - (TNA + 2.0 * TDCA);
+      f = D - H + Kw / H + fHCO3 + 2.0 * fCO3 + fHSO3 + 2.0 * fSO3 + fHNO3 - fNH4 + fHCl + fFA + fAA;
+      df = -1.0 - Kw / H / H + dHCO3 + 2.0 * dCO3 + dHSO3 + 2.0 * dSO3 + dHNO3 - dNH4 + dHCl + dFA + dAA;
+    } else {
+      const double D = (2.0 * SO4nss) - TNA;
+      f = D - H + Kw / H + fHCO3 + 2.0 * fCO3 + fHSO3 + 2.0 * fSO3 + fHNO3 - fNH4 + fHCl + fFA + fAA - 2.0 * fCa;
+      df = -1.0 - Kw / H / H + dHCO3 + 2.0 * dCO3 + dHSO3 + 2.0 * dSO3 + dHNO3 - dNH4 + dHCl + dFA + dAA - 2.0 * dCa;
+    }
+    double nn = H - f / df;
+    nn = fmax(nn, 1.0e-14);
+    nn = fmin(nn, 1.0e-1);
+    if (count > 50) {
+      newpH = ((-log10(nn)) + (-log10(H))) / 2.0;
+      break;
+    }
+    newpH = -log10(nn);
+    if (isnan(newpH)) break;  // the reference stops the model here
+  }
+  *niter = count;
+  return pow(10.0, -newpH);
+}
+
+__global__ void sulfur_cld_kernel(SulfurCldArgs a) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= a.ncell) return;
+  auto in = [&](int f) { return a.in[(long long)f * a.ldi + cell]; };
+  auto c = [&](int sp) {
+    const int i = a.ind[sp];
+    return i >= 0 ? a.c[(long long)i * a.ldc + cell] : 0.0;
+  };
+  double kcld[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double hso3 = 1.0e-32, so3 = 1.0e-32, phcloud = 0.0;
+  int size_res = 0, niter = 0;
+  const double RHO = in(HETIN_AIRDEN);
+  const double CNVFAC = 1.E3 * AIRMW / (RHO * AVO);  // molec/cm3 -> v/v
+  const double SO2_AfterSS = c(HSS_SO2) * CNVFAC;
+  const double H2O20 = c(HSS_H2O2) * CNVFAC;
+  const double PATM = in(HETIN_PMID_DRY) / (ATM * 1.e-2);
+  const double TK = in(HETIN_T), FC = in(HETIN_CLDF);
+  double LWC = in(HETIN_QL) * in(HETIN_AIRDEN) * 1e-3;
+  LWC = fmax(0.0, LWC);
+  LWC = gcrates::SafeDiv(LWC, FC, 0.0);
+  if ((FC > 1.0e-4) && (SO2_AfterSS > 1.e-20) && (TK > 258.0) && (LWC > 1.0e-20)) {
+    const double SO4nss = 1.e+3 * (c(HSS_SO4) * 0.7 + c(HSS_SO4s)) / (LWC * AVO);
+    const double TNH3 = ((in(HETIN_NH4) * 0.7) + in(HETIN_NH3)) * CNVFAC;
+    double CL = (c(HSS_SALACL) * 0.7) + c(HSS_SALCCL);
+    CL = (CL + c(HSS_HCl)) * CNVFAC;
+    const double TFA = c(HSS_HCOOH) * CNVFAC, TAA = c(HSS_ACTA) * CNVFAC;
+    const double TNA = 1.e3 * (in(HETIN_SALA) * 0.7 + in(HETIN_SALC)) * (31.6 * 0.359 / 23.0) / (LWC * AVO);
+    double dsum = in(HETIN_DSTbin);
+    for (int b = 1; b < 7; ++b) dsum = dsum + in(HETIN_DSTbin + b);
+    const double DUST = dsum * 1.e+15 * HSS_MW_DSTbin1 / AVO;
+    const double TDCA = DUST * 2.22e-15 / LWC;
+    const double TNO3 = (c(HSS_HNO3) + (c(HSS_NIT) * 0.7) + c(HSS_NITs)) * CNVFAC;
+    SO2Equil E;
+    equil_init(E, TK, PATM, LWC, SO2_AfterSS, TNO3, TNH3, CL, TFA, TAA);
+    const double HPLUS = get_hplus(E, SO4nss, TNA, TDCA, TK, LWC, 3.16227766016837953e-5, &niter);
+    phcloud = -1.0 * log10(HPLUS);
+    double FeIII = 0.0, MnII = 0.0;
+    if (a.lmetalcatso2) {
+      const double Fe_nat = DUST * 35e-3;
+      const double Mn_nat = Fe_nat / 50.0;
+      const double Fe_ant = in(HETIN_pFe) * CNVFAC * 1.e+12 * in(HETIN_AD) / (AIRMW / HSS_MW_pFe) / in(HETIN_AIRVOL);
+      const double Mn_ant = Fe_ant / 10.0;
+      const double Mn_tot = Mn_ant + Mn_nat;
+      const double Mn_d = Mn_tot * 1e-9 / 54.94 / LWC * 1e-3 * 0.5;  // LWC > 0 in this branch
+      const double Fe_d_ant = Fe_ant * 1e-9 / HSS_MW_pFe / LWC * 1e-3;
+      const double Fe_d_nat = Fe_nat * 1e-9 / HSS_MW_pFe / LWC * 1e-3;
+      const double Fe_d = Fe_d_ant * 0.1 + Fe_d_nat * 0.01;
+      FeIII = in(HETIN_SUNCOS) > 0.0 ? Fe_d * 0.1 : Fe_d * 0.9;
+      MnII = Mn_d;
+    }
+    // AQCHEM_SO2
+    const double T = TK, P = PATM, Hplus = HPLUS;
+    const double KH2O2 = 6.31e+14 * exp(-4.76e+3 / T);
+    const double Ks1 = 1.30e-2 * exp(6.75 * (298.15 / T - 1.0));
+    const double Ks2 = 6.31e-8 * exp(5.05 * (298.15 / T - 1.0));
+    const double XSO2aq = 1.0 / (1.0 + Ks1 / Hplus + Ks1 * Ks2 / (Hplus * Hplus));
+    const double XHSO3 = 1.0 / (1.0 + Hplus / Ks1 + Ks2 / Hplus);
+    const double XSO3 = 1.0 / (1.0 + Hplus / Ks2 + Hplus * Hplus / (Ks1 * Ks2));
+    const double HCSO2 = 1.22 * exp(10.55 * (298.15 / T - 1.0));
+    const double FHCSO2 = HCSO2 * (1.0 + (Ks1 / Hplus) + (Ks1 * Ks2 / (Hplus * Hplus)));
+    const double XSO2g = 1.0 / (1.0 + (FHCSO2 * RL * T * LWC));
+    const double SIV = FHCSO2 * XSO2g * SO2_AfterSS * P;
+    const double Kh1 = 2.20e-12 * exp(-12.52 * (298.15 / T - 1.0));
+    const double HCH2O2 = 7.45e+4 * exp(22.21 * (298.15 / T - 1.0));
+    const double FHCH2O2 = HCH2O2 * (1.0 + (Kh1 / Hplus));
+    const double XH2O2g = 1.0 / (1.0 + (FHCH2O2 * RL * T * LWC));
+    const double KaqH2O2 = KH2O2 * Ks1 * FHCH2O2 * HCSO2 * XH2O2g * XSO2g * P * LWC * RL * T;
+    const double KO0 = 2.40e+4, KO1 = 3.49e+12 * exp(-4.83e+3 / T), KO2 = 7.32e+14 * exp(-4.03e+3 / T);
+    const double HCO3 = 1.13e-2 * exp(8.51 * (298.15 / T - 1.0));
+    const double XO3g = 1.0 / (1.0 + (HCO3 * RL * T * LWC));
+    const double KaqO3 = (KO0 * XSO2aq + KO1 * XHSO3 + KO2 * XSO3) * FHCSO2 * XSO2g * P * HCO3 * XO3g * LWC * RL * T;
+    const double KaqO2 = FHCSO2 * XSO2g * ((750.0 * MnII) + (2600.0 * FeIII) + (1e+10 * MnII * FeIII)) * LWC * RL * T;
+    const double KHCHO1 = 7.9e+2 * exp(-16.44 * (298.15 / T - 1.0));
+    const double KHCHO2 = 2.5e+7 * exp(-6.04 * (298.15 / T - 1.0));
+    const double KHMS = 3.6e+3 * exp(-15.09 * (298.15 / T - 1.0));
+    const double KHMS2 = 2.65e+8 * exp(-5.03 * (298.15 / T - 1.0));
+    const double Khc1 = 2.53e+3 * exp(13.48 * (298.15 / T - 1.0));
+    const double Kw1 = 1e-14 * exp(-22.51 * (298.15 / T - 1.0));
+    const double HCHCHO = 2.5 * exp(21.6 * (298.15 / T - 1.0));
+    const double FHCHCHO = HCHCHO * (1.0 + Khc1);
+    const double XHCHOg = 1.0 / (1.0 + (FHCHCHO * RL * T * LWC));
+    const double KaqHCHO = (KHCHO1 * XHSO3 + KHCHO2 * XSO3) * FHCSO2 * XSO2g * P * HCHCHO * XHCHOg * LWC * RL * T;
+    const double KaqHMS = KHMS * (Kw1 / Hplus) * 0.7;
+    const double KaqHMS2 = KHMS2 * 1.0e-19 * 0.7;
+    kcld[0] = KaqH2O2 * FC * CNVFAC;
+    kcld[1] = KaqO3 * FC * CNVFAC;
+    kcld[2] = KaqO2 * FC;
+    kcld[3] = KaqHCHO * FC * CNVFAC;
+    kcld[4] = KaqHMS * FC;
+    kcld[5] = KaqHMS2 * FC / c(HSS_SO2);
+    // Fahey and Seinfeld's decision (:1421-1540).  size_res starts false;
+    // the first branch keeps it false, the second (LWC < 0.1e-6) sets it,
+    // and every other branch only ever sets it false again (its final ELSE
+    // is unreachable: LWC is a number > 1e-20 here).  So the alkalinity,
+    // NH3 and HNO3 tests of those branches cannot change the result and are
+    // not evaluated.
+    size_res = (!(H2O20 > SO2_AfterSS + 1e-9) && LWC < 0.1e-6) ? 1 : 0;
+    hso3 = SIV * XHSO3;
+    so3 = SIV * XSO3;
+  }
+  for (int k = 0; k < 6; ++k) a.met[(long long)(a.row_kcld + k) * a.ldm + cell] = kcld[k];
+  a.in[(long long)HETIN_HSO3_aq * a.ldi + cell] = hso3;
+  a.in[(long long)HETIN_SO3_aq * a.ldi + cell] = so3;
+  a.in[(long long)HETIN_pHCloud * a.ldi + cell] = phcloud;
+  a.in[(long long)HETIN_fupdateHOBr * a.ldi + cell] = 1.0;
+  a.in[(long long)HETIN_fupdateHOCl * a.ldi + cell] = 1.0;
+  if (a.size_res) a.size_res[cell] = size_res;
+  if (a.niter) a.niter[cell] = niter;
+}
+
+}  // namespace so2
+
 }  // namespace
+
+cudaError_t sulfur_cld_rates(const SulfurCldArgs& a, cudaStream_t s) {
+  if (a.ncell <= 0) return cudaSuccess;
+  const int block = 128;
+  so2::sulfur_cld_kernel<<<(a.ncell + block - 1) / block, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
 
 cudaError_t sulfur_aq_rates(const SulfurAqArgs& a, cudaStream_t s) {
   if (a.ncell <= 0) return cudaSuccess;

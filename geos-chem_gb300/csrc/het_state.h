@@ -40,4 +40,27 @@ struct SulfurAqArgs {
 
 cudaError_t sulfur_aq_rates(const SulfurAqArgs& a, cudaStream_t s);
 
+// SET_SO2 (fullchem_SulfurCldChem): K_CLD(1:6) of the in-cloud sulfur
+// chemistry into the K_CLD rows of met; the cloud water's HSO3-, SO3-- and
+// pH into the HSO3_aq, SO3_aq and pHCloud rows of `in` (which
+// fullchem_SetStateHet reads next) and fupdateHOBr/HOCl = 1 there, as
+// Set_Sulfur_Chem_Rates leaves them; Fahey and Seinfeld's size_res (whether
+// HetDropChem would run) per cell.
+struct SulfurCldArgs {
+  int ncell;
+  double* in;        // HETIN_NFIELD rows: read, and the rows above written
+  long long ldi;
+  const double* c;   // NSPEC rows
+  long long ldc;
+  int ind[HSS_N];    // KPP index of each HSS_* species
+  double* met;       // K_CLD rows written, the others untouched
+  long long ldm;
+  int row_kcld;
+  int* size_res;     // [ncell] out, or nullptr
+  int* niter;        // [ncell] GET_HPLUS Newton iterations (0 outside cloud), or nullptr
+  int lmetalcatso2;  // Input_Opt%LMETALCATSO2
+};
+
+cudaError_t sulfur_cld_rates(const SulfurCldArgs& a, cudaStream_t s);
+
 }  // namespace gchet

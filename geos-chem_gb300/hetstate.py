@@ -57,16 +57,22 @@ NFIELD = _o
 DU1, SUL, BKC, ORC, SSA, SSC, SLA, IIC = 1, 8, 9, 10, 11, 12, 13, 14
 
 
-# Inputs of fullchem_SetStateHet (KPP/fullchem/fullchem_HetStateFuncs.F90:48-244)
-# per cell, as rows of a cell-interleaved array ``hetin[f * ldi + cell]``:
-# the State_Met and State_Chm fields it reads for the grid box, in its units
-# (State_Met: T [K], CLDF [1], QI/QL [kg/kg], AIRVOL [m3], AIRDEN [kg/m3],
-# AD [kg], FRLAND/FROCEAN [1], InStratosphere 0/1; State_Chm: aerosol areas
-# [cm2/cm3], radii [cm], AeroH2O [cm3/m3], ISORROPIA/HETP water, molalities,
-# H+ and pH, cloud pH, HSO3_aq/SO3_aq [mol/L], the sea-salt species SALA,
-# SALAAL, SALC, SALCAL (any one unit: only their ratios are used),
-# fupdateHOBr/HOCl, KHETI_SLA, STATE_PSC), and SUNCOS, which is copied to
-# the HetState array's last row.  The KPP species it reads come from C.
+# Grid-box inputs of the per-cell producers before Update_RCONST --
+# fullchem_SetStateHet (KPP/fullchem/fullchem_HetStateFuncs.F90:48-244),
+# fullchem_SulfurAqChem and fullchem_SulfurCldChem / SET_SO2
+# (KPP/fullchem/fullchem_SulfurChemFuncs.F90:120-305, 865-1620) -- per cell,
+# as rows of a cell-interleaved array ``hetin[f * ldi + cell]``: the State_Met
+# and State_Chm fields they read, in their units (State_Met: T [K], CLDF [1],
+# QI/QL [kg/kg], AIRVOL [m3], AIRDEN [kg/m3], AD [kg], FRLAND/FROCEAN [1],
+# InStratosphere 0/1, PMID_DRY [hPa]; State_Chm: aerosol areas [cm2/cm3],
+# radii [cm], AeroH2O [cm3/m3], ISORROPIA/HETP water, molalities, H+ and pH,
+# cloud pH, HSO3_aq/SO3_aq [mol/L], fupdateHOBr/HOCl, KHETI_SLA, STATE_PSC,
+# and the concentrations [molec/cm3] of the species that are not KPP
+# species: sea salt SALA, SALAAL, SALC, SALCAL, NH4, NH3, the seven dust
+# bins, pFe), and SUNCOS, which is copied to the HetState array's last row.
+# The KPP species they read come from C.  SET_SO2 writes HSO3_aq, SO3_aq and
+# pHCloud, and Set_Sulfur_Chem_Rates sets fupdateHOBr/HOCl to 1, before
+# fullchem_SetStateHet reads them (GeosCore/fullchem_mod.F90:861-936).
 HETIN_FIELDS = [
     ("T", 1), ("CLDF", 1), ("QI", 1), ("QL", 1), ("AIRVOL", 1), ("AIRDEN", 1), ("AD", 1), ("FRLAND", 1),
     ("FROCEAN", 1), ("InStratosphere", 1), ("aClArea", 1), ("aClRadi", 1), ("IsorropAeroH2O", 2),
@@ -74,6 +80,8 @@ HETIN_FIELDS = [
     ("HSO3_aq", 1), ("SO3_aq", 1), ("IsorropBisulfate", 1), ("IsorropNitrate", 1), ("IsorropSulfate", 1),
     ("IsorropHplus", 1), ("pHCloud", 1), ("IsorropAeropH", 2), ("SALA", 1), ("SALAAL", 1), ("SALC", 1),
     ("SALCAL", 1), ("fupdateHOBr", 1), ("fupdateHOCl", 1), ("KHETI_SLA", 11), ("STATE_PSC", 1), ("SUNCOS", 1),
+    # read by SET_SO2 only
+    ("PMID_DRY", 1), ("NH4", 1), ("NH3", 1), ("DSTbin", 7), ("pFe", 1),
 ]
 HETIN_OFFSET = {}
 _o = 0
@@ -84,7 +92,10 @@ NHETIN = _o
 # KPP species that fullchem_SetStateHet and fullchem_SulfurAqChem read
 # through C(ind_X)
 SETSTATE_SPECIES = ["SO2", "HNO3", "HCl", "HBr", "BrSALA", "BrSALC", "SALACL", "SALCCL", "NIT", "NITs", "SO4",
-                    "SALAAL", "SALCAL", "O3"]
+                    "SALAAL", "SALCAL", "O3", "H2O2", "CH2O", "SO4s", "HMS", "HCOOH", "ACTA"]
+# MW_g of the non-KPP species whose mass SET_SO2 converts (run/shared/
+# species_database.yml: DSTbin1, pFe, SALA)
+NONKPP_MW = {"DSTbin1": 29.0, "pFe": 55.85, "SALA": 31.4}
 
 
 def emit_c():
@@ -102,6 +113,9 @@ def emit_c():
     for k, name in enumerate(SETSTATE_SPECIES):
         lines.append("#define HSS_%s %d" % (name, k))
     lines.append("#define HSS_N %d" % len(SETSTATE_SPECIES))
+    lines.append("// MW_g of the non-KPP species SET_SO2 reads (species database)")
+    for name, mw in NONKPP_MW.items():
+        lines.append("#define HSS_MW_%s %r" % (name, mw))
     return "\n".join(lines) + "\n"
 
 
@@ -260,13 +274,19 @@ def hetin_cells(n, seed=0, strat_fraction=0.15, cloud_fraction=0.5):
     h[o["pHCloud"]] = np.where(cloudy, rng.uniform(3.0, 6.5, n), 0.0)
     h[o["IsorropAeropH"]] = rng.uniform(1.0, 8.0, n)
     h[o["IsorropAeropH"] + 1] = rng.uniform(1.0, 8.0, n)
-    h[o["SALA"]] = lu(1e-3, 10.0)
+    h[o["SALA"]] = lu(1e5, 1e11)
     h[o["SALAAL"]] = h[o["SALA"]] * np.where(rng.uniform(size=n) < 0.5, rng.uniform(0.0, 1.2, n), 0.0)
-    h[o["SALC"]] = np.where(rng.uniform(size=n) < 0.9, lu(1e-3, 10.0), 0.0)
+    h[o["SALC"]] = np.where(rng.uniform(size=n) < 0.9, lu(1e5, 1e11), 0.0)
     h[o["SALCAL"]] = h[o["SALC"]] * rng.uniform(0.0, 0.05, n)
     h[o["fupdateHOBr"]] = rng.uniform(0.5, 1.0, n)
     h[o["fupdateHOCl"]] = rng.uniform(0.5, 1.0, n)
     h[o["KHETI_SLA"]:o["KHETI_SLA"] + 11] = lu(1e-12, 1e-5, (11, n)) * strat
     h[o["STATE_PSC"]] = np.where(strat, rng.integers(0, 4, n), 0)
     h[o["SUNCOS"]] = rng.uniform(-1.0, 1.0, n)
+    # dry pressure from density and temperature (R_dry = 287.05 J/kg/K)
+    h[o["PMID_DRY"]] = h[o["AIRDEN"]] * 287.05 * h[o["T"]] / 100.0
+    h[o["NH4"]] = lu(1e6, 1e11)
+    h[o["NH3"]] = lu(1e6, 1e11)
+    h[o["DSTbin"]:o["DSTbin"] + 7] = lu(1e2, 1e8, (7, n)) * (rng.uniform(size=n) < 0.7)
+    h[o["pFe"]] = lu(1e1, 1e6)
     return h

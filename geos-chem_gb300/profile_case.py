@@ -41,6 +41,9 @@ def main(argv=None):
                     help="block-per-cell kernel form (GC_KPP_OPT_BLOCK_SPLIT 1 or 0)")
     ap.add_argument("--repeat", type=int, default=1,
                     help="grid step: run the timed step this many times from the same state (the last is reported)")
+    ap.add_argument("--copies", action="store_true",
+                    help="grid step: after it, time 1 GB host<->device copies of page-locked buffers by the copy "
+                         "engine and by gc_kpp_copy_rows (SM copies), each right after a step")
     ap.add_argument("--probe", action="store_true")
     ap.add_argument("--routines", type=int, default=0,
                     help="> 0: only launch each mechanism routine once over this many cells (decomp, solve, "
@@ -152,6 +155,36 @@ def main(argv=None):
         sel = order[:nb].long().cpu().numpy()
         print("block-per-cell cells %d: ISTATUS sums %s" % (nb, ih[:8, sel].sum(axis=1).tolist()))
     print("algorithmic FP64 flops %.4e" % flops)
+    if args.copies and args.grid:
+        # first pass over a page-locked buffer right after a chemistry step:
+        # copy engine against SM copies, each direction
+        nb_ = 1 << 27
+        bufs = [torch.ones(nb_, dtype=torch.float64).pin_memory() for _ in range(2)]
+        dbuf = torch.empty(nb_, dtype=torch.float64, device=dev)
+
+        def ev_time(fn):
+            torch.cuda.synchronize()
+            t0.record()
+            fn()
+            t1.record()
+            torch.cuda.synchronize()
+            return t0.elapsed_time(t1)
+
+        def again():
+            c.copy_(c0)
+            hs.copy_(hs0)
+            s.fullchem_step(1200.0, met, ph, c, at, rt, ic_t, rc_t, hs, ist, rst, ierr, order=order, nblock=nb)
+            torch.cuda.synchronize()
+
+        for rep in range(2):
+            again()
+            ce = ev_time(lambda: dbuf.copy_(bufs[0], non_blocking=True))
+            smc = ev_time(lambda: capi.copy_rows(dbuf, bufs[1], lib=s.lib))
+            again()
+            ce2 = ev_time(lambda: bufs[0].copy_(dbuf, non_blocking=True))
+            smc2 = ev_time(lambda: capi.copy_rows(bufs[1], dbuf, lib=s.lib))
+            print("1 GB after a step: host->device copy engine %.1f ms, SM copy %.1f ms; device->host copy engine "
+                  "%.1f ms, SM copy %.1f ms" % (ce, smc, ce2, smc2))
     if args.probe:
         probe = ctypes.CDLL(build.probe_path())
         probe.gc_probe_fp64_gflops.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]

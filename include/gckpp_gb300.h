@@ -198,17 +198,20 @@ int gc_kpp_update_rconst_batch(gc_kpp_ctx* ctx, int ncell, const double* met, lo
  * species database and RELHUM from TEMP and H2O as Set_Kpp_GridBox_Values
  * computes it.  Mechanisms other than fullchem keep their heterogeneous
  * rates at 0. */
-/* Rows of the input array of gc_kpp_set_state_het_batch: the State_Met and
- * State_Chm fields of the grid box that fullchem_SetStateHet reads, in its
- * units (T, CLDF, QI, QL, AIRVOL, AIRDEN, AD, FRLAND, FROCEAN,
- * InStratosphere, aClArea, aClRadi, IsorropAeroH2O(2), AeroArea(14),
- * AeroRadi(14), WetAeroArea(14), AeroH2O(14), OMOC_POA, OMOC_OPOA, HSO3_aq,
- * SO3_aq, IsorropBisulfate, IsorropNitrate, IsorropSulfate, IsorropHplus,
- * pHCloud, IsorropAeropH(2), the sea-salt species SALA, SALAAL, SALC,
- * SALCAL, fupdateHOBr, fupdateHOCl, KHETI_SLA(11), STATE_PSC), then SUNCOS;
- * 100 rows.  Row offsets: the HETIN_* macros of
+/* Rows of the grid-box input array of gc_kpp_set_state_het_batch,
+ * gc_kpp_sulfur_aq_rates_batch and gc_kpp_sulfur_cld_rates_batch: the
+ * State_Met and State_Chm fields of the grid box that fullchem_SetStateHet,
+ * fullchem_SulfurAqChem and SET_SO2 read, in their units (T, CLDF, QI, QL,
+ * AIRVOL, AIRDEN, AD, FRLAND, FROCEAN, InStratosphere, aClArea, aClRadi,
+ * IsorropAeroH2O(2), AeroArea(14), AeroRadi(14), WetAeroArea(14),
+ * AeroH2O(14), OMOC_POA, OMOC_OPOA, HSO3_aq, SO3_aq, IsorropBisulfate,
+ * IsorropNitrate, IsorropSulfate, IsorropHplus, pHCloud, IsorropAeropH(2),
+ * the sea-salt species SALA, SALAAL, SALC, SALCAL [molec/cm3],
+ * fupdateHOBr, fupdateHOCl, KHETI_SLA(11), STATE_PSC), then SUNCOS, then
+ * SET_SO2's PMID_DRY [hPa] and the non-KPP species NH4, NH3, DSTbin1..7,
+ * pFe [molec/cm3]; 111 rows.  Row offsets: the HETIN_* macros of
  * geos-chem_gb300/csrc/het_layout.h. */
-#define GC_KPP_NHETIN 100
+#define GC_KPP_NHETIN 111
 
 /* Batched fullChem_SetStateHet (KPP/fullchem/fullchem_HetStateFuncs.F90:
  * 48-244, with Cld_Params, Get_Theta_Ice and Halide_Conc; called at
@@ -234,7 +237,9 @@ int gc_kpp_set_state_het_batch(gc_kpp_ctx* ctx, int ncell, const double* hetin, 
  * 861): K_MT(1:6), the uptake of SO2 (by O3), HCl and HNO3 on alkaline fine
  * and coarse sea salt, from the wet area and radius of aerosol types 11 and
  * 12 (AeroArea/WetAeroArea/AeroRadi rows of hetin) and C(SALAAL), C(SALCAL),
- * C(O3), C(SO2), C(HCl), C(HNO3).
+ * C(O3), C(SO2), C(HCl), C(HNO3) -- C as fullchem_ConvertAlkToEquiv leaves
+ * it before the call (SALAAL and SALCAL times MW * 7e-5, fullchem_mod.F90's
+ * Set_Sulfur_Chem_Rates; the caller converts them, and back after the solve).
  *
  *   met  [GC_KPP_NMET][ldm]  in/out  TEMP and NUMDEN read; the six K_MT rows
  *                                     (GC_KPP_MET_K_MT..+5) written, the
@@ -242,6 +247,36 @@ int gc_kpp_set_state_het_batch(gc_kpp_ctx* ctx, int ncell, const double* hetin, 
 int gc_kpp_sulfur_aq_rates_batch(gc_kpp_ctx* ctx, int ncell, const double* hetin, long long ldi,
                                  const double* c, long long ldc, double* met, long long ldm, int mem,
                                  void* stream);
+
+/* Batched fullchem_SulfurCldChem, i.e. SET_SO2
+ * (KPP/fullchem/fullchem_SulfurChemFuncs.F90:320-398 and 865-1620, with
+ * GET_HPLUS :1635-1853, its equilibrium functions :1867-3156 and AQCHEM_SO2
+ * :3171-3549; called from Set_Sulfur_Chem_Rates at GeosCore/fullchem_mod.F90:
+ * 861 after fullchem_SulfurAqChem): for cloudy cells (CLDF > 1e-4,
+ * T > 258 K, in-cloud liquid water > 1e-20, SO2 present) the cloud water's
+ * pH by Newton's method on its electroneutrality, then K_CLD(1:6), the
+ * aqueous oxidation of S(IV) by H2O2, O3, O2 (metal catalysed, when
+ * lmetalcatso2 = Input_Opt%LMETALCATSO2 = 1) and HCHO and the HMS rates.
+ *
+ *   hetin [GC_KPP_NHETIN][ldi] in/out  grid-box fields (rows above); the
+ *                                      HSO3_aq, SO3_aq and pHCloud rows are
+ *                                      overwritten (1e-32, 1e-32, 0 outside
+ *                                      cloud) and fupdateHOBr/HOCl set to 1,
+ *                                      as Set_Sulfur_Chem_Rates leaves them
+ *                                      for fullchem_SetStateHet
+ *   c     [NSPEC][ldc]  in            KPP concentrations (SO2, H2O2, O3,
+ *                                      CH2O, SO4, SO4s, HMS, SALACL, SALCCL,
+ *                                      HCl, HCOOH, ACTA, HNO3, NIT, NITs read)
+ *   met   [GC_KPP_NMET][ldm] in/out   the six K_CLD rows (GC_KPP_MET_K_CLD..
+ *                                      +5) written, the other rows untouched
+ *   size_res [ncell] out or NULL       1 where the reference would call
+ *                                      fullchem_HetDropChem (not built here)
+ *
+ * Where the reference stops the model (a NaN pH), the cell's pHCloud and
+ * K_CLD come out NaN. */
+int gc_kpp_sulfur_cld_rates_batch(gc_kpp_ctx* ctx, int ncell, double* hetin, long long ldi, const double* c,
+                                  long long ldc, double* met, long long ldm, int lmetalcatso2, int* size_res,
+                                  int mem, void* stream);
 
 /* HetState of the cells of the following chemistry steps on this context
  * (gc_kpp_fullchem_step and its ordered/binned/learned forms evaluate the

@@ -58,6 +58,7 @@ def load(variant="strict", mech="fullchem"):
     lib.oracle_max_threads.restype = i32
     lib.oracle_set_state_het_batch.argtypes = [i32, vp, i64, vp, i64, f64, i32, i32, vp, i64]
     lib.oracle_sulfur_aq_rates_batch.argtypes = [i32, vp, i64, vp, i64, vp, vp, vp, i64]
+    lib.oracle_sulfur_cld_rates_batch.argtypes = [i32, vp, i64, vp, i64, i32, vp, i64, vp, vp]
     _libs[key] = lib
     return lib
 
@@ -150,6 +151,22 @@ def sulfur_aq_rates(hetin, c, temp, numden, mech="fullchem"):
     out = np.zeros((6, n), np.float64)
     lib.oracle_sulfur_aq_rates_batch(n, _p(hetin), n, _p(c), n, _p(temp), _p(numden), _p(out), n)
     return out
+
+
+def sulfur_cld_rates(hetin, c, lmetalcatso2=1, mech="fullchem"):
+    """Batched SET_SO2 (fullchem_SulfurCldChem) with Set_Sulfur_Chem_Rates'
+    fupdateHOBr/HOCl = 1: returns (hetin with HSO3_aq, SO3_aq, pHCloud,
+    fupdateHOBr, fupdateHOCl rewritten, K_CLD [6, n], size_res [n],
+    GET_HPLUS iterations [n])."""
+    lib = load("strict", mech)
+    hetin = _c(hetin, np.float64).copy()
+    c = _c(c, np.float64)
+    n = hetin.shape[1]
+    kcld = np.zeros((6, n), np.float64)
+    sr = np.zeros(n, np.int32)
+    it = np.zeros(n, np.int32)
+    lib.oracle_sulfur_cld_rates_batch(n, _p(hetin), n, _p(c), n, int(lmetalcatso2), _p(kcld), n, _p(sr), _p(it))
+    return hetin, kcld, sr, it
 
 
 def fun_split(v, f, rct, mech="fullchem"):

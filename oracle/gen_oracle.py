@@ -318,6 +318,8 @@ def write_het_layout(outdir, mech="fullchem"):
         k = species.index(name) if name in species else -1
         lines.append("#define OSS_%s %d" % (name, k))
         lines.append("#define OSS_SRMW_%s %s" % (name, repr(math.sqrt(mw[k])) if k >= 0 else "0.0"))
+    for name, v in hetstate.NONKPP_MW.items():
+        lines.append("#define OSS_MW_%s %r" % (name, v))
     text = "\n".join(lines) + "\n"
     path = os.path.join(outdir, "oracle_het_layout.h")
     old = open(path).read() if os.path.exists(path) else None

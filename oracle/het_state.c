@@ -482,3 +482,494 @@ void oracle_sulfur_aq_rates_batch(int ncell, const double* in, long long ldi, co
     for (int r = 0; r < 6; ++r) kmt[(long long)r * ldk + cell] = k[r];
   }
 }
+
+/* ------------------------------------------------------------------------
+ * fullchem_SulfurCldChem -> SET_SO2, restated statement by statement:
+ *   SET_SO2 (in-cloud branch)  KPP/fullchem/fullchem_SulfurChemFuncs.F90:865-1620
+ *   GET_HPLUS                  :1635-1853
+ *   kCO21 .. dkAA              :1867-3091 (one function each)
+ *   CaCO3_PRECIP               :3106-3156
+ *   AQCHEM_SO2                 :3171-3549
+ *   AIRMW, AVO, ATM            Headers/physconstants.F90:26, 32, 70
+ * Literals written without a kind suffix in the Fortran (e.g. Kc1 = 4.3e-7)
+ * are default REAL: their value is the single-precision rounding, written
+ * here as (double)<literal>f.
+ */
+#define S_AIRMW 28.9644
+#define S_ATMPA 1.01325e+5
+
+/* the temperature factor exp(D * (1/T - 1/298)) of the Henry and
+ * dissociation constants of GET_HPLUS's functions */
+static double so2_tf(double D, double T) { return exp(D * ((1.0 / T) - (1.0 / 298.0))); }
+
+static double kCO21(double P, double T, double LWC, double HPLUS) {
+  const double Kc1 = (double)4.3e-7f, Kc2 = (double)4.68e-11f, DhrKc1 = -1000.0, DhrKc2 = -1760.0;
+  const double Hco2 = (double)3.4e-2f, Dhco2 = 2.44e+3, CO2 = 390.0e-6;
+  double Hco2_T = Hco2 * so2_tf(Dhco2, T);
+  double Kc1_T = Kc1 * so2_tf(DhrKc1, T);
+  double Kc2_T = Kc2 * so2_tf(DhrKc2, T);
+  double Hco2eff = Hco2_T * (1.0 + (Kc1_T / HPLUS) + ((Kc1_T * Kc2_T) / (HPLUS * HPLUS)));
+  double xCO2 = 1.0 / (1.0 + (Hco2eff * 0.08205 * T * LWC));
+  double pCO2 = CO2 * P * xCO2;
+  return Hco2_T / HPLUS * Kc1_T * pCO2;
+}
+
+static double sq(double x) { return x * x; }
+
+static double dkCO21(double P, double T, double LWC, double HPLUS) {
+  const double Kc1 = (double)4.3e-7f, Kc2 = (double)4.68e-11f, DhrKc1 = -1000.0, DhrKc2 = -1760.0;
+  const double Hco2 = (double)3.4e-2f, Dhco2 = 2.44e+3, CO2 = 390.0e-6;
+  double Hco2_T = Hco2 * so2_tf(Dhco2, T);
+  double Kc1_T = Kc1 * so2_tf(DhrKc1, T);
+  double Kc2_T = Kc2 * so2_tf(DhrKc2, T);
+  return Kc1_T * Hco2_T * CO2 * P *
+         (Kc1_T * Kc2_T * Hco2_T * 0.08205 * T * LWC - Hco2_T * 0.08205 * T * LWC * HPLUS * HPLUS - HPLUS * HPLUS) /
+         sq(Kc1_T * Kc2_T * Hco2_T * 0.08205 * T * LWC + Kc1_T * Hco2_T * 0.08205 * T * LWC * HPLUS +
+            Hco2_T * 0.08205 * T * LWC * HPLUS * HPLUS + HPLUS * HPLUS);
+}
+
+static double kCO22(double P, double T, double LWC, double HPLUS) {
+  const double Kc1 = (double)4.3e-7f, Kc2 = (double)4.68e-11f, DhrKc1 = -1000.0, DhrKc2 = -1760.0;
+  const double Hco2 = (double)3.4e-2f, Dhco2 = 2.44e+3, CO2 = 390.0e-6;
+  double Hco2_T = Hco2 * so2_tf(Dhco2, T);
+  double Kc1_T = Kc1 * so2_tf(DhrKc1, T);
+  double Kc2_T = Kc2 * so2_tf(DhrKc2, T);
+  double Hco2eff = Hco2_T * (1.0 + (Kc1_T / HPLUS) + ((Kc1_T * Kc2_T) / (HPLUS * HPLUS)));
+  double xCO2 = 1.0 / (1.0 + (Hco2eff * 0.08205 * T * LWC));
+  double pCO2 = CO2 * P * xCO2;
+  return Kc1_T * Kc2_T * Hco2_T / HPLUS / HPLUS * pCO2;
+}
+
+static double dkCO22(double P, double T, double LWC, double HPLUS) {
+  const double Kc1 = (double)4.3e-7f, Kc2 = (double)4.68e-11f, DhrKc1 = -1000.0, DhrKc2 = -1760.0;
+  const double Hco2 = (double)3.4e-2f, Dhco2 = 2.44e+3, CO2 = 390.0e-6;
+  double Hco2_T = Hco2 * so2_tf(Dhco2, T);
+  double Kc1_T = Kc1 * so2_tf(DhrKc1, T);
+  double Kc2_T = Kc2 * so2_tf(DhrKc2, T);
+  return -1.0 * Kc1_T * Kc2_T * Hco2_T * CO2 * P *
+         (Kc1_T * Hco2_T * 0.08205 * T * LWC + 2.0 * Hco2_T * 0.08205 * T * LWC * HPLUS + 2.0 * HPLUS) /
+         sq(Kc1_T * Kc2_T * Hco2_T * 0.08205 * T * LWC + Kc1_T * Hco2_T * 0.08205 * T * LWC * HPLUS +
+            Hco2_T * 0.08205 * T * LWC * HPLUS * HPLUS + HPLUS * HPLUS);
+}
+
+static double kSO21(double P, double T, double LWC, double HPLUS, double SO2) {
+  const double Ks1 = (double)1.3e-2f, Ks2 = (double)6.6e-8f, Hso2 = (double)1.23f, Dhso2 = 3.14e+3;
+  const double DhrKso21 = 1960.0, DhrKso22 = 1500.0;
+  double Hso2_T = Hso2 * so2_tf(Dhso2, T);
+  double Ks1_T = Ks1 * so2_tf(DhrKso21, T);
+  double Ks2_T = Ks2 * so2_tf(DhrKso22, T);
+  double Hso2eff = Hso2_T * (1.0 + (Ks1_T / HPLUS) + ((Ks1_T * Ks2_T) / (HPLUS * HPLUS)));
+  double xSO2 = 1.0 / (1.0 + (Hso2eff * 0.08205 * T * LWC));
+  double pSO2 = SO2 * P * xSO2;
+  return Hso2_T * Ks1_T * pSO2 / HPLUS;
+}
+
+static double dkSO21(double P, double T, double LWC, double HPLUS, double SO2) {
+  const double Ks1 = (double)1.3e-2f, Ks2 = (double)6.6e-8f, Hso2 = (double)1.23f, Dhso2 = 3.14e+3;
+  const double DhrKso21 = 1960.0, DhrKso22 = 1500.0;
+  double Hso2_T = Hso2 * so2_tf(Dhso2, T);
+  double Ks1_T = Ks1 * so2_tf(DhrKso21, T);
+  double Ks2_T = Ks2 * so2_tf(DhrKso22, T);
+  return Ks1_T * Hso2_T * SO2 * P *
+         (Ks1_T * Ks2_T * Hso2_T * 0.08205 * T * LWC - Hso2_T * 0.08205 * T * LWC * HPLUS * HPLUS - HPLUS * HPLUS) /
+         sq(Ks1_T * Ks2_T * Hso2_T * 0.08205 * T * LWC + Ks1_T * Hso2_T * 0.08205 * T * LWC * HPLUS +
+            Hso2_T * 0.08205 * T * LWC * HPLUS * HPLUS + HPLUS * HPLUS);
+}
+
+static double kSO22(double P, double T, double LWC, double HPLUS, double SO2) {
+  const double Ks1 = (double)1.3e-2f, Ks2 = (double)6.6e-8f, Hso2 = (double)1.23f, Dhso2 = 3.14e+3;
+  const double DhrKso21 = 1960.0, DhrKso22 = 1500.0;
+  double Hso2_T = Hso2 * so2_tf(Dhso2, T);
+  double Ks1_T = Ks1 * so2_tf(DhrKso21, T);
+  double Ks2_T = Ks2 * so2_tf(DhrKso22, T);
+  double Hso2eff = Hso2_T * (1.0 + (Ks1_T / HPLUS) + ((Ks1_T * Ks2_T) / (HPLUS * HPLUS)));
+  double xSO2 = 1.0 / (1.0 + (Hso2eff * 0.08205 * T * LWC));
+  double pSO2 = SO2 * P * xSO2;
+  return Ks1_T * Ks2_T * Hso2_T / HPLUS / HPLUS * pSO2;
+}
+
+static double dkSO22(double P, double T, double LWC, double HPLUS, double SO2) {
+  const double Ks1 = (double)1.3e-2f, Ks2 = (double)6.6e-8f, Hso2 = (double)1.23f, Dhso2 = 3.14e+3;
+  const double DhrKso21 = 1960.0, DhrKso22 = 1500.0;
+  double Hso2_T = Hso2 * so2_tf(Dhso2, T);
+  double Ks1_T = Ks1 * so2_tf(DhrKso21, T);
+  double Ks2_T = Ks2 * so2_tf(DhrKso22, T);
+  return -1.0 * Ks1_T * Ks2_T * Hso2_T * SO2 * P *
+         (Ks1_T * Hso2_T * 0.08205 * T * LWC + 2.0 * Hso2_T * 0.08205 * T * LWC * HPLUS + 2.0 * HPLUS) /
+         sq(Ks1_T * Ks2_T * Hso2_T * 0.08205 * T * LWC + Ks1_T * Hso2_T * 0.08205 * T * LWC * HPLUS +
+            Hso2_T * 0.08205 * T * LWC * HPLUS * HPLUS + HPLUS * HPLUS);
+}
+
+static double kHNO3(double P, double T, double LWC, double HPLUS, double HNO3) {
+  const double Kn1 = (double)15.4f, Hhno3 = (double)2.1e5f, Dhhno3 = 0.0, DhrKn1 = 8700.0;
+  double Hhno3_T = Hhno3 * so2_tf(Dhhno3, T);
+  double Kn1_T = Kn1 * so2_tf(DhrKn1, T);
+  double Hhno3eff = Hhno3_T * (1.0 + (Kn1_T / HPLUS));
+  double xHNO3 = 1.0 / (1.0 + (Hhno3eff * 0.08205 * T * LWC));
+  double pHNO3 = HNO3 * P * xHNO3;
+  return Hhno3_T * Kn1_T * pHNO3 / HPLUS;
+}
+
+static double dkHNO3(double P, double T, double LWC, double HPLUS, double HNO3) {
+  const double Kn1 = (double)15.4f, Hhno3 = (double)2.1e5f, Dhhno3 = 0.0, DhrKn1 = 8700.0;
+  double Hhno3_T = Hhno3 * so2_tf(Dhhno3, T);
+  double Kn1_T = Kn1 * so2_tf(DhrKn1, T);
+  return -1.0 * Kn1_T * Hhno3_T * HNO3 * P * (1.0 + Hhno3_T * 0.08205 * T * LWC) /
+         sq(Kn1_T * Hhno3_T * 0.08205 * T * LWC + Hhno3_T * 0.08205 * T * LWC * HPLUS + HPLUS);
+}
+
+static double kHCl(double P, double T, double LWC, double HPLUS, double Cl) {
+  const double Kcl = 1.74e+6, Hcl = 1.5e+3, Dhcl = 2.3e+3, DhrKcl = 6900.0;
+  double Hcl_T = Hcl * so2_tf(Dhcl, T);
+  double Kcl_T = Kcl * so2_tf(DhrKcl, T);
+  double Hcleff = Hcl_T * (1.0 + (Kcl_T / HPLUS));
+  double xCl = 1.0 / (1.0 + (Hcleff * 0.08205 * T * LWC));
+  double pHCl = Cl * P * xCl;
+  return Hcl_T * Kcl_T * pHCl / HPLUS;
+}
+
+static double dkHCl(double P, double T, double LWC, double HPLUS, double Cl) {
+  const double Kcl = 1.74e+6, Hcl = 1.5e+3, Dhcl = 2.3e+3, DhrKcl = 6900.0;
+  double Hcl_T = Hcl * so2_tf(Dhcl, T);
+  double Kcl_T = Kcl * so2_tf(DhrKcl, T);
+  return -1.0 * Kcl_T * Hcl_T * Cl * P * (1.0 + Hcl_T * 0.08205 * T * LWC) /
+         sq(Kcl_T * Hcl_T * 0.08205 * T * LWC + Hcl_T * 0.08205 * T * LWC * HPLUS + HPLUS);
+}
+
+static double kNH3(double P, double T, double LWC, double HPLUS, double NH3, double Kw) {
+  const double Ka1 = (double)1.7e-5f, Hnh3 = 60.0, Dhnh3 = 4200.0, DhrKa1 = -450.0;
+  double Hnh3_T = Hnh3 * so2_tf(Dhnh3, T);
+  double Ka1_T = Ka1 * so2_tf(DhrKa1, T);
+  double Hnh3eff = Hnh3_T * (1.0 + ((Ka1_T * HPLUS) / Kw));
+  double xNH3 = 1.0 / (1.0 + (Hnh3eff * 0.08205 * T * LWC));
+  double pNH3 = NH3 * P * xNH3;
+  return HPLUS * Hnh3_T * Ka1_T * pNH3 / Kw;
+}
+
+static double dkNH3(double P, double T, double LWC, double HPLUS, double NH3, double Kw) {
+  const double Ka1 = (double)1.7e-5f, Hnh3 = 60.0, Dhnh3 = 4200.0, DhrKa1 = -450.0;
+  double Hnh3_T = Hnh3 * so2_tf(Dhnh3, T);
+  double Ka1_T = Ka1 * so2_tf(DhrKa1, T);
+  return Ka1_T * Hnh3_T * NH3 * Kw * P * (1.0 + Hnh3_T * 0.08205 * T * LWC) /
+         sq(Hnh3_T * 0.08205 * T * LWC * (Kw + Ka1_T * HPLUS) + Kw);
+}
+
+static double kFA(double P, double T, double LWC, double HPLUS, double FA) {
+  const double Kformate = 1.8e-4, Hfa = 8800.0, Dhfa = 6100.0, DhrKfa = 151.0;
+  double Hfa_T = Hfa * so2_tf(Dhfa, T);
+  double Kfa_T = Kformate * so2_tf(DhrKfa, T);
+  double Hfaeff = Hfa_T * (1.0 + (Kfa_T / HPLUS));
+  double xFA = 1.0 / (1.0 + (Hfaeff * 0.08205 * T * LWC));
+  double pFA = FA * P * xFA;
+  return Hfa_T * Kfa_T * pFA / HPLUS;
+}
+
+static double dkFA(double P, double T, double LWC, double HPLUS, double FA) {
+  const double Kformate = 1.8e-4, Hfa = 8800.0, Dhfa = 6100.0, DhrKfa = 151.0;
+  double Hfa_T = Hfa * so2_tf(Dhfa, T);
+  double Kfa_T = Kformate * so2_tf(DhrKfa, T);
+  return -1.0 * Kfa_T * Hfa_T * FA * P * (1.0 + Hfa_T * 0.08205 * T * LWC) /
+         sq(Kfa_T * Hfa_T * 0.08205 * T * LWC + Hfa_T * 0.08205 * T * LWC * HPLUS + HPLUS);
+}
+
+static double kAA(double P, double T, double LWC, double HPLUS, double AA) {
+  const double Kacetate = 1.75e-5, Haa = 4100.0, Dhaa = 6200.0, DhrKaa = 50.0;
+  double Haa_T = Haa * so2_tf(Dhaa, T);
+  double Kaa_T = Kacetate * so2_tf(DhrKaa, T);
+  double Haaeff = Haa_T * (1.0 + (Kaa_T / HPLUS));
+  double xAA = 1.0 / (1.0 + (Haaeff * 0.08205 * T * LWC));
+  double pAA = AA * P * xAA;
+  return Haa_T * Kaa_T * pAA / HPLUS;
+}
+
+static double dkAA(double P, double T, double LWC, double HPLUS, double AA) {
+  const double Kacetate = 1.75e-5, Haa = 4100.0, Dhaa = 6200.0, DhrKaa = 50.0;
+  double Haa_T = Haa * so2_tf(Dhaa, T);
+  double Kaa_T = Kacetate * so2_tf(DhrKaa, T);
+  return -1.0 * Kaa_T * Haa_T * AA * P * (1.0 + Haa_T * 0.08205 * T * LWC) /
+         sq(Kaa_T * Haa_T * 0.08205 * T * LWC + Haa_T * 0.08205 * T * LWC * HPLUS + HPLUS);
+}
+
+static void CaCO3_PRECIP(double P, double T, double HPLUS, double* fCa, double* dCa) {
+  const double Kc1 = 4.3e-7, Kc2 = 4.68e-11, DhrKc1 = -1000.0, DhrKc2 = -1760.0;
+  const double Hco2 = 3.4e-2, Dhco2 = 2.44e+3, CO2 = 390.0e-6, Ksp = 3.3e-9, DHrKsp = -1200.0;
+  double Hco2_T = Hco2 * so2_tf(Dhco2, T);
+  double Kc1_T = Kc1 * so2_tf(DhrKc1, T);
+  double Kc2_T = Kc2 * so2_tf(DhrKc2, T);
+  double Ksp_T = Ksp * so2_tf(DHrKsp, T);
+  *fCa = Ksp_T * HPLUS * HPLUS / (Kc1_T * Kc2_T * Hco2_T * CO2 * P);
+  *dCa = 2.0 * Ksp_T * HPLUS / (Kc1_T * Kc2_T * Hco2_T * CO2 * P);
+}
+
+/* Newton iteration on the cloud water's electroneutrality; returns [H+] */
+static double GET_HPLUS(double SO4nss, double HMSc, double TNH3, double TNO3, double SO2, double CL, double TNA,
+                        double TDCA, double TFA, double TAA, double T, double PRES, double LWC, double iHPLUS,
+                        int* niter) {
+  const double Kw = 1.0e-14, DhrKw = -6710.0, MINVAL_ = (double)0.01f;
+  double D, Kw_T, ipH, newpH, nHPLUS;
+  double fHCO3, fCO3, fHSO3, fSO3, fHNO3, fNH4, fHCl, fFA, fAA;
+  double dHCO3, dCO3, dHSO3, dSO3, dHNO3, dNH4, dHCl, dFA, dAA;
+  double f, df, nnHPLUS, fCa, dCa;
+  int count;
+  ipH = -log10(iHPLUS);
+  D = (2.0 * SO4nss) - TNA - (2.0 * TDCA) + (1.0 * HMSc);
+  (void)D;
+  Kw_T = Kw * exp(DhrKw * ((1.0 / T) - (1.0 / 298.0)));
+  newpH = 0.0;
+  count = 0;
+  while (fabs(ipH - newpH) > MINVAL_) {
+    count = count + 1;
+    if (count != 1) ipH = newpH;
+    nHPLUS = pow(10.0, -ipH);
+    fHCO3 = kCO21(PRES, T, LWC, nHPLUS);
+    fCO3 = kCO22(PRES, T, LWC, nHPLUS);
+    fHSO3 = kSO21(PRES, T, LWC, nHPLUS, SO2);
+    fSO3 = kSO22(PRES, T, LWC, nHPLUS, SO2);
+    fHNO3 = kHNO3(PRES, T, LWC, nHPLUS, TNO3);
+    fNH4 = kNH3(PRES, T, LWC, nHPLUS, TNH3, Kw_T);
+    fHCl = kHCl(PRES, T, LWC, nHPLUS, CL);
+    fFA = kFA(PRES, T, LWC, nHPLUS, TFA);
+    fAA = kAA(PRES, T, LWC, nHPLUS, TAA);
+    dHCO3 = dkCO21(PRES, T, LWC, nHPLUS);
+    dCO3 = dkCO22(PRES, T, LWC, nHPLUS);
+    dHSO3 = dkSO21(PRES, T, LWC, nHPLUS, SO2);
+    dSO3 = dkSO22(PRES, T, LWC, nHPLUS, SO2);
+    dHNO3 = dkHNO3(PRES, T, LWC, nHPLUS, TNO3);
+    dNH4 = dkNH3(PRES, T, LWC, nHPLUS, TNH3, Kw_T);
+    dHCl = dkHCl(PRES, T, LWC, nHPLUS, CL);
+    dFA = dkFA(PRES, T, LWC, nHPLUS, TFA);
+    dAA = dkAA(PRES, T, LWC, nHPLUS, TAA);
+    CaCO3_PRECIP(PRES, T, nHPLUS, &fCa, &dCa);
+    if (fCa >= TDCA) {
+      D = (2.0 * SO4nss) - (TNA + 2.0 * TDCA);
+      f = D - nHPLUS + Kw / nHPLUS + fHCO3 + 2.0 * fCO3 + fHSO3 + 2.0 * fSO3 + fHNO3 - fNH4 + fHCl + fFA + fAA;
+      df = -1.0 - Kw / nHPLUS / nHPLUS + dHCO3 + 2.0 * dCO3 + dHSO3 + 2.0 * dSO3 + dHNO3 - dNH4 + dHCl + dFA + dAA;
+    } else {
+      D = (2.0 * SO4nss) - TNA;
+      f = D - nHPLUS + Kw / nHPLUS + fHCO3 + 2.0 * fCO3 + fHSO3 + 2.0 * fSO3 + fHNO3 - fNH4 + fHCl + fFA + fAA -
+          2.0 * fCa;
+      df = -1.0 - Kw / nHPLUS / nHPLUS + dHCO3 + 2.0 * dCO3 + dHSO3 + 2.0 * dSO3 + dHNO3 - dNH4 + dHCl + dFA + dAA -
+           2.0 * dCa;
+    }
+    nnHPLUS = nHPLUS - f / df;
+    nnHPLUS = fmax(nnHPLUS, 1.0e-14);
+    nnHPLUS = fmin(nnHPLUS, 1.0e-1);
+    if (count > 50) {
+      newpH = ((-log10(nnHPLUS)) + (-log10(nHPLUS))) / 2.0;
+      break; /* the reference stops the model when newpH is NaN */
+    } else {
+      newpH = -log10(nnHPLUS);
+      if (isnan(newpH)) break;
+    }
+  }
+  *niter = count;
+  return pow(10.0, -newpH);
+}
+
+typedef struct {
+  double KaqH2O2, KaqO3, KaqO3_1, KaqO2, HSO3aq, SO3aq, KaqHCHO, KaqHMS, KaqHMS2;
+} so2_aq_t;
+
+static void AQCHEM_SO2(double LWC, double T, double P, double SO2, double H2O2, double O3, double HCHO,
+                       double Hplus, double MnII, double FeIII, so2_aq_t* o) {
+  const double R = 0.08205, dOH = 1.0e-19;
+  double KH2O2, Ks1, Ks2, HCSO2, FHCSO2, XSO2g, SIV, XSO2aq, XHSO3, XSO3, Kh1, HCH2O2, FHCH2O2, XH2O2g;
+  double KO0, KO1, KO2, HCO3, XO3g, XHCHOg, HCHCHO, FHCHCHO, KHCHO1, KHCHO2, KHMS, Kw1, Khc1, KHMS2;
+  (void)O3;
+  (void)H2O2;
+  (void)HCHO;
+  KH2O2 = 6.31e+14 * exp(-4.76e+3 / T);
+  Ks1 = 1.30e-2 * exp(6.75 * (298.15 / T - 1.0));
+  Ks2 = 6.31e-8 * exp(5.05 * (298.15 / T - 1.0));
+  XSO2aq = 1.0 / (1.0 + Ks1 / Hplus + Ks1 * Ks2 / (Hplus * Hplus));
+  XHSO3 = 1.0 / (1.0 + Hplus / Ks1 + Ks2 / Hplus);
+  XSO3 = 1.0 / (1.0 + Hplus / Ks2 + Hplus * Hplus / (Ks1 * Ks2));
+  HCSO2 = 1.22 * exp(10.55 * (298.15 / T - 1.0));
+  FHCSO2 = HCSO2 * (1.0 + (Ks1 / Hplus) + (Ks1 * Ks2 / (Hplus * Hplus)));
+  XSO2g = 1.0 / (1.0 + (FHCSO2 * R * T * LWC));
+  SIV = FHCSO2 * XSO2g * SO2 * P;
+  o->HSO3aq = SIV * XHSO3;
+  o->SO3aq = SIV * XSO3;
+  Kh1 = 2.20e-12 * exp(-12.52 * (298.15 / T - 1.0));
+  HCH2O2 = 7.45e+4 * exp(22.21 * (298.15 / T - 1.0));
+  FHCH2O2 = HCH2O2 * (1.0 + (Kh1 / Hplus));
+  XH2O2g = 1.0 / (1.0 + (FHCH2O2 * R * T * LWC));
+  o->KaqH2O2 = KH2O2 * Ks1 * FHCH2O2 * HCSO2 * XH2O2g * XSO2g * P * LWC * R * T;
+  KO0 = 2.40e+4;
+  KO1 = 3.49e+12 * exp(-4.83e+3 / T);
+  KO2 = 7.32e+14 * exp(-4.03e+3 / T);
+  HCO3 = 1.13e-2 * exp(8.51 * (298.15 / T - 1.0));
+  XO3g = 1.0 / (1.0 + (HCO3 * R * T * LWC));
+  o->KaqO3 = (KO0 * XSO2aq + KO1 * XHSO3 + KO2 * XSO3) * FHCSO2 * XSO2g * P * HCO3 * XO3g * LWC * R * T;
+  o->KaqO3_1 = KO2 * XSO3 * FHCSO2 * XSO2g * P * HCO3 * XO3g * LWC * R * T;
+  o->KaqO2 = FHCSO2 * XSO2g * ((750.0 * MnII) + (2600.0 * FeIII) + (1e+10 * MnII * FeIII)) * LWC * R * T;
+  KHCHO1 = 7.9e+2 * exp(-16.44 * (298.15 / T - 1.0));
+  KHCHO2 = 2.5e+7 * exp(-6.04 * (298.15 / T - 1.0));
+  KHMS = 3.6e+3 * exp(-15.09 * (298.15 / T - 1.0));
+  KHMS2 = 2.65e+8 * exp(-5.03 * (298.15 / T - 1.0));
+  Khc1 = 2.53e+3 * exp(13.48 * (298.15 / T - 1.0));
+  Kw1 = 1e-14 * exp(-22.51 * (298.15 / T - 1.0));
+  HCHCHO = 2.5 * exp(21.6 * (298.15 / T - 1.0));
+  FHCHCHO = HCHCHO * (1.0 + Khc1);
+  XHCHOg = 1.0 / (1.0 + (FHCHCHO * R * T * LWC));
+  o->KaqHCHO = (KHCHO1 * XHSO3 + KHCHO2 * XSO3) * FHCSO2 * XSO2g * P * HCHCHO * XHCHOg * LWC * R * T;
+  o->KaqHMS = KHMS * (Kw1 / Hplus) * 0.7;
+  o->KaqHMS2 = KHMS2 * dOH * 0.7;
+}
+
+/* SET_SO2 for one cell: K_CLD(1:6) into kcld[6]; HSO3_aq, SO3_aq, pHCloud
+ * into *hso3, *so3, *phcloud; size_res and the GET_HPLUS iteration count
+ * (0 outside the cloud branch) into *size_res, *niter. */
+static void set_so2_cell(const double* in, long long ldi, const double* C, long long ldc, int lmetalcatso2,
+                         double* kcld, double* hso3, double* so3, double* phcloud, int* size_res, int* niter) {
+#define IN(f) in[(long long)(f) * ldi]
+  const double HPLUS_45 = 3.16227766016837953e-5, MINDAT = 1.e-20;
+  double RHO, CNVFAC, SO20, SO2_AfterSS, H2O20, PATM, TK, FC, LWC;
+  double SO4nss, HMSc, TNH3, CL, TFA, TAA, TNA, DUST, TDCA, TNO3, GNO3, HPLUS;
+  double FeIII, MnII, Fe_nat, Mn_nat, Fe_ant, Mn_ant, Mn_tot, Mn_d, Fe_d_ant, Fe_d_nat, Fe_d;
+  double ALKdst, ALKss, ALKds, NH3;
+  so2_aq_t aq;
+  int sr = 0;
+  *hso3 = 1.0e-32;
+  *so3 = 1.0e-32;
+  *phcloud = 0.0;
+  *niter = 0;
+  for (int k = 0; k < 6; ++k) kcld[k] = 0.0;
+  RHO = IN(OHIN_AIRDEN);
+  CNVFAC = 1.E3 * S_AIRMW / (RHO * S_AVO);
+  SO20 = ss_C(C, ldc, OSS_SO2) * CNVFAC;
+  SO2_AfterSS = ss_C(C, ldc, OSS_SO2) * CNVFAC;
+  H2O20 = ss_C(C, ldc, OSS_H2O2) * CNVFAC;
+  PATM = IN(OHIN_PMID_DRY) / (S_ATMPA * 1.e-2);
+  TK = IN(OHIN_T);
+  FC = IN(OHIN_CLDF);
+  LWC = IN(OHIN_QL) * IN(OHIN_AIRDEN) * 1e-3;
+  LWC = fmax(0.0, LWC);
+  LWC = ss_SafeDiv(LWC, FC, 0.0);
+  if ((FC > 1.0e-4) && (SO2_AfterSS > MINDAT) && (TK > 258.0) && (LWC > 1.0e-20)) {
+    SO4nss = 1.e+3 * (ss_C(C, ldc, OSS_SO4) * 0.7 + ss_C(C, ldc, OSS_SO4s)) / (LWC * S_AVO);
+    HMSc = 1.e+3 * ss_C(C, ldc, OSS_HMS) * 0.7 / (LWC * S_AVO);
+    TNH3 = ((IN(OHIN_NH4) * 0.7) + IN(OHIN_NH3)) * CNVFAC;
+    CL = (ss_C(C, ldc, OSS_SALACL) * 0.7) + ss_C(C, ldc, OSS_SALCCL);
+    CL = (CL + ss_C(C, ldc, OSS_HCl)) * CNVFAC;
+    TFA = ss_C(C, ldc, OSS_HCOOH) * CNVFAC;
+    TAA = ss_C(C, ldc, OSS_ACTA) * CNVFAC;
+    TNA = 1.e3 * (IN(OHIN_SALA) * 0.7 + IN(OHIN_SALC)) * (31.6 * 0.359 / 23.0) / (LWC * S_AVO);
+    DUST = (IN(OHIN_DSTbin) + IN(OHIN_DSTbin + 1) + IN(OHIN_DSTbin + 2) + IN(OHIN_DSTbin + 3) +
+            IN(OHIN_DSTbin + 4) + IN(OHIN_DSTbin + 5) + IN(OHIN_DSTbin + 6)) *
+           1.e+15 * OSS_MW_DSTbin1 / S_AVO;
+    TDCA = DUST * 2.22e-15 / LWC;
+    TNO3 = (ss_C(C, ldc, OSS_HNO3) + (ss_C(C, ldc, OSS_NIT) * 0.7) + ss_C(C, ldc, OSS_NITs)) * CNVFAC;
+    GNO3 = ss_C(C, ldc, OSS_HNO3) * CNVFAC;
+    HPLUS = GET_HPLUS(SO4nss, HMSc, TNH3, TNO3, SO2_AfterSS, CL, TNA, TDCA, TFA, TAA, TK, PATM, LWC, HPLUS_45,
+                      niter);
+    *phcloud = -1.0 * log10(HPLUS);
+    FeIII = 0.0;
+    MnII = 0.0;
+    if (lmetalcatso2) {
+      Fe_nat = DUST * 35e-3;
+      Mn_nat = Fe_nat / 50.0;
+      Fe_ant = IN(OHIN_pFe) * CNVFAC * 1.e+12 * IN(OHIN_AD) / (S_AIRMW / OSS_MW_pFe) / IN(OHIN_AIRVOL);
+      Mn_ant = Fe_ant / 10.0;
+      Mn_tot = Mn_ant + Mn_nat;
+      if (LWC > 0.0) {
+        Mn_d = Mn_tot * 1e-9 / 54.94 / LWC * 1e-3;
+        Mn_d = Mn_d * 0.5;
+      } else {
+        Mn_d = 0.0;
+      }
+      if (LWC > 0.0) {
+        Fe_d_ant = Fe_ant * 1e-9 / OSS_MW_pFe / LWC * 1e-3;
+        Fe_d_nat = Fe_nat * 1e-9 / OSS_MW_pFe / LWC * 1e-3;
+        Fe_d = Fe_d_ant * 0.1 + Fe_d_nat * 0.01;
+      } else {
+        Fe_d = 0.0;
+      }
+      if (IN(OHIN_SUNCOS) > 0.0)
+        FeIII = Fe_d * 0.1;
+      else
+        FeIII = Fe_d * 0.9;
+      MnII = Mn_d;
+    }
+    AQCHEM_SO2(LWC, TK, PATM, SO2_AfterSS, ss_C(C, ldc, OSS_H2O2) * CNVFAC, ss_C(C, ldc, OSS_O3) * CNVFAC,
+               ss_C(C, ldc, OSS_CH2O) * CNVFAC, HPLUS, MnII, FeIII, &aq);
+    kcld[0] = aq.KaqH2O2 * FC * CNVFAC;
+    kcld[1] = aq.KaqO3 * FC * CNVFAC;
+    kcld[2] = aq.KaqO2 * FC;
+    kcld[3] = aq.KaqHCHO * FC * CNVFAC;
+    kcld[4] = aq.KaqHMS * FC;
+    kcld[5] = aq.KaqHMS2 * FC / ss_C(C, ldc, OSS_SO2);
+    ALKdst = (IN(OHIN_DSTbin) + IN(OHIN_DSTbin + 1) + IN(OHIN_DSTbin + 2) + IN(OHIN_DSTbin + 3) +
+              IN(OHIN_DSTbin + 4) + IN(OHIN_DSTbin + 5) + IN(OHIN_DSTbin + 6)) *
+             CNVFAC * 1.e+9 * IN(OHIN_AD) / (S_AIRMW / OSS_MW_DSTbin1) / IN(OHIN_AIRVOL);
+    ALKss = (IN(OHIN_SALA) + IN(OHIN_SALC)) * CNVFAC * 1.e+9 * IN(OHIN_AD) / (S_AIRMW / OSS_MW_SALA) /
+            IN(OHIN_AIRVOL);
+    ALKds = ALKdst + ALKss;
+    NH3 = IN(OHIN_NH3) * CNVFAC;
+    sr = 0;
+    if (H2O20 > SO2_AfterSS + 1e-9) {
+      sr = 0;
+    } else if (LWC < 0.1e-6) {
+      sr = 1;
+    } else if (GNO3 > NH3) {
+      if (SO2_AfterSS >= 5.e-9 && H2O20 >= SO20) sr = 0;
+      if (LWC >= 0.3e-6 && SO2_AfterSS >= 3.e-9 && H2O20 >= SO2_AfterSS) sr = 0;
+      if (ALKds >= 5.0 && LWC >= 0.5e-6 && H2O20 >= SO2_AfterSS) sr = 0;
+      if (LWC >= 0.1e-6 && GNO3 <= (NH3 + 2.e-9)) sr = 0;
+    } else if (LWC >= 0.5e-6) {
+      if (H2O20 >= (0.9 * SO2_AfterSS)) sr = 0;
+      if (NH3 <= 1.e-9 && ALKds >= 5.0 && SO2_AfterSS <= 10.e-9) sr = 0;
+    } else if (LWC >= 0.3e-6) {
+      if (NH3 >= (GNO3 + 5.e-9) && SO2_AfterSS <= 10.e-9) sr = 0;
+      if (GNO3 <= 1.e-9 && NH3 >= (GNO3 + 2.e-9)) sr = 0;
+      if (GNO3 <= 7.e-9 && NH3 >= (GNO3 + 3.e-9)) sr = 0;
+      if (ALKds >= 3.0 && NH3 <= 10e-9 && SO2_AfterSS <= 5e-9) sr = 0;
+      if (ALKds >= 5.0 && NH3 <= 10.e-9 && SO2_AfterSS <= 5.e-9) sr = 0;
+      if (SO2_AfterSS >= 1.5e-9 && H2O20 >= SO2_AfterSS) sr = 0;
+      if (NH3 <= 12.e-9 && ALKds >= 10.0) sr = 0;
+      if (NH3 <= 1.e-9 && ALKds >= 4.0 && SO2_AfterSS <= 10.e-9) sr = 0;
+      if (NH3 <= 5.e-9 && ALKds >= 6.0 && SO2_AfterSS <= 10.e-9) sr = 0;
+      if (NH3 <= 7.e-9 && ALKds > -8.0 && SO2_AfterSS <= 10.e-9) sr = 0;
+    } else if (LWC >= 0.1e-6) {
+      if (NH3 <= 1.e-9 && ALKds >= 5.0) sr = 0;
+      if (NH3 <= 5.e-9 && ALKds >= 10.0) sr = 0;
+      if (GNO3 <= 1.e-9 && NH3 >= (GNO3 + 2.e-9) && SO2_AfterSS <= 7.e-9) sr = 0;
+      if (GNO3 <= 1.e-9 && NH3 >= (GNO3 + 2.e-9) && ALKds >= 2.0) sr = 0;
+      if (GNO3 <= 3.e-9 && NH3 >= (GNO3 + 4.e-9)) sr = 0;
+      if (GNO3 <= 7.e-9 && NH3 >= (GNO3 + 3.e-9) && SO2_AfterSS <= 5.e-9) sr = 0;
+      if (GNO3 <= 7.e-9 && NH3 >= (GNO3 + 3.e-9) && ALKds >= 4.0 && SO2_AfterSS <= 9.e-9) sr = 0;
+      if (ALKds >= 3.0 && NH3 <= 3.e-9 && SO2_AfterSS <= 4.e-9) sr = 0;
+      if (ALKds >= 5.0 && SO2_AfterSS <= 5.e-9 && NH3 <= 7.e-9) sr = 0;
+      if (NH3 >= (GNO3 + 2.e-9) && SO2_AfterSS <= 5.e-9) sr = 0;
+      if (NH3 >= (GNO3 + 4.e-9) && SO2_AfterSS <= 10.e-9) sr = 0;
+      if (ALKds >= 2.0 && NH3 <= 10.e-9 && H2O20 >= SO2_AfterSS) sr = 0;
+      if (NH3 <= 1.e-9 && SO2_AfterSS >= 3.e-9 && H2O20 >= SO2_AfterSS) sr = 0;
+    } else {
+      sr = 1;
+    }
+    *hso3 = aq.HSO3aq;
+    *so3 = aq.SO3aq;
+  }
+  *size_res = sr;
+#undef IN
+}
+
+/* SET_SO2 for every cell (with Set_Sulfur_Chem_Rates' fupdateHOBr/HOCl = 1):
+ * in/out hetin rows HSO3_aq, SO3_aq, pHCloud, fupdateHOBr, fupdateHOCl;
+ * kcld [6][ldk] out; size_res/niter [n] out (either may be NULL). */
+void oracle_sulfur_cld_rates_batch(int ncell, double* in, long long ldi, const double* C, long long ldc,
+                                   int lmetalcatso2, double* kcld, long long ldk, int* size_res, int* niter) {
+  for (int cell = 0; cell < ncell; ++cell) {
+    double k[6], hso3, so3, ph;
+    int sr, it;
+    set_so2_cell(in + cell, ldi, C + cell, ldc, lmetalcatso2, k, &hso3, &so3, &ph, &sr, &it);
+    for (int r = 0; r < 6; ++r) kcld[(long long)r * ldk + cell] = k[r];
+    in[(long long)OHIN_HSO3_aq * ldi + cell] = hso3;
+    in[(long long)OHIN_SO3_aq * ldi + cell] = so3;
+    in[(long long)OHIN_pHCloud * ldi + cell] = ph;
+    in[(long long)OHIN_fupdateHOBr * ldi + cell] = 1.0;
+    in[(long long)OHIN_fupdateHOCl * ldi + cell] = 1.0;
+    if (size_res) size_res[cell] = sr;
+    if (niter) niter[cell] = it;
+  }
+}

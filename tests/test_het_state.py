@@ -139,7 +139,7 @@ def test_setstatehet_layout_in_public_header():
     with open(os.path.join(ROOT, "include", "gckpp_gb300.h")) as fh:
         text = fh.read()
     assert "#define GC_KPP_NHETIN %d" % hs.NHETIN in text
-    assert hs.NHETIN == 100
+    assert hs.NHETIN == 111
 
 
 @pytest.mark.parametrize("lpscchem,turn_off", [(1, 0), (0, 1)])
@@ -349,3 +349,318 @@ def test_gpu_sulfur_aq_matches_oracle(orc):
     # the other met rows are untouched
     others = [i for i, f in enumerate(MET_FIELDS) if not f.startswith("K_MT")]
     assert np.array_equal(met[others], cells["met"][others])
+
+
+# ---------------------------------------------------------------------------
+# SET_SO2 (fullchem_SulfurCldChem), KPP/fullchem/fullchem_SulfurChemFuncs.F90:
+# 865-1620 with GET_HPLUS (:1635-1853), the equilibrium functions
+# (:1867-3156) and AQCHEM_SO2 (:3171-3549).  The Python restatement below is
+# written from the Fortran independently of oracle/het_state.c: the nine
+# Henry/dissociation pairs as data, evaluated by two generic functions.
+
+def _f32(x):
+    return float(np.float32(x))
+
+
+# (Henry constant, its temperature coefficient, K1, its coefficient[, K2, its
+# coefficient]) of the species of GET_HPLUS, with the Fortran's literal kinds
+_SO2_DI = {"CO2": (_f32(3.4e-2), 2.44e+3, _f32(4.3e-7), _f32(-1000.0), _f32(4.68e-11), _f32(-1760.0)),
+           "SO2": (_f32(1.23), 3.14e+3, _f32(1.3e-2), _f32(1960.0), _f32(6.6e-8), _f32(1500.0))}
+_SO2_MONO = {"HNO3": (_f32(2.1e5), _f32(0.0), _f32(15.4), _f32(8700.0)),
+             "HCl": (1.5e+3, 2.3e+3, 1.74e+6, 6900.0),
+             "FA": (8800.0, 6100.0, 1.8e-4, 151.0),
+             "AA": (4100.0, 6200.0, 1.75e-5, 50.0)}
+
+
+def _py_set_so2(hin_col, cvec, sp, lmetal, mw):
+    """One cell of SET_SO2: (kcld[6], HSO3_aq, SO3_aq, pHCloud, size_res, niter)."""
+    import math
+
+    import gcchem.hetstate as hs
+
+    o = hs.HETIN_OFFSET
+    X = lambda f, k=0: float(hin_col[o[f] + k])
+    C = lambda name: float(cvec[sp.index(name)])
+    AIRMW, AVO_, ATM = 28.9644, 6.022140857e+23, 1.01325e+5
+    RL = 0.08205
+    tf = lambda D, T: math.exp(D * ((1.0 / T) - (1.0 / 298.0)))
+    kcld = [0.0] * 6
+    rho = X("AIRDEN")
+    cnv = 1.0e3 * AIRMW / (rho * AVO_)
+    so2 = C("SO2") * cnv
+    h2o2 = C("H2O2") * cnv
+    patm = X("PMID_DRY") / (ATM * 1.e-2)
+    T = X("T")
+    fc = X("CLDF")
+    lwc = max(0.0, X("QL") * X("AIRDEN") * 1e-3)
+    e = lambda v: 0 if v == 0 else math.frexp(v)[1]
+    if fc == 0.0 or e(lwc) - e(fc) > 1023:
+        lwc = 0.0
+    elif e(lwc) - e(fc) < -1020:
+        lwc = 0.0
+    else:
+        lwc = lwc / fc
+    if not (fc > 1.0e-4 and so2 > 1e-20 and T > 258.0 and lwc > 1.0e-20):
+        return kcld, 1.0e-32, 1.0e-32, 0.0, 0, 0
+    so4nss = 1.e+3 * (C("SO4") * 0.7 + C("SO4s")) / (lwc * AVO_)
+    tnh3 = ((X("NH4") * 0.7) + X("NH3")) * cnv
+    cl = ((C("SALACL") * 0.7) + C("SALCCL") + C("HCl")) * cnv
+    tfa, taa = C("HCOOH") * cnv, C("ACTA") * cnv
+    tna = 1.e3 * (X("SALA") * 0.7 + X("SALC")) * (31.6 * 0.359 / 23.0) / (lwc * AVO_)
+    dsum = 0.0
+    for b in range(7):
+        dsum = X("DSTbin", b) if b == 0 else dsum + X("DSTbin", b)
+    dust = dsum * 1.e+15 * mw["DSTbin1"] / AVO_
+    tdca = dust * 2.22e-15 / lwc
+    tno3 = (C("HNO3") + (C("NIT") * 0.7) + C("NITs")) * cnv
+    amount = {"CO2": 390.0e-6, "SO2": so2, "HNO3": tno3, "HCl": cl, "FA": tfa, "AA": taa}
+
+    def di(name, H):
+        Hc, Dh, K1, D1, K2, D2 = _SO2_DI[name]
+        H_T, K1_T, K2_T = Hc * tf(Dh, T), K1 * tf(D1, T), K2 * tf(D2, T)
+        heff = H_T * (1.0 + (K1_T / H) + ((K1_T * K2_T) / (H * H)))
+        p = amount[name] * patm * (1.0 / (1.0 + (heff * RL * T * lwc)))
+        if name == "CO2":
+            f1 = H_T / H * K1_T * p
+        else:
+            f1 = H_T * K1_T * p / H
+        f2 = K1_T * K2_T * H_T / H / H * p
+        den = (K1_T * K2_T * H_T * RL * T * lwc + K1_T * H_T * RL * T * lwc * H + H_T * RL * T * lwc * H * H
+               + H * H) ** 2
+        d1 = K1_T * H_T * amount[name] * patm * (K1_T * K2_T * H_T * RL * T * lwc - H_T * RL * T * lwc * H * H
+                                                - H * H) / den
+        d2 = -1.0 * K1_T * K2_T * H_T * amount[name] * patm * (K1_T * H_T * RL * T * lwc + 2.0 * H_T * RL * T * lwc * H
+                                                               + 2.0 * H) / den
+        return f1, f2, d1, d2
+
+    def mono(name, H):
+        Hc, Dh, K, D = _SO2_MONO[name]
+        H_T, K_T = Hc * tf(Dh, T), K * tf(D, T)
+        heff = H_T * (1.0 + (K_T / H))
+        p = amount[name] * patm * (1.0 / (1.0 + (heff * RL * T * lwc)))
+        f = H_T * K_T * p / H
+        d = (-1.0 * K_T * H_T * amount[name] * patm * (1.0 + H_T * RL * T * lwc)
+             / (K_T * H_T * RL * T * lwc + H_T * RL * T * lwc * H + H) ** 2)
+        return f, d
+
+    Kw = 1.0e-14
+    Kw_T = Kw * math.exp(-6710.0 * ((1.0 / T) - (1.0 / 298.0)))
+    Hn, Kn = 60.0 * tf(4200.0, T), _f32(1.7e-5) * tf(_f32(-450.0), T)
+    ca_den = 4.3e-7 * tf(-1000.0, T) * 4.68e-11 * tf(-1760.0, T)
+    ca_den = (4.3e-7 * tf(-1000.0, T)) * (4.68e-11 * tf(-1760.0, T)) * (3.4e-2 * tf(2.44e+3, T)) * 390.0e-6 * patm
+    ksp = 3.3e-9 * tf(-1200.0, T)
+    ipH, newpH, count = -math.log10(3.16227766016837953e-5), 0.0, 0
+    while abs(ipH - newpH) > _f32(0.01):
+        count += 1
+        if count > 1:
+            ipH = newpH
+        H = 10.0 ** (-ipH)
+        fHCO3, fCO3, dHCO3, dCO3 = di("CO2", H)
+        fHSO3, fSO3, dHSO3, dSO3 = di("SO2", H)
+        (fHNO3, dHNO3), (fHCl, dHCl), (fFA, dFA), (fAA, dAA) = (mono(k, H) for k in ("HNO3", "HCl", "FA", "AA"))
+        heff = Hn * (1.0 + ((Kn * H) / Kw_T))
+        fNH4 = H * Hn * Kn * (tnh3 * patm * (1.0 / (1.0 + (heff * RL * T * lwc)))) / Kw_T
+        dNH4 = (Kn * Hn * tnh3 * Kw_T * patm * (1.0 + Hn * RL * T * lwc)
+                / (Hn * RL * T * lwc * (Kw_T + Kn * H) + Kw_T) ** 2)
+        fCa, dCa = ksp * H * H / ca_den, 2.0 * ksp * H / ca_den
+        if fCa >= tdca:
+            D = (2.0 * so4nss) - (tna + 2.0 * tdca)
+            fca_t, dca_t = 0.0, 0.0
+        else:
+            D = (2.0 * so4nss) - tna
+            fca_t, dca_t = 2.0 * fCa, 2.0 * dCa
+        f = D - H + Kw / H + fHCO3 + 2.0 * fCO3 + fHSO3 + 2.0 * fSO3 + fHNO3 - fNH4 + fHCl + fFA + fAA
+        df = -1.0 - Kw / H / H + dHCO3 + 2.0 * dCO3 + dHSO3 + 2.0 * dSO3 + dHNO3 - dNH4 + dHCl + dFA + dAA
+        if fca_t:
+            f, df = f - fca_t, df - dca_t
+        nn = min(max(H - f / df, 1.0e-14), 1.0e-1)
+        if count > 50:
+            newpH = ((-math.log10(nn)) + (-math.log10(H))) / 2.0
+            break
+        newpH = -math.log10(nn)
+    hplus = 10.0 ** (-newpH)
+    ph = -1.0 * math.log10(hplus)
+    mn, fe = 0.0, 0.0
+    if lmetal:
+        fe_nat = dust * 35e-3
+        fe_ant = X("pFe") * cnv * 1.e+12 * X("AD") / (AIRMW / mw["pFe"]) / X("AIRVOL")
+        mn = ((fe_ant / 10.0) + (fe_nat / 50.0)) * 1e-9 / 54.94 / lwc * 1e-3 * 0.5
+        fe_d = (fe_ant * 1e-9 / mw["pFe"] / lwc * 1e-3) * 0.1 + (fe_nat * 1e-9 / mw["pFe"] / lwc * 1e-3) * 0.01
+        fe = fe_d * (0.1 if X("SUNCOS") > 0.0 else 0.9)
+    # AQCHEM_SO2
+    ex = lambda a, b: a * math.exp(b * (298.15 / T - 1.0))
+    Ks1, Ks2 = ex(1.30e-2, 6.75), ex(6.31e-8, 5.05)
+    xso2aq = 1.0 / (1.0 + Ks1 / hplus + Ks1 * Ks2 / (hplus * hplus))
+    xhso3 = 1.0 / (1.0 + hplus / Ks1 + Ks2 / hplus)
+    xso3 = 1.0 / (1.0 + hplus / Ks2 + hplus * hplus / (Ks1 * Ks2))
+    hcso2 = ex(1.22, 10.55)
+    fhcso2 = hcso2 * (1.0 + (Ks1 / hplus) + (Ks1 * Ks2 / (hplus * hplus)))
+    xso2g = 1.0 / (1.0 + (fhcso2 * RL * T * lwc))
+    siv = fhcso2 * xso2g * so2 * patm
+    fhch2o2 = ex(7.45e+4, 22.21) * (1.0 + (ex(2.20e-12, -12.52) / hplus))
+    xh2o2g = 1.0 / (1.0 + (fhch2o2 * RL * T * lwc))
+    kaq_h2o2 = 6.31e+14 * math.exp(-4.76e+3 / T) * Ks1 * fhch2o2 * hcso2 * xh2o2g * xso2g * patm * lwc * RL * T
+    hco3 = ex(1.13e-2, 8.51)
+    xo3g = 1.0 / (1.0 + (hco3 * RL * T * lwc))
+    ko1, ko2 = 3.49e+12 * math.exp(-4.83e+3 / T), 7.32e+14 * math.exp(-4.03e+3 / T)
+    kaq_o3 = (2.40e+4 * xso2aq + ko1 * xhso3 + ko2 * xso3) * fhcso2 * xso2g * patm * hco3 * xo3g * lwc * RL * T
+    kaq_o2 = fhcso2 * xso2g * ((750.0 * mn) + (2600.0 * fe) + (1e+10 * mn * fe)) * lwc * RL * T
+    hchcho = ex(2.5, 21.6)
+    xhchog = 1.0 / (1.0 + (hchcho * (1.0 + ex(2.53e+3, 13.48)) * RL * T * lwc))
+    kaq_hcho = ((ex(7.9e+2, -16.44) * xhso3 + ex(2.5e+7, -6.04) * xso3) * fhcso2 * xso2g * patm * hchcho * xhchog
+                * lwc * RL * T)
+    kaq_hms = ex(3.6e+3, -15.09) * (ex(1e-14, -22.51) / hplus) * 0.7
+    kaq_hms2 = ex(2.65e+8, -5.03) * 1.0e-19 * 0.7
+    kcld = [kaq_h2o2 * fc * cnv, kaq_o3 * fc * cnv, kaq_o2 * fc, kaq_hcho * fc * cnv, kaq_hms * fc,
+            kaq_hms2 * fc / C("SO2")]
+    size_res = 1 if (not (h2o2 > so2 + 1e-9) and lwc < 0.1e-6) else 0
+    return kcld, siv * xhso3, siv * xso3, ph, size_res, count
+
+
+def _cld_case(n, seed):
+    ir, cells, hin = _case(n, seed)
+    rng = np.random.default_rng(seed + 11)
+    sp = ir["species"]
+    lu = lambda lo, hi: np.exp(rng.uniform(np.log(lo), np.log(hi), n))
+    for name, lo, hi in (("SO2", 1e7, 1e12), ("H2O2", 1e7, 1e12), ("HCOOH", 1e6, 1e11), ("ACTA", 1e6, 1e11),
+                         ("HMS", 1e3, 1e9), ("CH2O", 1e8, 1e12), ("SO4s", 1e2, 1e8), ("HNO3", 1e6, 1e11)):
+        cells["c"][sp.index(name)] = lu(lo, hi)
+    return ir, cells, hin
+
+
+@pytest.mark.parametrize("lmetal", [1, 0])
+def test_oracle_set_so2_matches_python_restatement(orc, lmetal):
+    import gcchem.hetstate as hs
+
+    n = 1024
+    ir, cells, hin = _cld_case(n, 31)
+    hout, kcld, sr, it = orc.sulfur_cld_rates(hin, cells["c"], lmetal)
+    o = hs.HETIN_OFFSET
+    cloud = 0
+    for j in range(n):
+        k, hso3, so3, ph, s_, nit = _py_set_so2(hin[:, j], cells["c"][:, j], ir["species"], lmetal, hs.NONKPP_MW)
+        cloud += nit > 0
+        assert nit == it[j] and s_ == sr[j], j
+        got = [kcld[r, j] for r in range(6)] + [hout[o["HSO3_aq"], j], hout[o["SO3_aq"], j], hout[o["pHCloud"], j]]
+        np.testing.assert_allclose(got, k + [hso3, so3, ph], rtol=1e-12, atol=0, err_msg=str(j))
+    assert cloud > 100 and sr.sum() > 0 and (sr == 0).sum() > 0, (cloud, sr.sum())
+    assert np.all(hout[o["fupdateHOBr"]] == 1.0) and np.all(hout[o["fupdateHOCl"]] == 1.0)
+    # the rows SET_SO2 does not write are untouched
+    others = [r for r in range(hs.NHETIN)
+              if r not in (o["HSO3_aq"], o["SO3_aq"], o["pHCloud"], o["fupdateHOBr"], o["fupdateHOCl"])]
+    assert np.array_equal(hout[others], hin[others])
+
+
+@pytest.mark.gpu
+def test_gpu_set_so2_matches_oracle(orc):
+    import torch
+    import gcchem.capi as capi
+    import gcchem.hetstate as hs
+    from gcchem.rates_program import MET_FIELDS
+
+    n = 8192
+    ir, cells, hin = _cld_case(n, 32)
+    hout, kcld, sr, it = orc.sulfur_cld_rates(hin, cells["c"], 1)
+    o = hs.HETIN_OFFSET
+    k0 = MET_FIELDS.index("K_CLD0")
+    s = capi.Solver(0)
+    # host memory (numpy) and device memory (torch) give the same bits
+    met_h, hin_h = cells["met"].copy(), hin.copy()
+    met_h[k0:k0 + 6] = -1.0
+    sr_h = np.zeros(n, np.int32)
+    s.sulfur_cld_rates(hin_h, cells["c"], met_h, 1, sr_h)
+    T = lambda a: torch.tensor(a, device="cuda").contiguous()
+    met_d, hin_d, sr_d = T(met_h), T(hin), torch.zeros(n, dtype=torch.int32, device="cuda")
+    s.sulfur_cld_rates(hin_d, T(cells["c"]), met_d, 1, sr_d)
+    torch.cuda.synchronize()
+    assert np.array_equal(met_d.cpu().numpy(), met_h) and np.array_equal(hin_d.cpu().numpy(), hin_h)
+    assert np.array_equal(sr_d.cpu().numpy(), sr_h)
+    s.close()
+    others = [i for i, f in enumerate(MET_FIELDS) if not f.startswith("K_CLD")]
+    assert np.array_equal(met_h[others], cells["met"][others])
+    got = np.vstack([met_h[k0:k0 + 6], hin_h[[o["HSO3_aq"], o["SO3_aq"], o["pHCloud"]]]])
+    ref = np.vstack([kcld, hout[[o["HSO3_aq"], o["SO3_aq"], o["pHCloud"]]]])
+    cloud = it > 0
+    assert cloud.sum() > 1000
+    # CUDA's exp/log10/pow against glibc's: a Newton step whose |dpH| lands
+    # within rounding of the 0.01 stopping test may stop one iteration apart
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+    same = np.all(rel < 1e-11, axis=0)
+    print("SET_SO2 GPU vs oracle: %d cloudy cells, worst %.2e, %d cells off by a Newton step"
+          % (cloud.sum(), rel[:, same].max(), (~same).sum()))
+    assert (~same).sum() <= 0.005 * n
+    assert np.all(np.abs(got[8, ~same] - ref[8, ~same]) <= 0.011)  # pHCloud within one stopping tolerance
+    assert np.array_equal(sr_h[same], sr[same])
+
+
+@pytest.mark.gpu
+def test_gpu_sulfur_and_hetstate_producers_drive_a_step(orc):
+    """The producers in Do_FullChem's order on the GPU -- SulfurAqChem (K_MT),
+    SET_SO2 (K_CLD, cloud pH, HSO3/SO3 into the grid-box rows),
+    SetStateHet (HetState from those rows) -- then one chemistry step on
+    them; against the oracle's producers in the same order and its loop body
+    integrating the GPU's rates."""
+    import torch
+
+    import gcchem.capi as capi
+    import gcchem.inputs as inputs
+    from gcchem.rates_program import MET_FIELDS
+
+    n = 256
+    ir, cells, hin = _cld_case(n, 41)
+    atol, rtol = inputs.tolerances()
+    ic, rc = inputs.default_controls()
+    c = cells["c"].copy()
+    for fam in ir["families"]:
+        c[ir["species"].index(fam)] = 0.0
+    dev = torch.device("cuda", 0)
+    T = lambda a: torch.tensor(a, device=dev).contiguous()
+    s = capi.Solver(0, arith="strict", schedule="queue")
+    hin_d, c_d, met_d = T(hin), T(c), T(cells["met"])
+    het_d = torch.zeros((168, n), dtype=torch.float64, device=dev)
+    s.sulfur_aq_rates(hin_d, c_d, met_d)
+    s.sulfur_cld_rates(hin_d, c_d, met_d, 1)
+    s.set_state_het(hin_d, c_d, het_d, gamma_ho2=0.2, lpscchem=1, turn_off_het_rates=0)
+    torch.cuda.synchronize()
+    # oracle chain
+    kmt = orc.sulfur_aq_rates(hin, c, cells["met"][MET_FIELDS.index("TEMP")], cells["met"][MET_FIELDS.index("NUMDEN")])
+    hin_o, kcld, _, it = orc.sulfur_cld_rates(hin, c, 1)
+    h_ref = orc.set_state_het(hin_o, c, gamma_ho2=0.2, lpscchem=1, turn_off_het_rates=0)
+    met_g = met_d.cpu().numpy()
+    km, kc = MET_FIELDS.index("K_MT0"), MET_FIELDS.index("K_CLD0")
+    assert (it > 0).sum() > 30
+    np.testing.assert_allclose(met_g[km:km + 6], kmt, rtol=1e-13, atol=0)
+    # cells whose cloud pH agrees (a Newton step may stop one iteration
+    # apart where |dpH| is within rounding of 0.01: see the SET_SO2 test)
+    import gcchem.hetstate as hs
+    ph_g, ph_o = hin_d.cpu().numpy()[hs.HETIN_OFFSET["pHCloud"]], hin_o[hs.HETIN_OFFSET["pHCloud"]]
+    ok = np.abs(ph_g - ph_o) <= 1e-10 * np.abs(ph_o)
+    assert ok.mean() >= 0.98
+    np.testing.assert_allclose(met_g[kc:kc + 6, ok], kcld[:, ok], rtol=1e-10, atol=0)
+    np.testing.assert_allclose(het_d.cpu().numpy()[:, ok], h_ref[:, ok], rtol=1e-10, atol=0)
+    # one step on the GPU's rates and HetState
+    r = np.zeros((len(ir["rconst"]), n))
+    s.update_rconst(met_g, cells["photol"], c, r, het=het_d.cpu().numpy())
+    assert np.any(r[:, :] != orc.update_rconst(cells["met"], cells["photol"], c, het=h_ref))  # K_MT/K_CLD enter
+    c_ref, ist_ref, _, ierr_ref = orc.integrate(c, r, atol, rtol, 0.0, 600.0, ic, rc)
+    bad = ierr_ref < 0
+    if bad.any():
+        c2, ist2, _, ierr2 = orc.integrate(c[:, bad], r[:, bad], atol, rtol, 0.0, 600.0, ic, rc)
+        c_ref[:, bad], ist_ref[:, bad], ierr_ref[bad] = c2, ist2, ierr2
+    c_ref = np.maximum(c_ref, 0.0)
+    s.set_hetstate(het_d)
+    cg = T(cells["c"])
+    ist = torch.zeros((20, n), dtype=torch.int32, device=dev)
+    rst = torch.zeros((20, n), dtype=torch.float64, device=dev)
+    ierr = torch.zeros(n, dtype=torch.int32, device=dev)
+    s.fullchem_step(600.0, met_d, T(cells["photol"]), cg, T(atol), T(rtol), ic, rc, None, ist, rst, ierr)
+    torch.cuda.synchronize()
+    s.set_hetstate(None)
+    s.close()
+    cg, ist, ierr = cg.cpu().numpy(), ist.cpu().numpy(), ierr.cpu().numpy()
+    assert np.array_equal(ierr, ierr_ref)
+    same = np.all(ist[:8] == ist_ref[:8], axis=0)
+    assert same.mean() >= 0.99
+    big = np.abs(c_ref) > 1e4
+    rel = np.abs(cg - c_ref) / np.maximum(np.abs(c_ref), 1e-300)
+    assert np.max(np.where(big, rel, 0.0)[:, same]) < 1e-9
