@@ -51,6 +51,7 @@ EXPORTED = [
     "gc_kpp_set_state_het_batch",
     "gc_kpp_sulfur_aq_rates_batch",
     "gc_kpp_sulfur_cld_rates_batch",
+    "gc_kpp_het_drop_chem_batch",
     "gc_kpp_ctx_set_hetstate",
     "gc_kpp_ctx_set_autoreduce",
     "gc_kpp_fullchem_step",
@@ -100,6 +101,7 @@ def load_library(path=None, mech="fullchem"):
     lib.gc_kpp_set_state_het_batch.argtypes = [vp, i32, vp, i64, vp, i64, f64, i32, i32, vp, i64, i32, vp]
     lib.gc_kpp_sulfur_aq_rates_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, i32, vp]
     lib.gc_kpp_sulfur_cld_rates_batch.argtypes = [vp, i32, vp, i64, vp, i64, vp, i64, i32, vp, i32, vp]
+    lib.gc_kpp_het_drop_chem_batch.argtypes = [vp, i32, f64, vp, i64, vp, i64, vp, i64, vp, vp, i64, i32, vp]
     lib.gc_kpp_copy_rows.argtypes = [vp, i64, vp, i64, i64, i64, vp]
     lib.gc_kpp_photol_rows.argtypes = [vp]
     if path == _build.lib_path(mech):
@@ -357,6 +359,26 @@ class Solver:
         rc = self.lib.gc_kpp_sulfur_cld_rates_batch(self.ctx, ncell, _ptr(hetin), _ld(hetin, ncell), _ptr(c),
                                                     _ld(c, ncell), _ptr(met), _ld(met, ncell), int(lmetalcatso2),
                                                     _ptr(size_res), MEM_DEVICE if dev else MEM_HOST, s)
+        self._check(rc)
+
+    def het_drop_chem(self, dt, hetin, c, het, size_res, met, stream=None):
+        """Batched fullchem_HetDropChem (gc_kpp_het_drop_chem_batch): the
+        SRHOCl and SRHOBr rows of met [NMET, ncell] (in/out) from the grid-box
+        rows after SET_SO2, c, the HetState het [168, ncell] and size_res
+        [ncell] int32.  All numpy (host) or all CUDA torch tensors (device)."""
+        dev = _is_torch(met) and met.is_cuda
+        ncell = met.shape[1]
+        if not dev:
+            if not (isinstance(met, np.ndarray) and met.flags.c_contiguous and met.dtype == np.float64):
+                raise ValueError("met is written in place: a C-contiguous float64 numpy array")
+            hetin = np.ascontiguousarray(hetin, dtype=np.float64)
+            c = np.ascontiguousarray(c, dtype=np.float64)
+            het = np.ascontiguousarray(het, dtype=np.float64)
+            size_res = np.ascontiguousarray(size_res, dtype=np.int32)
+        s = ctypes.c_void_p(stream) if stream else None
+        rc = self.lib.gc_kpp_het_drop_chem_batch(self.ctx, ncell, float(dt), _ptr(hetin), _ld(hetin, ncell), _ptr(c),
+                                                 _ld(c, ncell), _ptr(het), _ld(het, ncell), _ptr(size_res),
+                                                 _ptr(met), _ld(met, ncell), MEM_DEVICE if dev else MEM_HOST, s)
         self._check(rc)
 
     def sulfur_aq_rates(self, hetin, c, met, stream=None):

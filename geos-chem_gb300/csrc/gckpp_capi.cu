@@ -1277,6 +1277,73 @@ int gc_kpp_sulfur_aq_rates_batch(gc_kpp_ctx* c, int ncell, const double* hetin, 
   return GC_KPP_OK;
 }
 
+int gc_kpp_het_drop_chem_batch(gc_kpp_ctx* c, int ncell, double dt, const double* hetin, long long ldi,
+                               const double* conc, long long ldc, const double* het, long long ldh, const int* size_res,
+                               double* met, long long ldm, int mem, void* stream) {
+  if (!c) return fail(GC_KPP_EINVAL, "ctx is NULL");
+  if (ncell < 0) return fail(GC_KPP_EINVAL, "ncell < 0");
+  if (ncell == 0) return GC_KPP_OK;
+  if (!hetin || !conc || !het || !size_res || !met) return fail(GC_KPP_EINVAL, "required array is NULL");
+  if (ldi < ncell || ldc < ncell || ldh < ncell || ldm < ncell)
+    return fail(GC_KPP_EINVAL, "leading dimension smaller than ncell");
+  if (!(dt > 0.0)) return fail(GC_KPP_EINVAL, "dt must be positive");
+  if (mem != GC_KPP_MEM_HOST && mem != GC_KPP_MEM_DEVICE) return fail(GC_KPP_EINVAL, "bad mem kind");
+  GC_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  gchet::HetDropArgs a{};
+  a.ncell = ncell;
+  a.dt = dt;
+  for (int k = 0; k < HSS_N; ++k) a.ind[k] = RT::hss_ind[k];
+  const gcrates::RatesDev& rp = c->rates;
+  a.hs_ind = rp.hs_ind;
+  a.hs_mw = rp.hs_mw;
+  a.hs_srmw = rp.hs_srmw;
+  a.hs_hk0 = rp.hs_hk0;
+  a.hs_hcr = rp.hs_hcr;
+  const size_t n = (size_t)ncell;
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(c->h_hetin.ensure((size_t)HETIN_NFIELD * n * sizeof(double)));
+    GC_CUDA(c->h_c.ensure(T::NSPEC * n * sizeof(double)));
+    GC_CUDA(c->h_het.ensure((size_t)HET_NFIELD * n * sizeof(double)));
+    GC_CUDA(c->h_met.ensure(RT::NMET * n * sizeof(double)));
+    GC_CUDA(c->h_ie.ensure(n * sizeof(int)));
+    GC_CUDA(gcutil::copy_rows(c->h_hetin.p, n * sizeof(double), hetin, ldi * sizeof(double), n * sizeof(double),
+                              HETIN_NFIELD, s));
+    GC_CUDA(gcutil::copy_rows(c->h_c.p, n * sizeof(double), conc, ldc * sizeof(double), n * sizeof(double),
+                              T::NSPEC, s));
+    GC_CUDA(gcutil::copy_rows(c->h_het.p, n * sizeof(double), het, ldh * sizeof(double), n * sizeof(double),
+                              HET_NFIELD, s));
+    GC_CUDA(gcutil::copy_rows(c->h_met.p, n * sizeof(double), met, ldm * sizeof(double), n * sizeof(double),
+                              RT::NMET, s));
+    GC_CUDA(gcutil::copy_rows(c->h_ie.p, n * sizeof(int), size_res, n * sizeof(int), n * sizeof(int), 1, s));
+    a.in = (const double*)c->h_hetin.p;
+    a.c = (const double*)c->h_c.p;
+    a.het = (const double*)c->h_het.p;
+    a.met = (double*)c->h_met.p;
+    a.size_res = (const int*)c->h_ie.p;
+    a.ldi = a.ldc = a.ldh = a.ldm = ncell;
+  } else {
+    a.in = hetin;
+    a.ldi = ldi;
+    a.c = conc;
+    a.ldc = ldc;
+    a.het = het;
+    a.ldh = ldh;
+    a.met = met;
+    a.ldm = ldm;
+    a.size_res = size_res;
+  }
+  cudaError_t e = gchet::het_drop_chem(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "HetDropChem kernel launch");
+  if (mem == GC_KPP_MEM_HOST) {
+    GC_CUDA(gcutil::copy_rows(met + (long long)GC_KPP_MET_SRHOCL * ldm, ldm * sizeof(double),
+                              a.met + (long long)GC_KPP_MET_SRHOCL * ncell, n * sizeof(double), n * sizeof(double), 2,
+                              s));
+    GC_CUDA(cudaStreamSynchronize(s));
+  }
+  return GC_KPP_OK;
+}
+
 int gc_kpp_sulfur_cld_rates_batch(gc_kpp_ctx* c, int ncell, double* hetin, long long ldi, const double* conc,
                                   long long ldc, double* met, long long ldm, int lmetalcatso2, int* size_res, int mem,
                                   void* stream) {

@@ -94,7 +94,7 @@
 #define HET_TurnOffHetRates 166
 #define HET_SUNCOS 167
 // rows of the cell-interleaved fullchem_SetStateHet input array
-#define HETIN_NFIELD 111
+#define HETIN_NFIELD 115
 #define HETIN_T 0
 #define HETIN_CLDF 1
 #define HETIN_QI 2
@@ -136,6 +136,10 @@
 #define HETIN_NH3 102
 #define HETIN_DSTbin 103  /* 7 rows */
 #define HETIN_pFe 110
+#define HETIN_OMEGA 111
+#define HETIN_U 112
+#define HETIN_V 113
+#define HETIN_IsWater 114
 // KPP species read by fullchem_SetStateHet and fullchem_SulfurAqChem, in the order of the index table
 #define HSS_SO2 0
 #define HSS_HNO3 1
@@ -157,8 +161,12 @@
 #define HSS_HMS 17
 #define HSS_HCOOH 18
 #define HSS_ACTA 19
-#define HSS_N 20
+#define HSS_HOCl 20
+#define HSS_HOBr 21
+#define HSS_N 22
 // MW_g of the non-KPP species SET_SO2 reads (species database)
 #define HSS_MW_DSTbin1 29.0
 #define HSS_MW_pFe 55.85
 #define HSS_MW_SALA 31.4
+#define HSS_MW_SALC 31.4
+#define HSS_MW_SO4 96.06

@@ -12,6 +12,7 @@
 //   fullchem_SulfurAqChem (K_MT)    KPP/fullchem/fullchem_SulfurChemFuncs.F90:120-305
 //   fullchem_SulfurCldChem / SET_SO2 (K_CLD, cloud pH, HSO3_aq, SO3_aq)
 //                                   :320-398, 865-1620, 1635-3549
+//   fullchem_HetDropChem (SRHOCl, SRHOBr)  :414-790, 808-849
 //
 // One thread per cell.  Inputs are rows of a cell-interleaved array
 // (HETIN_* of het_layout.h); outputs the HET_NFIELD rows of the HetState
@@ -600,7 +601,133 @@ __global__ void sulfur_cld_kernel(SulfurCldArgs a) {
 
 }  // namespace so2
 
+// ---------------------------------------------------------------------------
+// fullchem_HetDropChem (KPP/fullchem/fullchem_SulfurChemFuncs.F90:414-790,
+// WhenExpCantBeDone :808-849) where Do_FullChem calls it
+// (GeosCore/fullchem_mod.F90:913-934): the share of SO2 that the
+// size-resolved droplet chemistry (Yuen et al. 1996) adds to the HOCl and
+// HOBr oxidation, as the rate coefficients SRHOCl and SRHOBr.
+namespace drop {
+
+constexpr double AIRMW = 28.9644, G0 = 9.80665, PI_PHYS = 3.14159265358979323;
+constexpr double SS_DEN = 2200.0;
+// RG_S**3 and NINE_HALVES * LOG(SIG_S)**2 of the Fortran are constant
+// expressions of PARAMETERs, folded by the compiler with correct rounding of
+// each operation: (0.4e-6)**3 and 4.5 * log(1.8)**2
+constexpr double RG_S3 = 0x1.2e3b40a0e9b4fp-64, ARG_SS = 0x1.8e02146ec938fp+0;
+
+// second-order loss of R1 with R2 over DT at rate K, or WhenExpCantBeDone
+__device__ __forceinline__ double loss2(double R1, double R2, double K, double DT) {
+  const double Arg = (R1 - R2) * (K * DT);
+  if (fabs(Arg) < 709.0 && fabs(Arg) > 0.0) {
+    const double XX = exp(Arg);
+    return (R1 * R2) * (XX - 1.0) / ((R1 * XX) - R2);
+  }
+  const double DIFF = R1 - R2;
+  if (DIFF < 0.0) return R1;
+  if (DIFF > 0.0) return R2;
+  return R1 - 1.0 / (K * DT + (1.0 / R1));
+}
+
+__global__ void het_drop_kernel(HetDropArgs a) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= a.ncell) return;
+  auto in = [&](int f) { return a.in[(long long)f * a.ldi + cell]; };
+  auto c = [&](int sp) {
+    const int i = a.ind[sp];
+    return i >= 0 ? a.c[(long long)i * a.ldc + cell] : 0.0;
+  };
+  auto met = [&](int f) { return a.met[(long long)f * a.ldm + cell]; };
+  double srhocl = 0.0, srhobr = 0.0;
+  const double FC = in(HETIN_CLDF), TEMP = met(0);
+  if (FC > 1.0e-4) {
+    const double LWC = (in(HETIN_QL) * in(HETIN_AIRDEN) * 1.0e-3 / FC);
+    if (a.size_res[cell] && in(HETIN_IsWater) != 0.0 && TEMP > 268.15 && LWC > 1.0e-20) {
+      // the four sulfite uptake laws at this cell's HetState
+      gcrates::Env E;
+      gcrates::env_init(E, met(0), met(1), met(2), met(3), met(4), met(5));
+      gcrates::HetCell X;
+      X.H = a.het;
+      X.ldh = a.ldh;
+      X.C = a.c;
+      X.ldc = a.ldc;
+      X.cell = cell;
+      X.sp = gcrates::HetSpecies{a.hs_ind, a.hs_mw, a.hs_srmw, a.hs_hk0, a.hs_hcr};
+      gcrates::het_cell_init(X, E);
+      const double CVF = 1.0e3 * AIRMW / (in(HETIN_AIRDEN) * AVO);
+      const double DT = a.dt;
+      const double so2 = c(HSS_SO2) * CVF;
+      const double XX1 = loss2(so2, c(HSS_H2O2) * CVF, met(12) / CVF / FC, DT);
+      const double XX2 = loss2(so2, c(HSS_O3) * CVF, met(13) / CVF / FC, DT);
+      double XX3 = 0.0;
+      const double Arg3 = (-met(14) / FC) * DT;
+      if (fabs(Arg3) < 709.0) XX3 = so2 * (1.0 - exp(Arg3));
+      const double r_hso3 = c(HSS_SO2) * CVF * in(HETIN_HSO3_aq);
+      const double r_so3 = c(HSS_SO2) * CVF * in(HETIN_SO3_aq);
+      const double hocl = c(HSS_HOCl) * CVF, hobr = c(HSS_HOBr) * CVF;
+      double XX4 = loss2(r_hso3, hocl, gcrates::HOClUptkByHSO3m(X) / CVF, DT);
+      XX4 = XX4 + loss2(r_so3, hocl, gcrates::HOClUptkBySO3mm(X) / CVF, DT);
+      double XX5 = loss2(r_hso3, hobr, gcrates::HOBrUptkByHSO3m(X) / CVF, DT);
+      XX5 = XX5 + loss2(r_so3, hobr, gcrates::HOBrUptkBySO3mm(X) / CVF, DT);
+      // the Fortran's R1 is the SO3-- term at this point
+      double xx[5] = {XX1, XX2, XX3, XX4, XX5};
+      double LST = xx[0] + xx[1] + xx[2] + xx[3] + xx[4];
+      if (LST > r_so3) {
+        for (int k = 0; k < 5; ++k) xx[k] = (r_so3 * xx[k]) / LST;
+        LST = xx[0] + xx[1] + xx[2] + xx[3] + xx[4];
+      }
+      const double NH3 = in(HETIN_NH3) * CVF * 1.0e+12;
+      const double SO2 = fmax(c(HSS_SO2) * CVF - (LST * FC), 1.0e-20) * 1.0e+12;
+      const double H2O2 = c(HSS_H2O2) * CVF * 1.0e12;
+      const double HNO3 = c(HSS_HNO3) * CVF * 1.0e12;
+      const double AD = in(HETIN_AD), AIRVOL = in(HETIN_AIRVOL);
+      const double SO4 = (c(HSS_SO4) * CVF * AD * 1.0e+9) / ((AIRMW / HSS_MW_SO4) * AIRVOL);
+      const double B = (LST * AD * 1.0e+9) / ((AIRMW / HSS_MW_SO4) * AIRVOL);
+      const double CNss = in(HETIN_SALC) * CVF * AD / ((AIRMW / HSS_MW_SALC) * AIRVOL);
+      const double CN = (0.75 * CNss) / (PI_PHYS * SS_DEN * RG_S3 * exp(ARG_SS)) * 1.e-6;
+      // Yuen et al.'s coefficients by SO2 [pptv]: B, NH3, SO2, H2O2, HNO3, W, CN, SO4
+      static constexpr double AL[4][8] = {
+          {0.5318, -1.67e-7, 2.59e-6, -1.77e-7, -1.72e-7, 1.22e-6, 4.58e-6, -1.00e-5},
+          {0.5591, 3.62e-6, 1.66e-6, 1.06e-7, -5.45e-7, -5.79e-7, 1.63e-5, -7.40e-6},
+          {1.1547, -4.28e-8, -1.23e-7, -9.05e-7, 1.73e-7, 7.22e-6, 2.44e-5, 3.25e-5},
+          {1.1795, 2.57e-7, -5.54e-7, -1.08e-6, 1.95e-6, 6.14e-6, 1.64e-5, 2.48e-6}};
+      const int bin = SO2 <= 200.0 ? 0 : SO2 <= 500.0 ? 1 : SO2 < 1000.0 ? 2 : 3;
+      const double* al = AL[bin];
+      const double W = -in(HETIN_OMEGA) / (in(HETIN_AIRDEN) * G0) * 100.0;
+      const double APV = sqrt(in(HETIN_U) * in(HETIN_U) + in(HETIN_V) * in(HETIN_V)) + (W * W * 1.0e-4);
+      const double H = DT * APV;
+      const double sum_gas = (al[1] * NH3) + (al[2] * SO2) + (al[3] * H2O2) + (al[4] * HNO3);
+      const double DSVI = (al[0] * B) + (((al[6] * CN) + (al[5] * W) + (al[7] * SO4) + sum_gas) * H);
+      double SR = 0.0;
+      if (W > 0.0 && c(HSS_SO2) > 0.0) {
+        SR = fmax((DSVI - B), 0.0);
+        if (SR > 0.0) {
+          SR = SR * (AIRMW / HSS_MW_SO4) * 1.e-9 / in(HETIN_AIRDEN);
+          SR = fmin(SR, SO2 / 1.0e12);
+        }
+      }
+      SR = SR / CVF / DT;
+      const double DENOM = xx[1] + xx[3] + xx[4];
+      srhocl = SR * gcrates::SafeDiv(xx[3], DENOM, 0.0);
+      srhobr = SR * gcrates::SafeDiv(xx[4], DENOM, 0.0);
+      srhocl = gcrates::SafeDiv(srhocl, (c(HSS_SO2) * c(HSS_HOCl)), 0.0);
+      srhobr = gcrates::SafeDiv(srhobr, (c(HSS_SO2) * c(HSS_HOBr)), 0.0);
+    }
+  }
+  a.met[(long long)4 * a.ldm + cell] = srhocl;
+  a.met[(long long)5 * a.ldm + cell] = srhobr;
+}
+
+}  // namespace drop
+
 }  // namespace
+
+cudaError_t het_drop_chem(const HetDropArgs& a, cudaStream_t s) {
+  if (a.ncell <= 0) return cudaSuccess;
+  const int block = 128;
+  drop::het_drop_kernel<<<(a.ncell + block - 1) / block, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
 
 cudaError_t sulfur_cld_rates(const SulfurCldArgs& a, cudaStream_t s) {
   if (a.ncell <= 0) return cudaSuccess;

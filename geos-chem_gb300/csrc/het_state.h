@@ -63,4 +63,26 @@ struct SulfurCldArgs {
 
 cudaError_t sulfur_cld_rates(const SulfurCldArgs& a, cudaStream_t s);
 
+// fullchem_HetDropChem under Do_FullChem's call conditions: SRHOCl and
+// SRHOBr, the size-resolved cloud-droplet S(IV) oxidation by HOCl and HOBr
+// (Yuen et al. 1996), into their met rows (0 where it is not called).
+struct HetDropArgs {
+  int ncell;
+  double dt;             // chemistry time step [s]
+  const double* in;      // HETIN_NFIELD rows (after SET_SO2)
+  long long ldi;
+  const double* c;       // NSPEC rows
+  long long ldc;
+  const double* het;     // HET_NFIELD rows of fullchem_SetStateHet
+  long long ldh;
+  const int* size_res;   // [ncell] from SET_SO2
+  double* met;           // TEMP, NUMDEN, H2O, PRESS and K_CLD read; SRHOCl, SRHOBr written
+  long long ldm;
+  int ind[HSS_N];        // KPP index of each HSS_* species
+  const int* hs_ind;     // the heterogeneous laws' species tables (gcrates::HetSpecies)
+  const double *hs_mw, *hs_srmw, *hs_hk0, *hs_hcr;
+};
+
+cudaError_t het_drop_chem(const HetDropArgs& a, cudaStream_t s);
+
 }  // namespace gchet

@@ -59,12 +59,14 @@ DU1, SUL, BKC, ORC, SSA, SSC, SLA, IIC = 1, 8, 9, 10, 11, 12, 13, 14
 
 # Grid-box inputs of the per-cell producers before Update_RCONST --
 # fullchem_SetStateHet (KPP/fullchem/fullchem_HetStateFuncs.F90:48-244),
-# fullchem_SulfurAqChem and fullchem_SulfurCldChem / SET_SO2
-# (KPP/fullchem/fullchem_SulfurChemFuncs.F90:120-305, 865-1620) -- per cell,
+# fullchem_SulfurAqChem, fullchem_SulfurCldChem / SET_SO2 and
+# fullchem_HetDropChem (KPP/fullchem/fullchem_SulfurChemFuncs.F90:120-305,
+# 414-790, 865-1620) -- per cell,
 # as rows of a cell-interleaved array ``hetin[f * ldi + cell]``: the State_Met
 # and State_Chm fields they read, in their units (State_Met: T [K], CLDF [1],
 # QI/QL [kg/kg], AIRVOL [m3], AIRDEN [kg/m3], AD [kg], FRLAND/FROCEAN [1],
-# InStratosphere 0/1, PMID_DRY [hPa]; State_Chm: aerosol areas [cm2/cm3],
+# InStratosphere 0/1, PMID_DRY [hPa], OMEGA [Pa/s], U/V [m/s], IsWater 0/1;
+# State_Chm: aerosol areas [cm2/cm3],
 # radii [cm], AeroH2O [cm3/m3], ISORROPIA/HETP water, molalities, H+ and pH,
 # cloud pH, HSO3_aq/SO3_aq [mol/L], fupdateHOBr/HOCl, KHETI_SLA, STATE_PSC,
 # and the concentrations [molec/cm3] of the species that are not KPP
@@ -82,6 +84,9 @@ HETIN_FIELDS = [
     ("SALCAL", 1), ("fupdateHOBr", 1), ("fupdateHOCl", 1), ("KHETI_SLA", 11), ("STATE_PSC", 1), ("SUNCOS", 1),
     # read by SET_SO2 only
     ("PMID_DRY", 1), ("NH4", 1), ("NH3", 1), ("DSTbin", 7), ("pFe", 1),
+    # read by fullchem_HetDropChem only: pressure velocity [Pa/s], winds
+    # [m/s], State_Met%IsWater 0/1
+    ("OMEGA", 1), ("U", 1), ("V", 1), ("IsWater", 1),
 ]
 HETIN_OFFSET = {}
 _o = 0
@@ -92,10 +97,10 @@ NHETIN = _o
 # KPP species that fullchem_SetStateHet and fullchem_SulfurAqChem read
 # through C(ind_X)
 SETSTATE_SPECIES = ["SO2", "HNO3", "HCl", "HBr", "BrSALA", "BrSALC", "SALACL", "SALCCL", "NIT", "NITs", "SO4",
-                    "SALAAL", "SALCAL", "O3", "H2O2", "CH2O", "SO4s", "HMS", "HCOOH", "ACTA"]
-# MW_g of the non-KPP species whose mass SET_SO2 converts (run/shared/
-# species_database.yml: DSTbin1, pFe, SALA)
-NONKPP_MW = {"DSTbin1": 29.0, "pFe": 55.85, "SALA": 31.4}
+                    "SALAAL", "SALCAL", "O3", "H2O2", "CH2O", "SO4s", "HMS", "HCOOH", "ACTA", "HOCl", "HOBr"]
+# MW_g of the species whose mass SET_SO2 and HetDropChem convert
+# (run/shared/species_database.yml: DSTbin1, pFe, SALA, SALC, SO4)
+NONKPP_MW = {"DSTbin1": 29.0, "pFe": 55.85, "SALA": 31.4, "SALC": 31.4, "SO4": 96.06}
 
 
 def emit_c():
@@ -289,4 +294,8 @@ def hetin_cells(n, seed=0, strat_fraction=0.15, cloud_fraction=0.5):
     h[o["NH3"]] = lu(1e6, 1e11)
     h[o["DSTbin"]:o["DSTbin"] + 7] = lu(1e2, 1e8, (7, n)) * (rng.uniform(size=n) < 0.7)
     h[o["pFe"]] = lu(1e1, 1e6)
+    h[o["OMEGA"]] = rng.normal(0.0, 0.3, n)
+    h[o["U"]] = rng.normal(0.0, 10.0, n)
+    h[o["V"]] = rng.normal(0.0, 8.0, n)
+    h[o["IsWater"]] = 1.0 - land.round()
     return h

@@ -199,7 +199,8 @@ int gc_kpp_update_rconst_batch(gc_kpp_ctx* ctx, int ncell, const double* met, lo
  * computes it.  Mechanisms other than fullchem keep their heterogeneous
  * rates at 0. */
 /* Rows of the grid-box input array of gc_kpp_set_state_het_batch,
- * gc_kpp_sulfur_aq_rates_batch and gc_kpp_sulfur_cld_rates_batch: the
+ * gc_kpp_sulfur_aq_rates_batch, gc_kpp_sulfur_cld_rates_batch and
+ * gc_kpp_het_drop_chem_batch: the
  * State_Met and State_Chm fields of the grid box that fullchem_SetStateHet,
  * fullchem_SulfurAqChem and SET_SO2 read, in their units (T, CLDF, QI, QL,
  * AIRVOL, AIRDEN, AD, FRLAND, FROCEAN, InStratosphere, aClArea, aClRadi,
@@ -209,9 +210,10 @@ int gc_kpp_update_rconst_batch(gc_kpp_ctx* ctx, int ncell, const double* met, lo
  * the sea-salt species SALA, SALAAL, SALC, SALCAL [molec/cm3],
  * fupdateHOBr, fupdateHOCl, KHETI_SLA(11), STATE_PSC), then SUNCOS, then
  * SET_SO2's PMID_DRY [hPa] and the non-KPP species NH4, NH3, DSTbin1..7,
- * pFe [molec/cm3]; 111 rows.  Row offsets: the HETIN_* macros of
+ * pFe [molec/cm3], then HetDropChem's OMEGA [Pa/s], U, V [m/s] and IsWater
+ * (0/1); 115 rows.  Row offsets: the HETIN_* macros of
  * geos-chem_gb300/csrc/het_layout.h. */
-#define GC_KPP_NHETIN 111
+#define GC_KPP_NHETIN 115
 
 /* Batched fullChem_SetStateHet (KPP/fullchem/fullchem_HetStateFuncs.F90:
  * 48-244, with Cld_Params, Get_Theta_Ice and Halide_Conc; called at
@@ -277,6 +279,29 @@ int gc_kpp_sulfur_aq_rates_batch(gc_kpp_ctx* ctx, int ncell, const double* hetin
 int gc_kpp_sulfur_cld_rates_batch(gc_kpp_ctx* ctx, int ncell, double* hetin, long long ldi, const double* c,
                                   long long ldc, double* met, long long ldm, int lmetalcatso2, int* size_res,
                                   int mem, void* stream);
+
+/* Batched fullchem_HetDropChem (KPP/fullchem/fullchem_SulfurChemFuncs.F90:
+ * 414-790) with Do_FullChem's call conditions (GeosCore/fullchem_mod.F90:
+ * 913-934: CLDF > 1e-4, size_res from gc_kpp_sulfur_cld_rates_batch, the
+ * IsWater row set, TEMP > 268.15 K, in-cloud liquid water > 1e-20): the
+ * size-resolved cloud-droplet oxidation of S(IV) by HOCl and HOBr (Yuen et
+ * al. 1996) as the rate coefficients SRHOCl and SRHOBr, which the step's
+ * HOCl + SO2 and HOBr + SO2 rates add (0 where the conditions fail, as
+ * fullchem_mod.F90:575-577 resets them).  Call after
+ * gc_kpp_set_state_het_batch: the sulfite uptake laws read its HetState.
+ *
+ *   dt       chemistry time step [s]
+ *   hetin    [GC_KPP_NHETIN][ldi] in  grid-box rows after SET_SO2 (HSO3_aq,
+ *                                     SO3_aq, CLDF, QL, AIRDEN, AD, AIRVOL,
+ *                                     NH3, SALC, OMEGA, U, V, IsWater read)
+ *   c        [NSPEC][ldc] in          SO2, H2O2, O3, HOCl, HOBr, HNO3, SO4
+ *   het      [GC_KPP_NHET][ldh] in    HetState rows
+ *   size_res [ncell] in
+ *   met      [GC_KPP_NMET][ldm] in/out TEMP, NUMDEN, H2O, PRESS, K_CLD(1:3)
+ *                                     read; the SRHOCL and SRHOBR rows written */
+int gc_kpp_het_drop_chem_batch(gc_kpp_ctx* ctx, int ncell, double dt, const double* hetin, long long ldi,
+                               const double* c, long long ldc, const double* het, long long ldh, const int* size_res,
+                               double* met, long long ldm, int mem, void* stream);
 
 /* HetState of the cells of the following chemistry steps on this context
  * (gc_kpp_fullchem_step and its ordered/binned/learned forms evaluate the

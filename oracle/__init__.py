@@ -59,6 +59,8 @@ def load(variant="strict", mech="fullchem"):
     lib.oracle_set_state_het_batch.argtypes = [i32, vp, i64, vp, i64, f64, i32, i32, vp, i64]
     lib.oracle_sulfur_aq_rates_batch.argtypes = [i32, vp, i64, vp, i64, vp, vp, vp, i64]
     lib.oracle_sulfur_cld_rates_batch.argtypes = [i32, vp, i64, vp, i64, i32, vp, i64, vp, vp]
+    lib.oracle_het_drop_chem_batch.argtypes = [i32, f64, vp, i64, vp, i64, vp, i64, vp, vp, i64]
+    lib.oracle_sulfite_uptakes.argtypes = [vp, vp, vp, i64, vp]
     _libs[key] = lib
     return lib
 
@@ -167,6 +169,35 @@ def sulfur_cld_rates(hetin, c, lmetalcatso2=1, mech="fullchem"):
     it = np.zeros(n, np.int32)
     lib.oracle_sulfur_cld_rates_batch(n, _p(hetin), n, _p(c), n, int(lmetalcatso2), _p(kcld), n, _p(sr), _p(it))
     return hetin, kcld, sr, it
+
+
+def sulfite_uptakes(met, c, het, mech="fullchem"):
+    """HOClUptkByHSO3m, HOClUptkBySO3mm, HOBrUptkByHSO3m, HOBrUptkBySO3mm of
+    every cell [4, n] (met [18, n], c [NSPEC, n], HetState het [168, n])."""
+    lib = load("strict", mech)
+    met, c, het = _c(met, np.float64), _c(c, np.float64), _c(het, np.float64)
+    n = met.shape[1]
+    out = np.zeros((4, n))
+    for j in range(n):
+        m = np.ascontiguousarray(met[:, j])
+        cc = np.ascontiguousarray(c[:, j])
+        o = np.zeros(4)
+        lib.oracle_sulfite_uptakes(_p(m), _p(cc), _p(het[:, j:]), n, _p(o))
+        out[:, j] = o
+    return out
+
+
+def het_drop_chem(dt, hetin, c, het, size_res, met, mech="fullchem"):
+    """Batched fullchem_HetDropChem under Do_FullChem's call conditions:
+    returns met [18, n] with the SRHOCl and SRHOBr rows rewritten (0 where
+    it is not called)."""
+    lib = load("strict", mech)
+    hetin, c, het = _c(hetin, np.float64), _c(c, np.float64), _c(het, np.float64)
+    sr = _c(size_res, np.int32)
+    met = _c(met, np.float64).copy()
+    n = met.shape[1]
+    lib.oracle_het_drop_chem_batch(n, float(dt), _p(hetin), n, _p(c), n, _p(het), n, _p(sr), _p(met), n)
+    return met
 
 
 def fun_split(v, f, rct, mech="fullchem"):

@@ -294,6 +294,23 @@ def generate_rates(ir):
     L.append("void oracle_update_rconst(const double* met, const double* PHOTOL, const double* C, double* RCONST) {")
     L.append("  oracle_update_rconst_het(met, PHOTOL, C, 0, 0, RCONST);")
     L.append("}")
+    # the four sulfite uptake laws that fullchem_HetDropChem calls
+    # (KPP/fullchem/fullchem_SulfurChemFuncs.F90:565-640)
+    L += ["void oracle_sulfite_uptakes(const double* met, const double* C, const double* het, long long ldh,",
+          "                            double* out) {"]
+    if het_laws:
+        L += ["  rate_env_t E;",
+              "  rate_env_init(&E, met[0], met[1], met[2], met[3], met[4], met[5]);",
+              "  het_cell_t X;",
+              "  het_cell_load(&X, &E, het, ldh, C);",
+              "  out[0] = o_HOClUptkByHSO3m(&X);",
+              "  out[1] = o_HOClUptkBySO3mm(&X);",
+              "  out[2] = o_HOBrUptkByHSO3m(&X);",
+              "  out[3] = o_HOBrUptkBySO3mm(&X);"]
+    else:
+        L += ["  (void)met; (void)C; (void)het; (void)ldh;",
+              "  out[0] = out[1] = out[2] = out[3] = 0.0;"]
+    L.append("}")
     return "\n".join(L) + "\n", sorted(het)
 
 

@@ -24,6 +24,7 @@
 #include <stdbool.h>
 #include <string.h>
 
+#include "kpp_dims.h"
 #include "oracle_het_layout.h"
 
 #define S_AVO 6.022140857e+23
@@ -971,5 +972,162 @@ void oracle_sulfur_cld_rates_batch(int ncell, double* in, long long ldi, const d
     in[(long long)OHIN_fupdateHOCl * ldi + cell] = 1.0;
     if (size_res) size_res[cell] = sr;
     if (niter) niter[cell] = it;
+  }
+}
+
+/* ------------------------------------------------------------------------
+ * fullchem_HetDropChem (KPP/fullchem/fullchem_SulfurChemFuncs.F90:414-790)
+ * with WhenExpCantBeDone (:808-849), IsSafeExp / SafeExp (KPP/fullchem/
+ * rateLawUtilFuncs.F90:497-523), called from Do_FullChem where
+ * (GeosCore/fullchem_mod.F90:913-934) the box is cloudy (CLDF > 1e-4),
+ * SET_SO2 set size_res, the surface is water, TEMP > 268.15 K and the
+ * in-cloud liquid water content exceeds 1e-20; elsewhere SRHOCl = SRHOBr =
+ * 0 (fullchem_mod.F90:575-577).  The four sulfite uptake laws come from the
+ * oracle's rate laws (oracle_sulfite_uptakes, generated with Update_RCONST).
+ * RG_S**3 and NINE_HALVES * LOG(SIG_S)**2 are constant expressions of
+ * PARAMETERs, which the Fortran compiler folds with correct rounding of each
+ * operation; their values are written out as such.
+ */
+void oracle_sulfite_uptakes(const double* met, const double* C, const double* het, long long ldh, double* out);
+
+#define S_G0 9.80665
+#define S_PI_PHYS 3.14159265358979323
+
+static double when_exp_cant(double R1, double R2, double K, double DT) {
+  double DIFF = R1 - R2;
+  if (DIFF < 0.0) return R1;
+  if (DIFF > 0.0) return R2;
+  return R1 - 1.0 / (K * DT + (1.0 / R1));
+}
+
+static int is_safe_exp(double x) { return fabs(x) < 709.0; }
+
+/* the second-order loss of R1 and R2 over DT at rate K (the XX1/XX2/XX4/XX5
+ * blocks of the Fortran) */
+static double loss2(double R1, double R2, double K, double DT) {
+  double Arg = (R1 - R2) * (K * DT);
+  if (is_safe_exp(Arg) && fabs(Arg) > 0.0) {
+    double XX = exp(Arg);
+    return (R1 * R2) * (XX - 1.0) / ((R1 * XX) - R2);
+  }
+  return when_exp_cant(R1, R2, K, DT);
+}
+
+static void het_drop_cell(const double* in, long long ldi, const double* c, long long ldc, const double* met,
+                          long long ldm, const double* het, long long ldh, double DT, int size_res, double* srhocl,
+                          double* srhobr) {
+#define IN(f) in[(long long)(f) * ldi]
+#define CC(s) ss_C(c, ldc, s)
+  const double SS_DEN = 2200.0, RG_S3 = 0x1.2e3b40a0e9b4fp-64 /* (0.4e-6)**3 */;
+  const double THREE_FOURTHS = 3.0 / 4.0, ARG_SS = 0x1.8e02146ec938fp+0 /* 9/2 * LOG(1.8)**2 */;
+  double M[18], Cc[ORACLE_NSPEC], up[4];
+  double CVF, DTCHEM, FC, R1, R2, K, Arg, XX, XX1, XX2, XX3, XX4, XX5, LST;
+  double NH3, SO2, H2O2, HNO3, SO4, B, CNss, NDss, CN, W, APV, H, sum_gas, DSVI, SR, DENOM, LWC;
+  double aB, aNH3, aSO2, aH2O2, aHNO3, aW, aCN, aSO4;
+  double TEMP = met[0];
+  *srhocl = 0.0;
+  *srhobr = 0.0;
+  if (!(IN(OHIN_CLDF) > 1.0e-4)) return;
+  LWC = (IN(OHIN_QL) * IN(OHIN_AIRDEN) * 1.0e-3 / IN(OHIN_CLDF));
+  if (!(size_res && IN(OHIN_IsWater) != 0.0 && TEMP > 268.15 && LWC > 1.0e-20)) return;
+  for (int k = 0; k < 18; ++k) M[k] = met[(long long)k * ldm];
+  for (int k = 0; k < ORACLE_NSPEC; ++k) Cc[k] = c[(long long)k * ldc];
+  oracle_sulfite_uptakes(M, Cc, het, ldh, up);
+  CVF = 1.0e3 * S_AIRMW / (IN(OHIN_AIRDEN) * S_AVO);
+  DTCHEM = DT;
+  FC = IN(OHIN_CLDF);
+  R1 = CC(OSS_SO2) * CVF;
+  R2 = CC(OSS_H2O2) * CVF;
+  K = M[12] / CVF / FC;
+  XX1 = loss2(R1, R2, K, DTCHEM);
+  R2 = CC(OSS_O3) * CVF;
+  K = M[13] / CVF / FC;
+  XX2 = loss2(R1, R2, K, DTCHEM);
+  K = -M[14] / FC;
+  Arg = K * DTCHEM;
+  XX3 = 0.0;
+  if (is_safe_exp(Arg)) {
+    XX = exp(Arg);
+    XX3 = R1 * (1.0 - XX);
+  }
+  R1 = CC(OSS_SO2) * CVF * IN(OHIN_HSO3_aq);
+  R2 = CC(OSS_HOCl) * CVF;
+  K = up[0] / CVF;
+  XX4 = loss2(R1, R2, K, DTCHEM);
+  R1 = CC(OSS_SO2) * CVF * IN(OHIN_SO3_aq);
+  K = up[1] / CVF;
+  XX4 = XX4 + loss2(R1, R2, K, DTCHEM);
+  R1 = CC(OSS_SO2) * CVF * IN(OHIN_HSO3_aq);
+  R2 = CC(OSS_HOBr) * CVF;
+  K = up[2] / CVF;
+  XX5 = loss2(R1, R2, K, DTCHEM);
+  R1 = CC(OSS_SO2) * CVF * IN(OHIN_SO3_aq);
+  K = up[3] / CVF;
+  XX5 = XX5 + loss2(R1, R2, K, DTCHEM);
+  LST = XX1 + XX2 + XX3 + XX4 + XX5;
+  if (LST > R1) {
+    XX1 = (R1 * XX1) / LST;
+    XX2 = (R1 * XX2) / LST;
+    XX3 = (R1 * XX3) / LST;
+    XX4 = (R1 * XX4) / LST;
+    XX5 = (R1 * XX5) / LST;
+    LST = XX1 + XX2 + XX3 + XX4 + XX5;
+  }
+  NH3 = IN(OHIN_NH3) * CVF * 1.0e+12;
+  SO2 = fmax(CC(OSS_SO2) * CVF - (LST * FC), 1.0e-20) * 1.0e+12;
+  H2O2 = CC(OSS_H2O2) * CVF * 1.0e12;
+  HNO3 = CC(OSS_HNO3) * CVF * 1.0e12;
+  SO4 = (CC(OSS_SO4) * CVF * IN(OHIN_AD) * 1.0e+9) / ((S_AIRMW / OSS_MW_SO4) * IN(OHIN_AIRVOL));
+  B = (LST * IN(OHIN_AD) * 1.0e+9) / ((S_AIRMW / OSS_MW_SO4) * IN(OHIN_AIRVOL));
+  CNss = IN(OHIN_SALC) * CVF * IN(OHIN_AD) / ((S_AIRMW / OSS_MW_SALC) * IN(OHIN_AIRVOL));
+  NDss = (THREE_FOURTHS * CNss) / (S_PI_PHYS * SS_DEN * RG_S3 * (is_safe_exp(ARG_SS) ? exp(ARG_SS) : 0.0)) * 1.e-6;
+  CN = NDss;
+  if (SO2 <= 200.00) {
+    aB = 0.5318; aNH3 = -1.67e-7; aSO2 = 2.59e-6; aH2O2 = -1.77e-7; aHNO3 = -1.72e-7; aW = 1.22e-6; aCN = 4.58e-6;
+    aSO4 = -1.00e-5;
+  } else if (SO2 > 200.00 && SO2 <= 500.0) {
+    aB = 0.5591; aNH3 = 3.62e-6; aSO2 = 1.66e-6; aH2O2 = 1.06e-7; aHNO3 = -5.45e-7; aW = -5.79e-7; aCN = 1.63e-5;
+    aSO4 = -7.40e-6;
+  } else if (SO2 > 500.0 && SO2 < 1000.0) {
+    aB = 1.1547; aNH3 = -4.28e-8; aSO2 = -1.23e-7; aH2O2 = -9.05e-7; aHNO3 = 1.73e-7; aW = 7.22e-6; aCN = 2.44e-5;
+    aSO4 = 3.25e-5;
+  } else {
+    aB = 1.1795; aNH3 = 2.57e-7; aSO2 = -5.54e-7; aH2O2 = -1.08e-6; aHNO3 = 1.95e-6; aW = 6.14e-6; aCN = 1.64e-5;
+    aSO4 = 2.48e-6;
+  }
+  W = -IN(OHIN_OMEGA) / (IN(OHIN_AIRDEN) * S_G0) * 100.0;
+  APV = sqrt(IN(OHIN_U) * IN(OHIN_U) + IN(OHIN_V) * IN(OHIN_V)) + (W * W * 1.0e-4);
+  H = DTCHEM * APV;
+  sum_gas = (aNH3 * NH3) + (aSO2 * SO2) + (aH2O2 * H2O2) + (aHNO3 * HNO3);
+  DSVI = (aB * B) + (((aCN * CN) + (aW * W) + (aSO4 * SO4) + sum_gas) * H);
+  SR = 0.0;
+  if (W > 0.0 && CC(OSS_SO2) > 0.0) {
+    SR = fmax((DSVI - B), 0.0);
+    if (SR > 0.0) {
+      SR = SR * (S_AIRMW / OSS_MW_SO4) * 1.e-9 / IN(OHIN_AIRDEN);
+      SR = fmin(SR, SO2 / 1.0e12);
+    }
+  }
+  SR = SR / CVF / DT;
+  DENOM = XX2 + XX4 + XX5;
+  *srhocl = SR * ss_SafeDiv(XX4, DENOM, 0.0);
+  *srhobr = SR * ss_SafeDiv(XX5, DENOM, 0.0);
+  *srhocl = ss_SafeDiv(*srhocl, (CC(OSS_SO2) * CC(OSS_HOCl)), 0.0);
+  *srhobr = ss_SafeDiv(*srhobr, (CC(OSS_SO2) * CC(OSS_HOBr)), 0.0);
+#undef IN
+#undef CC
+}
+
+/* fullchem_HetDropChem for every cell: SRHOCl, SRHOBr into met rows 4, 5
+ * (0 where Do_FullChem does not call it); met [18][ldm] in/out (TEMP and
+ * K_CLD read), het the HetState rows of fullchem_SetStateHet. */
+void oracle_het_drop_chem_batch(int ncell, double dt, const double* in, long long ldi, const double* C,
+                                long long ldc, const double* het, long long ldh, const int* size_res, double* met,
+                                long long ldm) {
+  for (int cell = 0; cell < ncell; ++cell) {
+    double a, b;
+    het_drop_cell(in + cell, ldi, C + cell, ldc, met + cell, ldm, het + cell, ldh, dt, size_res[cell], &a, &b);
+    met[4 * ldm + cell] = a;
+    met[5 * ldm + cell] = b;
   }
 }
