@@ -389,6 +389,8 @@ def run_ours(args):
     achieved_tf = flops / (head["kernel_ms"] * 1e-3) / 1e12
     flops_plain = algorithmic_flops(tabs, res["plain"]["ist"])
     achieved_plain_tf = flops_plain / (res["plain"]["kernel_ms"] * 1e-3) / 1e12
+    flops_ho = algorithmic_flops(tabs, res["handover"]["ist"])
+    achieved_ho_tf = flops_ho / (res["handover"]["kernel_ms"] * 1e-3) / 1e12
 
     # FP64 peak measured on this GPU (roofline denominator)
     peak_gf = None
@@ -579,7 +581,12 @@ def run_ours(args):
                          "peak_source": "measured FP64 FMA probe on this GPU (of measured)",
                          "plain_kernel": {"kernel": "gckpp::ros_kernel, plain arm", "achieved": achieved_plain_tf,
                                           "frac": (achieved_plain_tf / (peak_gf / 1e3)) if peak_gf else None,
-                                          "kernel_ms": res["plain"]["kernel_ms"], "flops_per_launch": flops_plain}},
+                                          "kernel_ms": res["plain"]["kernel_ms"], "flops_per_launch": flops_plain},
+                         "handover_only_kernel": {
+                             "kernel": "gckpp::ros_kernel + block-per-cell hand-over after 16 steps, no network",
+                             "achieved": achieved_ho_tf,
+                             "frac": (achieved_ho_tf / (peak_gf / 1e3)) if peak_gf else None,
+                             "kernel_ms": res["handover"]["kernel_ms"], "flops_per_launch": flops_ho}},
             "cpu_baseline": cpu,
             "clocks": head["clocks"],
         }

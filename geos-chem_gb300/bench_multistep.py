@@ -9,7 +9,8 @@ Hstart = 0, the rest on the KPPHvalue chain, as a model run does):
 
 * plain   - gc_kpp_fullchem_step per step, synchronous;
 * learned - gc_kpp_fullchem_step_learned per step (H0 proposals, stiffness
-            bins, top bin block-per-cell, hand-over after 2 steps), the whole
+            bins, top bin block-per-cell, hand-over after 4 steps on the cold
+            first step and 1 on the chain), the whole
             run captured once in a CUDA graph (GC_KPP_OPT_ASYNC) and replayed.
 
 Each run starts from the same spun-up state; the time is CUDA-event time on
@@ -78,7 +79,10 @@ def main(argv=None):
     cp = learned.CProposer(prop)
 
     def learned_run(stream_ptr=sp):
-        for _ in range(args.steps):
+        for k in range(args.steps):
+            # hand-over after 4 steps from the cold start (H0 proposals are
+            # capped at learned.H0_CAP), after 1 on the KPPHvalue chain
+            solver.set(evict_after=4 if k == 0 else 1)
             solver.fullchem_step_learned(cp.handle, args.dt, met, ph, c, at, rt, ic, rc, hs, ist, rst, ierr,
                                          stream=stream_ptr)
 
@@ -101,7 +105,7 @@ def main(argv=None):
     plain_ms = timed(plain_run)
     plain_steps = steps_sum[-args.steps:]
     # learned: one synchronous run sizes the buffers, then one graph per run
-    solver.set(evict_after=2, cell_block=256)
+    solver.set(cell_block=256)
     c.copy_(c0)
     hs.zero_()
     learned_run()

@@ -77,12 +77,13 @@ def main(argv=None):
     prop.load_state(dict(np.load(learned.WEIGHTS)))
     cp = learned.CProposer(prop)
     res = {}
-    for name, proposer, evict in (("plain", None, 0), ("learned", cp, 2)):
+    # hand-over after 4 steps from the cold start (H0 proposals capped at learned.H0_CAP)
+    for name, proposer, evict in (("plain", None, 0), ("learned", cp, 4)):
         for ch, c0k in zip(chunks, c0):
             ch["c"].copy_(c0k)
             ch["hs"].zero_()
         solver.set(evict_after=evict)
-        st = stream.Streamer(solver, n, chunk, proposer=proposer)
+        st = stream.Streamer(solver, n, chunk, proposer=proposer, photol_rows=stream.photol_runs())
         torch.cuda.synchronize()
         t = time.perf_counter()
         retried = st.step(chunks, args.dt, at, rt, ic, rc)
