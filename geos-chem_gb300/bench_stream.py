@@ -65,9 +65,8 @@ def main(argv=None):
     for i0 in range(0, n, chunk):
         i1 = min(n, i0 + chunk)
         idx = (np.arange(i0, i1, dtype=np.int64) * stride) % npool
-        chunks.append({"met": torch.from_numpy(pool["met"][:, idx]).pin_memory(),
-                       "ph": torch.from_numpy(pool["photol"][:, idx]).pin_memory(),
-                       "c": torch.from_numpy(pool_c[:, idx]).pin_memory(),
+        rows = lambda a: torch.from_numpy(np.ascontiguousarray(a[:, idx])).pin_memory()
+        chunks.append({"met": rows(pool["met"]), "ph": rows(pool["photol"]), "c": rows(pool_c),
                        "hs": torch.zeros(i1 - i0, dtype=torch.float64).pin_memory(),
                        "steps": torch.zeros(i1 - i0, dtype=torch.int32).pin_memory(),
                        "ierr": torch.zeros(i1 - i0, dtype=torch.int32).pin_memory()})

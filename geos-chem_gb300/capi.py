@@ -419,24 +419,29 @@ class Solver:
 
 
 def copy_rows(dst, src, stream=None, lib=None):
-    """dst.copy_(src) for two 2-D arrays of the same shape and dtype (rows of
-    contiguous elements, any row stride; torch tensors, host or CUDA) through
-    gc_kpp_copy_rows: page-locked host memory is read and written by the
-    SMs, which after a chemistry step is an order of magnitude faster than a
-    copy engine.  Stream-ordered on `stream` (a CUDA stream handle, default
-    the current torch stream)."""
+    """dst.copy_(src) for two 1-D or 2-D torch tensors of the same shape and
+    dtype, host or CUDA.  Rows of contiguous elements (any row stride) go
+    through gc_kpp_copy_rows: page-locked host memory is read and written by
+    the SMs, which after a chemistry step is an order of magnitude faster
+    than a copy engine.  Other layouts use torch's copy.  Stream-ordered on
+    `stream` (a CUDA stream handle, default the current torch stream)."""
     import torch
 
     lib = lib or load_library()
     if dst.shape != src.shape or dst.dtype != src.dtype:
         raise ValueError("copy_rows: shapes or dtypes differ")
-    d2 = dst if dst.dim() == 2 else dst.reshape(1, -1)
-    s2 = src if src.dim() == 2 else src.reshape(1, -1)
-    if d2.stride(1) != 1 or s2.stride(1) != 1:
-        raise ValueError("copy_rows: rows must be contiguous")
-    es = dst.element_size()
     if stream is None:
         stream = torch.cuda.current_stream().cuda_stream
+    rowwise = lambda t: t.dim() == 1 and t.stride(0) == 1 or t.dim() == 2 and t.stride(1) == 1
+    if not (rowwise(dst) and rowwise(src)):
+        # a layout that is not rows of contiguous elements (column-major host
+        # arrays, say): torch's own copy, on the same stream
+        with torch.cuda.stream(torch.cuda.ExternalStream(stream)):
+            dst.copy_(src, non_blocking=True)
+        return
+    d2 = dst if dst.dim() == 2 else dst.reshape(1, -1)
+    s2 = src if src.dim() == 2 else src.reshape(1, -1)
+    es = dst.element_size()
     rc = lib.gc_kpp_copy_rows(ctypes.c_void_p(d2.data_ptr()), d2.stride(0) * es, ctypes.c_void_p(s2.data_ptr()),
                               s2.stride(0) * es, d2.shape[1] * es, d2.shape[0], ctypes.c_void_p(stream))
     if rc != GC_KPP_OK:

@@ -58,3 +58,15 @@ def test_photol_rows_of_the_mechanism():
     for a, b in runs:
         want[a:b] = True
     assert np.array_equal(mask, want) and mask.sum() == 168
+
+
+def test_copy_rows_other_layouts_fall_back_to_torch():
+    import torch
+    import gcchem.capi as capi
+
+    src = torch.arange(3 * 50, dtype=torch.float64).reshape(50, 3).pin_memory().t()  # column-major [3, 50]
+    assert src.stride(1) != 1
+    dev = torch.empty((3, 50), dtype=torch.float64, device="cuda")
+    capi.copy_rows(dev, src)
+    torch.cuda.synchronize()
+    assert torch.equal(dev.cpu(), src)
