@@ -41,6 +41,8 @@ def main(argv=None):
                     help="block-per-cell kernel form (GC_KPP_OPT_BLOCK_SPLIT 1 or 0)")
     ap.add_argument("--repeat", type=int, default=1,
                     help="grid step: run the timed step this many times from the same state (the last is reported)")
+    ap.add_argument("--producers", action="store_true",
+                    help="grid step: after it, time the per-cell producers (sulfur, SET_SO2, HetState, HetDropChem)")
     ap.add_argument("--copies", action="store_true",
                     help="grid step: after it, time 1 GB host<->device copies of page-locked buffers by the copy "
                          "engine and by gc_kpp_copy_rows (SM copies), each right after a step")
@@ -155,6 +157,32 @@ def main(argv=None):
         sel = order[:nb].long().cpu().numpy()
         print("block-per-cell cells %d: ISTATUS sums %s" % (nb, ih[:8, sel].sum(axis=1).tolist()))
     print("algorithmic FP64 flops %.4e" % flops)
+    if args.producers and args.grid:
+        # Do_FullChem's per-cell producers on this grid (synthetic grid-box
+        # fields): SulfurAqChem, SET_SO2, SetStateHet, HetDropChem, timed
+        # together with CUDA events (device arrays)
+        import gcchem.hetstate as hetstate
+
+        hin = T(hetstate.hetin_cells(n, seed=2))
+        het = torch.zeros((168, n), dtype=torch.float64, device=dev)
+        sres = torch.zeros(n, dtype=torch.int32, device=dev)
+        metp = met.clone()
+
+        def producers():
+            s.sulfur_aq_rates(hin, c, metp)
+            s.sulfur_cld_rates(hin, c, metp, 1, sres)
+            s.set_state_het(hin, c, het)
+            s.het_drop_chem(1200.0, hin, c, het, sres, metp)
+
+        producers()
+        for rep in range(2):
+            torch.cuda.synchronize()
+            t0.record()
+            producers()
+            t1.record()
+            torch.cuda.synchronize()
+            print("producers (SulfurAqChem, SET_SO2, SetStateHet, HetDropChem) over %d cells: %.3f ms"
+                  % (n, t0.elapsed_time(t1)))
     if args.copies and args.grid:
         # first pass over a page-locked buffer right after a chemistry step:
         # copy engine against SM copies, each direction
