@@ -145,8 +145,9 @@ def test_grid_learned_step_matches_oracle(solver, orc, grid_case):
     ist = torch.zeros((20, n), dtype=torch.int32, device=dev)
     rst = torch.zeros((20, n), dtype=torch.float64, device=dev)
     ierr = torch.zeros(n, dtype=torch.int32, device=dev)
-    # the benchmark's learned arm: plan, binned step, hand-over after 2 steps
-    solver.set(arith="fast", schedule="queue", block=0, evict_after=2)
+    # the benchmark's learned arm: plan (H0 capped at learned.H0_CAP), binned
+    # step, hand-over after 4 steps
+    solver.set(arith="fast", schedule="queue", block=0, evict_after=4)
     try:
         _, _, order = learned.plan(prop, met, ph, c, hstart=hs, hmax=1200.0)
         h0 = hs.cpu().numpy().copy()
