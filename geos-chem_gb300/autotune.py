@@ -5,8 +5,10 @@ each candidate of
 
 * threads per block of the thread-per-cell queue kernel (32, 64, 128, 256),
 * cells per thread (the layout: 1 or 2 cells per thread share a table walk),
-* the block-per-cell form (split sums, or the level form with 128 or 256
-  threads per block; 32 = warp per cell),
+* the queue chunk: queue positions a lane takes per claim (1, 2, 4, 8; the
+  reference's cell loop is SCHEDULE(DYNAMIC, 24)),
+* the block-per-cell form: split sums (256 threads), or the level form with
+  32 (one warp per cell), 128 or 256 threads per block,
 * the hand-over point k (steps after which a cell moves to the block kernel),
 
 one axis at a time from the defaults (coordinate descent, two sweeps), and
@@ -14,9 +16,7 @@ returns the fastest settings.  Candidates without the split form give
 bit-identical results (the schedule never changes a cell's arithmetic); the
 split form regroups sums, so its candidates must agree to rounding (same IERR,
 1e-8 relative on species above 1e4 molec/cm3 for 99 % of the cells); `tune`
-checks both.  The
-queue hands out one cell per lane through warp-aggregated claims: its "chunk"
-is a warp of 32 cells and is not a tuning axis.
+checks both.
 
     python geos-chem_gb300/autotune.py --grid 72x46x72 --out tuned.json
 """
@@ -29,11 +29,23 @@ import time
 AXES = {
     "block": [32, 64, 128, 256],
     "arith": ["fast", "fast2"],
-    "cell_block": [128, 256],
+    "queue_chunk": [1, 2, 4, 8],
+    "cell_block": [32, 128, 256],
     "block_split": [True, False],
     "evict_after": [0, 2, 4, 8, 16],
 }
-DEFAULTS = {"block": 128, "arith": "fast", "cell_block": 256, "block_split": True, "evict_after": 0}
+DEFAULTS = {"block": 128, "arith": "fast", "queue_chunk": 1, "cell_block": 256, "block_split": True,
+            "evict_after": 0}
+SETTINGS = ("arith", "block", "queue_chunk", "cell_block", "block_split", "evict_after")
+
+
+def canonical(cfg):
+    """The split form always runs 256 threads per block, so its candidates
+    differ in nothing when only cell_block differs."""
+    cfg = dict(cfg)
+    if cfg.get("block_split", True):
+        cfg["cell_block"] = 256
+    return cfg
 
 
 def time_step(solver, cfg, case, hs0, order=None, nblock=0):
@@ -41,7 +53,8 @@ def time_step(solver, cfg, case, hs0, order=None, nblock=0):
     import torch
 
     solver.set(arith=cfg["arith"], schedule="queue", block=cfg["block"], cell_block=cfg["cell_block"],
-               evict_after=cfg["evict_after"], block_split=cfg.get("block_split", True))
+               evict_after=cfg["evict_after"], block_split=cfg.get("block_split", True),
+               queue_chunk=cfg.get("queue_chunk", 1))
     c = case["c"].clone()
     hs = hs0.clone()
     torch.cuda.synchronize()
@@ -72,12 +85,13 @@ def tune(solver, case, hs0, order=None, nblock=0, sweeps=2, reps=2, axes=None, l
     import gcchem.capi as capi
 
     axes = axes or AXES
-    best = {k: (DEFAULTS[k] if k not in axes or DEFAULTS[k] in axes[k] else axes[k][0]) for k in DEFAULTS}
+    best = canonical({k: (DEFAULTS[k] if k not in axes or DEFAULTS[k] in axes[k] else axes[k][0]) for k in DEFAULTS})
     nvar = capi.dims(getattr(solver, "mech", "fullchem"))["nvar"]
     _, ref = time_step(solver, best, case, hs0, order, nblock)
     seen = {}
 
     def measure(cfg):
+        cfg = canonical(cfg)
         key = json.dumps(cfg, sort_keys=True)
         if key not in seen:
             ts = []
@@ -95,11 +109,11 @@ def tune(solver, case, hs0, order=None, nblock=0, sweeps=2, reps=2, axes=None, l
     for _ in range(sweeps):
         for axis, values in axes.items():
             for v in values:
-                cand = dict(best, **{axis: v})
+                cand = canonical(dict(best, **{axis: v}))
                 t = measure(cand)
                 if t < best_t:
                     best, best_t = cand, t
-    solver.set(**{k: best[k] for k in ("arith", "block", "cell_block", "evict_after")})
+    solver.set(**{k: best[k] for k in SETTINGS})
     table = [dict(json.loads(k), ms=v * 1e3) for k, v in sorted(seen.items(), key=lambda kv: kv[1])]
     return best, best_t, table
 

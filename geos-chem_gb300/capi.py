@@ -38,6 +38,7 @@ OPT_EVICT_AFTER = 10
 OPT_EVICT_DRAINED = 11
 OPT_BLOCK_SPLIT = 12
 OPT_RATES_DIRECT = 13
+OPT_QUEUE_CHUNK = 14
 
 EXPORTED = [
     "gc_kpp_mechanism_dims",
@@ -152,7 +153,8 @@ class Solver:
             raise GcKppError(rc, self.lib.gc_kpp_last_error().decode())
 
     def set(self, arith=None, schedule=None, block=None, blocks_per_sm=None, max_slots=None, cell_block=None,
-            async_steps=None, evict_after=None, evict_drained=None, block_split=None, rates_direct=None):
+            async_steps=None, evict_after=None, evict_drained=None, block_split=None, rates_direct=None,
+            queue_chunk=None):
         if arith is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_ARITH, {"fast": 0, "strict": 1, "fast2": 2, "fast4": 3}[arith]))
         if schedule is not None:
@@ -175,6 +177,8 @@ class Solver:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_BLOCK_SPLIT, 1 if block_split else 0))
         if rates_direct is not None:
             self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_RATES_DIRECT, 1 if rates_direct else 0))
+        if queue_chunk is not None:
+            self._check(self.lib.gc_kpp_ctx_set_option(self.ctx, OPT_QUEUE_CHUNK, int(queue_chunk)))
 
     def close(self):
         if self.ctx:

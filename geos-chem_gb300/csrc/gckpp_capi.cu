@@ -147,6 +147,7 @@ struct gc_kpp_ctx {
   int occ_arith = -1, occ_block = -1, occ_value = 1;  // cached occupancy query
   int evict_after = 0;  // hand cells over to the block-per-cell kernel after this many steps
   int evict_drained = 0;  // ... only once the queue has no unclaimed cell left
+  int queue_chunk = 1;    // queue positions a lane takes per claim
   DevBuf evict_buf;     // ids of the handed-over cells
   DevBuf bws;           // Jac0 slots of the block-per-cell kernel, one per block of its grid
   int bocc_key = -1, bocc_value = 1;  // cached occupancy of the block-per-cell kernel
@@ -240,6 +241,11 @@ int gc_kpp_ctx_create(gc_kpp_ctx** out, int device) {
   UPSPLIT(gckpp::SP_LU, lu, LU) UPSPLIT(gckpp::SP_FS, fs, FS) UPSPLIT(gckpp::SP_BS, bs, BS)
   UPSPLIT(gckpp::SP_FUN, fun, FUN) UPSPLIT(gckpp::SP_JAC, jac, JAC)
 #undef UPSPLIT
+  e = upload(reinterpret_cast<const uint4*>(T::split_fs_rec), sizeof(T::split_fs_rec) / 16, &m.sp_rec[0], c->owned);
+  if (e == cudaSuccess)
+    e = upload(reinterpret_cast<const uint4*>(T::split_bs_rec), sizeof(T::split_bs_rec) / 16, &m.sp_rec[1],
+               c->owned);
+  if (e != cudaSuccess) { gc_kpp_ctx_destroy(c); return cuda_fail(e, "upload split substitution records"); }
   gcrates::RatesDev& rp = c->rates;
   rp.nreact = T::NREACT;
   rp.nmet = RT::NMET;
@@ -309,6 +315,11 @@ int gc_kpp_ctx_set_option(gc_kpp_ctx* c, int key, long long v) {
     case GC_KPP_OPT_EVICT_AFTER:
       if (v < 0 || v > 1000000) return fail(GC_KPP_EINVAL, "evict-after steps out of range");
       c->evict_after = (int)v;
+      return GC_KPP_OK;
+    case GC_KPP_OPT_QUEUE_CHUNK:
+      if (v == 0) v = 1;
+      if (v < 1 || v > 64) return fail(GC_KPP_EINVAL, "queue chunk must be in [1, 64]");
+      c->queue_chunk = (int)v;
       return GC_KPP_OK;
     case GC_KPP_OPT_EVICT_DRAINED:
       if (v != 0 && v != 1) return fail(GC_KPP_EINVAL, "evict-drained must be 0 or 1");
@@ -476,9 +487,10 @@ int variant_cells_per_thread(int arith) {
 // Grid of the block-per-cell kernel (resident blocks per SM x SMs, at most
 // `want` if positive) and its Jac0 slots.
 int block_grid(gc_kpp_ctx* c, const Resolved& R, int autonomous, long long want, int* grid, double** ws) {
-  const size_t smem = c->arith == 1 ? gckpp_block_smem_strict(c->mech, R.meth, autonomous)
-                                    : gckpp_block_smem_fast(c->mech, R.meth, autonomous);
   const bool split = c->arith != 1 && c->block_split;
+  const size_t smem = c->arith == 1 ? gckpp_block_smem_strict(c->mech, R.meth, autonomous)
+                      : split       ? gckpp_block_smem_split(c->mech, R.meth, autonomous)
+                                    : gckpp_block_smem_fast(c->mech, R.meth, autonomous);
   // smem < 2^18 bytes, arith < 4, cell_block / 32 <= 32
   const int key = (int)smem + (c->arith << 18) + ((c->cell_block / 32) << 20) + ((split ? 1 : 0) << 26);
   if (c->bocc_key != key) {
@@ -598,6 +610,7 @@ int launch_integrate(gc_kpp_ctx* c, const Resolved& R, double tin, double tout, 
   }
   p.cell_limit = a.cell_limit > 0 ? a.cell_limit : a.ncell;
   p.queue_counter = (int*)c->counter.p;
+  p.queue_chunk = c->queue_chunk;
   p.c_in = a.c_in;
   p.c_out = a.c_out;
   p.ldc = a.ldc;

@@ -263,20 +263,6 @@ struct SplitLu {
   }
 };
 
-// Substitution row i: X(i) - sum G(kk) X(icol(kk)); BACK multiplies by the
-// stored reciprocal pivot G(z).  The term index kk is the position in G.
-template <bool BACK>
-struct SplitSolve {
-  const MechDev& m;
-  const double* G;
-  double* X;
-  __device__ const unsigned* terms(int) const { return reinterpret_cast<const unsigned*>(m.lu_icol); }
-  __device__ double pre(int, unsigned) const { return 0.0; }
-  __device__ double base(int i, unsigned, double) const { return X[i]; }
-  __device__ double term(int, int kk, unsigned w, double acc) const { return fma(-G[kk], X[w], acc); }
-  __device__ void finish(int i, unsigned z, double v) const { X[i] = BACK ? v * G[z] : v; }
-};
-
 // Fun_SPLIT sums: items [0, NVAR) are P_VAR rows over A (into Vdot), items
 // [NVAR, 2 NVAR) D_VAR rows over B (into D).
 struct SplitFun {
@@ -422,11 +408,94 @@ __device__ inline void bk_decomp_split(const MechDev& m, const double* J0, doubl
   __syncthreads();
 }
 
-// Forward and backward substitution in the split form.  Ends with a barrier.
-__device__ inline void bk_solve_split(const MechDev& m, const double* G, double* X) {
-  split_run(m, SP_FS, SplitSolve<false>{m, G, X});
-  if (m.sp_nt[SP_FS] != m.sp_nt[SP_BS]) __syncthreads();
-  split_run(m, SP_BS, SplitSolve<true>{m, G, X});
+// Substitution passes with staged lane records.  The forward and backward
+// substitutions run on the first warp, one dependency level after another,
+// and a pass is shorter than an L2 round trip, so table words loaded one pass
+// ahead would still be in flight when the pass ends.  Here every lane copies
+// its own 32-byte record of pass p + SPLIT_STAGE - 1 into a ring of
+// SPLIT_STAGE slots in shared memory (cp.async) while pass p computes, and
+// waits only for its own copies (cp.async.wait_group), so no barrier orders
+// the copies and nothing waits on another thread.  Record (tables.py
+// _solve_records): x | level end << 24, first term | finish word << 16, the
+// columns of the lane's terms as 16-bit words.  Row i's sum is X(i) - sum
+// G(kk) X(icol(kk)) over the LU positions kk of its chunk; the backward
+// substitution multiplies by the stored reciprocal pivot G(finish word).
+constexpr int SPLIT_STAGE = 4;
+constexpr int SPLIT_RING_BYTES = SPLIT_STAGE * 32 * 32;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <bool BACK>
+__device__ __forceinline__ void split_solve_staged(const MechDev& m, int ph, const double* __restrict__ G,
+                                                   double* X, uint4* ring) {
+  const int np = m.sp_npass[ph];
+  const int lane = threadIdx.x;  // the first warp
+  const uint4* rec = m.sp_rec[ph - SP_FS] + 2 * lane;
+  uint4* mine = ring + 2 * lane;  // slot k of this lane: mine[64 k], mine[64 k + 1]
+#pragma unroll
+  for (int d = 0; d < SPLIT_STAGE - 1; ++d) {
+    if (d < np) {
+      cp_async16(mine + 64 * d, rec + 64 * d);
+      cp_async16(mine + 64 * d + 1, rec + 64 * d + 1);
+    }
+    cp_async_commit();
+  }
+  for (int p = 0; p < np; ++p) {
+    const int q = p + SPLIT_STAGE - 1;
+    if (q < np) {
+      const int sq = 64 * (q % SPLIT_STAGE);
+      cp_async16(mine + sq, rec + 64 * q);
+      cp_async16(mine + sq + 1, rec + 64 * q + 1);
+    }
+    cp_async_commit();
+    cp_async_wait<SPLIT_STAGE - 1>();  // this pass's copies (committed SPLIT_STAGE - 1 groups ago) landed
+    const int sp = 64 * (p % SPLIT_STAGE);
+    const uint4 a = mine[sp], b = mine[sp + 1];
+    const unsigned cw[6] = {a.z, a.w, b.x, b.y, b.z, b.w};
+    const int item = a.x & 0xffff;
+    const bool busy = item != 0xffff;
+    const int seglog = (a.x >> 16) & 7;
+    const int seg = 1 << seglog;
+    const int n = (a.x >> 19) & 31;
+    const int y = a.y & 0xffff;
+    if (__any_sync(0xffffffffu, busy)) {
+      const int nmax = __reduce_max_sync(0xffffffffu, (unsigned)n);
+      const int lmax = __reduce_max_sync(0xffffffffu, (unsigned)seglog);
+      const bool lead = busy && (lane & (seg - 1)) == 0;
+      double acc = lead ? X[item] : 0.0;
+#pragma unroll
+      for (int k = 0; k < SPLIT_MAXCH; ++k) {
+        if (k >= nmax) break;
+        if (k < n) acc = fma(-G[y + k], X[(cw[k >> 1] >> (16 * (k & 1))) & 0xffffu], acc);
+      }
+      for (int o = (1 << lmax) >> 1; o > 0; o >>= 1) {
+        const double v = __shfl_xor_sync(0xffffffffu, acc, o);
+        if (o < seg) acc += v;
+      }
+      if (lead) X[item] = BACK ? acc * G[a.y >> 16] : acc;
+    }
+    if ((a.x >> 24) & 1u) __syncwarp();
+  }
+  cp_async_wait<0>();
+}
+
+// Forward and backward substitution in the split form, on the first warp
+// with staged records (the host checks that both phases use 32 lanes).
+// Ends with a barrier.
+__device__ inline void bk_solve_split(const MechDev& m, const double* G, double* X, uint4* ring) {
+  if (threadIdx.x < 32) {
+    split_solve_staged<false>(m, SP_FS, G, X, ring);
+    __syncwarp();
+    split_solve_staged<true>(m, SP_BS, G, X, ring);
+  }
   __syncthreads();
 }
 
@@ -460,6 +529,9 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
   double* J0 = slot + lay.j0;
   double* G = sm + lay.g;
   double* E = sm + lay.e;
+  // split form: the ring of staged substitution records after the cell's
+  // arrays (16-byte aligned)
+  uint4* ring = reinterpret_cast<uint4*>(sm + ((lay.total + 1) & ~1));
   const int nvar = m.nvar;
   const int tid = threadIdx.x, nt = blockDim.x;
   const double dir = (p.tend >= p.tstart) ? 1.0 : -1.0;
@@ -592,7 +664,7 @@ __device__ void ros_block_driver(const MechDev& m, const RosMethod& r, const Ros
           }
           __syncthreads();
           if constexpr (SPLIT)
-            bk_solve_split(m, G, Ks);
+            bk_solve_split(m, G, Ks, ring);
           else
             bk_solve<STRICT>(m, G, Ks);
           if (tid == 0) sh.L.nsol += 1;

@@ -108,6 +108,13 @@ __global__ void __launch_bounds__(GCKPP_SPLIT_NT, 3) ros_block_split_kernel(Mech
   ros_block_driver<false, true>(m, r, p);
 }
 
+// the cell's arrays, 16-byte aligned, and the ring of staged substitution
+// records
+size_t gckpp_block_smem_split(const MechDev& m, const RosMethod& r, int autonomous) {
+  const int total = block_layout(m.naux, m.nspec, m.nvar, m.nreact, m.nb, m.lu_nonzero, r.S, autonomous).total;
+  return sizeof(double) * (size_t)((total + 1) & ~1) + SPLIT_RING_BYTES;
+}
+
 cudaError_t gckpp_block_occupancy_split(size_t smem, int* nblocks) {
   static int smem_set[64] = {};
   int dev = 0;
@@ -125,7 +132,8 @@ cudaError_t gckpp_launch_block_split(int grid, const MechDev& m, const RosMethod
                                      cudaStream_t s) {
   for (int ph = 0; ph < 5; ++ph)  // each phase runs on one warp or on the whole block
     if (m.sp_nt[ph] != 32 && m.sp_nt[ph] != GCKPP_SPLIT_NT) return cudaErrorInvalidConfiguration;
-  const size_t smem = gckpp_block_smem_fast(m, r, p.autonomous);
+  if (m.sp_nt[SP_FS] != 32 || m.sp_nt[SP_BS] != 32) return cudaErrorInvalidConfiguration;  // staged records
+  const size_t smem = gckpp_block_smem_split(m, r, p.autonomous);
   int nblk = 0;  // also sets the shared-memory attribute
   cudaError_t e = gckpp_block_occupancy_split(smem, &nblk);
   if (e != cudaSuccess) return e;

@@ -27,6 +27,7 @@ cudaError_t gckpp_launch_block_fast(int grid, int block, const MechDev& m, const
                                     cudaStream_t s);
 size_t gckpp_block_smem_strict(const MechDev& m, const RosMethod& r, int autonomous);
 size_t gckpp_block_smem_fast(const MechDev& m, const RosMethod& r, int autonomous);
+size_t gckpp_block_smem_split(const MechDev& m, const RosMethod& r, int autonomous);
 cudaError_t gckpp_block_occupancy_strict(int block, size_t smem, int* nblocks);
 cudaError_t gckpp_block_occupancy_fast(int block, size_t smem, int* nblocks);
 // split form (fast arithmetic, SPLIT_NT threads per block)

@@ -71,6 +71,9 @@ struct MechDev {
   const unsigned* sp_pass[5];
   int sp_npass[5];
   int sp_nt[5];
+  // the substitution passes (SP_FS, SP_BS) as 32-byte lane records
+  // (tables.py _solve_records), two uint4 per lane per pass
+  const uint4* sp_rec[2];
 };
 
 enum SplitPhase : int { SP_LU = 0, SP_FS = 1, SP_BS = 2, SP_FUN = 3, SP_JAC = 4 };

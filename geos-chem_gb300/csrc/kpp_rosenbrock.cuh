@@ -55,6 +55,7 @@ struct RosParams {
   const int* qrange;      // optional device {begin, end}: queue positions [begin, end) of order
                           // instead of [0, ncell) (sizes known only on the device)
   int* queue_counter;     // queue schedule: next queue position
+  int queue_chunk;        // queue schedule: positions a lane takes per claim (0 or 1: one)
   // boundary arrays, cell-interleaved: X[k*ld + cell]
   const double* c_in;
   double* c_out;
@@ -587,16 +588,34 @@ struct Rosenbrock {
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
-// Claim the next queue position for each calling lane (warp-aggregated).
-__device__ __forceinline__ int queue_claim(int* counter) {
-  const unsigned mask = __activemask();
-  const int leader = __ffs(mask) - 1;
-  const unsigned lt = mask & ((1u << lane_id()) - 1u);
-  const int n = __popc(mask);
-  int base = 0;
-  if ((int)lane_id() == leader) base = atomicAdd(counter, n);
-  base = __shfl_sync(mask, base, leader);
-  return base + __popc(lt);
+// Queue positions held by one cell slot of a lane: the next one, the
+// distance to the one after it, and how many of its last claim remain.
+struct QueueSlot {
+  int next, stride, left;
+};
+
+// Next queue position of a slot.  A slot with none left claims `chunk`
+// positions per calling lane in one warp-aggregated atomic: the n calling
+// lanes reserve n*chunk consecutive positions and lane r of them takes
+// positions r, r+n, r+2n, ... of that range, so lanes that claim together
+// start on consecutive positions.  chunk 1 is one position per claim.
+__device__ __forceinline__ int queue_take(int* counter, int chunk, QueueSlot& s) {
+  if (s.left <= 0) {
+    const unsigned mask = __activemask();
+    const int leader = __ffs(mask) - 1;
+    const unsigned lt = mask & ((1u << lane_id()) - 1u);
+    const int n = __popc(mask);
+    int base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(counter, n * chunk);
+    base = __shfl_sync(mask, base, leader);
+    s.next = base + __popc(lt);
+    s.stride = n;
+    s.left = chunk;
+  }
+  const int idx = s.next;
+  s.next += s.stride;
+  --s.left;
+  return idx;
 }
 
 template <bool STRICT, bool QUEUE, int NC, bool AR = false>
@@ -609,6 +628,8 @@ __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams
   double* w = p.ws + warp * (long long)p.lay.total * TSN + lane;
   Lane L[NC];
   bool has[NC];
+  QueueSlot qs[NC];
+  const int chunk = p.queue_chunk > 1 ? p.queue_chunk : 1;
   int qlo = 0, qhi = p.ncell;
   if (p.qrange) {
     qlo = p.qrange[0];
@@ -617,8 +638,9 @@ __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
     long long idx;
+    qs[q].left = 0;
     if (QUEUE) {
-      idx = (long long)qlo + queue_claim(p.queue_counter);
+      idx = (long long)qlo + queue_take(p.queue_counter, chunk, qs[q]);
     } else {
       idx = (long long)qlo + warp * TSN + q * TS + lane;
     }
@@ -640,7 +662,7 @@ __device__ void ros_driver(const MechDev& m, const RosMethod& r, const RosParams
           ros.evict_cell(w, q, L[q]);
         has[q] = false;
         if (QUEUE) {
-          const long long idx = (long long)qlo + queue_claim(p.queue_counter);
+          const long long idx = (long long)qlo + queue_take(p.queue_counter, chunk, qs[q]);
           if (idx < qhi) {
             const int cell = p.order ? p.order[idx] : idx;
             if ((unsigned)cell < (unsigned)p.cell_limit) {

@@ -30,6 +30,7 @@ def main(argv=None):
     ap.add_argument("--schedule", default="queue", choices=["plain", "queue"])
     ap.add_argument("--block", type=int, default=128)
     ap.add_argument("--max-slots", type=int, default=0, help="cap on cells in flight (0: all resident threads)")
+    ap.add_argument("--queue-chunk", type=int, default=1, help="queue positions a lane takes per claim")
     ap.add_argument("--grid", default=None, help="NLONxNLATxNLEV: grid step instead of box cells")
     ap.add_argument("--binned", type=int, default=0, help="grid step: cells sent block-per-cell")
     ap.add_argument("--cold", action="store_true",
@@ -82,7 +83,7 @@ def main(argv=None):
     dev = torch.device("cuda", 0)
     T = lambda x: torch.tensor(x, device=dev).contiguous()
     s = capi.Solver(0, arith=args.arith, schedule=args.schedule, block=args.block, max_slots=args.max_slots)
-    s.set(block_split=args.block_form == "split")
+    s.set(block_split=args.block_form == "split", queue_chunk=args.queue_chunk)
     atol, rtol = inputs.tolerances()
     ic, rc = inputs.default_controls()
     ic_t, rc_t = ic.copy(), rc.copy()  # controls of the timed step

@@ -39,11 +39,11 @@ from . import mechanism
 NOCOEF = 0x7FF
 # threads of the split block-per-cell kernel, the lanes each phase's passes
 # use (the substitutions run on the first warp alone, with warp barriers), and
-# the largest number of terms a lane sums before a segment combines its
-# partial sums
+# per phase the largest number of terms a lane sums before a segment combines
+# its partial sums
 SPLIT_NT = 256
 SPLIT_PHASE_NT = {"lu": 256, "fs": 32, "bs": 32, "fun": 256, "jac": 256}
-SPLIT_CHUNK = 8
+SPLIT_CHUNK = {"lu": 8, "fs": 8, "bs": 8, "fun": 8, "jac": 8}
 SPLIT_MAXCH = 12  # register slots of a lane's chunk in the kernel
 
 
@@ -283,7 +283,7 @@ class Tables:
         Every sum of the block phases (an LU entry's dot product, a
         substitution row, a Fun_SPLIT P or D row, a Jac_SP entry) is one item;
         an item of L terms gets a segment of s lanes (s a power of two, the
-        smallest with ceil(L/s) <= SPLIT_CHUNK, at most 32), each lane sums a
+        smallest with ceil(L/s) <= SPLIT_CHUNK[phase], at most 32), each lane sums a
         contiguous chunk of the terms and the segment adds its partial sums
         with a butterfly of warp shuffles.  Within a dependency level the
         segments are placed largest first, so each starts at a multiple of its
@@ -297,9 +297,9 @@ class Tables:
         substitution: position of the row's diagonal), 0; item 0xFFFF is an
         idle lane.  pass word: max seglog of the pass | barrier << 3."""
         nvar, nz = self.nvar, self.lu_nonzero
-        CH = SPLIT_CHUNK
 
-        def passes(levels, NT):
+        def passes(levels, ph):
+            NT, CH = SPLIT_PHASE_NT[ph], SPLIT_CHUNK[ph]
             task, info = [], []
             for items in levels:
                 segs = []
@@ -343,23 +343,49 @@ class Tables:
         self.split["lu"] = passes(levels_of(
             self.lu_lvl_entry, self.lu_lvl_start,
             lambda e: (e, int(self.dot_start[e]), int(self.dot_start[e + 1] - self.dot_start[e]), lu_z(e))),
-            SPLIT_PHASE_NT["lu"])
+            "lu")
         # substitution terms are positions kk of the LU pattern (G[kk] times
         # X[icol[kk]]); forward rows without terms are left out
         fs = levels_of(self.fs_lvl_row, self.fs_lvl_start,
                        lambda i: (i, int(crow[i]), int(diag[i] - crow[i]), 0))
-        self.split["fs"] = passes([[x for x in lv if x[2] > 0] for lv in fs], SPLIT_PHASE_NT["fs"])
+        self.split["fs"] = passes([[x for x in lv if x[2] > 0] for lv in fs], "fs")
         self.split["bs"] = passes(levels_of(self.bs_lvl_row, self.bs_lvl_start,
                                             lambda i: (i, int(diag[i]) + 1, int(crow[i + 1] - diag[i] - 1),
                                                        int(diag[i]))),
-                                  SPLIT_PHASE_NT["bs"])
+                                  "bs")
         # Fun_SPLIT: items [0, NVAR) are P rows (p_sterm), [NVAR, 2 NVAR) D rows (d_sterm)
         self.split["fun"] = passes([
             [(i, int(self.p_start[i]), int(self.p_start[i + 1] - self.p_start[i]), 0) for i in range(nvar)] +
             [(nvar + i, int(self.d_start[i]), int(self.d_start[i + 1] - self.d_start[i]), 0) for i in range(nvar)]],
-            SPLIT_PHASE_NT["fun"])
+            "fun")
         self.split["jac"] = passes([[(e, int(self.j_start[e]), int(self.j_start[e + 1] - self.j_start[e]), 0)
-                                     for e in range(nz)]], SPLIT_PHASE_NT["jac"])
+                                     for e in range(nz)]], "jac")
+        self.split_rec = {ph: self._solve_records(ph) for ph in ("fs", "bs")}
+
+    def _solve_records(self, ph):
+        """Lane records of the substitution passes, which the kernel copies
+        into shared memory a few passes ahead: eight uint32 per lane per pass,
+        x | level end << 24 (set on every lane of a pass that ends a level),
+        first term | finish word << 16, then the columns icol[first + k] of
+        the lane's terms, two 16-bit columns per word (SPLIT_MAXCH of them)."""
+        task, info = self.split[ph]
+        nt = SPLIT_PHASE_NT[ph]
+        assert nt == 32 and 2 + (SPLIT_MAXCH + 1) // 2 <= 8
+        task = task.reshape(-1, 4)
+        rec = np.zeros((len(info) * nt, 8), np.uint32)
+        for p, w in enumerate(info):
+            end = (int(w) >> 3) & 1
+            for lane in range(nt):
+                x, y, z, _ = (int(v) for v in task[p * nt + lane])
+                n = (x >> 19) & 31
+                assert x < (1 << 24) and y < 0x10000 and z < 0x10000 and n <= SPLIT_MAXCH
+                words = [x | end << 24, y | z << 16] + [0] * 6
+                for k in range(n):
+                    col = int(self.icol[y + k])
+                    assert col < 0x10000
+                    words[2 + k // 2] |= col << (16 * (k & 1))
+                rec[p * nt + lane] = words
+        return rec.reshape(-1)
 
     # flop bookkeeping used by the roofline accounting (FP64 operations per
     # call, counting a multiply-add as 2, a division as 1, in STRICT form)
@@ -448,6 +474,9 @@ class Tables:
                 ph.upper(), SPLIT_PHASE_NT[ph], ph.upper(), len(info)))
             arr("split_%s_task" % ph, task if len(task) else np.zeros(4, np.uint32), "unsigned")
             arr("split_%s_pass" % ph, info if len(info) else np.zeros(1, np.uint32), "unsigned")
+            if ph in self.split_rec:
+                rec = self.split_rec[ph]
+                arr("split_%s_rec" % ph, rec if len(rec) else np.zeros(8, np.uint32), "unsigned")
         out.append("static const double lit[%d] = {%s};" % (
             len(self.literals), ",".join(_hexfloat(v) for v in self.literals)))
         out.append("}  // namespace gcmech_tables")

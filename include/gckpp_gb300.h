@@ -80,6 +80,12 @@ extern "C" {
                                       same order; results agree to rounding (within 1e-13
                                       relative: compile-time constants let the compiler
                                       specialise a few libm calls). */
+#define GC_KPP_OPT_QUEUE_CHUNK 14 /* queue schedule: queue positions a lane of the thread-per-cell
+                                      kernel takes per claim, in [1, 64]; 0 = default 1.  A lane
+                                      integrates its positions one after the other and claims
+                                      again when they are used up (the chunk of an OpenMP
+                                      SCHEDULE(DYNAMIC, chunk) cell loop).  Results do not
+                                      depend on it. */
 #define GC_KPP_OPT_ASYNC 9        /* 1 = chemistry steps never synchronise the host, so that a
                                      caller can capture them in a CUDA graph: the retry list and
                                      the block-per-cell count stay on the device, *nretry (and

@@ -23,8 +23,10 @@ def test_autotune_small_grid():
             "rst": torch.zeros((20, n), dtype=torch.float64, device=dev),
             "ierr": torch.zeros(n, dtype=torch.int32, device=dev)}
     solver = capi.Solver(0, arith="fast", schedule="queue")
-    axes = {"block": [64, 128], "arith": ["fast", "fast2"], "cell_block": [128], "evict_after": [0, 3]}
+    axes = {"block": [64, 128], "arith": ["fast", "fast2"], "queue_chunk": [1, 4], "cell_block": [32, 128],
+            "block_split": [False], "evict_after": [0, 3]}
     best, t, table = autotune.tune(solver, case, torch.zeros(n, dtype=torch.float64, device=dev), sweeps=1,
                                    reps=1, axes=axes)
     assert all(best[k] in axes[k] for k in axes)
+    assert {row["queue_chunk"] for row in table} == {1, 4} and {row["cell_block"] for row in table} == {32, 128}
     assert len(table) >= 4 and np.isclose(table[0]["ms"], t * 1e3)

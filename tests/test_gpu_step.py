@@ -386,3 +386,35 @@ def test_handover_to_block_per_cell_changes_nothing(solver, step_case, arith, ev
         for a, b in zip(got, base):
             assert np.array_equal(a, b)
     solver.set(evict_after=0, evict_drained=0, cell_block=0, block_split=True)
+
+
+@pytest.mark.parametrize("arith", ["fast", "strict"])
+def test_queue_chunk_changes_nothing(solver, step_case, arith):
+    """GC_KPP_OPT_QUEUE_CHUNK: lanes that take 2, 5 or 64 queue positions per
+    claim integrate the same cells with the same arithmetic, so the results
+    equal those of one-position claims bit for bit (also with a queue order
+    and the hand-over)."""
+    n = step_case["n"]
+    cells = step_case["cells"]
+
+    def run(chunk, evict, order):
+        solver.set(arith=arith, schedule="queue", block=64, queue_chunk=chunk, evict_after=evict, cell_block=128,
+                   block_split=False)
+        c = cells["c"].copy()
+        hs = np.full(n, 20.0)
+        ist = np.zeros((20, n), np.int32)
+        rst = np.zeros((20, n))
+        ierr = np.zeros(n, np.int32)
+        solver.fullchem_step(600.0, cells["met"], cells["photol"], c, step_case["atol"], step_case["rtol"],
+                             step_case["icntrl"], step_case["rcntrl"], hs, ist, rst, ierr, order=order)
+        return [c, hs, ist, rst, ierr]
+
+    perm = np.random.default_rng(9).permutation(n).astype(np.int32)
+    for evict, order in ((0, None), (2, perm)):
+        base = run(1, evict, order)
+        for chunk in (2, 5, 64):
+            for a, b in zip(run(chunk, evict, order), base):
+                assert np.array_equal(a, b)
+    with pytest.raises(capi.GcKppError):
+        solver.set(queue_chunk=65)
+    solver.set(queue_chunk=0, evict_after=0, cell_block=0, block_split=True)

@@ -173,3 +173,29 @@ def test_split_fun_and_jac_match_sequential(tab):
     _replay(t, "jac", lambda e, z: 0.0,
             lambda e, k, acc: acc - slit[int(js[k]) >> 20] * B[int(js[k]) & 0xFFFFF], jfinish)
     assert np.allclose(J, jref, rtol=1e-12, atol=1e-12 * np.abs(jref).max())
+
+
+def test_solve_records_carry_the_substitution_schedule(tab):
+    """The 32-byte lane records that the kernel stages for the substitution
+    passes hold each lane's task word, the level-end bit on every lane of a
+    level's last pass (all lanes of the warp then meet at the warp barrier),
+    the first term and finish word, and the columns of the lane's terms, so
+    the records replay the schedule above."""
+    import gcchem.tables as tables
+
+    t = tab
+    for ph in ("fs", "bs"):
+        task, info = t.split[ph]
+        npass = len(info)
+        rec = t.split_rec[ph].reshape(npass, 32, 8).astype(np.int64)
+        tk = task.reshape(npass, 32, 4).astype(np.int64)
+        assert np.array_equal(rec[:, :, 0] & 0xFFFFFF, tk[:, :, 0])
+        assert np.array_equal(rec[:, :, 0] >> 24, np.repeat(((info.astype(np.int64) >> 3) & 1)[:, None], 32, 1))
+        assert np.array_equal(rec[:, :, 1] & 0xFFFF, tk[:, :, 1])
+        assert np.array_equal(rec[:, :, 1] >> 16, tk[:, :, 2])
+        for p in range(npass):
+            for lane in range(32):
+                n = (int(rec[p, lane, 0]) >> 19) & 31
+                y = int(rec[p, lane, 1]) & 0xFFFF
+                cols = [(int(rec[p, lane, 2 + k // 2]) >> (16 * (k & 1))) & 0xFFFF for k in range(tables.SPLIT_MAXCH)]
+                assert cols[:n] == [int(c) for c in t.icol[y:y + n]] and not any(cols[n:])
