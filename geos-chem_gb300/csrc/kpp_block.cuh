@@ -301,7 +301,9 @@ struct SplitJac {
 };
 
 // Task of one lane in one pass: x = item | seglog << 16 | nterms << 19,
-// y = first term, z = the phase's finish word; item 0xFFFF is an idle lane.
+// y = first term, z = the phase's finish word, w = the warp's bounds (1 if
+// any lane has an item | longest chunk << 1 | widest seglog << 5); item
+// 0xFFFF is an idle lane.
 // With it travel the lane's term words, the functor's pre value and the
 // pass word.
 struct SplitTask {
@@ -355,10 +357,11 @@ __device__ __forceinline__ void split_run(const MechDev& m, int ph, const PH& f)
     // A warp runs as many multiply-adds as its longest chunk and as many
     // butterfly levels as its widest segment; a warp with no item in this
     // pass issues no arithmetic (predicated-off FP64 instructions still
-    // take the SM's FP64 pipe).
-    if (__any_sync(0xffffffffu, busy)) {
-      const int nmax = __reduce_max_sync(0xffffffffu, (unsigned)n);
-      const int lmax = __reduce_max_sync(0xffffffffu, (unsigned)seglog);
+    // take the SM's FP64 pipe).  The schedule stores these warp-uniform
+    // bounds in the task's fourth word.
+    if (cur.t.w & 1u) {
+      const int nmax = (cur.t.w >> 1) & 15;
+      const int lmax = (cur.t.w >> 5) & 7;
       const bool lead = busy && (tid & (seg - 1)) == 0;
       double acc = lead ? f.base(item, cur.t.z, cur.pre) : 0.0;
 #pragma unroll
@@ -416,8 +419,9 @@ __device__ inline void bk_decomp_split(const MechDev& m, const double* J0, doubl
 // SPLIT_STAGE slots in shared memory (cp.async) while pass p computes, and
 // waits only for its own copies (cp.async.wait_group), so no barrier orders
 // the copies and nothing waits on another thread.  Record (tables.py
-// _solve_records): x | level end << 24, first term | finish word << 16, the
-// columns of the lane's terms as 16-bit words.  Row i's sum is X(i) - sum
+// _solve_records): x | level end << 24 | the warp's longest chunk << 25 |
+// its widest seglog << 29, first term | finish word << 16, the columns of the
+// lane's terms as 16-bit words.  Row i's sum is X(i) - sum
 // G(kk) X(icol(kk)) over the LU positions kk of its chunk; the backward
 // substitution multiplies by the stored reciprocal pivot G(finish word).
 constexpr int SPLIT_STAGE = 4;
@@ -466,22 +470,20 @@ __device__ __forceinline__ void split_solve_staged(const MechDev& m, int ph, con
     const int seg = 1 << seglog;
     const int n = (a.x >> 19) & 31;
     const int y = a.y & 0xffff;
-    if (__any_sync(0xffffffffu, busy)) {
-      const int nmax = __reduce_max_sync(0xffffffffu, (unsigned)n);
-      const int lmax = __reduce_max_sync(0xffffffffu, (unsigned)seglog);
-      const bool lead = busy && (lane & (seg - 1)) == 0;
-      double acc = lead ? X[item] : 0.0;
+    const int nmax = (a.x >> 25) & 15;  // the warp's longest chunk and widest segment
+    const int lmax = a.x >> 29;
+    const bool lead = busy && (lane & (seg - 1)) == 0;
+    double acc = lead ? X[item] : 0.0;
 #pragma unroll
-      for (int k = 0; k < SPLIT_MAXCH; ++k) {
-        if (k >= nmax) break;
-        if (k < n) acc = fma(-G[y + k], X[(cw[k >> 1] >> (16 * (k & 1))) & 0xffffu], acc);
-      }
-      for (int o = (1 << lmax) >> 1; o > 0; o >>= 1) {
-        const double v = __shfl_xor_sync(0xffffffffu, acc, o);
-        if (o < seg) acc += v;
-      }
-      if (lead) X[item] = BACK ? acc * G[a.y >> 16] : acc;
+    for (int k = 0; k < SPLIT_MAXCH; ++k) {
+      if (k >= nmax) break;
+      if (k < n) acc = fma(-G[y + k], X[(cw[k >> 1] >> (16 * (k & 1))) & 0xffffu], acc);
     }
+    for (int o = (1 << lmax) >> 1; o > 0; o >>= 1) {
+      const double v = __shfl_xor_sync(0xffffffffu, acc, o);
+      if (o < seg) acc += v;
+    }
+    if (lead) X[item] = BACK ? acc * G[a.y >> 16] : acc;
     if ((a.x >> 24) & 1u) __syncwarp();
   }
   cp_async_wait<0>();

@@ -294,8 +294,11 @@ class Tables:
         y = index of the lane's first term in the phase's term array, z =
         the phase's finish word (LU: position of the pivot of an L entry,
         0xFFFFFFFF for a diagonal entry, 0xFFFFFFFE for a U entry; backward
-        substitution: position of the row's diagonal), 0; item 0xFFFF is an
-        idle lane.  pass word: max seglog of the pass | barrier << 3."""
+        substitution: position of the row's diagonal), and w, the same for
+        the 32 lanes of a warp: 1 if one of them has an item | their largest
+        nterms << 1 | their largest seglog << 5 (so a warp learns its chunk
+        loop and butterfly bounds without a warp reduction); item 0xFFFF is
+        an idle lane.  pass word: max seglog of the pass | barrier << 3."""
         nvar, nz = self.nvar, self.lu_nonzero
 
         def passes(levels, ph):
@@ -324,8 +327,13 @@ class Tables:
                     blk = lanes[p * NT:(p + 1) * NT]
                     maxlog = max((x >> 16) & 7 for x, _, _ in blk)
                     info.append(maxlog | (8 if p == npass - 1 else 0))
-                    for x, y, z in blk:
-                        task += [x, y, z, 0]
+                    for w0 in range(0, NT, 32):
+                        warp = blk[w0:w0 + 32]
+                        busy = [x for x, _, _ in warp if (x & 0xFFFF) != 0xFFFF]
+                        wd = (1 | max((x >> 19) & 31 for x in busy) << 1 | max((x >> 16) & 7 for x in busy) << 5
+                              if busy else 0)
+                        for x, y, z in warp:
+                            task += [x, y, z, wd]
             return np.array(task, np.uint32), np.array(info, np.uint32)
 
         def levels_of(order, start, item):
@@ -365,7 +373,8 @@ class Tables:
     def _solve_records(self, ph):
         """Lane records of the substitution passes, which the kernel copies
         into shared memory a few passes ahead: eight uint32 per lane per pass,
-        x | level end << 24 (set on every lane of a pass that ends a level),
+        x | level end << 24 | the warp's largest nterms << 25 | its largest
+        seglog << 29 (the last three the same on every lane of the pass),
         first term | finish word << 16, then the columns icol[first + k] of
         the lane's terms, two 16-bit columns per word (SPLIT_MAXCH of them)."""
         task, info = self.split[ph]
@@ -376,10 +385,11 @@ class Tables:
         for p, w in enumerate(info):
             end = (int(w) >> 3) & 1
             for lane in range(nt):
-                x, y, z, _ = (int(v) for v in task[p * nt + lane])
+                x, y, z, wd = (int(v) for v in task[p * nt + lane])
                 n = (x >> 19) & 31
-                assert x < (1 << 24) and y < 0x10000 and z < 0x10000 and n <= SPLIT_MAXCH
-                words = [x | end << 24, y | z << 16] + [0] * 6
+                nmax, lmax = (wd >> 1) & 15, (wd >> 5) & 7
+                assert x < (1 << 24) and y < 0x10000 and z < 0x10000 and n <= SPLIT_MAXCH <= 15 and lmax <= 5
+                words = [x | end << 24 | nmax << 25 | lmax << 29, y | z << 16] + [0] * 6
                 for k in range(n):
                     col = int(self.icol[y + k])
                     assert col < 0x10000

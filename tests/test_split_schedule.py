@@ -72,6 +72,13 @@ def test_split_chunks_fit_the_kernel(tab):
         assert ((x >> 19) & 31).max() <= tables.SPLIT_MAXCH
         assert len(task) == 4 * len(info) * tables.SPLIT_PHASE_NT[ph]
         assert np.all(info & 7 <= 5)
+        # the fourth word: the bounds of each warp of a pass, the same on its 32 lanes
+        tw = task.reshape(-1, 32, 4).astype(np.int64)
+        busy = (tw[:, :, 0] & 0xFFFF) != 0xFFFF
+        n = np.where(busy, (tw[:, :, 0] >> 19) & 31, 0)
+        slog = np.where(busy, (tw[:, :, 0] >> 16) & 7, 0)
+        want = np.where(busy.any(axis=1), 1 | n.max(axis=1) << 1 | slog.max(axis=1) << 5, 0)
+        assert np.array_equal(tw[:, :, 3], np.repeat(want[:, None], 32, axis=1))
 
 
 def test_split_lu_and_solves_match_sequential(tab):
@@ -179,8 +186,9 @@ def test_solve_records_carry_the_substitution_schedule(tab):
     """The 32-byte lane records that the kernel stages for the substitution
     passes hold each lane's task word, the level-end bit on every lane of a
     level's last pass (all lanes of the warp then meet at the warp barrier),
-    the first term and finish word, and the columns of the lane's terms, so
-    the records replay the schedule above."""
+    the warp's chunk and butterfly bounds, the first term and finish word,
+    and the columns of the lane's terms, so the records replay the schedule
+    above."""
     import gcchem.tables as tables
 
     t = tab
@@ -190,7 +198,9 @@ def test_solve_records_carry_the_substitution_schedule(tab):
         rec = t.split_rec[ph].reshape(npass, 32, 8).astype(np.int64)
         tk = task.reshape(npass, 32, 4).astype(np.int64)
         assert np.array_equal(rec[:, :, 0] & 0xFFFFFF, tk[:, :, 0])
-        assert np.array_equal(rec[:, :, 0] >> 24, np.repeat(((info.astype(np.int64) >> 3) & 1)[:, None], 32, 1))
+        assert np.array_equal((rec[:, :, 0] >> 24) & 1, np.repeat(((info.astype(np.int64) >> 3) & 1)[:, None], 32, 1))
+        assert np.array_equal((rec[:, :, 0] >> 25) & 15, (tk[:, :, 3] >> 1) & 15)
+        assert np.array_equal(rec[:, :, 0] >> 29, (tk[:, :, 3] >> 5) & 7)
         assert np.array_equal(rec[:, :, 1] & 0xFFFF, tk[:, :, 1])
         assert np.array_equal(rec[:, :, 1] >> 16, tk[:, :, 2])
         for p in range(npass):
