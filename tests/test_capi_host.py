@@ -58,3 +58,25 @@ def test_ctx_create_without_gpu_fails_cleanly(lib):
     rc = lib.gc_kpp_ctx_create(ctypes.byref(ctx), 0)
     assert rc == capi.GC_KPP_ECUDA
     assert not ctx.value
+
+
+def _header_ints():
+    vals = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        for name, v in re.findall(r"^#define\s+(GC_\w+)\s+\(?(-?\d+)\)?", open(h).read(), re.M):
+            vals[name] = int(v)
+    return vals
+
+
+def test_binding_constants_match_the_header():
+    """Every status code, memory kind and option key of the ctypes binding
+    has the value the C header gives it, and every option key of the header
+    is bound."""
+    vals = _header_ints()
+    for name in ("GC_KPP_OK", "GC_KPP_EINVAL", "GC_KPP_ECUDA", "GC_KPP_ENOMEM", "GC_KPP_EUNSUPPORTED"):
+        assert getattr(capi, name) == vals[name], name
+    assert (capi.MEM_HOST, capi.MEM_DEVICE) == (vals["GC_KPP_MEM_HOST"], vals["GC_KPP_MEM_DEVICE"])
+    opts = {k[len("GC_KPP_OPT_"):]: v for k, v in vals.items() if k.startswith("GC_KPP_OPT_")}
+    assert len(set(opts.values())) == len(opts)  # distinct keys
+    for k, v in opts.items():
+        assert getattr(capi, "OPT_" + k) == v, k
