@@ -7,7 +7,7 @@
   oracle), one 1200 s chemistry step through the path the benchmark times:
   the learned plan (H0 proposals, stiffness bins, queue order), fast
   arithmetic, the persistent queue, the top bin block-per-cell (split form),
-  hand-over after 2 steps, retry and clamp -- against the oracle's loop body
+  hand-over after 4 steps, retry and clamp -- against the oracle's loop body
   (KPP/fullchem/gckpp_Integrator.F90:578-786,
   GeosCore/fullchem_mod.F90:943-1350) started from the same H0.
 

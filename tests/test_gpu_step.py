@@ -3,9 +3,15 @@ reference's error behaviour, against the CPU oracle."""
 import numpy as np
 import pytest
 
+import os
+import sys
+
 import gcchem.capi as capi
 import gcchem.inputs as inputs
 import gcchem.mechanism as mechanism
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from parity_bars import check_other_sequences  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 NVAR = 353
@@ -39,6 +45,15 @@ def step_case():
     return dict(n=n, cells=cells, atol=atol, rtol=rtol, icntrl=icntrl, rcntrl=rcntrl)
 
 
+@pytest.fixture(scope="module")
+def step_tight(orc, step_case):
+    """The loop body of the step case integrated at RTOL 1e-8 (the accuracy
+    reference for cells whose step sequence differs from the oracle's)."""
+    k = step_case
+    return _oracle_step(orc, mechanism.load_ir(), k["cells"], 600.0, k["icntrl"], k["rcntrl"], k["atol"],
+                        np.full_like(k["rtol"], 1e-8))[0]
+
+
 def _gpu_step(solver, case, icntrl=None, hstart=None, dt=600.0, arith="strict"):
     solver.set(arith=arith, schedule="plain", block=0)
     n = case["n"]
@@ -52,7 +67,7 @@ def _gpu_step(solver, case, icntrl=None, hstart=None, dt=600.0, arith="strict"):
     return c, ist, rst, ierr, nretry, hs
 
 
-def test_fullchem_step_matches_oracle(solver, orc, step_case):
+def test_fullchem_step_matches_oracle(solver, orc, step_case, step_tight):
     ir = mechanism.load_ir()
     c, ist, rst, ierr, nretry, _ = _gpu_step(solver, step_case)
     c_ref, ist_ref, rst_ref, ierr_ref, nretry_ref = _oracle_step(orc, ir, step_case["cells"], 600.0,
@@ -64,13 +79,14 @@ def test_fullchem_step_matches_oracle(solver, orc, step_case):
     assert same.mean() >= 0.99
     big = np.abs(c_ref) > 1e4
     assert np.max(np.where(big, _rel(c, c_ref), 0.0)[:, same]) < 1e-9
+    check_other_sequences(c, c_ref, step_tight, same, step_case["atol"], step_case["rtol"])
     assert np.all(c >= 0.0)
     for fam in ir["families"]:
         # dummies were zeroed before the integration, then produced again
         assert np.all(np.isfinite(c[ir["species"].index(fam)]))
 
 
-def test_retry_policy_and_hnew_chain(solver, orc, step_case):
+def test_retry_policy_and_hnew_chain(solver, orc, step_case, step_tight):
     """Cells that fail (step cap, IERR=-6) are integrated once more from the
     saved concentrations with Hstart = 0; KPPHvalue = RSTATE(Nhnew)."""
     ir = mechanism.load_ir()
@@ -89,6 +105,9 @@ def test_retry_policy_and_hnew_chain(solver, orc, step_case):
     assert np.allclose(hs_out, rst[2])
     big = np.abs(c_ref) > 1e4
     assert np.max(np.where(big, _rel(c, c_ref), 0.0)[:, same]) < 1e-9
+    # cells that end the step successfully with another step sequence: bounded
+    # against the uncapped RTOL 1e-8 loop body
+    check_other_sequences(c, c_ref, step_tight, same, step_case["atol"], step_case["rtol"], sel=ierr == 1)
 
 
 @pytest.mark.parametrize("field,value,code", [("rtol", 1.0, -5), ("atol", 0.0, -5), ("method", 9, -2),
