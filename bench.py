@@ -181,7 +181,7 @@ def run_reference(args):
     atol, rtol = inputs.tolerances()
     icntrl, rcntrl = inputs.default_controls()
     # sample cells evenly over the grid; spin them up on the CPU
-    m = min(ncell, 64 * threads)
+    m = min(ncell, 256 * threads)
     idx = np.linspace(0, ncell - 1, m).astype(np.int64)
     met = cells["met"][:, idx]
     ph = cells["photol"][:, idx]
@@ -191,23 +191,25 @@ def run_reference(args):
         c, _, _, _ = orc.integrate(c, r, atol, rtol, 0.0, args.spinup, icntrl, rcntrl, variant="fast",
                                    nthreads=threads)
         c = np.maximum(c, 0.0)
-    sample = {"c": c}
     times = []
-    per = None
+    sel = None
     for it in range(args.warmup + args.steps):
-        if per is None:
+        if sel is None:
             t0 = time.perf_counter()
             orc.integrate(c[:, : 2 * threads], r[:, : 2 * threads], atol, rtol, 0.0, DT, icntrl, rcntrl,
                           variant="fast", nthreads=threads)
             dt0 = time.perf_counter() - t0
             per = int(min(m, max(threads, 2 * threads * 8.0 / max(dt0, 1e-3))))
+            # the timed cells: evenly spaced over the sample, so over the whole grid
+            sel = np.unique(np.linspace(0, m - 1, per).astype(np.int64))
+            met_s, ph_s, c_s = (np.ascontiguousarray(x[:, sel]) for x in (met, ph, c))
         t0 = time.perf_counter()
-        rr = orc.update_rconst(met[:, :per], ph[:, :per], c[:, :per], variant="fast")
-        orc.integrate(sample["c"][:, :per], rr, atol, rtol, 0.0, DT, icntrl, rcntrl, variant="fast",
-                      nthreads=threads)
+        rr = orc.update_rconst(met_s, ph_s, c_s, variant="fast")
+        orc.integrate(c_s, rr, atol, rtol, 0.0, DT, icntrl, rcntrl, variant="fast", nthreads=threads)
         dt = time.perf_counter() - t0
         if it >= args.warmup:
             times.append(dt)
+    per = len(sel)
     value = per / float(np.mean(times))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": args.gpus,
@@ -217,7 +219,8 @@ def run_reference(args):
         "config": {"workload": "fullchem 4x5x72 grid (238,464 cells), one 1200 s step, Rodas3, RTOL 5e-3",
                    "cells": ncell, "dt_s": DT, "sample_cells_per_step": per},
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
-                         "sample": "%d evenly spaced cells of the grid per step (rates + integrate)" % per},
+                         "sample": "%d evenly spaced cells of the grid per step (rates + integrate from "
+                                   "Hstart = 0, from the CPU-spun state)" % per},
         "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
