@@ -139,6 +139,36 @@ def build(verbose=False, force=False):
     return lib
 
 
+def phase_cycles_path():
+    """Profiling copy of the fullchem library whose split block-per-cell
+    kernel counts its cycles per phase (gc_kpp_phase_cycles); not built by
+    build()."""
+    return os.path.join(LIBDIR, "libgckpp_gb300_phases.so")
+
+
+def build_phase_cycles(verbose=False):
+    """Builds phase_cycles_path(): the objects of build() with the fast
+    one-cell-per-thread kernels recompiled with -DGCKPP_PHASE_CYCLES."""
+    lib = build(verbose=verbose)
+    exe = nvcc()
+    obj = os.path.join(BUILD, "kpp_kernels_fast_phases.o")
+    src, name, extra = next(u for u in _units() if u[1] == "kpp_kernels_fast.o")
+    cmd = [exe] + NVCC_FLAGS + extra + ["-DGCKPP_PHASE_CYCLES", "-c", src, "-o", obj]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed: %s\n%s" % (" ".join(cmd), r.stdout.decode()))
+    objs = [os.path.join(BUILD, u[1]) for u in _units() if u[1] != name] + [obj]
+    objs += [os.path.join(BUILD, o) for o in ("gckpp_capi_fullchem.o", "rates_direct_fullchem.o")]
+    out = phase_cycles_path()
+    cmd = [exe] + ARCH + ["-shared", "-cudart", "shared", "-o", out] + objs
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), r.stdout.decode()))
+    if verbose:
+        print(out)
+    return lib, out
+
+
 def routines_path():
     """Per-routine launches of the fullchem tables for profiling, not part of the C ABI."""
     return os.path.join(LIBDIR, "libgckpp_routines.so")

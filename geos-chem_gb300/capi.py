@@ -141,8 +141,9 @@ class Solver:
     """A solver context on one CUDA device (gc_kpp_ctx)."""
 
     def __init__(self, device=0, arith="fast", schedule="plain", block=0, blocks_per_sm=0, max_slots=0,
-                 mech="fullchem"):
-        self.lib = load_library(mech=mech)
+                 mech="fullchem", lib_path=None):
+        # lib_path: another build of the mechanism's library (a profiling copy)
+        self.lib = load_library(lib_path, mech=mech)
         self.mech = mech
         self.ctx = ctypes.c_void_p()
         self._check(self.lib.gc_kpp_ctx_create(ctypes.byref(self.ctx), device))

@@ -234,6 +234,23 @@ __device__ void bk_solve(const MechDev& m, const double* G, double* X) {
 // rounding, not bit for bit.
 constexpr int SPLIT_MAXCH = 12;
 
+// Profiling build only (GCKPP_PHASE_CYCLES, build.build_phase_cycles): the
+// first thread of each phase adds the phase's clock64 cycles to
+// g_phase_cycles[phase] and its calls to g_phase_cycles[8 + phase]; entry 7
+// is the whole kernel, per block.  Read by gc_kpp_phase_cycles.
+#ifdef GCKPP_PHASE_CYCLES
+__device__ unsigned long long g_phase_cycles[16];
+#define GCKPP_PHASE_BEGIN() const long long phase_c0_ = clock64()
+#define GCKPP_PHASE_END(ph, first)                                                          \
+  if (first) {                                                                              \
+    atomicAdd(&g_phase_cycles[(ph)], (unsigned long long)(clock64() - phase_c0_));          \
+    atomicAdd(&g_phase_cycles[8 + (ph)], 1ull);                                             \
+  }
+#else
+#define GCKPP_PHASE_BEGIN()
+#define GCKPP_PHASE_END(ph, first)
+#endif
+
 // Each phase is a functor: terms(item) is the term array of the item,
 // pre(item, z) a value loaded together with the task of the next pass (it
 // may only depend on data that the phase does not change), base(item, z,
@@ -336,6 +353,7 @@ __device__ __forceinline__ void split_run(const MechDev& m, int ph, const PH& f)
   const int np = m.sp_npass[ph];
   const int tid = threadIdx.x;
   if (tid >= nt || np == 0) return;
+  GCKPP_PHASE_BEGIN();
   const uint4* task = m.sp_task[ph];
   const unsigned* pw = m.sp_pass[ph];
   const uint4 idle = make_uint4(0xffffu, 0u, 0u, 0u);
@@ -383,6 +401,7 @@ __device__ __forceinline__ void split_run(const MechDev& m, int ph, const PH& f)
     }
     cur = nxt;
   }
+  GCKPP_PHASE_END(ph, tid == 0)
 }
 
 // Fun_SPLIT at V in the split form; B must hold the B products at V.  D is a
@@ -441,6 +460,7 @@ template <bool BACK>
 __device__ __forceinline__ void split_solve_staged(const MechDev& m, int ph, const double* __restrict__ G,
                                                    double* X, uint4* ring) {
   const int np = m.sp_npass[ph];
+  GCKPP_PHASE_BEGIN();
   const int lane = threadIdx.x;  // the first warp
   const uint4* rec = m.sp_rec[ph - SP_FS] + 2 * lane;
   uint4* mine = ring + 2 * lane;  // slot k of this lane: mine[64 k], mine[64 k + 1]
@@ -487,6 +507,7 @@ __device__ __forceinline__ void split_solve_staged(const MechDev& m, int ph, con
     if ((a.x >> 24) & 1u) __syncwarp();
   }
   cp_async_wait<0>();
+  GCKPP_PHASE_END(ph, lane == 0)
 }
 
 // Forward and backward substitution in the split form, on the first warp

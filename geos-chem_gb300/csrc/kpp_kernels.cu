@@ -105,8 +105,26 @@ cudaError_t GCKPP_CAT(gckpp_launch_block_, GCKPP_VARIANT)(int grid, int block, c
 #if GCKPP_NC == 1 && GCKPP_STRICT == 0
 // Split block-per-cell form: SPLIT_NT threads, sums cut across warp lanes.
 __global__ void __launch_bounds__(GCKPP_SPLIT_NT, 3) ros_block_split_kernel(MechDev m, RosMethod r, RosParams p) {
+  GCKPP_PHASE_BEGIN();
   ros_block_driver<false, true>(m, r, p);
+  GCKPP_PHASE_END(7, threadIdx.x == 0)
 }
+
+#ifdef GCKPP_PHASE_CYCLES
+// Profiling build only: copies the split kernel's phase counters (16
+// values: cycles of LU, forward and backward substitution, Fun_SPLIT,
+// Jac_SP, -, -, whole kernel; then the call counts) and optionally clears
+// them.  Synchronises the device.
+extern "C" int gc_kpp_phase_cycles(unsigned long long* out, int reset) {
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(g_phase_cycles));
+  if (e == cudaSuccess && reset) {
+    const unsigned long long zero[16] = {};
+    e = cudaMemcpyToSymbol(g_phase_cycles, zero, sizeof(zero));
+  }
+  return (int)e;
+}
+#endif
 
 // the cell's arrays, 16-byte aligned, and the ring of staged substitution
 // records

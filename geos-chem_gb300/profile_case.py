@@ -1,7 +1,7 @@
 """A small, self-contained chemistry case for profiling the kernels.
 
     python geos-chem_gb300/profile_case.py --cells 4096 --tout 60 --arith fast [--probe]
-    python geos-chem_gb300/profile_case.py --grid 72x46x8 --binned 64
+    python geos-chem_gb300/profile_case.py --grid 72x46x8 --binned 64 [--phase-cycles]
     python geos-chem_gb300/profile_case.py --grid 72x46x24 --learned
     python geos-chem_gb300/profile_case.py --grid 72x46x24 --autoreduce 100 [--append]
     python geos-chem_gb300/profile_case.py --routines 4096
@@ -31,6 +31,9 @@ def main(argv=None):
     ap.add_argument("--block", type=int, default=128)
     ap.add_argument("--max-slots", type=int, default=0, help="cap on cells in flight (0: all resident threads)")
     ap.add_argument("--queue-chunk", type=int, default=1, help="queue positions a lane takes per claim")
+    ap.add_argument("--phase-cycles", action="store_true",
+                    help="with --grid: build and use the profiling library whose split block-per-cell kernel "
+                         "counts clock64 cycles per phase, and print them per step attempt of the timed step")
     ap.add_argument("--grid", default=None, help="NLONxNLATxNLEV: grid step instead of box cells")
     ap.add_argument("--binned", type=int, default=0, help="grid step: cells sent block-per-cell")
     ap.add_argument("--cold", action="store_true",
@@ -82,7 +85,12 @@ def main(argv=None):
 
     dev = torch.device("cuda", 0)
     T = lambda x: torch.tensor(x, device=dev).contiguous()
-    s = capi.Solver(0, arith=args.arith, schedule=args.schedule, block=args.block, max_slots=args.max_slots)
+    phase_lib = build.build_phase_cycles()[1] if args.phase_cycles else None
+    s = capi.Solver(0, arith=args.arith, schedule=args.schedule, block=args.block, max_slots=args.max_slots,
+                    lib_path=phase_lib)
+    phase_buf = (ctypes.c_ulonglong * 16)()
+    if phase_lib:
+        s.lib.gc_kpp_phase_cycles.argtypes = [ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]
     s.set(block_split=args.block_form == "split", queue_chunk=args.queue_chunk)
     atol, rtol = inputs.tolerances()
     ic, rc = inputs.default_controls()
@@ -132,6 +140,8 @@ def main(argv=None):
             print("run %d: %.3f ms" % (rep, t0.elapsed_time(t1)))
             c.copy_(c0)
             hs.copy_(hs0)
+        if phase_lib:
+            s.lib.gc_kpp_phase_cycles(phase_buf, 1)
         torch.cuda.synchronize()
         t0.record()
         s.fullchem_step(1200.0, met, ph, c, at, rt, ic_t, rc_t, hs, ist, rst, ierr, order=order, nblock=nb)
@@ -157,6 +167,17 @@ def main(argv=None):
     if args.grid and nb > 0:
         sel = order[:nb].long().cpu().numpy()
         print("block-per-cell cells %d: ISTATUS sums %s" % (nb, ih[:8, sel].sum(axis=1).tolist()))
+        if phase_lib:
+            # cycles of the block-per-cell launches of the timed step, summed
+            # over blocks, per step attempt (ISTATUS(6), decompositions) of
+            # the block-per-cell cells
+            rc_ = s.lib.gc_kpp_phase_cycles(phase_buf, 0)
+            att = max(int(ih[5, sel].sum()), 1)
+            names = ["LU", "forward subst.", "backward subst.", "Fun_SPLIT", "Jac_SP", "", "", "whole kernel"]
+            print("phase cycles (rc %d), per step attempt of a block:" % rc_)
+            for k in (0, 1, 2, 3, 4, 7):
+                if phase_buf[8 + k]:
+                    print("  %-16s %10.0f  (%d calls)" % (names[k], phase_buf[k] / att, phase_buf[8 + k]))
     print("algorithmic FP64 flops %.4e" % flops)
     if args.producers and args.grid:
         # Do_FullChem's per-cell producers on this grid (synthetic grid-box
