@@ -15,7 +15,7 @@ rows after a "Name, Value, Absolute Tolerance" line:
 Such files turn cells of a real model run into inputs of this solver
 (`cells_from_states`) and fixtures of its tests.  `write_state` produces the
 same layout, with numbers in the writer's formats (ES25.16E3 values, ES10.2E2
-tolerances).
+tolerances, the metadata's I6, F11.4, F11.2 and E11.4 fields).
 """
 import re
 
@@ -44,6 +44,22 @@ META_LABELS = {
 }
 _NUMERIC = {"lon", "lat", "press", "temp", "numden", "h2o_vmr", "cldf", "suncos", "h_init", "h_exit", "dt"}
 _INTEGER = {"level", "steps"}
+
+
+def fortran_e(x, width=11, digits=4):
+    """A real in Fortran Ew.d form, as the writer's e11.4 fields print it:
+    0.ddddE+ee (mantissa in [0.1, 1), two exponent digits; for 99 < |e| <=
+    999 the E is dropped, +eee), right-justified in `width` columns."""
+    x = float(x)
+    if x == 0.0:
+        body = "0." + "0" * digits + "E+00"
+    else:
+        m, e = ("%.*E" % (digits - 1, abs(x))).split("E")
+        ev = int(e) + 1
+        exp = ("E%s%02d" % ("-" if ev < 0 else "+", abs(ev)) if abs(ev) <= 99
+               else "%s%03d" % ("-" if ev < 0 else "+", abs(ev)))
+        body = ("-" if x < 0 else "") + "0." + m.replace(".", "") + exp
+    return body.rjust(width)
 
 
 def fortran_es(x, digits=16, expdigits=3):
@@ -96,13 +112,18 @@ def write_state(path, c, rconst, atol, meta=None, icntrl=None, rcntrl=None, ir=N
         if key in ("h_init",):
             head += ["", "KPP Integrator-specific parameters               ", ""]
         v = meta.get(key, "" if key in ("location", "timestamp") else 0)
+        # the writer's formats: i6, e11.4, f11.2 (temperature), f11.4
         if key in _INTEGER:
             txt = "%6d" % int(v)
+        elif key in ("numden", "h2o_vmr", "cldf", "suncos"):
+            txt = fortran_e(v)
+        elif key == "temp":
+            txt = "%11.2f" % float(v)
         elif key in _NUMERIC:
-            txt = ("%11.4E" if key in ("numden", "h2o_vmr", "cldf", "suncos") else "%11.4f") % float(v)
+            txt = "%11.4f" % float(v)
         else:
             txt = str(v)
-        head.append("%-50s%s" % (label, txt))
+        head.append("%-49s%s" % (label, txt))  # the writer's labels are 49 characters
     head.append("ICNTRL integrator options used:")
     head.append("".join("%6d" % int(v) for v in icntrl[:10]))
     head.append("".join("%6d" % int(v) for v in icntrl[10:20]))

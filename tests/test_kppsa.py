@@ -1,6 +1,7 @@
 """KPP-Standalone state files (GeosCore/kppsa_interface_mod.F90:569-870
 layout): write -> read round trip, reaction rates, batch assembly."""
 import os
+import re
 import sys
 
 import numpy as np
@@ -57,3 +58,106 @@ def test_fortran_es_format():
     assert kppsa.fortran_es(-1.5e-300).endswith("E-300") and float(kppsa.fortran_es(-1.5e-300)) == -1.5e-300
     assert kppsa.fortran_es(0.0) == "0.0000000000000000E+000"
     assert kppsa.fortran_es(1e-2, 2, 2) == "1.00E-02"
+
+
+def _field(desc):
+    """Regex of one output field of a Fortran edit descriptor (i6, f11.4,
+    e11.4, es25.16e3, es10.2e2, i0)."""
+    m = re.fullmatch(r"(?i)(es|e|f|i)(\d+)(?:\.(\d+))?(?:e(\d+))?", desc)
+    kind, w = m.group(1).lower(), int(m.group(2))
+    d = int(m.group(3) or 0)
+    if kind == "i":  # the width is checked by _fits
+        return r" *-?\d+"
+    if kind == "f":
+        return r" *-?\d*\.\d{%d}" % d
+    if kind == "e":  # 0.ddddE+ee (or +eee without the E)
+        return r" *-?0\.\d{%d}(?:E[+-]\d\d|[+-]\d{3})" % d
+    e = int(m.group(4))
+    return r" *-?\d\.\d{%d}E[+-]\d{%d}" % (d, e)
+
+
+def _fits(value, desc):
+    w = int(re.search(r"\d+", desc).group())
+    return (w == 0 or len(value) == w) and re.fullmatch(_field(desc), value) is not None
+
+
+def test_writer_follows_the_reference_layout(tmp_path):
+    """The header lines from 'Meteorological and general grid cell metadata'
+    on, and every CSV row, in the order and edit descriptors of the
+    reference writer (tests/golden/kppsa_layout.json, extracted from
+    GeosCore/kppsa_interface_mod.F90 by tests/golden/make_kppsa_layout.py)."""
+    import json
+
+    import gcchem.inputs as inputs
+    import gcchem.kppsa as kppsa
+    import gcchem.mechanism as mechanism
+
+    layout = json.load(open(os.path.join(ROOT, "tests", "golden", "kppsa_layout.json")))
+    ir = mechanism.load_ir()
+    cells = inputs.box_cells(1, seed=4)
+    nspec = ir["dims"]["nspec"]
+    atol = np.r_[inputs.tolerances()[0], np.ones(nspec - ir["dims"]["nvar"])]
+    rconst = np.random.default_rng(2).lognormal(-20, 5, ir["dims"]["nreact"])
+    ic, rc = inputs.default_controls()
+    meta = {"location": "cell_A", "timestamp": "20190701_1200z", "lon": -70.25, "lat": 40.5, "level": 3,
+            "press": 850.123, "temp": 280.567, "numden": 2.1e19, "h2o_vmr": 0.004, "cldf": 0.0, "suncos": -0.7,
+            "h_init": 12.5, "h_exit": 300.0, "dt": 600.0, "steps": 7}
+    path = str(tmp_path / "cell.txt")
+    kppsa.write_state(path, cells["c"][:, 0], rconst, atol, meta, ic, rc, ir)
+    lines = open(path).read().splitlines()
+    name_at = lines.index("Name,   Value,   Absolute Tolerance")
+    assert int(lines[0]) == name_at + 1  # the first line counts the header lines
+    k = lines.index(layout["lines"][0]["text"])
+    for entry in layout["lines"]:
+        fmt, text = entry["format"].strip("()"), entry["text"]
+        parts = fmt.split(",")
+        if parts[0] == "/":
+            assert lines[k] == "", (k, lines[k])
+            k += 1
+            parts = parts[1:]
+        line = lines[k]
+        if parts[0] == "a" and len(parts) > 1 and parts[1] not in ("/",):
+            w = len(text)
+            assert line[:w] == text, (line, text)
+            if parts[1] != "a":
+                assert _fits(line[w:], parts[1]), (line, parts[1])
+        elif parts[0] == "a":
+            assert line == ("=" * 76 if text is None else text), (line, text)
+        else:  # 10i6, 5F13.6: repeated fields
+            n, desc = re.fullmatch(r"(\d+)(\w+\.?\d*)", parts[0]).groups()
+            w = int(re.search(r"\d+", desc).group())
+            assert len(line) == int(n) * w
+            assert all(_fits(line[j:j + w], desc) for j in range(0, len(line), w)), line
+        k += 1
+        if parts[-1] == "/":
+            assert lines[k] == ""
+            k += 1
+    assert k == name_at + 1
+    # CSV rows: species (FORMAT 130; 120 for unmapped species), R (140), A (150)
+    f = layout["csv_formats"]
+    desc = lambda fmt: re.findall(r"(?i)\b(es\d+\.\d+e\d+|i0|a)\b", re.sub(r'"[^"]*"', "", fmt))
+    assert desc(f["130"]) == ["a", "es25.16e3", "es10.2e2"] and desc(f["120"]) == ["i0", "es25.16e3", "es10.2e2"]
+    assert desc(f["140"]) == desc(f["150"]) == ["i0", "es25.16e3"]
+    rows = lines[name_at + 1:]
+    nreact = ir["dims"]["nreact"]
+    assert len(rows) == nspec + 2 * nreact
+    for row, name in zip(rows[:nspec], ir["species"]):
+        nm, v, t = row.split(",")
+        assert nm == name and _fits(v, "es25.16e3") and _fits(t, "es10.2e2"), row
+    for pre, rows_ in (("R", rows[nspec:nspec + nreact]), ("A", rows[nspec + nreact:])):
+        assert f["140" if pre == "R" else "150"].startswith('"%s"' % pre)
+        for n, row in enumerate(rows_):
+            key, v = row.split(",")
+            assert key == "%s%d" % (pre, n + 1) and _fits(v, "es25.16e3"), row
+
+
+def test_fortran_e_format():
+    import gcchem.kppsa as kppsa
+
+    # Ew.d: 0.dddd mantissa, two exponent digits (E dropped beyond 99)
+    assert kppsa.fortran_e(2.1e19) == " 0.2100E+20"
+    assert kppsa.fortran_e(0.004) == " 0.4000E-02"
+    assert kppsa.fortran_e(-1.5e-5) == "-0.1500E-04"
+    assert kppsa.fortran_e(0.0) == " 0.0000E+00"
+    assert kppsa.fortran_e(999995.0) == " 0.1000E+07"
+    assert kppsa.fortran_e(1e-120) == " 0.1000-119"
